@@ -1,0 +1,150 @@
+/*
+ * libnl2d_gpu — GB300 (sm_103a) NEMOLite2D time step behind the PSyKAl C
+ * boundary of the reference's manual C/C++ version.
+ *
+ * Reference paths are relative to benchmarks/nemo/nemolite2d/ of
+ * stfc/PSycloneBench.
+ *
+ * Data residency follows the reference's GPU PSy layers
+ * (manual_versions/psykal_cpp/time_step_omp_gpu.cpp:58,
+ * manual_versions/psykal_c_opencl/time_step.c:179-640): the first
+ * c_invoke_time_step for a set of arrays copies all 25 of them to the GPU
+ * and every later call advances the device-resident copy.  The host arrays
+ * are NOT updated by a step; the caller (dl_esm_inf's get_data(), through
+ * the read_from_device hook installed in time_step_mod.f90:96-123) pulls a
+ * field back with c_read_from_device.  A call with different array
+ * addresses, extents or internal bounds registers a new problem (the old
+ * device copy is dropped).
+ *
+ * Errors never abort the process and never trap the GPU: void entry points
+ * record a sticky status that nl2d_last_error() returns.  Calls are not
+ * re-entrant; one host thread drives the library, as in the reference.
+ */
+#ifndef NL2D_GPU_H
+#define NL2D_GPU_H
+
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes of nl2d_last_error() and the int-returning entry points. */
+#define NL2D_OK 0
+#define NL2D_ERR_CUDA 1        /* a CUDA call failed (message has the text) */
+#define NL2D_ERR_ARGS 2        /* inconsistent extents, bounds or pointers   */
+#define NL2D_ERR_STATE 3       /* no problem registered yet                  */
+#define NL2D_ERR_UNKNOWN_FIELD 4 /* pointer is not a registered field        */
+#define NL2D_ERR_NONFINITE 5   /* a checksum found a NaN or an infinity      */
+
+/* Step paths (nl2d_set_mode). */
+#define NL2D_MODE_AUTO 0       /* fused one-launch step whenever its preconditions hold */
+#define NL2D_MODE_REFERENCE 1  /* always the 11-kernel reference-structured step        */
+
+/*
+ * One NEMOLite2D time step.  Replaces c_invoke_time_step of
+ * manual_versions/psykal_cpp/time_step.cpp:10-51 (argument meaning and
+ * order unchanged) in the 7-int form that the Fortran interface
+ * manual_versions/psykal_cpp/time_step_mod.f90:8-31 declares and
+ * time_step_omp_gpu.cpp:48 defines: `height` (size(data,2)) follows
+ * `width`.  Internal bounds are 0-based (time_step_mod.f90:82-85).  As in
+ * the reference, the caller may pass dx_v / dx_t in the dy_v / dy_t slots
+ * (time_step_mod.f90:76-77); the arrays are used as given.
+ */
+void c_invoke_time_step(
+    double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
+    double *hu, double *hv, double *un, double *vn, double *ua, double *ht,
+    double *ssha_u, double *va, double *ssha_v,
+    int *tmask, double *area_t, double *area_u, double *area_v,
+    double *dx_u, double *dx_v, double *dx_t, double *dy_u, double *dy_v,
+    double *dy_t, double *gphiu, double *gphiv,
+    int istep, int internal_xstart, int internal_xstop, int internal_ystart,
+    int internal_ystop, int width, int height,
+    double rdt, double cbfr, double visc, double omega, double d2r, double g);
+
+/*
+ * Device -> host copy of one field.  Replaces c_read_from_device of
+ * manual_versions/psykal_c_opencl/time_step.c:788-798 (the read_from_device
+ * hook of time_step_mod.f90:96-123).  `from` is the field's handle: the
+ * host address that was passed for it to c_invoke_time_step (the psykal_cpp
+ * contract has no separate device handle).  `to` is a host array with the
+ * field's layout (row length = width); the region of columns
+ * [startx, startx+nx) and rows [starty, starty+ny) (1-based, as dl_esm_inf
+ * passes them) is copied into the same positions of `to`.  With blocking
+ * false the copy is only ordered on the library's stream; nl2d_sync()
+ * completes it.
+ */
+void c_read_from_device(void *from, void *to, int startx, int starty, int nx,
+                        int ny, bool blocking);
+
+/*
+ * Host -> device copy of one field.  Replaces c_write_to_device of
+ * manual_versions/psykal_c_opencl/time_step.c:802-810.  `from` is the host
+ * source (field layout), `to` is the field's handle (its registered host
+ * address).  The next step after a write runs the reference-structured path.
+ */
+void c_write_to_device(void *from, void *to, int startx, int starty, int nx,
+                       int ny, bool blocking);
+
+/* ---- additions (no counterpart in the reference; the reference path
+ *      above does not depend on them) ---- */
+
+/* Sticky status of the last failing call (NL2D_OK if none) and its text;
+ * reading it clears it. */
+int nl2d_last_error(char *msg, int msg_len);
+
+/* Frees every device allocation (the reference keeps its device copies
+ * until exit). */
+void nl2d_finalize(void);
+
+/* Selects the step path; returns the previous mode. */
+int nl2d_set_mode(int mode);
+
+/* Which path the last step took: 0 none, 1 reference-structured, 2 fused. */
+int nl2d_last_path(void);
+
+/* Registers and uploads a problem without stepping (same arguments as
+ * c_invoke_time_step minus istep).  Returns a status code. */
+int nl2d_register(
+    double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
+    double *hu, double *hv, double *un, double *vn, double *ua, double *ht,
+    double *ssha_u, double *va, double *ssha_v,
+    int *tmask, double *area_t, double *area_u, double *area_v,
+    double *dx_u, double *dx_v, double *dx_t, double *dy_u, double *dy_v,
+    double *dy_t, double *gphiu, double *gphiv,
+    int internal_xstart, int internal_xstop, int internal_ystart,
+    int internal_ystop, int width, int height,
+    double rdt, double cbfr, double visc, double omega, double d2r, double g);
+
+/* Advances the registered problem by nsteps steps, istep = istep0 ...
+ * istep0+nsteps-1, as a captured CUDA graph on the fused path (or the
+ * reference-structured launches where the fused path does not apply).  When
+ * checksum_every > 0, the ssh / u / v checksums (nl2d_checksums) after every
+ * checksum_every-th step are written to checksums_out[3*k .. 3*k+2], k = 0,
+ * 1, ...; checksums_out must hold 3*(nsteps/checksum_every) doubles.
+ * Returns a status code. */
+int nl2d_run_steps(int istep0, int nsteps, int checksum_every,
+                   double *checksums_out);
+
+/* Checksums of the current state: sum |sshn_t| over the internal T region,
+ * sum |un| over [xs, xe-1] x [ys, ye] and sum |vn| over [xs, xe] x
+ * [ys, ye-1] — the regions the PSy layer updates (time_step.cpp:53-77).
+ * Returns NL2D_ERR_NONFINITE if any sum is not finite. */
+int nl2d_checksums(double out[3]);
+
+/* Sum of |field| over columns [x0,x1], rows [y0,y1] (0-based, inclusive)
+ * of a registered field (handle as for c_read_from_device). */
+int nl2d_field_checksum(const void *field, int x0, int x1, int y0, int y1,
+                        double *out);
+
+/* Waits for all work queued by the library. */
+int nl2d_sync(void);
+
+/* Device address currently holding a registered field (for callers that
+ * share device memory); NULL if unknown.  Valid until the next step. */
+void *nl2d_device_ptr(const void *field);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

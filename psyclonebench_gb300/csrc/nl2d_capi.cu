@@ -1,0 +1,688 @@
+// C-ABI of libnl2d_gpu (declared in include/nl2d_gpu.h): problem
+// registration and residency, step-path selection, the reference-facing
+// c_invoke_time_step / c_read_from_device / c_write_to_device, graph-captured
+// multi-step runs and checksums.
+#include "nl2d_internal.h"
+#include "../../include/nl2d_gpu.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace nl2d {
+namespace {
+
+constexpr int kNumFields = 13, kNumGrid = 12;
+
+struct Registration {
+  void* host[kNumFields + kNumGrid];  // caller's arrays, in ABI order
+  int xs, xe, ys, ye, width, height;
+};
+
+struct State {
+  bool registered = false;
+  Registration reg{};
+  Fields dev{};                // "primary" device arrays, one per reference array
+  double* shadow[3] = {};      // ping-pong partners of sshn_t, un, vn
+  int cur = 0;                 // 1: current sshn_t/un/vn live in the shadows
+  bool consistent = false;     // a reference-structured step ran since the upload
+  bool shadows_synced = false; // shadows equal primaries outside the copy region
+  bool materialized = true;    // primaries hold the reference's arrays exactly
+  bool fused_ok = false, chain_u = false, chain_v = false;
+  UniformMetrics um{};
+  Scalars sc{};
+  double sin_d2r = NAN;
+  int mode = NL2D_MODE_AUTO;
+  int last_path = 0;
+  cudaStream_t stream = nullptr;
+  double* partials = nullptr;  // checksum scratch
+  double* sums = nullptr;      // device checksum results
+  int sums_cap = 0;
+  double* tide_table = nullptr;
+  int tide_cap = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_key[4] = {-1, -1, -1, -1};
+  int status = NL2D_OK;
+  char msg[512] = {0};
+};
+
+State g_state;
+
+void set_error(int code, const char* fmt, ...) {
+  if (g_state.status != NL2D_OK) return;  // keep the first error
+  g_state.status = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_state.msg, sizeof g_state.msg, fmt, ap);
+  va_end(ap);
+}
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  set_error(NL2D_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+#define CK(call) cuda_ok((call), #call)
+
+double** field_slot(Fields& f, int k) {
+  double** slots[kNumFields] = {&f.ssha_t, &f.sshn_t, &f.sshn_u, &f.sshn_v, &f.hu,
+                                &f.hv,     &f.un,     &f.vn,     &f.ua,     &f.ht,
+                                &f.ssha_u, &f.va,     &f.ssha_v};
+  return slots[k];
+}
+double** grid_slot(Fields& f, int k) {  // k = 1..11 (0 is tmask)
+  double** slots[kNumGrid] = {nullptr,  &f.area_t, &f.area_u, &f.area_v,
+                              &f.dx_u,  &f.dx_v,   &f.dx_t,   &f.dy_u,
+                              &f.dy_v,  &f.dy_t,   &f.gphiu,  &f.gphiv};
+  return slots[k];
+}
+
+void invalidate_graph();
+
+void free_device() {
+  State& s = g_state;
+  invalidate_graph();
+  if (s.registered) {
+    for (int k = 0; k < kNumFields; k++) cudaFree(*field_slot(s.dev, k));
+    cudaFree(s.dev.tmask);
+    for (int k = 1; k < kNumGrid; k++) cudaFree(*grid_slot(s.dev, k));
+    cudaFree(s.dev.sin_u);
+    cudaFree(s.dev.sin_v);
+    for (double* p : s.shadow) cudaFree(p);
+  }
+  s.dev = Fields{};
+  for (double*& p : s.shadow) p = nullptr;
+  s.registered = false;
+}
+
+Dims dims() {
+  const Registration& r = g_state.reg;
+  return Dims{r.xs, r.xe, r.ys, r.ye, r.width, r.height};
+}
+
+// sin(gphi * d2r) per point with the host libm, reusing the last value for
+// runs of equal latitudes (a uniform grid costs one call).
+void host_sines(const double* gphi, size_t n, double d2r, std::vector<double>& out) {
+  out.resize(n);
+  double last_in = NAN, last_out = 0.0;
+  for (size_t k = 0; k < n; k++) {
+    if (!(gphi[k] == last_in) || std::signbit(gphi[k]) != std::signbit(last_in)) {
+      last_in = gphi[k];
+      last_out = std::sin(gphi[k] * d2r);
+    }
+    out[k] = last_out;
+  }
+}
+
+bool upload_sines(double d2r) {
+  State& s = g_state;
+  const size_t n = (size_t)s.reg.width * s.reg.height;
+  std::vector<double> su, sv;
+  host_sines((const double*)s.reg.host[kNumFields + 10], n, d2r, su);
+  host_sines((const double*)s.reg.host[kNumFields + 11], n, d2r, sv);
+  if (!CK(cudaMemcpy(s.dev.sin_u, su.data(), n * 8, cudaMemcpyHostToDevice))) return false;
+  if (!CK(cudaMemcpy(s.dev.sin_v, sv.data(), n * 8, cudaMemcpyHostToDevice))) return false;
+  s.sin_d2r = d2r;
+  // Uniform-metric check over every point a step reads them at.
+  const Registration& r = s.reg;
+  bool uniform = true;
+  const int W = r.width;
+  auto uniform_over = [&](const double* a, double& v) {
+    v = a[(size_t)(r.ys - 1) * W + (r.xs - 1)];
+    for (int j = r.ys - 1; j <= r.ye + 1; j++)
+      for (int i = r.xs - 1; i <= r.xe + 1; i++) {
+        const double x = a[(size_t)j * W + i];
+        if (memcmp(&x, &v, 8) != 0) return false;
+      }
+    return true;
+  };
+  const double** h = (const double**)(r.host + kNumFields);
+  uniform &= uniform_over(h[1], s.um.area_t);
+  uniform &= uniform_over(h[2], s.um.area_u);
+  uniform &= uniform_over(h[3], s.um.area_v);
+  uniform &= uniform_over(h[4], s.um.dx_u);
+  uniform &= uniform_over(h[5], s.um.dx_v);
+  uniform &= uniform_over(h[6], s.um.dx_t);
+  uniform &= uniform_over(h[7], s.um.dy_u);
+  uniform &= uniform_over(h[8], s.um.dy_v);
+  uniform &= uniform_over(h[9], s.um.dy_t);
+  uniform &= uniform_over(su.data(), s.um.sin_u);
+  uniform &= uniform_over(sv.data(), s.um.sin_v);
+  // Flather chains (a Flather face reading another Flather face) and reads
+  // that would leave the array make the one-launch update differ from the
+  // reference's serial Flather loops.
+  const int* m = (const int*)r.host[kNumFields];
+  auto writes = [&](int c, int step) {
+    return m[c] + m[c + step] > -1 && (m[c] < 0 || m[c + step] < 0);
+  };
+  s.chain_u = s.chain_v = false;
+  bool inside = true;
+  for (int j = r.ys - 1; j <= r.ye + 1; j++)
+    for (int i = r.xs - 1; i <= r.xe; i++) {
+      const int c = j * W + i;
+      if (!writes(c, 1)) continue;
+      const int nb = m[c] < 0 ? i + 1 : i - 1;
+      if (nb < 0) { inside = false; continue; }
+      if (nb >= r.xs - 1 && nb <= r.xe && writes(j * W + nb, 1)) s.chain_u = true;
+    }
+  for (int j = r.ys - 1; j <= r.ye; j++)
+    for (int i = r.xs - 1; i <= r.xe + 1; i++) {
+      const int c = j * W + i;
+      if (!writes(c, W)) continue;
+      const int nb = m[c] < 0 ? j + 1 : j - 1;
+      if (nb < 0) { inside = false; continue; }
+      if (nb >= r.ys - 1 && nb <= r.ye && writes(nb * W + i, W)) s.chain_v = true;
+    }
+  s.fused_ok = uniform && inside && !s.chain_u && !s.chain_v;
+  return true;
+}
+
+bool same_registration(void* const* ptrs, int xs, int xe, int ys, int ye, int width,
+                       int height) {
+  const State& s = g_state;
+  if (!s.registered) return false;
+  const Registration& r = s.reg;
+  if (r.xs != xs || r.xe != xe || r.ys != ys || r.ye != ye || r.width != width ||
+      r.height != height)
+    return false;
+  for (int k = 0; k < kNumFields + kNumGrid; k++)
+    if (r.host[k] != ptrs[k]) return false;
+  return true;
+}
+
+bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, int height,
+                 const Scalars& sc) {
+  State& s = g_state;
+  if (xs < 1 || ys < 1 || xe < xs || ye < ys || xe > width - 2 || ye > height - 2) {
+    set_error(NL2D_ERR_ARGS,
+              "internal region [%d,%d]x[%d,%d] does not fit a %dx%d array with a "
+              "one-cell ring on each side",
+              xs, xe, ys, ye, width, height);
+    return false;
+  }
+  for (int k = 0; k < kNumFields + kNumGrid; k++)
+    if (!ptrs[k]) {
+      set_error(NL2D_ERR_ARGS, "array argument %d is NULL", k);
+      return false;
+    }
+  free_device();
+  if (!s.stream && !CK(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking)))
+    return false;
+  Registration& r = s.reg;
+  for (int k = 0; k < kNumFields + kNumGrid; k++) r.host[k] = ptrs[k];
+  r.xs = xs, r.xe = xe, r.ys = ys, r.ye = ye, r.width = width, r.height = height;
+  const size_t n = (size_t)width * height;
+  s.registered = true;  // so free_device releases partial allocations
+  for (int k = 0; k < kNumFields; k++) {
+    if (!CK(cudaMalloc(field_slot(s.dev, k), n * 8))) return false;
+    if (!CK(cudaMemcpyAsync(*field_slot(s.dev, k), ptrs[k], n * 8, cudaMemcpyHostToDevice,
+                            s.stream)))
+      return false;
+  }
+  if (!CK(cudaMalloc(&s.dev.tmask, n * 4))) return false;
+  if (!CK(cudaMemcpyAsync(s.dev.tmask, ptrs[kNumFields], n * 4, cudaMemcpyHostToDevice,
+                          s.stream)))
+    return false;
+  for (int k = 1; k < kNumGrid; k++) {
+    if (!CK(cudaMalloc(grid_slot(s.dev, k), n * 8))) return false;
+    if (!CK(cudaMemcpyAsync(*grid_slot(s.dev, k), ptrs[kNumFields + k], n * 8,
+                            cudaMemcpyHostToDevice, s.stream)))
+      return false;
+  }
+  if (!CK(cudaMalloc(&s.dev.sin_u, n * 8)) || !CK(cudaMalloc(&s.dev.sin_v, n * 8)))
+    return false;
+  for (double*& p : s.shadow)
+    if (!CK(cudaMalloc(&p, n * 8))) return false;
+  if (!s.partials &&
+      !CK(cudaMalloc(&s.partials, sizeof(double) * checksum_partials_needed())))
+    return false;
+  if (!CK(cudaStreamSynchronize(s.stream))) return false;
+  s.sc = sc;
+  if (!upload_sines(sc.d2r)) return false;
+  s.cur = 0;
+  s.consistent = false;
+  s.shadows_synced = false;
+  s.materialized = true;
+  s.last_path = 0;
+  return true;
+}
+
+// Current device buffers of sshn_t / un / vn.
+double* cur_sshn() { return g_state.cur ? g_state.shadow[0] : g_state.dev.sshn_t; }
+double* cur_un() { return g_state.cur ? g_state.shadow[1] : g_state.dev.un; }
+double* cur_vn() { return g_state.cur ? g_state.shadow[2] : g_state.dev.vn; }
+
+// Brings the primary device arrays to exactly what the reference would hold
+// after the steps taken so far.
+bool materialize() {
+  State& s = g_state;
+  if (s.materialized) return true;
+  if (s.cur) {  // the current state lives in the shadows: swap the roles
+    std::swap(s.dev.sshn_t, s.shadow[0]);
+    std::swap(s.dev.un, s.shadow[1]);
+    std::swap(s.dev.vn, s.shadow[2]);
+    s.cur = 0;
+    invalidate_graph();  // it holds the old buffer roles
+  }
+  const Dims d = dims();
+  // The copies of time_step.cpp:114-122 make un == ua, vn == va and
+  // sshn_t == ssha_t on the copy region; outside it the fused step leaves
+  // those arrays unchanged.  sshn_u / sshn_v are what next_sshu / next_sshv
+  // make of the current sshn_t.
+  launch_copy_region(s.dev.un, s.dev.ua, d, s.stream);
+  launch_copy_region(s.dev.vn, s.dev.va, d, s.stream);
+  launch_copy_region(s.dev.sshn_t, s.dev.ssha_t, d, s.stream);
+  launch_next_ssh(s.dev, d, s.stream);
+  if (!CK(cudaGetLastError())) return false;
+  s.materialized = true;
+  return true;
+}
+
+bool sync_shadows() {
+  State& s = g_state;
+  if (s.shadows_synced) return true;
+  const size_t n = (size_t)s.reg.width * s.reg.height * 8;
+  double* prim[3] = {s.dev.sshn_t, s.dev.un, s.dev.vn};
+  for (int k = 0; k < 3; k++)
+    if (!CK(cudaMemcpyAsync(s.shadow[k], prim[k], n, cudaMemcpyDeviceToDevice, s.stream)))
+      return false;
+  s.shadows_synced = true;
+  return true;
+}
+
+bool can_fuse() {
+  const State& s = g_state;
+  return s.mode == NL2D_MODE_AUTO && s.fused_ok && s.consistent;
+}
+
+bool reference_step(int istep) {
+  State& s = g_state;
+  if (!materialize()) return false;
+  launch_reference_step(s.dev, dims(), s.sc, istep, s.chain_u, s.chain_v, s.stream);
+  if (!CK(cudaGetLastError())) return false;
+  s.consistent = true;
+  s.shadows_synced = false;
+  s.last_path = 1;
+  return true;
+}
+
+void fused_launch(const double* tide_table, int tide_index, double tide) {
+  State& s = g_state;
+  FusedState fs;
+  fs.sshn_in = cur_sshn();
+  fs.un_in = cur_un();
+  fs.vn_in = cur_vn();
+  const int nxt = 1 - s.cur;
+  fs.sshn_out = nxt ? s.shadow[0] : s.dev.sshn_t;
+  fs.un_out = nxt ? s.shadow[1] : s.dev.un;
+  fs.vn_out = nxt ? s.shadow[2] : s.dev.vn;
+  launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
+  s.cur = nxt;
+}
+
+bool fused_step(int istep) {
+  State& s = g_state;
+  if (!sync_shadows()) return false;
+  fused_launch(nullptr, 0, tide_value(istep, s.sc.rdt));
+  if (!CK(cudaGetLastError())) return false;
+  s.materialized = false;
+  s.last_path = 2;
+  return true;
+}
+
+bool one_step(int istep) { return can_fuse() ? fused_step(istep) : reference_step(istep); }
+
+bool ensure_sums(int n) {
+  State& s = g_state;
+  if (s.sums_cap >= n) return true;
+  invalidate_graph();  // a captured graph holds the old address
+  if (s.sums) cudaFree(s.sums);
+  s.sums = nullptr;
+  s.sums_cap = 0;
+  if (!CK(cudaMalloc(&s.sums, sizeof(double) * n))) return false;
+  s.sums_cap = n;
+  return true;
+}
+
+void enqueue_checksums(double* out3) {
+  State& s = g_state;
+  const Registration& r = s.reg;
+  launch_checksum(cur_sshn(), r.width, r.xs, r.xe, r.ys, r.ye, s.partials, out3, s.stream);
+  launch_checksum(cur_un(), r.width, r.xs, r.xe - 1, r.ys, r.ye, s.partials, out3 + 1,
+                  s.stream);
+  launch_checksum(cur_vn(), r.width, r.xs, r.xe, r.ys, r.ye - 1, s.partials, out3 + 2,
+                  s.stream);
+}
+
+int find_field(const void* handle) {
+  const State& s = g_state;
+  if (!s.registered) return -1;
+  for (int k = 0; k < kNumFields + kNumGrid; k++)
+    if (s.reg.host[k] == handle) return k;
+  return -1;
+}
+
+void* device_of(int k) {
+  State& s = g_state;
+  if (k < kNumFields) return *field_slot(s.dev, k);
+  if (k == kNumFields) return s.dev.tmask;
+  return *grid_slot(s.dev, k - kNumFields);
+}
+
+// Status handling for the int-returning entry points: each returns the
+// error it raised itself; an older sticky error (from a void entry point)
+// stays pending for nl2d_last_error().
+struct CallScope {
+  int saved;
+  CallScope() : saved(g_state.status) { g_state.status = NL2D_OK; }
+  int rc() const { return g_state.status; }
+  ~CallScope() {
+    if (g_state.status == NL2D_OK) g_state.status = saved;
+  }
+};
+
+void invalidate_graph() {
+  if (g_state.graph) cudaGraphExecDestroy(g_state.graph);
+  g_state.graph = nullptr;
+  for (int k = 0; k < 4; k++) g_state.graph_key[k] = -1;
+}
+
+}  // namespace
+}  // namespace nl2d
+
+using namespace nl2d;
+
+#define NL2D_PTRS                                                                          \
+  void* ptrs[kNumFields + kNumGrid] = {ssha_t, sshn_t, sshn_u, sshn_v, hu,   hv,    un,    \
+                                       vn,     ua,     ht,     ssha_u, va,   ssha_v, tmask, \
+                                       area_t, area_u, area_v, dx_u,   dx_v, dx_t,  dy_u,  \
+                                       dy_v,   dy_t,   gphiu,  gphiv}
+
+extern "C" {
+
+void c_invoke_time_step(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v,
+                        double* hu, double* hv, double* un, double* vn, double* ua,
+                        double* ht, double* ssha_u, double* va, double* ssha_v, int* tmask,
+                        double* area_t, double* area_u, double* area_v, double* dx_u,
+                        double* dx_v, double* dx_t, double* dy_u, double* dy_v, double* dy_t,
+                        double* gphiu, double* gphiv, int istep, int internal_xstart,
+                        int internal_xstop, int internal_ystart, int internal_ystop,
+                        int width, int height, double rdt, double cbfr, double visc,
+                        double omega, double d2r, double g) {
+  NL2D_PTRS;
+  State& s = g_state;
+  const Scalars sc{rdt, cbfr, visc, omega, d2r, g};
+  if (!same_registration(ptrs, internal_xstart, internal_xstop, internal_ystart,
+                         internal_ystop, width, height)) {
+    if (!do_register(ptrs, internal_xstart, internal_xstop, internal_ystart, internal_ystop,
+                     width, height, sc))
+      return;
+  } else {
+    s.sc = sc;
+    if (!(d2r == s.sin_d2r) && !upload_sines(d2r)) return;
+  }
+  one_step(istep);
+}
+
+int nl2d_register(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v, double* hu,
+                  double* hv, double* un, double* vn, double* ua, double* ht, double* ssha_u,
+                  double* va, double* ssha_v, int* tmask, double* area_t, double* area_u,
+                  double* area_v, double* dx_u, double* dx_v, double* dx_t, double* dy_u,
+                  double* dy_v, double* dy_t, double* gphiu, double* gphiv,
+                  int internal_xstart, int internal_xstop, int internal_ystart,
+                  int internal_ystop, int width, int height, double rdt, double cbfr,
+                  double visc, double omega, double d2r, double g) {
+  NL2D_PTRS;
+  CallScope scope;
+  const Scalars sc{rdt, cbfr, visc, omega, d2r, g};
+  do_register(ptrs, internal_xstart, internal_xstop, internal_ystart, internal_ystop, width,
+              height, sc);
+  return scope.rc();
+}
+
+void c_read_from_device(void* from, void* to, int startx, int starty, int nx, int ny,
+                        bool blocking) {
+  State& s = g_state;
+  const int k = find_field(from);
+  if (k < 0) {
+    set_error(NL2D_ERR_UNKNOWN_FIELD, "c_read_from_device: %p is not a registered field",
+              from);
+    return;
+  }
+  const Registration& r = s.reg;
+  if (startx < 1 || starty < 1 || nx < 0 || ny < 0 || startx - 1 + nx > r.width ||
+      starty - 1 + ny > r.height) {
+    set_error(NL2D_ERR_ARGS, "c_read_from_device: region outside the %dx%d field", r.width,
+              r.height);
+    return;
+  }
+  if (!materialize()) return;
+  const size_t esz = k == kNumFields ? 4 : 8, pitch = (size_t)r.width * esz;
+  const size_t off = ((size_t)(starty - 1) * r.width + (startx - 1)) * esz;
+  if (nx == 0 || ny == 0) return;
+  if (!CK(cudaMemcpy2DAsync((char*)to + off, pitch, (const char*)device_of(k) + off, pitch,
+                            nx * esz, ny, cudaMemcpyDeviceToHost, s.stream)))
+    return;
+  if (blocking) CK(cudaStreamSynchronize(s.stream));
+}
+
+void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int ny,
+                       bool blocking) {
+  State& s = g_state;
+  const int k = find_field(to);
+  if (k < 0) {
+    set_error(NL2D_ERR_UNKNOWN_FIELD, "c_write_to_device: %p is not a registered field", to);
+    return;
+  }
+  const Registration& r = s.reg;
+  if (startx < 1 || starty < 1 || nx < 0 || ny < 0 || startx - 1 + nx > r.width ||
+      starty - 1 + ny > r.height) {
+    set_error(NL2D_ERR_ARGS, "c_write_to_device: region outside the %dx%d field", r.width,
+              r.height);
+    return;
+  }
+  if (k >= kNumFields && from != to) {
+    set_error(NL2D_ERR_ARGS,
+              "c_write_to_device: a grid array is written from its registered host array");
+    return;
+  }
+  if (!materialize()) return;
+  const size_t esz = k == kNumFields ? 4 : 8, pitch = (size_t)r.width * esz;
+  const size_t off = ((size_t)(starty - 1) * r.width + (startx - 1)) * esz;
+  if (nx > 0 && ny > 0 &&
+      !CK(cudaMemcpy2DAsync((char*)device_of(k) + off, pitch, (const char*)from + off, pitch,
+                            nx * esz, ny, cudaMemcpyHostToDevice, s.stream)))
+    return;
+  // Any written array may break the fused path's preconditions: re-derive
+  // them from the host copies where they can change, and take the next step
+  // on the reference-structured path.
+  s.consistent = false;
+  s.shadows_synced = false;
+  if (k >= kNumFields && !upload_sines(s.sc.d2r)) return;
+  if (blocking) CK(cudaStreamSynchronize(s.stream));
+}
+
+int nl2d_last_error(char* msg, int msg_len) {
+  State& s = g_state;
+  const int st = s.status;
+  if (msg && msg_len > 0) {
+    strncpy(msg, s.msg, msg_len - 1);
+    msg[msg_len - 1] = '\0';
+  }
+  s.status = NL2D_OK;
+  s.msg[0] = '\0';
+  return st;
+}
+
+void nl2d_finalize(void) {
+  State& s = g_state;
+  if (s.stream) cudaStreamSynchronize(s.stream);
+  free_device();
+  if (s.partials) cudaFree(s.partials);
+  if (s.sums) cudaFree(s.sums);
+  if (s.tide_table) cudaFree(s.tide_table);
+  s.partials = s.sums = s.tide_table = nullptr;
+  s.sums_cap = s.tide_cap = 0;
+  if (s.stream) cudaStreamDestroy(s.stream);
+  s.stream = nullptr;
+}
+
+int nl2d_set_mode(int mode) {
+  State& s = g_state;
+  const int old = s.mode;
+  if (mode != NL2D_MODE_AUTO && mode != NL2D_MODE_REFERENCE) {
+    set_error(NL2D_ERR_ARGS, "nl2d_set_mode: unknown mode %d", mode);
+    return old;
+  }
+  s.mode = mode;
+  return old;
+}
+
+int nl2d_last_path(void) { return g_state.last_path; }
+
+int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums_out) {
+  State& s = g_state;
+  CallScope scope;
+  auto take_status = [&]() { return scope.rc(); };
+  if (!s.registered) {
+    set_error(NL2D_ERR_STATE, "nl2d_run_steps: no problem registered");
+    return take_status();
+  }
+  if (nsteps < 0 || checksum_every < 0) {
+    set_error(NL2D_ERR_ARGS, "nl2d_run_steps: negative count");
+    return take_status();
+  }
+  const int nsums = checksum_every > 0 ? nsteps / checksum_every : 0;
+  if (nsums > 0 && !checksums_out) {
+    set_error(NL2D_ERR_ARGS, "nl2d_run_steps: checksums_out is NULL");
+    return take_status();
+  }
+  if (!ensure_sums(3 * (nsums > 0 ? nsums : 1))) return take_status();
+  int k = 0;
+  // The first step after an upload (or in reference mode, every step) runs
+  // on the reference-structured path.
+  while (k < nsteps && !can_fuse()) {
+    if (!reference_step(istep0 + k)) return take_status();
+    k++;
+    if (checksum_every > 0 && k % checksum_every == 0)
+      enqueue_checksums(s.sums + 3 * (k / checksum_every - 1));
+  }
+  const int rest = nsteps - k;
+  if (rest > 0) {
+    if (!sync_shadows()) return take_status();
+    // Tidal values for the remaining steps, evaluated on the host.
+    if (s.tide_cap < rest) {
+      invalidate_graph();  // it holds the old table address
+      if (s.tide_table) cudaFree(s.tide_table);
+      s.tide_table = nullptr;
+      s.tide_cap = 0;
+      if (!CK(cudaMalloc(&s.tide_table, sizeof(double) * rest))) return take_status();
+      s.tide_cap = rest;
+    }
+    std::vector<double> tides(rest);
+    for (int q = 0; q < rest; q++) tides[q] = tide_value(istep0 + k + q, s.sc.rdt);
+    if (!CK(cudaMemcpyAsync(s.tide_table, tides.data(), sizeof(double) * rest,
+                            cudaMemcpyHostToDevice, s.stream)))
+      return take_status();
+    // The graph depends on the step count, the checksum cadence and phase,
+    // and which ping-pong buffer holds the state.
+    const int key[4] = {rest, checksum_every, checksum_every > 0 ? k % checksum_every : 0,
+                        s.cur};
+    const bool hit = s.graph && memcmp(key, s.graph_key, sizeof key) == 0;
+    const int cur0 = s.cur;
+    if (!hit) {
+      invalidate_graph();
+      cudaGraph_t graph;
+      if (!CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal)))
+        return take_status();
+      for (int q = 0; q < rest; q++) {
+        fused_launch(s.tide_table, q, 0.0);
+        const int done = k + q + 1;
+        if (checksum_every > 0 && done % checksum_every == 0)
+          enqueue_checksums(s.sums + 3 * (done / checksum_every - 1));
+      }
+      const bool cap_ok = CK(cudaStreamEndCapture(s.stream, &graph));
+      if (!cap_ok) return take_status();
+      const bool inst_ok = CK(cudaGraphInstantiate(&s.graph, graph, 0));
+      cudaGraphDestroy(graph);
+      if (!inst_ok) return take_status();
+      memcpy(s.graph_key, key, sizeof key);
+    } else {
+      s.cur = (cur0 + rest) & 1;
+    }
+    if (!CK(cudaGraphLaunch(s.graph, s.stream))) return take_status();
+    s.materialized = false;
+    s.last_path = 2;
+  }
+  if (nsums > 0) {
+    if (!CK(cudaMemcpyAsync(checksums_out, s.sums, sizeof(double) * 3 * nsums,
+                            cudaMemcpyDeviceToHost, s.stream)))
+      return take_status();
+    if (!CK(cudaStreamSynchronize(s.stream))) return take_status();
+  }
+  return take_status();
+}
+
+int nl2d_checksums(double out[3]) {
+  State& s = g_state;
+  CallScope scope;
+  auto take_status = [&]() { return scope.rc(); };
+  if (!s.registered) {
+    set_error(NL2D_ERR_STATE, "nl2d_checksums: no problem registered");
+    return take_status();
+  }
+  if (!ensure_sums(3)) return take_status();
+  enqueue_checksums(s.sums);
+  if (!CK(cudaMemcpyAsync(out, s.sums, sizeof(double) * 3, cudaMemcpyDeviceToHost,
+                          s.stream)))
+    return take_status();
+  if (!CK(cudaStreamSynchronize(s.stream))) return take_status();
+  for (int k = 0; k < 3; k++)
+    if (!std::isfinite(out[k])) {
+      set_error(NL2D_ERR_NONFINITE, "checksum %d is not finite", k);
+      break;
+    }
+  return take_status();
+}
+
+int nl2d_field_checksum(const void* field, int x0, int x1, int y0, int y1, double* out) {
+  State& s = g_state;
+  CallScope scope;
+  auto take_status = [&]() { return scope.rc(); };
+  const int k = find_field(field);
+  if (k < 0 || k >= kNumFields) {
+    set_error(NL2D_ERR_UNKNOWN_FIELD, "nl2d_field_checksum: %p is not a registered field",
+              field);
+    return take_status();
+  }
+  const Registration& r = s.reg;
+  if (x0 < 0 || y0 < 0 || x1 >= r.width || y1 >= r.height) {
+    set_error(NL2D_ERR_ARGS, "nl2d_field_checksum: region outside the field");
+    return take_status();
+  }
+  if (!materialize() || !ensure_sums(3)) return take_status();
+  launch_checksum((const double*)device_of(k), r.width, x0, x1, y0, y1, s.partials, s.sums,
+                  s.stream);
+  if (!CK(cudaMemcpyAsync(out, s.sums, sizeof(double), cudaMemcpyDeviceToHost, s.stream)))
+    return take_status();
+  CK(cudaStreamSynchronize(s.stream));
+  return take_status();
+}
+
+int nl2d_sync(void) {
+  State& s = g_state;
+  CallScope scope;
+  if (s.stream) CK(cudaStreamSynchronize(s.stream));
+  return scope.rc();
+}
+
+void* nl2d_device_ptr(const void* field) {
+  const int k = find_field(field);
+  if (k < 0) return nullptr;
+  if (!materialize()) return nullptr;
+  return device_of(k);
+}
+
+}  // extern "C"

@@ -1,0 +1,82 @@
+// Internal types shared by the NEMOLite2D GPU translation units.
+//
+// Layout in HBM: every field is a row-major [height][width] FP64 array with
+// element (ji, jj) at jj*width + ji (0-based), exactly the layout of a
+// dl_esm_inf r2d_field's `data(width, height)` seen from C.  The T-mask is
+// the same shape in int32.  The internal T region is [xs,xe] x [ys,ye].
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace nl2d {
+
+// Device copies of the 13 fields and 12 grid arrays that
+// c_invoke_time_step receives (psykal_cpp/time_step.cpp:10-51), plus the
+// Coriolis sines sin(gphi*d2r) evaluated once on the host with the host's
+// libm (the reference evaluates them per point with the same libm).
+struct Fields {
+  double *ssha_t, *sshn_t, *sshn_u, *sshn_v, *hu, *hv, *un, *vn, *ua, *ht,
+      *ssha_u, *va, *ssha_v;
+  int* tmask;
+  double *area_t, *area_u, *area_v, *dx_u, *dx_v, *dx_t, *dy_u, *dy_v, *dy_t,
+      *gphiu, *gphiv;
+  double *sin_u, *sin_v;
+};
+
+struct Dims {
+  int xs, xe, ys, ye;  // internal T region, 0-based inclusive
+  int width, height;
+};
+
+struct Scalars {
+  double rdt, cbfr, visc, omega, d2r, g;
+};
+
+// Grid metrics when every metric array is uniform over the region the step
+// reads (true for every dl_esm_inf grid built by grid_init with constant
+// dx, dy and the f-plane latitude).  The fused kernel then takes them as
+// scalars; each value is the array's value, so results do not change.
+struct UniformMetrics {
+  double area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t;
+  double sin_u, sin_v;
+};
+
+// Tidal sea-surface height of bc_ssh_code
+// (kernels/c_family/boundary_conditions_kern.c:183-192) at step `istep`,
+// evaluated on the host with the host's libm.
+double tide_value(int istep, double rdt);
+
+// ---- launchers (nl2d_perkernel.cu) ----
+// The reference-structured step: 11 launches in time_step.cpp's order.
+// `chain_u` / `chain_v` select the ordered Flather kernels for masks in
+// which one Flather face reads another Flather face.
+void launch_reference_step(const Fields& f, const Dims& d, const Scalars& s,
+                           int istep, bool chain_u, bool chain_v,
+                           cudaStream_t st);
+// next_sshu / next_sshv alone (time_update_kern.c:90-155).
+void launch_next_ssh(const Fields& f, const Dims& d, cudaStream_t st);
+// Copy of the copy region [xs-1, xe+1] x [ys-1, ye] from src to dst.
+void launch_copy_region(const double* src, double* dst, const Dims& d,
+                        cudaStream_t st);
+
+// ---- fused FP64 step (nl2d_fused.cu) ----
+struct FusedState {
+  const double *sshn_in, *un_in, *vn_in;
+  double *sshn_out, *un_out, *vn_out;
+};
+// `tide` is the bc_ssh value of this step, or, when `tide_table` is not
+// null, tide_table[tide_index] (a device table; used by captured graphs).
+void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
+                       const Scalars& s, const UniformMetrics& um, double tide,
+                       const double* tide_table, int tide_index,
+                       cudaStream_t st);
+
+// ---- checksums (nl2d_checksum.cu) ----
+// Sum of |f| over [x0,x1] x [y0,y1]; per-block partial sums go to
+// `partials` (at least checksum_partials_needed() doubles) and the final
+// FP64 value to *out, both on the device.
+int checksum_partials_needed();
+void launch_checksum(const double* f, int width, int x0, int x1, int y0,
+                     int y1, double* partials, double* out, cudaStream_t st);
+
+}  // namespace nl2d

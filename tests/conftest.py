@@ -1,0 +1,29 @@
+import os
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+for p in (HERE, REPO):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import nl2d_testlib as T
+    return T.load_oracle()
+
+
+@pytest.fixture(scope="session")
+def gpulib():
+    import psyclonebench_gb300 as P
+    import torch  # noqa: F401  (only to probe for a device)
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test run without a CUDA device")
+    return P.load_library()

@@ -1,0 +1,180 @@
+"""GPU parity: the CUDA step, called through the C-ABI, against the CPU
+oracle (and the golden fixtures made by the reference's own serial build).
+
+Bar: bit-identical FP64 fields (both sides perform the same IEEE operations
+in the same order; the oracle is built with -ffp-contract=off, the kernels
+with -fmad=false).  Checksums are reduced in a different order on the GPU,
+so they are compared to 10 significant digits (rtol 1e-10), the bar the
+reference's E16.8 print-out cannot even resolve.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import nl2d_testlib as T
+from test_oracle import CASES, bits_equal, load_case
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CHECKSUM_RTOL = 1e-10
+
+
+def assert_fields_equal(got, want, tag=""):
+    bad = [k for k in T.FIELDS if not bits_equal(got.f[k], want.f[k])]
+    if bad:
+        k = bad[0]
+        diff = np.argwhere(got.f[k].view(np.int64) != want.f[k].view(np.int64))
+        raise AssertionError("%s: fields differ %s; first %s at %s: %r vs %r" % (
+            tag, bad, k, diff[0], got.f[k][tuple(diff[0])], want.f[k][tuple(diff[0])]))
+
+
+@pytest.mark.parametrize("mode", [1, 0], ids=["reference_path", "fused_path"])
+def test_cfg0_2000_steps_bitwise(gpulib, oracle, mode):
+    """130x130 namelist (128x128 interior), 2000 steps through
+    c_invoke_time_step: all 13 fields bit-identical to the oracle."""
+    m = T.make_model(130, 130, 1, oracle=oracle)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 2000)
+    paths = T.gpu_run_calls(gpulib, m, 2000, mode=mode)
+    if mode == 0:
+        assert paths[0] == 1 and set(paths[1:]) == {2}, "fused path not taken"
+    else:
+        assert set(paths) == {1}
+    assert_fields_equal(m, want, "mode %d" % mode)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("mode", [1, 0], ids=["reference_path", "fused_path"])
+def test_golden_fields_bitwise(gpulib, name, mode):
+    """The reference serial build's final fields (tests/golden, made by
+    make_golden.py) on small, odd and padded grids with jphgr_msh 1, 2, 3
+    and a seeded bathymetry."""
+    m, nsteps, want = load_case(name)
+    T.gpu_run_calls(gpulib, m, nsteps, mode=mode)
+    for k in T.FIELDS:
+        assert bits_equal(m.f[k], want[k]), (name, k)
+
+
+def test_graph_run_checksums_cfg0(gpulib, oracle):
+    """nl2d_run_steps (CUDA graph, in-graph checksums every 100 steps) over
+    2000 steps: checksums within 1e-10 of the reference's, fields bitwise."""
+    want_sums = np.loadtxt(os.path.join(GOLDEN, "cfg0_checksums.txt"))
+    m = T.make_model(130, 130, 1, oracle=oracle)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 2000)
+    sums = T.gpu_run_graph(gpulib, m, 2000, every=100)
+    np.testing.assert_allclose(sums, want_sums[:, :3], rtol=CHECKSUM_RTOL, atol=0)
+    assert_fields_equal(m, want, "graph")
+
+
+def test_graph_rerun_and_split(gpulib, oracle):
+    """Two graph runs back to back (cached graph, both ping-pong phases) equal
+    one long oracle run; so does a run split by per-step calls."""
+    m = T.make_model(40, 33, 3, width=48, oracle=oracle)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 3 * 37 + 5)
+    T.gpu_register(gpulib, m)
+    import psyclonebench_gb300 as P
+    out = np.zeros(3)
+    for k in range(3):
+        P.check(gpulib.nl2d_run_steps(1 + 37 * k, 37, 0, T.dptr(out)), "run")
+    T.gpu_read_all(gpulib, m)
+    # continue with per-step calls on the same registration
+    for k in range(5):
+        gpulib.c_invoke_time_step(*m.step_args(1 + 111 + k))
+    T.gpu_read_all(gpulib, m)
+    assert_fields_equal(m, want, "graph+calls")
+
+
+def test_random_masks_and_bathymetry(gpulib, oracle):
+    """Random land cells, random depths, padded widths: every step path."""
+    rng = np.random.default_rng(11)
+    for trial in range(4):
+        nx, ny = (int(v) for v in rng.integers(9, 40, size=2))
+        m = T.make_model(nx, ny, int(rng.integers(1, 4)),
+                         width=nx + 1 + int(rng.integers(0, 9)), oracle=oracle)
+        inner = m.grid["tmask"][m.ys + 1:m.ye, m.xs + 1:m.xe]
+        inner[rng.random(inner.shape) < 0.08] = 0
+        for k in ("ht", "hu", "hv"):
+            m.f[k][:] = rng.uniform(50, 500, size=m.f[k].shape)
+        want = m.copy()
+        T.run(oracle.oracle_invoke_time_step, want, 60)
+        got = m.copy()
+        T.gpu_run_calls(gpulib, got, 60, mode=0)
+        assert_fields_equal(got, want, "trial %d" % trial)
+
+
+def test_chained_flather_mask_uses_reference_path(gpulib, oracle):
+    """A one-cell-wide wet column between two open columns makes a Flather
+    face read another Flather face; the library then keeps to the ordered
+    reference-structured step and still matches bit for bit."""
+    m = T.make_model(16, 12, 1, oracle=oracle)
+    t = m.grid["tmask"]
+    t[m.ys:m.ye + 1, 5] = -1
+    t[m.ys:m.ye + 1, 7] = -1
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 50)
+    paths = T.gpu_run_calls(gpulib, m, 50, mode=0)
+    assert set(paths) == {1}
+    assert_fields_equal(m, want, "chained")
+
+
+def test_write_to_device_then_step(gpulib, oracle):
+    """c_write_to_device of a perturbed sshn_t mid-run: the next step uses
+    it (reference path), later steps fuse again; all bitwise."""
+    m = T.make_model(30, 26, 1, oracle=oracle)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 20)
+    T.gpu_run_calls(gpulib, m, 20, mode=0)
+    pert = np.random.default_rng(5).normal(0, 1e-3, size=m.f["sshn_t"].shape)
+    for mm in (m, want):
+        mm.f["sshn_t"] += pert
+    gpulib.c_write_to_device(m.f["sshn_t"].ctypes.data, m.f["sshn_t"].ctypes.data, 1, 1,
+                             m.width, m.height, True)
+    T.run(oracle.oracle_invoke_time_step, want, 30, nit000=21)
+    paths = T.gpu_run_calls(gpulib, m, 30, nit000=21, mode=0)
+    assert paths[0] == 1 and paths[-1] == 2
+    assert_fields_equal(m, want, "after write")
+
+
+def test_partial_read(gpulib, oracle):
+    m = T.make_model(20, 20, 1, oracle=oracle)
+    T.gpu_run_calls(gpulib, m, 10, mode=0)
+    full = m.f["un"].copy()
+    dst = np.full_like(full, 7.0)
+    gpulib.c_read_from_device(m.f["un"].ctypes.data, dst.ctypes.data, 3, 4, 5, 6, True)
+    T.gpu_check(gpulib, "partial read")
+    assert bits_equal(dst[3:9, 2:7], full[3:9, 2:7])
+    dst[3:9, 2:7] = 7.0
+    assert (dst == 7.0).all()
+
+
+def test_errors_are_reported_not_fatal(gpulib, oracle):
+    import psyclonebench_gb300 as P
+    m = T.make_model(12, 12, 1, oracle=oracle)
+    args = m.step_args(1)
+    args[26] = 0  # internal_xstart = 0 leaves no ring
+    gpulib.c_invoke_time_step(*args)
+    with pytest.raises(P.Nl2dError):
+        P.check(None, "bad bounds")
+    junk = np.zeros(4)
+    gpulib.c_read_from_device(junk.ctypes.data, junk.ctypes.data, 1, 1, 2, 2, True)
+    with pytest.raises(P.Nl2dError):
+        P.check(None, "unknown field")
+    # the library still works afterwards
+    m2 = T.make_model(12, 12, 1, oracle=oracle)
+    want = m2.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 5)
+    T.gpu_run_calls(gpulib, m2, 5)
+    assert_fields_equal(m2, want)
+
+
+def test_deterministic(gpulib, oracle):
+    a = T.make_model(64, 48, 1, oracle=oracle)
+    b = a.copy()
+    sa = T.gpu_run_graph(gpulib, a, 200, every=50)
+    sb = T.gpu_run_graph(gpulib, b, 200, every=50)
+    assert bits_equal(sa, sb)
+    assert_fields_equal(a, b, "determinism")
