@@ -1,0 +1,327 @@
+"""Benchmark: NEMOLite2D FP64 time step at 4096 x 4096 interior cells.
+
+`python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]`
+
+A "step" is one NEMOLite2D time step over the whole 4096^2 domain
+(namelist jpiglo = jpjglo = 4098, jphgr_msh = 1, dx = dy = 1000 m,
+depth 100 m, rdt = 20 s, cbfr = 1.5e-4, visc = 0.1, tide 0.2 m / 12.42 h,
+rest start).  The domain does not shard: with N > 1 every rank runs an
+independent replica and `value` counts all ranks' cell-steps ("replicas
+only").
+
+ours:
+  value  Mcell-steps/s over K fused FP64 steps with the state resident in
+         HBM: one CUDA-graph launch timed with CUDA events on the library's
+         stream.  Every field is larger than L2 (4098 x 4104 FP64 = 135 MB >
+         129 MB), and the per-step working set is ~1.3 GB, so no flush is
+         needed.
+  e2e    the same K steps through the reference-facing C-ABI from HOST
+         buffers: c_invoke_time_step per step (the first call uploads all 25
+         arrays), then c_read_from_device of sshn_t, un and vn; host wall
+         clock around all of it.
+  roofline  HBM: 76 algorithmic bytes per interior cell-step (read sshn_t,
+         un, vn, ht, hu, hv as FP64 + tmask as int32; write sshn_t, un, vn)
+         divided by the fused kernel's event time, against the measured HBM
+         copy bandwidth.  `fp64` adds the FP64-pipe view of the same kernel.
+  cpu_baseline  the CPU reference timed on this host's cores (the
+         reference's OpenMP PSy layer where it was compiled here, else the
+         oracle's OpenMP port) on a bounded sample of the same domain.
+reference:
+  the reference's CPU implementation on all host threads, K steps of the
+  same domain.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+ALG_BYTES_PER_CELL = 76  # 6 x 8 B read + 4 B mask + 3 x 8 B write
+NPTS = 4096
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=NPTS, help="interior cells per side")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_problem(n):
+    """The reference's initial state for an n x n interior (jpiglo = n + 2),
+    rows padded to a multiple of 8 doubles."""
+    import nl2d_testlib as T
+    jp = n + 2
+    width = ((jp + 1 + 7) // 8) * 8
+    return T.make_model(jp, jp, 1, width=width)
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def load_profile_figures():
+    """Per-launch DRAM traffic and FP64 instruction counts of the fused
+    kernel from the committed ncu summary, if present."""
+    p = os.path.join(REPO, "profiles", "fused_fp64_step.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_step_fn():
+    """The reference's OpenMP PSy layer where oracle/_ref holds it (compiled
+    from the reference sources on this machine), else the oracle's OpenMP
+    port.  Returns (callable, kind, description)."""
+    import nl2d_testlib as T
+    ref = T.load_ref("omp")
+    if ref is not None:
+        return ref.c_invoke_time_step, "reference", "psykal_cpp/time_step_omp.cpp (-O3 -fopenmp)"
+    o = T.load_oracle()
+    return o.oracle_invoke_time_step_omp, "port", "oracle OpenMP port of time_step_omp.cpp"
+
+
+def time_cpu(m, nsteps, target_s=None):
+    """Times CPU steps; if target_s is given, runs until ~target_s seconds
+    (at least one step) and returns (steps, seconds)."""
+    import nl2d_testlib as T
+    fn, kind, desc = cpu_step_fn()
+    nargs = len(fn.argtypes)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        args = m.step_args(1 + done)
+        if nargs == len(T.REF_ARGTYPES):
+            del args[31]
+        fn(*args)
+        done += 1
+        el = time.perf_counter() - t0
+        if target_s is None and done >= nsteps:
+            break
+        if target_s is not None and (el >= target_s or done >= nsteps):
+            break
+    return done, time.perf_counter() - t0, kind, desc
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    n = args.size
+    m = make_problem(n)
+    # warm-up steps, then K timed steps (bounded: stop after ~120 s)
+    time_cpu(m, max(args.warmup, 1))
+    steps, secs, kind, desc = time_cpu(m, args.steps, target_s=120.0)
+    cells = n * n
+    val = cells * steps / secs / 1e6
+    line = {
+        "metric": "Mcell-steps/s", "value": val, "unit": "Mcell-steps/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state)",
+        "config": {"workload": "nemolite2d_fp64_%dx%d" % (n, n), "interior": [n, n],
+                   "jphgr_msh": 1, "rdt": 20.0, "parallelism": "replicas"},
+        "cpu_baseline": {"value": val, "unit": "Mcell-steps/s", "cores": cores,
+                         "kind": kind, "sample": "%d steps of the %dx%d domain (%s)" % (
+                             steps, n, n, desc)},
+        "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local):
+    import nl2d_testlib as T
+    import psyclonebench_gb300 as P
+    import torch
+    import torch.distributed as dist
+
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    lib = P.load_library()
+    n = args.size
+    cells = n * n
+
+    # ---- value: resident state, one graph launch of K fused steps ----
+    m = make_problem(n)
+    T.gpu_register(lib, m)
+    ms = ctypes.c_double(0.0)
+    P.check(lib.nl2d_timed_run(1, 1 + args.warmup, ctypes.byref(ms)), "warm-up")
+    istep = 2 + args.warmup
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        P.check(lib.nl2d_timed_run(istep, args.steps, ctypes.byref(ms)), "timed run")
+    torch.cuda.synchronize()
+    kernel_ms = ms.value
+    if world > 1:
+        t = torch.tensor([kernel_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        kernel_ms = float(t.item())
+    sums = np.zeros(3)
+    P.check(lib.nl2d_checksums(T.dptr(sums)), "checksums")
+    value = cells * args.steps * world / (kernel_ms * 1e-3) / 1e6
+    ms_step = kernel_ms / args.steps
+    lib.nl2d_finalize()
+
+    # ---- e2e: host buffers through c_invoke_time_step ----
+    e2e = None
+    if not args.no_e2e:
+        m2 = make_problem(n)
+        nbytes_in = sum(a.nbytes for a in m2.f.values()) + sum(a.nbytes for a in m2.grid.values())
+        nbytes_out = 3 * m2.f["sshn_t"].nbytes
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            lib.c_invoke_time_step(*m2.step_args(1 + k))
+        for k in ("sshn_t", "un", "vn"):
+            a = m2.f[k]
+            lib.c_read_from_device(a.ctypes.data, a.ctypes.data, 1, 1, m2.width, m2.height, True)
+        P.check(None, "e2e")
+        secs = time.perf_counter() - t0
+        e2e = {"value": cells * args.steps * world / secs / 1e6, "unit": "Mcell-steps/s",
+               "h2d_bytes_per_step": nbytes_in / args.steps,
+               "d2h_bytes_per_step": nbytes_out / args.steps,
+               "seconds": secs}
+        lib.nl2d_finalize()
+
+    hbm, peak_kind = peaks()
+    prof = load_profile_figures()
+    achieved = ALG_BYTES_PER_CELL * cells / (ms_step * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_kind": peak_kind,
+            "traffic": prof.get("dram_bytes_per_launch"),
+            "kernel": "k_fused_step", "alg_bytes_per_cell": ALG_BYTES_PER_CELL}
+    if prof.get("fp64_ops_per_launch"):
+        roof["fp64"] = {
+            "achieved_gops": prof["fp64_ops_per_launch"] / (ms_step * 1e-3) / 1e9,
+            "ops_per_cell": prof["fp64_ops_per_launch"] / cells,
+            "peak_gops": prof.get("fp64_peak_gops"),
+        }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        mc = make_problem(n)
+        steps, secs, kind, desc = time_cpu(mc, 10 ** 6, target_s=15.0)
+        cpu = {"value": cells * steps / secs / 1e6, "unit": "Mcell-steps/s",
+               "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": kind,
+               "sample": "%d steps of the %dx%d domain from rest (%s), ~15 s" % (
+                   steps, n, n, desc)}
+
+    if rank == 0:
+        line = {
+            "metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (reference initial state: rest, constant depth)",
+            "config": {"workload": "nemolite2d_fp64_%dx%d" % (n, n), "interior": [n, n],
+                       "jphgr_msh": 1, "rdt": 20.0, "width": m.width,
+                       "l2": "inputs larger than L2 (135 MB per field)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "checksums": {"ssh": sums[0], "u": sums[1], "v": sums[2]},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -126,6 +126,14 @@ int nl2d_register(
 int nl2d_run_steps(int istep0, int nsteps, int checksum_every,
                    double *checksums_out);
 
+/* Advances the registered problem by nsteps fused steps from istep0 as one
+ * graph launch timed with CUDA events on the library's stream; *ms_out gets
+ * the device time of the launch.  Untimed set-up (a first
+ * reference-structured step if the state needs one, graph capture) is done
+ * before the timed region.  Returns NL2D_ERR_STATE if the fused path does
+ * not apply to the problem. */
+int nl2d_timed_run(int istep0, int nsteps, double *ms_out);
+
 /* Checksums of the current state: sum |sshn_t| over the internal T region,
  * sum |un| over [xs, xe-1] x [ys, ye] and sum |vn| over [xs, xe] x
  * [ys, ye-1] — the regions the PSy layer updates (time_step.cpp:53-77).

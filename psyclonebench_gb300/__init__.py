@@ -42,6 +42,7 @@ EXPORTS = {
     "nl2d_last_path": (ctypes.c_int, []),
     "nl2d_register": (ctypes.c_int, REGISTER_ARGTYPES),
     "nl2d_run_steps": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP]),
+    "nl2d_timed_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP]),
     "nl2d_checksums": (ctypes.c_int, [_DP]),
     "nl2d_field_checksum": (ctypes.c_int, [_VP] + [ctypes.c_int] * 4 + [_DP]),
     "nl2d_sync": (ctypes.c_int, []),

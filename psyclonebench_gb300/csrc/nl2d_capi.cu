@@ -389,6 +389,49 @@ void invalidate_graph() {
   for (int k = 0; k < 4; k++) g_state.graph_key[k] = -1;
 }
 
+// Uploads the tidal values of steps istep0 .. istep0+rest-1 and makes
+// s.graph a graph of `rest` fused steps (with checksums after every
+// checksum_every-th step counted from `done_before`), capturing it unless
+// the cached one matches.  Nothing is launched; s.cur is left unchanged.
+bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
+  State& s = g_state;
+  if (!sync_shadows()) return false;
+  if (s.tide_cap < rest) {
+    invalidate_graph();  // it holds the old table address
+    if (s.tide_table) cudaFree(s.tide_table);
+    s.tide_table = nullptr;
+    s.tide_cap = 0;
+    if (!CK(cudaMalloc(&s.tide_table, sizeof(double) * rest))) return false;
+    s.tide_cap = rest;
+  }
+  std::vector<double> tides(rest);
+  for (int q = 0; q < rest; q++) tides[q] = tide_value(istep0 + q, s.sc.rdt);
+  if (!CK(cudaMemcpyAsync(s.tide_table, tides.data(), sizeof(double) * rest,
+                          cudaMemcpyHostToDevice, s.stream)))
+    return false;
+  // pageable source: the copy is staged before the call returns
+  const int phase = checksum_every > 0 ? done_before % checksum_every : 0;
+  const int key[4] = {rest, checksum_every, phase, s.cur};
+  if (s.graph && memcmp(key, s.graph_key, sizeof key) == 0) return true;
+  invalidate_graph();
+  const int cur0 = s.cur;
+  cudaGraph_t graph;
+  if (!CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal))) return false;
+  for (int q = 0; q < rest; q++) {
+    fused_launch(s.tide_table, q, 0.0);
+    const int done = done_before + q + 1;
+    if (checksum_every > 0 && done % checksum_every == 0)
+      enqueue_checksums(s.sums + 3 * (done / checksum_every - 1));
+  }
+  s.cur = cur0;
+  if (!CK(cudaStreamEndCapture(s.stream, &graph))) return false;
+  const bool ok = CK(cudaGraphInstantiate(&s.graph, graph, 0));
+  cudaGraphDestroy(graph);
+  if (!ok) return false;
+  memcpy(s.graph_key, key, sizeof key);
+  return true;
+}
+
 }  // namespace
 }  // namespace nl2d
 
@@ -545,84 +588,83 @@ int nl2d_last_path(void) { return g_state.last_path; }
 int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums_out) {
   State& s = g_state;
   CallScope scope;
-  auto take_status = [&]() { return scope.rc(); };
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_run_steps: no problem registered");
-    return take_status();
+    return scope.rc();
   }
   if (nsteps < 0 || checksum_every < 0) {
     set_error(NL2D_ERR_ARGS, "nl2d_run_steps: negative count");
-    return take_status();
+    return scope.rc();
   }
   const int nsums = checksum_every > 0 ? nsteps / checksum_every : 0;
   if (nsums > 0 && !checksums_out) {
     set_error(NL2D_ERR_ARGS, "nl2d_run_steps: checksums_out is NULL");
-    return take_status();
+    return scope.rc();
   }
-  if (!ensure_sums(3 * (nsums > 0 ? nsums : 1))) return take_status();
+  if (!ensure_sums(3 * (nsums > 0 ? nsums : 1))) return scope.rc();
   int k = 0;
   // The first step after an upload (or in reference mode, every step) runs
   // on the reference-structured path.
   while (k < nsteps && !can_fuse()) {
-    if (!reference_step(istep0 + k)) return take_status();
+    if (!reference_step(istep0 + k)) return scope.rc();
     k++;
     if (checksum_every > 0 && k % checksum_every == 0)
       enqueue_checksums(s.sums + 3 * (k / checksum_every - 1));
   }
   const int rest = nsteps - k;
   if (rest > 0) {
-    if (!sync_shadows()) return take_status();
-    // Tidal values for the remaining steps, evaluated on the host.
-    if (s.tide_cap < rest) {
-      invalidate_graph();  // it holds the old table address
-      if (s.tide_table) cudaFree(s.tide_table);
-      s.tide_table = nullptr;
-      s.tide_cap = 0;
-      if (!CK(cudaMalloc(&s.tide_table, sizeof(double) * rest))) return take_status();
-      s.tide_cap = rest;
-    }
-    std::vector<double> tides(rest);
-    for (int q = 0; q < rest; q++) tides[q] = tide_value(istep0 + k + q, s.sc.rdt);
-    if (!CK(cudaMemcpyAsync(s.tide_table, tides.data(), sizeof(double) * rest,
-                            cudaMemcpyHostToDevice, s.stream)))
-      return take_status();
-    // The graph depends on the step count, the checksum cadence and phase,
-    // and which ping-pong buffer holds the state.
-    const int key[4] = {rest, checksum_every, checksum_every > 0 ? k % checksum_every : 0,
-                        s.cur};
-    const bool hit = s.graph && memcmp(key, s.graph_key, sizeof key) == 0;
-    const int cur0 = s.cur;
-    if (!hit) {
-      invalidate_graph();
-      cudaGraph_t graph;
-      if (!CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal)))
-        return take_status();
-      for (int q = 0; q < rest; q++) {
-        fused_launch(s.tide_table, q, 0.0);
-        const int done = k + q + 1;
-        if (checksum_every > 0 && done % checksum_every == 0)
-          enqueue_checksums(s.sums + 3 * (done / checksum_every - 1));
-      }
-      const bool cap_ok = CK(cudaStreamEndCapture(s.stream, &graph));
-      if (!cap_ok) return take_status();
-      const bool inst_ok = CK(cudaGraphInstantiate(&s.graph, graph, 0));
-      cudaGraphDestroy(graph);
-      if (!inst_ok) return take_status();
-      memcpy(s.graph_key, key, sizeof key);
-    } else {
-      s.cur = (cur0 + rest) & 1;
-    }
-    if (!CK(cudaGraphLaunch(s.graph, s.stream))) return take_status();
+    if (!prepare_graph(istep0 + k, rest, checksum_every, k)) return scope.rc();
+    if (!CK(cudaGraphLaunch(s.graph, s.stream))) return scope.rc();
+    s.cur = (s.cur + rest) & 1;
     s.materialized = false;
     s.last_path = 2;
   }
   if (nsums > 0) {
     if (!CK(cudaMemcpyAsync(checksums_out, s.sums, sizeof(double) * 3 * nsums,
                             cudaMemcpyDeviceToHost, s.stream)))
-      return take_status();
-    if (!CK(cudaStreamSynchronize(s.stream))) return take_status();
+      return scope.rc();
+    CK(cudaStreamSynchronize(s.stream));
   }
-  return take_status();
+  return scope.rc();
+}
+
+int nl2d_timed_run(int istep0, int nsteps, double* ms_out) {
+  State& s = g_state;
+  CallScope scope;
+  if (ms_out) *ms_out = 0.0;
+  if (!s.registered) {
+    set_error(NL2D_ERR_STATE, "nl2d_timed_run: no problem registered");
+    return scope.rc();
+  }
+  if (nsteps < 1) return scope.rc();
+  if (!can_fuse()) {
+    if (s.mode != NL2D_MODE_AUTO || !s.fused_ok) {
+      set_error(NL2D_ERR_STATE, "nl2d_timed_run: the fused path does not apply");
+      return scope.rc();
+    }
+    // The untimed first step makes the state step-consistent.
+    if (!reference_step(istep0)) return scope.rc();
+    istep0++;
+    if (--nsteps < 1) return scope.rc();
+  }
+  // Everything before the timed launch (shadow copies, tide upload, graph
+  // capture) completes first, outside the timed region.
+  if (!prepare_graph(istep0, nsteps, 0, 0) || !CK(cudaStreamSynchronize(s.stream)))
+    return scope.rc();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (CK(cudaEventCreate(&e0)) && CK(cudaEventCreate(&e1)) &&
+      CK(cudaEventRecord(e0, s.stream)) && CK(cudaGraphLaunch(s.graph, s.stream)) &&
+      CK(cudaEventRecord(e1, s.stream)) && CK(cudaEventSynchronize(e1))) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms_out) *ms_out = ms;
+    s.cur = (s.cur + nsteps) & 1;
+    s.materialized = false;
+    s.last_path = 2;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return scope.rc();
 }
 
 int nl2d_checksums(double out[3]) {

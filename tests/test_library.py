@@ -1,0 +1,73 @@
+"""CPU tests of the C-ABI library: it loads, exports every function that
+include/nl2d_gpu.h declares, and reports errors instead of crashing when no
+GPU is usable.  No compute call runs here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import nl2d_testlib as T
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "nl2d_gpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\(", src)) -
+                  {"defined", "if"})
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300 import build
+    if not os.path.exists(P.LIB_PATH):
+        build.build()
+    return P.load_library()
+
+
+def test_header_lists_expected_entry_points():
+    names = declared_functions()
+    for must in ("c_invoke_time_step", "c_read_from_device", "c_write_to_device"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    import psyclonebench_gb300 as P
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+        assert name in P.EXPORTS, "binding missing for %s" % name
+
+
+def test_no_gpu_is_an_error_not_a_crash(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import psyclonebench_gb300 as P
+    m = T.make_model(12, 12, 1)
+    args = m.step_args(0)
+    del args[25]
+    rc = lib.nl2d_register(*args)
+    assert rc == P.NL2D_ERR_CUDA
+    buf = ctypes.create_string_buffer(256)
+    assert lib.nl2d_last_error(buf, 256) in (P.NL2D_OK, P.NL2D_ERR_CUDA)
+    out = np.zeros(3)
+    assert lib.nl2d_checksums(T.dptr(out)) == P.NL2D_ERR_STATE
+    assert lib.nl2d_last_error(buf, 256) == P.NL2D_ERR_STATE  # message kept until read
+    assert lib.nl2d_set_mode(7) == 0  # unknown mode: kept, error recorded
+    assert lib.nl2d_last_error(buf, 256) == P.NL2D_ERR_ARGS
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    import psyclonebench_gb300 as P
+    saved = P._lib
+    P._lib = None
+    try:
+        with pytest.raises(P.Nl2dError):
+            P.load_library(str(tmp_path / "nope.so"))
+    finally:
+        P._lib = saved
