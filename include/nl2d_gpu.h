@@ -36,6 +36,7 @@ extern "C" {
 #define NL2D_ERR_STATE 3       /* no problem registered yet                  */
 #define NL2D_ERR_UNKNOWN_FIELD 4 /* pointer is not a registered field        */
 #define NL2D_ERR_NONFINITE 5   /* a checksum found a NaN or an infinity      */
+#define NL2D_ERR_TOO_LARGE 6   /* beyond a fixed capacity (no-alloc entry)   */
 
 /* Step paths (nl2d_set_mode). */
 #define NL2D_MODE_AUTO 0       /* fused one-launch step whenever its preconditions hold */
@@ -144,6 +145,23 @@ int nl2d_checksums(double out[3]);
  * of a registered field (handle as for c_read_from_device). */
 int nl2d_field_checksum(const void *field, int x0, int x1, int y0, int y1,
                         double *out);
+
+/* Sum of |f| over columns [x0,x1], rows [y0,y1] (0-based, inclusive) of a
+ * device-resident FP64 field `d_field` with row length `width`, written to
+ * the device double `d_out`, queued on `stream` (a cudaStream_t; NULL for
+ * the default stream).  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc (a host model whose own memory
+ * manager owns all device buffers, or a loop that must not trigger the
+ * synchronisation an allocation can cause) and allocates nothing.  Its
+ * scratch is a fixed 128 KiB device array inside the library, held by every
+ * GPU that loads it until exit; rectangles above 8192 x 8192 cells return
+ * NL2D_ERR_TOO_LARGE.  The first call on a device looks up that array (make
+ * it before any stream capture); calls that overlap on the GPU race on the
+ * shared array.  Returns a status code; errors are not recorded for
+ * nl2d_last_error(). */
+int nl2d_field_checksum_noalloc(const double *d_field, int width, int x0,
+                                int x1, int y0, int y1, double *d_out,
+                                void *stream);
 
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);

@@ -17,6 +17,7 @@ NL2D_ERR_ARGS = 2
 NL2D_ERR_STATE = 3
 NL2D_ERR_UNKNOWN_FIELD = 4
 NL2D_ERR_NONFINITE = 5
+NL2D_ERR_TOO_LARGE = 6
 NL2D_MODE_AUTO = 0
 NL2D_MODE_REFERENCE = 1
 
@@ -45,6 +46,7 @@ EXPORTS = {
     "nl2d_timed_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP]),
     "nl2d_checksums": (ctypes.c_int, [_DP]),
     "nl2d_field_checksum": (ctypes.c_int, [_VP] + [ctypes.c_int] * 4 + [_DP]),
+    "nl2d_field_checksum_noalloc": (ctypes.c_int, [_VP] + [ctypes.c_int] * 5 + [_VP, _VP]),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }

@@ -10,6 +10,8 @@
 // relative), not bit for bit; repeated runs are bit-identical.
 #include "nl2d_internal.h"
 
+#include "../../include/nl2d_gpu.h"
+
 namespace nl2d {
 namespace {
 
@@ -68,3 +70,67 @@ void launch_checksum(const double* f, int width, int x0, int x1, int y0, int y1,
 }
 
 }  // namespace nl2d
+
+// ---- allocation-free variant ------------------------------------------
+//
+// Some callers cannot call cudaMalloc: a host model whose own memory
+// manager owns every device buffer (an OpenACC / OpenMP-target Fortran
+// driver that maps the fields itself), or a time loop that must not trigger
+// the device-wide synchronisation an allocation can cause.  For them the
+// partial sums live in this file-scope device array instead of a buffer the
+// library allocates.  Every GPU that loads the library holds it until the
+// process exits.
+namespace {
+
+constexpr int kNoAllocMaxPartials = 16384;  // 128 KiB per device
+constexpr long long kNoAllocCellsPerPartial = 256LL * 16;  // one block, 16 cells a thread
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
+
+constexpr int kMaxDevices = 64;
+double* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_partials on the current device.  In host
+// code the array's name is only a host-side stand-in, so the address comes
+// from cudaGetSymbolAddress, once per device, with that device current.
+cudaError_t noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (!g_noalloc_addr[dev]) {
+    double* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+// Sum of |d_field| over a rectangle without allocating: the library's two
+// checksum kernels, with one partial sum per block of 4096 cells kept in
+// g_noalloc_partials.  Rectangles of more than 16384 x 4096 = 67,108,864
+// cells (8192 x 8192) are rejected.  The first call on a device looks up
+// the array's device address; make that first call before any stream
+// capture.  All calls share the array: two calls that overlap on the GPU
+// (different streams, no ordering between them) race on it.
+extern "C" int nl2d_field_checksum_noalloc(const double* d_field, int width, int x0, int x1,
+                                           int y0, int y1, double* d_out, void* stream) {
+  if (!d_field || !d_out || width < 1 || x0 < 0 || y0 < 0 || x1 >= width || x1 < x0 ||
+      y1 < y0)
+    return NL2D_ERR_ARGS;
+  const long long cells = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
+  const long long blocks = (cells + kNoAllocCellsPerPartial - 1) / kNoAllocCellsPerPartial;
+  if (blocks > kNoAllocMaxPartials) return NL2D_ERR_TOO_LARGE;
+  double* scratch = nullptr;
+  if (noalloc_scratch(&scratch) != cudaSuccess) return NL2D_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Every partial the final pass reads is written by the first pass, so the
+  // array needs no clearing between calls.
+  nl2d::k_abs_sum_partial<<<(int)blocks, nl2d::kThreads, 0, st>>>(
+      d_field, width, x0, x1 - x0 + 1, y0, y1 - y0 + 1, scratch);
+  nl2d::k_abs_sum_final<<<1, nl2d::kThreads, 0, st>>>(scratch, (int)blocks, d_out);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
