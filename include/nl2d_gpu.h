@@ -163,6 +163,15 @@ int nl2d_field_checksum_noalloc(const double *d_field, int width, int x0,
                                 int x1, int y0, int y1, double *d_out,
                                 void *stream);
 
+/* Test hook: over n sampled doubles x (seeded), counts where the exact
+ * FP64 helpers of the fused step differ from the IEEE expressions they
+ * stand for — x / d (d in [2^-100, 2^100]), 0.5 * x, and the upwind pick
+ * (0.5 - copysign(0.5, w)) * x + (0.5 + copysign(0.5, w)) * p.  out[3]
+ * receives the three counts (NaN results compare equal).  Returns 0, 1 on
+ * a CUDA error, 2 for d out of range. */
+int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
+                        long long *out);
+
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
 

@@ -47,6 +47,9 @@ EXPORTS = {
     "nl2d_checksums": (ctypes.c_int, [_DP]),
     "nl2d_field_checksum": (ctypes.c_int, [_VP] + [ctypes.c_int] * 4 + [_DP]),
     "nl2d_field_checksum_noalloc": (ctypes.c_int, [_VP] + [ctypes.c_int] * 5 + [_VP, _VP]),
+    "nl2d_selftest_exact": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong,
+                                            ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_longlong)]),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }

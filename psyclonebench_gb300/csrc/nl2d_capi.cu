@@ -90,6 +90,8 @@ void free_device() {
     for (int k = 1; k < kNumGrid; k++) cudaFree(*grid_slot(s.dev, k));
     cudaFree(s.dev.sin_u);
     cudaFree(s.dev.sin_v);
+    cudaFree(s.dev.r_hu);
+    cudaFree(s.dev.r_hv);
     for (double* p : s.shadow) cudaFree(p);
   }
   s.dev = Fields{};
@@ -233,6 +235,9 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   }
   if (!CK(cudaMalloc(&s.dev.sin_u, n * 8)) || !CK(cudaMalloc(&s.dev.sin_v, n * 8)))
     return false;
+  if (!CK(cudaMalloc(&s.dev.r_hu, n * 8)) || !CK(cudaMalloc(&s.dev.r_hv, n * 8))) return false;
+  launch_depth_reciprocals(s.dev, dims(), s.stream);
+  if (!CK(cudaGetLastError())) return false;
   for (double*& p : s.shadow)
     if (!CK(cudaMalloc(&p, n * 8))) return false;
   if (!s.partials &&
@@ -543,6 +548,10 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
   // on the reference-structured path.
   s.consistent = false;
   s.shadows_synced = false;
+  if (k == 4 || k == 5 || k == 10 || k == 12) {  // hu, hv, ssha_u, ssha_v
+    launch_depth_reciprocals(s.dev, dims(), s.stream);
+    if (!CK(cudaGetLastError())) return;
+  }
   if (k >= kNumFields && !upload_sines(s.sc.d2r)) return;
   if (blocking) CK(cudaStreamSynchronize(s.stream));
 }

@@ -1,0 +1,71 @@
+// Exact FP64 building blocks for the fused NEMOLite2D step.
+//
+// On GB300 the FP64 pipe issues 2 thread-operations per clock per SM, ~60x
+// fewer than the integer and FP32 pipes, and an IEEE FP64 divide costs ~15
+// FP64 instructions.  Each helper below returns the SAME bits as the plain
+// IEEE expression it replaces, for every input, but spends fewer FP64
+// instructions:
+//
+//  * div_rn(x, d, r): x / d rounded to nearest for a divisor d > 0 whose
+//    reciprocal r = RN(1/d) was computed beforehand (Markstein, "Computation
+//    of elementary functions on the IBM RISC System/6000 processor", IBM J.
+//    Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point
+//    Arithmetic, 2nd ed., Sec. 4.7): a quotient refined once with an exact
+//    FMA remainder is faithful, and a faithful quotient corrected with the
+//    exact remainder and the correctly rounded reciprocal is the correctly
+//    rounded quotient.  1 DMUL + 4 DFMA.  The remainder is formed as
+//    q*d - x and subtracted, which also returns the correctly signed zero
+//    for x = +-0.  Dividends whose magnitude is tiny (below 2^-899, other
+//    than zero), huge (2^900 and above) or not finite use the IEEE divide,
+//    so no intermediate underflows or overflows; divisors are checked on
+//    the host to lie in [2^-100, 2^100].
+//  * half(x): 0.5 * x.  For normal x with a biased exponent >= 2 this is
+//    exact, i.e. the exponent minus one, done in integer arithmetic; zero
+//    keeps its bits; subnormal, smallest-normal and non-finite x use DMUL.
+//  * upwind(w, p, q): (0.5 - copysign(0.5, w)) * p + (0.5 + copysign(0.5, w)) * q,
+//    the first-order upwind pick of momentum_{u,v}_kern.c.  One weight is
+//    1 and the other +0, so the value is the picked operand plus a zero
+//    carrying the sign of the other operand; that is the picked operand,
+//    or a zero whose sign is the AND of both signs.  Integer select; a
+//    non-finite partner takes the IEEE expression.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace nl2d {
+
+__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
+
+__device__ __forceinline__ double div_rn(double x, double d, double r) {
+  const int hi = __double2hiint(x);
+  const int ex = (hi >> 20) & 0x7ff;
+  const bool zero = ((hi & 0x7fffffff) | __double2loint(x)) == 0;
+  if (!zero && (ex < 124 || ex > 1922)) return x / d;
+  const double q0 = x * r;
+  const double e0 = fma(q0, d, -x);
+  const double q1 = fma(-e0, r, q0);
+  const double e1 = fma(q1, d, -x);
+  return fma(-e1, r, q1);
+}
+
+__device__ __forceinline__ double half(double x) {
+  const long long b = bits(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex >= 2 && ex <= 2046) return from_bits(b - (1LL << 52));
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;
+  return 0.5 * x;
+}
+
+// a + (+0 * z): the operand with weight 1 plus the zero-weighted partner.
+__device__ __forceinline__ double pick(double a, double z) {
+  const long long ab = bits(a), zb = bits(z);
+  if (((zb >> 52) & 0x7ff) == 0x7ff) return a + 0.0 * z;
+  if ((ab & 0x7fffffffffffffffLL) != 0) return a;
+  return from_bits(ab & (zb | 0x7fffffffffffffffLL));
+}
+
+__device__ __forceinline__ double upwind(double w, double p, double q) {
+  return (bits(w) < 0) ? pick(p, q) : pick(q, p);
+}
+
+}  // namespace nl2d

@@ -26,6 +26,7 @@
 //
 // Built with -fmad=false, as the reference oracle is with
 // -ffp-contract=off: results are bit-identical to the reference serial build.
+#include "nl2d_exact.cuh"
 #include "nl2d_internal.h"
 
 namespace nl2d {
@@ -192,11 +193,49 @@ __device__ __forceinline__ double va_pre_flather(const Ctx& x, const double* va_
   return va;
 }
 
+// Step-invariant constants of the fast path, evaluated on the host with the
+// operations the reference performs per point (e.g. dx_v[c] + dx_v[e] on a
+// uniform grid is one add of two equal values), so they are bit-identical.
+struct FastConst {
+  double area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t;
+  double r_area_t, r_area_u, r_area_v, r_dx_t, r_dy_t;  // RN(1/d)
+  double dxv2, dyu2, r_dxv2, r_dyu2;                    // dx_v + dx_v, dy_u + dy_u
+  double fric, r_fric;                                  // 1.0 + cbfr * rdt
+  double cor_u, cor_v;                                  // 2. * omega * sin(gphi * d2r)
+  double neg_g, rdt, visc;
+  int fast_div;  // every constant divisor lies in [2^-100, 2^100]
+};
+
+// Division by a step constant: the Markstein form when the constants allow
+// it, otherwise the IEEE divide.  Both give the same bits.
+__device__ __forceinline__ double dvc(double x, double d, double r, int fast) {
+  return fast ? div_rn(x, d, r) : x / d;
+}
+// Division by a per-face depth with a precomputed reciprocal; r == 0 marks
+// a depth outside [2^-100, 2^100] (IEEE divide).
+__device__ __forceinline__ double dvf(double x, double d, double r) {
+  return r != 0.0 ? div_rn(x, d, r) : x / d;
+}
+
+// Shared-memory layout of one tile.  Phase 0 (halo 2) holds the loaded
+// fields and the sshn_u / sshn_v values this step sees; phase 1 (halo 1)
+// holds the terms that two neighbouring updates share.
+constexpr int S0 = SX * SY;            // 36 x 12 positions
+constexpr int P1X = TX + 2, P1Y = TY + 2;
+constexpr int S1 = P1X * P1Y;          // 34 x 10 positions
+enum { A_SN, A_UN, A_VN, A_HU, A_HV, A_SU, A_SV, A_HUS, A_HVS, N_A0 };
+enum { B_FLXU, B_FLXV, B_GX, B_GY, B_FXU, B_FYV, B_VSC, B_FYU, B_QY, B_UWC, B_FXV, B_QX, N_B1 };
+constexpr size_t kSmemBytes = sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * S0;
+
 __global__ void __launch_bounds__(TX* TY)
-    k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um,
+    k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
-  __shared__ double su_tile[SY * SX];
-  __shared__ double sv_tile[SY * SX];
+  extern __shared__ double smem[];
+  double* a0 = smem;                 // [N_A0][S0]
+  double* b1 = smem + N_A0 * S0;     // [N_B1][S1]
+  int* mk = (int*)(b1 + N_B1 * S1);  // [S0]
+#define A(q, t) a0[(q) * S0 + (t)]
+#define B(q, t) b1[(q) * S1 + (t)]
 
   const int W = d.width, H = d.height;
   // Tiles cover the copy region [xs-1, xe+1] x [ys-1, ye].
@@ -204,56 +243,175 @@ __global__ void __launch_bounds__(TX* TY)
   const int j0 = d.ys - 1 + blockIdx.y * TY;
   const int* __restrict__ m = f.tmask;
   const double* __restrict__ sn = fs.sshn_in;
+  const double* __restrict__ un = fs.un_in;
+  const double* __restrict__ vn = fs.vn_in;
+  const int tid = threadIdx.y * TX + threadIdx.x;
 
-  // Stage the sshn_u / sshn_v values this step reads (time_update_kern.c).
-  for (int t = threadIdx.y * TX + threadIdx.x; t < SX * SY; t += TX * TY) {
-    const int ti = t % SX, tj = t / SX;
-    const int i = i0 - HALO + ti, j = j0 - HALO + tj;
-    double su = 0.0, sv = 0.0;
+  // ---- phase 0: fields and the sshn_u / sshn_v this step reads ----
+  for (int t = tid; t < S0; t += TX * TY) {
+    const int i = i0 - HALO + t % SX, j = j0 - HALO + t / SX;
+    double vsn = 0.0, vun = 0.0, vvn = 0.0, vhu = 0.0, vhv = 0.0, su = 0.0, sv = 0.0;
+    int mm = 0;
     if (i >= 0 && i < W && j >= 0 && j < H) {
       const int c = j * W + i;
+      vsn = sn[c];
+      vun = un[c];
+      vvn = vn[c];
+      vhu = f.hu[c];
+      vhv = f.hv[c];
+      mm = m[c];
       su = f.sshn_u[c];
       sv = f.sshn_v[c];
+      // next_sshu_code / next_sshv_code (time_update_kern.c:90-155) over
+      // their loop ranges; other faces keep the stored value.
       if (j >= d.ys && j <= d.ye && i >= d.xs && i <= d.xe - 1) {
         const int n = c + 1;
-        if (m[c] + m[n] > 0) {
-          if (m[c] * m[n] > 0) {
-            double rtmp1 = um.area_t * sn[c] + um.area_t * sn[n];
-            su = 0.5 * rtmp1 / um.area_u;
-          } else if (m[c] <= 0) {
+        if (mm + m[n] > 0) {
+          if (mm * m[n] > 0) {
+            double rtmp1 = k.area_t * vsn + k.area_t * sn[n];
+            su = dvc(half(rtmp1), k.area_u, k.r_area_u, k.fast_div);
+          } else if (mm <= 0) {
             su = sn[n];
           } else {
-            su = sn[c];
+            su = vsn;
           }
         }
       }
       if (j >= d.ys && j <= d.ye - 1 && i >= d.xs && i <= d.xe) {
         const int n = c + W;
-        if (m[c] + m[n] > 0) {
-          if (m[c] * m[n] > 0) {
-            double rtmp1 = um.area_t * sn[c] + um.area_t * sn[n];
-            sv = 0.5 * rtmp1 / um.area_v;
-          } else if (m[c] <= 0) {
+        if (mm + m[n] > 0) {
+          if (mm * m[n] > 0) {
+            double rtmp1 = k.area_t * vsn + k.area_t * sn[n];
+            sv = dvc(half(rtmp1), k.area_v, k.r_area_v, k.fast_div);
+          } else if (mm <= 0) {
             sv = sn[n];
           } else {
-            sv = sn[c];
+            sv = vsn;
           }
         }
       }
     }
-    su_tile[t] = su;
-    sv_tile[t] = sv;
+    A(A_SN, t) = vsn;
+    A(A_UN, t) = vun;
+    A(A_VN, t) = vvn;
+    A(A_HU, t) = vhu;
+    A(A_HV, t) = vhv;
+    A(A_SU, t) = su;
+    A(A_SV, t) = sv;
+    A(A_HUS, t) = vhu + su;
+    A(A_HVS, t) = vhv + sv;
+    mk[t] = mm;
+  }
+  __syncthreads();
+
+  // ---- phase 1: terms shared by neighbouring updates ----
+  // Every term is the exact operation sequence of momentum_{u,v}_kern.c /
+  // continuity_kern.c for one of the two updates that use it; for the other
+  // update the reference evaluates the same operations on the same operands
+  // (addition commuted), so the bits agree.
+  for (int t = tid; t < S1; t += TX * TY) {
+    const int ti = t % P1X, tj = t / P1X;
+    const int i = i0 - 1 + ti, j = j0 - 1 + tj;
+    const int q = (tj + 1) * SX + (ti + 1);  // phase-0 slot of (i,j)
+    const int qw = q - 1, qs = q - SX, qse = qs + 1, qwn = qw + SX;
+    const double ht = (i >= 0 && i < W && j >= 0 && j < H) ? f.ht[j * W + i] : 0.0;
+    const double D = ht + A(A_SN, q);  // ht + sshn at T(i,j)
+    const double u_c = A(A_UN, q), u_w = A(A_UN, qw), u_s = A(A_UN, qs), u_wn = A(A_UN, qwn);
+    const double v_c = A(A_VN, q), v_w = A(A_VN, qw), v_s = A(A_VN, qs), v_se = A(A_VN, qse);
+    // continuity fluxes (sshn_u + hu) * un and (sshn_v + hv) * vn
+    B(B_FLXU, t) = A(A_HUS, q) * u_c;
+    B(B_FLXV, t) = A(A_HVS, q) * v_c;
+    // dudx at T(i,j) (dudx_w of u face i, dudx_e of face i-1); dvdy likewise
+    B(B_GX, t) = dvc(u_c - u_w, k.dx_t, k.r_dx_t, k.fast_div) * D;
+    B(B_GY, t) = dvc(v_c - v_s, k.dy_t, k.r_dy_t, k.fast_div) * D;
+    // x-advective flux of u through T(i,j): uu_w * u_w * depw of face i
+    const double U = half(u_c + u_w) * k.dy_t;
+    B(B_FXU, t) = (upwind(U, u_c, u_w) * U) * D;
+    // y-advective flux of v through T(i,j): vv_s * v_s * deps of face j
+    const double V = half(v_c + v_s) * k.dx_t;
+    B(B_FYV, t) = (upwind(V, v_c, v_s) * V) * D;
+    // south edge of u face (i,j): v_sc, v_s, deps, uu_s (unmasked form)
+    const double vsc = half(v_s + v_se);
+    B(B_VSC, t) = vsc;
+    const double Vs = half(vsc) * k.dxv2;
+    const double deps = half((A(A_HVS, qs) + A(A_HV, qse)) + A(A_SV, qse));
+    B(B_FYU, t) = (upwind(Vs, u_c, u_s) * Vs) * deps;
+    B(B_QY, t) = dvc(u_c - u_s, k.dyu2, k.r_dyu2, k.fast_div);
+    // west edge of v face (i,j): u_wc, u_w, depw, vv_w (unmasked form)
+    const double uwc = half(u_w + u_wn);
+    B(B_UWC, t) = uwc;
+    const double Uw = half(uwc) * k.dyu2;
+    const double depw = half((A(A_HUS, qw) + A(A_HU, qwn)) + A(A_SU, qwn));
+    B(B_FXV, t) = (upwind(Uw, v_c, v_w) * Uw) * depw;
+    B(B_QX, t) = dvc(v_c - v_w, k.dxv2, k.r_dxv2, k.fast_div);
   }
   __syncthreads();
 
   const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
   if (i > d.xe + 1 || j > d.ye) return;
   const int c = j * W + i;
+  const int q = (threadIdx.y + HALO) * SX + (threadIdx.x + HALO);
+  const int r = (threadIdx.y + 1) * P1X + (threadIdx.x + 1);
 
+  bool regular = i >= d.xs && i <= d.xe - 1 && j >= d.ys && j <= d.ye - 1;
+  if (regular) {
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+      for (int di = -1; di <= 1; di++) regular &= mk[q + dj * SX + di] > 0;
+  }
+
+  if (regular) {
+    // Wet cell whose 3x3 neighbourhood is wet: continuity without bc_ssh,
+    // unmasked momentum, no solid-wall or Flather change.
+    const double snc = A(A_SN, q), Hu = A(A_HUS, q), Hv = A(A_HVS, q);
+    double ssh = (((B(B_FLXU, r - 1) - B(B_FLXU, r)) + B(B_FLXV, r - P1X)) - B(B_FLXV, r)) *
+                 k.rdt;
+    fs.sshn_out[c] = snc + dvc(ssh, k.area_t, k.r_area_t, k.fast_div);
+
+    // u-momentum (momentum_u_kern.c:184-261)
+    {
+      const double adv = ((B(B_FXU, r) - B(B_FXU, r + 1)) + B(B_FYU, r)) - B(B_FYU, r + P1X);
+      const double dudy_s =
+          B(B_QY, r) * ((Hu + A(A_HU, q - SX)) + A(A_SU, q - SX));
+      const double dudy_n =
+          B(B_QY, r + P1X) * ((Hu + A(A_HU, q + SX)) + A(A_SU, q + SX));
+      double vis = (B(B_GX, r + 1) - B(B_GX, r)) * k.dy_u + half((dudy_n - dudy_s) * k.dx_u);
+      vis = k.visc * vis;
+      const double cor = (half(k.cor_u * (B(B_VSC, r) + B(B_VSC, r + P1X))) * k.area_u) * Hu;
+      const double hpg = ((k.neg_g * Hu) * k.dy_u) * (A(A_SN, q + 1) - snc);
+      const double num = A(A_UN, q) * Hu +
+                         dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_u, k.r_area_u,
+                             k.fast_div);
+      const double t1 = dvf(num, A(A_HU, q) + f.ssha_u[c], f.r_hu[c]);
+      fs.un_out[c] = dvc(t1, k.fric, k.r_fric, k.fast_div);
+    }
+    // v-momentum (momentum_v_kern.c:159-239)
+    {
+      const double adv = ((B(B_FXV, r) - B(B_FXV, r + 1)) + B(B_FYV, r)) - B(B_FYV, r + P1X);
+      const double dvdx_w = B(B_QX, r) * ((Hv + A(A_HV, q - 1)) + A(A_SV, q - 1));
+      const double dvdx_e = B(B_QX, r + 1) * ((Hv + A(A_HV, q + 1)) + A(A_SV, q + 1));
+      double vis =
+          (B(B_GY, r + P1X) - B(B_GY, r)) * k.dx_v + half((dvdx_e - dvdx_w) * k.dy_v);
+      vis = k.visc * vis;
+      const double cor = (-half(k.cor_v * (B(B_UWC, r + 1) + B(B_UWC, r))) * k.area_v) * Hv;
+      const double hpg = ((k.neg_g * Hv) * k.dx_v) * (A(A_SN, q + SX) - snc);
+      const double num = A(A_VN, q) * Hv +
+                         dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_v, k.r_area_v,
+                             k.fast_div);
+      const double t1 = dvf(num, A(A_HV, q) + f.ssha_v[c], f.r_hv[c]);
+      fs.vn_out[c] = dvc(t1, k.fric, k.r_fric, k.fast_div);
+    }
+    return;
+  }
+
+  // ---- general cell: the reference's per-point code, in its order ----
+  double* su_tile = &A(A_SU, 0);
+  double* sv_tile = &A(A_SV, 0);
   Ctx x;
   x.sn = sn;
-  x.un = fs.un_in;
-  x.vn = fs.vn_in;
+  x.un = un;
+  x.vn = vn;
   x.hu = f.hu;
   x.hv = f.hv;
   x.ht = f.ht;
@@ -268,54 +426,59 @@ __global__ void __launch_bounds__(TX* TY)
   x.d = d;
   x.p = p;
   x.um = um;
-  x.cor_u = 2. * p.omega * um.sin_u;
-  x.cor_v = 2. * p.omega * um.sin_v;
-  x.fric = 1.0 + p.cbfr * p.rdt;
+  x.cor_u = k.cor_u;
+  x.cor_v = k.cor_v;
+  x.fric = k.fric;
 
-  // ---- sea-surface height at T (continuity_kern.c:90-117, then bc_ssh) ----
+  // sea-surface height at T (continuity_kern.c:90-117, then bc_ssh)
   double ssh = sn[c];
   if (i >= d.xs && i <= d.xe && j >= d.ys && j <= d.ye) {
-    const int w = c - 1, s = c - W, t = x.slot(i, j);
-    double r1 = (su_tile[t] + f.hu[c]) * x.un[c];
-    double r2 = (su_tile[t - 1] + f.hu[w]) * x.un[w];
-    double r3 = (sv_tile[t] + f.hv[c]) * x.vn[c];
-    double r4 = (sv_tile[t - SX] + f.hv[s]) * x.vn[s];
+    const int w = c - 1, s = c - W;
+    double r1 = (su_tile[q] + f.hu[c]) * un[c];
+    double r2 = (su_tile[q - 1] + f.hu[w]) * un[w];
+    double r3 = (sv_tile[q] + f.hv[c]) * vn[c];
+    double r4 = (sv_tile[q - SX] + f.hv[s]) * vn[s];
     ssh = sn[c] + (r2 - r1 + r4 - r3) * p.rdt / um.area_t;
     if (m[c] > 0 && (m[c - W] < 0 || m[c + W] < 0 || m[c + 1] < 0 || m[c - 1] < 0))
       ssh = tide_table ? tide_table[tide_index] : tide;
   }
   fs.sshn_out[c] = ssh;
 
-  // ---- u at the east face (momentum_u, bc_solid_u, bc_flather_u) ----
-  const int t = x.slot(i, j);
-  double ua = x.un[c];
+  // u at the east face (momentum_u, bc_solid_u, bc_flather_u)
+  double ua = un[c];
   if (i <= d.xe) {  // u whole range [xs-1, xe] x [ys-1, ye+1] (tiling gives the rest)
     ua = ua_pre_flather(x, f.ua, i, j);
     if (m[c] + m[c + 1] > -1) {
       if (m[c] < 0) {
         ua = ua_pre_flather(x, f.ua, i + 1, j) +
-             sqrt(p.g / f.hu[c]) * (su_tile[t] - su_tile[t + 1]);
+             sqrt(p.g / f.hu[c]) * (su_tile[q] - su_tile[q + 1]);
       } else if (m[c + 1] < 0 && i >= 1) {  // i == 0 would read outside the array
         ua = ua_pre_flather(x, f.ua, i - 1, j) +
-             sqrt(p.g / f.hu[c]) * (su_tile[t] - su_tile[t - 1]);
+             sqrt(p.g / f.hu[c]) * (su_tile[q] - su_tile[q - 1]);
       }
     }
   }
   fs.un_out[c] = ua;
 
-  // ---- v at the north face (momentum_v, bc_solid_v, bc_flather_v) ----
-  // The copy region is exactly the v whole range [xs-1, xe+1] x [ys-1, ye].
+  // v at the north face (momentum_v, bc_solid_v, bc_flather_v); the copy
+  // region is exactly the v whole range [xs-1, xe+1] x [ys-1, ye].
   double va = va_pre_flather(x, f.va, i, j);
   if (m[c] + m[c + W] > -1) {
     if (m[c] < 0) {
       va = va_pre_flather(x, f.va, i, j + 1) +
-           sqrt(p.g / f.hv[c]) * (sv_tile[t] - sv_tile[t + SX]);
+           sqrt(p.g / f.hv[c]) * (sv_tile[q] - sv_tile[q + SX]);
     } else if (m[c + W] < 0 && j >= 1) {
       va = va_pre_flather(x, f.va, i, j - 1) +
-           sqrt(p.g / f.hv[c]) * (sv_tile[t] - sv_tile[t - SX]);
+           sqrt(p.g / f.hv[c]) * (sv_tile[q] - sv_tile[q - SX]);
     }
   }
   fs.vn_out[c] = va;
+#undef A
+#undef B
+}
+
+bool in_fast_range(double d) {
+  return d > 0.0 && d >= 0x1p-100 && d <= 0x1p100;
 }
 
 }  // namespace
@@ -323,9 +486,122 @@ __global__ void __launch_bounds__(TX* TY)
 void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,
                        const double* tide_table, int tide_index, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_fused_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemBytes);
+    attr_set = true;
+  }
+  FastConst k;
+  k.area_t = um.area_t, k.area_u = um.area_u, k.area_v = um.area_v;
+  k.dx_u = um.dx_u, k.dx_v = um.dx_v, k.dx_t = um.dx_t;
+  k.dy_u = um.dy_u, k.dy_v = um.dy_v, k.dy_t = um.dy_t;
+  k.dxv2 = um.dx_v + um.dx_v;
+  k.dyu2 = um.dy_u + um.dy_u;
+  k.fric = 1.0 + s.cbfr * s.rdt;
+  k.cor_u = 2. * s.omega * um.sin_u;
+  k.cor_v = 2. * s.omega * um.sin_v;
+  k.neg_g = -s.g;
+  k.rdt = s.rdt;
+  k.visc = s.visc;
+  const double divisors[8] = {k.area_t, k.area_u, k.area_v, k.dx_t, k.dy_t,
+                              k.dxv2,   k.dyu2,   k.fric};
+  bool fast = true;
+  for (double v : divisors) fast = fast && in_fast_range(v);
+  k.fast_div = fast ? 1 : 0;
+  k.r_area_t = 1.0 / k.area_t, k.r_area_u = 1.0 / k.area_u, k.r_area_v = 1.0 / k.area_v;
+  k.r_dx_t = 1.0 / k.dx_t, k.r_dy_t = 1.0 / k.dy_t;
+  k.r_dxv2 = 1.0 / k.dxv2, k.r_dyu2 = 1.0 / k.dyu2;
+  k.r_fric = 1.0 / k.fric;
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   const dim3 grid((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_fused_step<<<grid, dim3(TX, TY), 0, st>>>(f, fs, d, s, um, tide_table, tide_index, tide);
+  k_fused_step<<<grid, dim3(TX, TY), kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
+                                                       tide_index, tide);
+}
+
+// Reciprocals RN(1 / (h + ssha)) of the momentum denominators, or 0 where
+// the depth lies outside [2^-100, 2^100] (the kernel then divides).
+__global__ void k_depth_reciprocal(const double* __restrict__ h,
+                                   const double* __restrict__ ssha, double* __restrict__ r,
+                                   long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double dd = h[t] + ssha[t];
+    r[t] = (dd >= 0x1p-100 && dd <= 0x1p100) ? 1.0 / dd : 0.0;
+  }
+}
+
+void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st) {
+  const long long n = (long long)d.width * d.height;
+  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hu, f.ssha_u, f.r_hu, n);
+  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hv, f.ssha_v, f.r_hv, n);
 }
 
 }  // namespace nl2d
+
+// ---- self-test of the exact helpers against the plain IEEE operations ----
+namespace nl2d {
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+// A double from 64 random bits: mostly finite values with exponents across
+// the whole normal range, plus zeros, subnormals and non-finite values.
+__device__ __forceinline__ double sample(unsigned long long z) {
+  const unsigned sel = (unsigned)(z >> 59);  // 0..31
+  long long b = (long long)(z & 0x800fffffffffffffULL);
+  if (sel == 0) return from_bits(b & 0x8000000000000000LL);        // +-0
+  if (sel == 1) return from_bits(b);                                // subnormal
+  if (sel == 2) return from_bits(b | 0x7ff0000000000000LL);         // inf / nan
+  const long long ex = 1 + (long long)((z >> 40) % 2046ULL);
+  return from_bits(b | (ex << 52));
+}
+
+__global__ void k_selftest_exact(long long n, unsigned long long seed, double d, double r,
+                                 unsigned long long* bad) {
+  unsigned long long nd = 0, nh = 0, nu = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long z = mix64(seed ^ (unsigned long long)t);
+    const double x = sample(z);
+    // division: finite quotients must agree bit for bit
+    const double q_ref = x / d, q = div_rn(x, d, r);
+    if (bits(q_ref) != bits(q) && !(q_ref != q_ref && q != q)) nd++;
+    const double h_ref = 0.5 * x, h = half(x);
+    if (bits(h_ref) != bits(h) && !(h_ref != h_ref && h != h)) nh++;
+    const double p = sample(mix64(z + 1)), w = sample(mix64(z + 2));
+    const double u_ref = (0.5 - copysign(0.5, w)) * x + (0.5 + copysign(0.5, w)) * p;
+    const double u = upwind(w, x, p);
+    if (bits(u_ref) != bits(u) && !(u_ref != u_ref && u != u)) nu++;
+  }
+  if (nd) atomicAdd(&bad[0], nd);
+  if (nh) atomicAdd(&bad[1], nh);
+  if (nu) atomicAdd(&bad[2], nu);
+}
+
+}  // namespace
+}  // namespace nl2d
+
+// Test hook (no reference counterpart): counts, over n sampled doubles x,
+// the inputs where the exact helpers of the fused step differ from the IEEE
+// expressions they replace: x / d, 0.5 * x and the upwind pick.  d must be
+// in [2^-100, 2^100].  out[3] receives the three mismatch counts.
+extern "C" int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
+                                   long long* out) {
+  unsigned long long* bad = nullptr;
+  if (!(d >= 0x1p-100 && d <= 0x1p100)) return 2;
+  if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
+  nl2d::k_selftest_exact<<<152 * 16, 256>>>(n, seed, d, 1.0 / d, bad);
+  unsigned long long h[3] = {0, 0, 0};
+  const cudaError_t e = cudaMemcpy(h, bad, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return 1;
+  for (int k = 0; k < 3; k++) out[k] = (long long)h[k];
+  return 0;
+}

@@ -21,6 +21,9 @@ struct Fields {
   double *area_t, *area_u, *area_v, *dx_u, *dx_v, *dx_t, *dy_u, *dy_v, *dy_t,
       *gphiu, *gphiv;
   double *sin_u, *sin_v;
+  // RN(1 / (hu + ssha_u)) and RN(1 / (hv + ssha_v)) (0 where out of the
+  // range the exact reciprocal division needs), for the fused step.
+  double *r_hu, *r_hv;
 };
 
 struct Dims {
@@ -70,6 +73,9 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,
                        const double* tide_table, int tide_index,
                        cudaStream_t st);
+
+// Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.
+void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
 
 // ---- checksums (nl2d_checksum.cu) ----
 // Sum of |f| over [x0,x1] x [y0,y1]; per-block partial sums go to
