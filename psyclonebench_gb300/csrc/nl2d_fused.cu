@@ -32,21 +32,46 @@
 namespace nl2d {
 namespace {
 
-constexpr int TX = 32, TY = 8, HALO = 2;
+// A tile is TX x TY cells; its 256 threads (32 x 8) each update TY / 8 cells
+// of one column in the last phase.
+constexpr int TX = 32, TY = 16, HALO = 2, NTHREADS = 256, ROWS_PER_PASS = NTHREADS / TX;
 constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO;
+
+// Step-invariant constants of the fast path, evaluated on the host with the
+// operations the reference performs per point (e.g. dx_v[c] + dx_v[e] on a
+// uniform grid is one add of two equal values), so they are bit-identical.
+struct FastConst {
+  double area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t;
+  double r_area_t, r_area_u, r_area_v, r_dx_t, r_dy_t;  // RN(1/d)
+  double dxv2, dyu2, r_dxv2, r_dyu2;                    // dx_v + dx_v, dy_u + dy_u
+  double fric, r_fric;                                  // 1.0 + cbfr * rdt
+  double cor_u, cor_v;                                  // 2. * omega * sin(gphi * d2r)
+  double neg_g, rdt, visc, g;
+  int fast_div;  // every constant divisor lies in [2^-100, 2^100]
+};
+
+// Division by a step constant: the Markstein form when the constants allow
+// it, otherwise the IEEE divide.  Both give the same bits.
+__device__ __forceinline__ double dvc(double x, double d, double r, int fast) {
+  return fast ? div_rn(x, d, r) : x / d;
+}
+// Division by a per-face depth with a precomputed reciprocal; r == 0 marks
+// a depth outside [2^-100, 2^100] (IEEE divide).
+__device__ __forceinline__ double dvf(double x, double d, double r) {
+  return bits(r) != 0 ? div_rn(x, d, r) : x / d;
+}
 
 struct Ctx {
   const double *__restrict__ sn, *__restrict__ un, *__restrict__ vn;
   const double *__restrict__ hu, *__restrict__ hv, *__restrict__ ht;
   const double *__restrict__ ssha_u, *__restrict__ ssha_v;
+  const double *__restrict__ r_hu, *__restrict__ r_hv;
   const int* __restrict__ m;
   const double* su_tile;  // shared: sshn_u seen by this step
   const double* sv_tile;  // shared: sshn_v seen by this step
   int W, i0, j0;          // tile origin (cell coordinates of su_tile[0] + HALO)
   Dims d;
-  Scalars p;
-  UniformMetrics um;
-  double cor_u, cor_v, fric;
+  FastConst k;
 
   // Shared-memory slot of cell (i,j); the caller keeps (i,j) within the
   // tile plus its halo.
@@ -58,11 +83,24 @@ struct Ctx {
   }
 };
 
-__device__ __forceinline__ double wlo(double x) { return 0.5 - copysign(0.5, x); }
-__device__ __forceinline__ double whi(double x) { return 0.5 + copysign(0.5, x); }
+// (0.5 - copysign(0.5, w)) * p and (0.5 + copysign(0.5, w)) * p alone (the
+// masked upwind forms): p, or +0 * p.
+__device__ __forceinline__ double zero_times(double p) {
+  const long long b = bits(p);
+  if (((b >> 52) & 0x7ff) == 0x7ff) return 0.0 * p;
+  return from_bits(b & (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ double lo_only(double w, double p) {
+  return bits(w) < 0 ? p : zero_times(p);
+}
+__device__ __forceinline__ double hi_only(double w, double p) {
+  return bits(w) < 0 ? zero_times(p) : p;
+}
 
 // momentum_u_code (momentum_u_kern.c:150-262) at u face (i,j) in its loop
-// range; returns false where the kernel returns early (ua keeps its value).
+// range, with the masked (slip-wall) branches; returns false where the
+// kernel returns early (ua keeps its value).  Same operations as the
+// reference, with the exact helpers for halving, upwind picks and division.
 __device__ __forceinline__ bool mom_u(const Ctx& x, int i, int j, double& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             se = s + 1, ne = n + 1;
@@ -70,45 +108,48 @@ __device__ __forceinline__ bool mom_u(const Ctx& x, int i, int j, double& out) {
   if (m[c] + m[e] <= 0) return false;
   if (m[c] <= 0 || m[e] <= 0) return false;
   const double *un = x.un, *vn = x.vn, *hu = x.hu, *hv = x.hv, *ht = x.ht, *sn = x.sn;
+  const FastConst& k = x.k;
   const int t = x.slot(i, j);
   const double su_c = x.su_tile[t], su_s = x.su_tile[t - SX], su_n = x.su_tile[t + SX];
   const double sv_s = x.sv_tile[t - SX], sv_se = x.sv_tile[t - SX + 1], sv_c = x.sv_tile[t],
                sv_e = x.sv_tile[t + 1];
 
-  double u_e = 0.5 * (un[c] + un[e]) * x.um.dy_t;
+  double u_e = half(un[c] + un[e]) * k.dy_t;
   double depe = ht[e] + sn[e];
-  double u_w = 0.5 * (un[c] + un[wst]) * x.um.dy_t;
+  double u_w = half(un[c] + un[wst]) * k.dy_t;
   double depw = ht[c] + sn[c];
-  double v_sc = 0.5 * (vn[s] + vn[se]);
-  double v_s = 0.5 * v_sc * (x.um.dx_v + x.um.dx_v);
-  double deps = 0.5 * (hv[s] + sv_s + hv[se] + sv_se);
-  double v_nc = 0.5 * (vn[c] + vn[e]);
-  double v_n = 0.5 * v_nc * (x.um.dx_v + x.um.dx_v);
-  double depn = 0.5 * (hv[c] + sv_c + hv[e] + sv_e);
+  double v_sc = half(vn[s] + vn[se]);
+  double v_s = half(v_sc) * k.dxv2;
+  double deps = half(hv[s] + sv_s + hv[se] + sv_se);
+  double v_nc = half(vn[c] + vn[e]);
+  double v_n = half(v_nc) * k.dxv2;
+  double depn = half(hv[c] + sv_c + hv[e] + sv_e);
 
-  double uu_w = wlo(u_w) * un[c] + whi(u_w) * un[wst];
-  double uu_e = whi(u_e) * un[c] + wlo(u_e) * un[e];
+  double uu_w = upwind(u_w, un[c], un[wst]);
+  double uu_e = upwind(u_e, un[e], un[c]);
   const bool south_dry = m[s] <= 0 || m[se] <= 0;
   const bool north_dry = m[n] <= 0 || m[ne] <= 0;
-  double uu_s = south_dry ? wlo(v_s) * un[c] : wlo(v_s) * un[c] + whi(v_s) * un[s];
-  double uu_n = north_dry ? whi(v_n) * un[c] : whi(v_n) * un[c] + wlo(v_n) * un[n];
+  double uu_s = south_dry ? lo_only(v_s, un[c]) : upwind(v_s, un[c], un[s]);
+  double uu_n = north_dry ? hi_only(v_n, un[c]) : upwind(v_n, un[n], un[c]);
   double adv = uu_w * u_w * depw - uu_e * u_e * depe + uu_s * v_s * deps -
                uu_n * v_n * depn;
 
-  double dudx_e = (un[e] - un[c]) / x.um.dx_t * (ht[e] + sn[e]);
-  double dudx_w = (un[c] - un[wst]) / x.um.dx_t * (ht[c] + sn[c]);
+  double dudx_e = dvc(un[e] - un[c], k.dx_t, k.r_dx_t, k.fast_div) * (ht[e] + sn[e]);
+  double dudx_w = dvc(un[c] - un[wst], k.dx_t, k.r_dx_t, k.fast_div) * (ht[c] + sn[c]);
   double dudy_s = south_dry ? 0.0
-                            : (un[c] - un[s]) / (x.um.dy_u + x.um.dy_u) *
+                            : dvc(un[c] - un[s], k.dyu2, k.r_dyu2, k.fast_div) *
                                   (hu[c] + su_c + hu[s] + su_s);
   double dudy_n = north_dry ? 0.0
-                            : (un[n] - un[c]) / (x.um.dy_u + x.um.dy_u) *
+                            : dvc(un[n] - un[c], k.dyu2, k.r_dyu2, k.fast_div) *
                                   (hu[c] + su_c + hu[n] + su_n);
-  double vis = (dudx_e - dudx_w) * x.um.dy_u + (dudy_n - dudy_s) * x.um.dx_u * 0.5;
-  vis = x.p.visc * vis;
-  double cor = 0.5 * (x.cor_u * (v_sc + v_nc)) * x.um.area_u * (hu[c] + su_c);
-  double hpg = -x.p.g * (hu[c] + su_c) * x.um.dy_u * (sn[e] - sn[c]);
-  out = (un[c] * (hu[c] + su_c) + x.p.rdt * (adv + vis + cor + hpg) / x.um.area_u) /
-        (hu[c] + x.ssha_u[c]) / x.fric;
+  double vis = (dudx_e - dudx_w) * k.dy_u + half((dudy_n - dudy_s) * k.dx_u);
+  vis = k.visc * vis;
+  double cor = half(k.cor_u * (v_sc + v_nc)) * k.area_u * (hu[c] + su_c);
+  double hpg = k.neg_g * (hu[c] + su_c) * k.dy_u * (sn[e] - sn[c]);
+  const double num =
+      un[c] * (hu[c] + su_c) + dvc(k.rdt * (adv + vis + cor + hpg), k.area_u, k.r_area_u,
+                                   k.fast_div);
+  out = dvc(dvf(num, hu[c] + x.ssha_u[c], x.r_hu[c]), k.fric, k.r_fric, k.fast_div);
   return true;
 }
 
@@ -120,45 +161,48 @@ __device__ __forceinline__ bool mom_v(const Ctx& x, int i, int j, double& out) {
   if (m[c] + m[e] <= 0) return false;
   if (m[c] <= 0 || m[n] <= 0) return false;
   const double *un = x.un, *vn = x.vn, *hu = x.hu, *hv = x.hv, *ht = x.ht, *sn = x.sn;
+  const FastConst& k = x.k;
   const int t = x.slot(i, j);
   const double su_w = x.su_tile[t - 1], su_nw = x.su_tile[t + SX - 1], su_c = x.su_tile[t],
                su_n = x.su_tile[t + SX];
   const double sv_c = x.sv_tile[t], sv_w = x.sv_tile[t - 1], sv_e = x.sv_tile[t + 1];
 
-  double v_n = 0.5 * (vn[c] + vn[n]) * x.um.dx_t;
+  double v_n = half(vn[c] + vn[n]) * k.dx_t;
   double depn = ht[n] + sn[n];
-  double v_s = 0.5 * (vn[c] + vn[s]) * x.um.dx_t;
+  double v_s = half(vn[c] + vn[s]) * k.dx_t;
   double deps = ht[c] + sn[c];
-  double u_wc = 0.5 * (un[wst] + un[nw]);
-  double u_w = 0.5 * u_wc * (x.um.dy_u + x.um.dy_u);
-  double depw = 0.50 * (hu[wst] + su_w + hu[nw] + su_nw);
-  double u_ec = 0.5 * (un[c] + un[n]);
-  double u_e = 0.5 * u_ec * (x.um.dy_u + x.um.dy_u);
-  double depe = 0.50 * (hu[c] + su_c + hu[n] + su_n);
+  double u_wc = half(un[wst] + un[nw]);
+  double u_w = half(u_wc) * k.dyu2;
+  double depw = half(hu[wst] + su_w + hu[nw] + su_nw);
+  double u_ec = half(un[c] + un[n]);
+  double u_e = half(u_ec) * k.dyu2;
+  double depe = half(hu[c] + su_c + hu[n] + su_n);
 
-  double vv_s = wlo(v_s) * vn[c] + whi(v_s) * vn[s];
-  double vv_n = whi(v_n) * vn[c] + wlo(v_n) * vn[n];
+  double vv_s = upwind(v_s, vn[c], vn[s]);
+  double vv_n = upwind(v_n, vn[n], vn[c]);
   const bool west_dry = m[wst] <= 0 || m[nw] <= 0;
   const bool east_dry = m[e] <= 0 || m[ne] <= 0;
-  double vv_w = west_dry ? wlo(u_w) * vn[c] : wlo(u_w) * vn[c] + whi(u_w) * vn[wst];
-  double vv_e = east_dry ? whi(u_e) * vn[c] : whi(u_e) * vn[c] + wlo(u_e) * vn[e];
+  double vv_w = west_dry ? lo_only(u_w, vn[c]) : upwind(u_w, vn[c], vn[wst]);
+  double vv_e = east_dry ? hi_only(u_e, vn[c]) : upwind(u_e, vn[e], vn[c]);
   double adv = vv_w * u_w * depw - vv_e * u_e * depe + vv_s * v_s * deps -
                vv_n * v_n * depn;
 
-  double dvdy_n = (vn[n] - vn[c]) / x.um.dy_t * (ht[n] + sn[n]);
-  double dvdy_s = (vn[c] - vn[s]) / x.um.dy_t * (ht[c] + sn[c]);
+  double dvdy_n = dvc(vn[n] - vn[c], k.dy_t, k.r_dy_t, k.fast_div) * (ht[n] + sn[n]);
+  double dvdy_s = dvc(vn[c] - vn[s], k.dy_t, k.r_dy_t, k.fast_div) * (ht[c] + sn[c]);
   double dvdx_w = west_dry ? 0.0
-                           : (vn[c] - vn[wst]) / (x.um.dx_v + x.um.dx_v) *
+                           : dvc(vn[c] - vn[wst], k.dxv2, k.r_dxv2, k.fast_div) *
                                  (hv[c] + sv_c + hv[wst] + sv_w);
   double dvdx_e = east_dry ? 0.0
-                           : (vn[e] - vn[c]) / (x.um.dx_v + x.um.dx_v) *
+                           : dvc(vn[e] - vn[c], k.dxv2, k.r_dxv2, k.fast_div) *
                                  (hv[c] + sv_c + hv[e] + sv_e);
-  double vis = (dvdy_n - dvdy_s) * x.um.dx_v + (dvdx_e - dvdx_w) * x.um.dy_v * 0.5;
-  vis = x.p.visc * vis;
-  double cor = -0.5 * (x.cor_v * (u_ec + u_wc)) * x.um.area_v * (hv[c] + sv_c);
-  double hpg = -x.p.g * (hv[c] + sv_c) * x.um.dx_v * (sn[n] - sn[c]);
-  out = (vn[c] * (hv[c] + sv_c) + x.p.rdt * (adv + vis + cor + hpg) / x.um.area_v) /
-        ((hv[c] + x.ssha_v[c])) / x.fric;
+  double vis = (dvdy_n - dvdy_s) * k.dx_v + half((dvdx_e - dvdx_w) * k.dy_v);
+  vis = k.visc * vis;
+  double cor = -half(k.cor_v * (u_ec + u_wc)) * k.area_v * (hv[c] + sv_c);
+  double hpg = k.neg_g * (hv[c] + sv_c) * k.dx_v * (sn[n] - sn[c]);
+  const double num =
+      vn[c] * (hv[c] + sv_c) + dvc(k.rdt * (adv + vis + cor + hpg), k.area_v, k.r_area_v,
+                                   k.fast_div);
+  out = dvc(dvf(num, hv[c] + x.ssha_v[c], x.r_hv[c]), k.fric, k.r_fric, k.fast_div);
   return true;
 }
 
@@ -193,30 +237,6 @@ __device__ __forceinline__ double va_pre_flather(const Ctx& x, const double* va_
   return va;
 }
 
-// Step-invariant constants of the fast path, evaluated on the host with the
-// operations the reference performs per point (e.g. dx_v[c] + dx_v[e] on a
-// uniform grid is one add of two equal values), so they are bit-identical.
-struct FastConst {
-  double area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t;
-  double r_area_t, r_area_u, r_area_v, r_dx_t, r_dy_t;  // RN(1/d)
-  double dxv2, dyu2, r_dxv2, r_dyu2;                    // dx_v + dx_v, dy_u + dy_u
-  double fric, r_fric;                                  // 1.0 + cbfr * rdt
-  double cor_u, cor_v;                                  // 2. * omega * sin(gphi * d2r)
-  double neg_g, rdt, visc;
-  int fast_div;  // every constant divisor lies in [2^-100, 2^100]
-};
-
-// Division by a step constant: the Markstein form when the constants allow
-// it, otherwise the IEEE divide.  Both give the same bits.
-__device__ __forceinline__ double dvc(double x, double d, double r, int fast) {
-  return fast ? div_rn(x, d, r) : x / d;
-}
-// Division by a per-face depth with a precomputed reciprocal; r == 0 marks
-// a depth outside [2^-100, 2^100] (IEEE divide).
-__device__ __forceinline__ double dvf(double x, double d, double r) {
-  return r != 0.0 ? div_rn(x, d, r) : x / d;
-}
-
 // Shared-memory layout of one tile.  Phase 0 (halo 2) holds the loaded
 // fields and the sshn_u / sshn_v values this step sees; phase 1 (halo 1)
 // holds the terms that two neighbouring updates share.
@@ -227,7 +247,7 @@ enum { A_SN, A_UN, A_VN, A_HU, A_HV, A_SU, A_SV, A_HUS, A_HVS, N_A0 };
 enum { B_FLXU, B_FLXV, B_GX, B_GY, B_FXU, B_FYV, B_VSC, B_FYU, B_QY, B_UWC, B_FXV, B_QX, N_B1 };
 constexpr size_t kSmemBytes = sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * S0;
 
-__global__ void __launch_bounds__(TX* TY)
+__global__ void __launch_bounds__(NTHREADS)
     k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
   extern __shared__ double smem[];
@@ -248,7 +268,7 @@ __global__ void __launch_bounds__(TX* TY)
   const int tid = threadIdx.y * TX + threadIdx.x;
 
   // ---- phase 0: fields and the sshn_u / sshn_v this step reads ----
-  for (int t = tid; t < S0; t += TX * TY) {
+  for (int t = tid; t < S0; t += NTHREADS) {
     const int i = i0 - HALO + t % SX, j = j0 - HALO + t / SX;
     double vsn = 0.0, vun = 0.0, vvn = 0.0, vhu = 0.0, vhv = 0.0, su = 0.0, sv = 0.0;
     int mm = 0;
@@ -309,7 +329,7 @@ __global__ void __launch_bounds__(TX* TY)
   // continuity_kern.c for one of the two updates that use it; for the other
   // update the reference evaluates the same operations on the same operands
   // (addition commuted), so the bits agree.
-  for (int t = tid; t < S1; t += TX * TY) {
+  for (int t = tid; t < S1; t += NTHREADS) {
     const int ti = t % P1X, tj = t / P1X;
     const int i = i0 - 1 + ti, j = j0 - 1 + tj;
     const int q = (tj + 1) * SX + (ti + 1);  // phase-0 slot of (i,j)
@@ -347,11 +367,12 @@ __global__ void __launch_bounds__(TX* TY)
   }
   __syncthreads();
 
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  if (i > d.xe + 1 || j > d.ye) return;
+  for (int row = threadIdx.y; row < TY; row += ROWS_PER_PASS) {
+  const int i = i0 + threadIdx.x, j = j0 + row;
+  if (i > d.xe + 1 || j > d.ye) continue;
   const int c = j * W + i;
-  const int q = (threadIdx.y + HALO) * SX + (threadIdx.x + HALO);
-  const int r = (threadIdx.y + 1) * P1X + (threadIdx.x + 1);
+  const int q = (row + HALO) * SX + (threadIdx.x + HALO);
+  const int r = (row + 1) * P1X + (threadIdx.x + 1);
 
   bool regular = i >= d.xs && i <= d.xe - 1 && j >= d.ys && j <= d.ye - 1;
   if (regular) {
@@ -402,7 +423,7 @@ __global__ void __launch_bounds__(TX* TY)
       const double t1 = dvf(num, A(A_HV, q) + f.ssha_v[c], f.r_hv[c]);
       fs.vn_out[c] = dvc(t1, k.fric, k.r_fric, k.fast_div);
     }
-    return;
+    continue;
   }
 
   // ---- general cell: the reference's per-point code, in its order ----
@@ -417,6 +438,8 @@ __global__ void __launch_bounds__(TX* TY)
   x.ht = f.ht;
   x.ssha_u = f.ssha_u;
   x.ssha_v = f.ssha_v;
+  x.r_hu = f.r_hu;
+  x.r_hv = f.r_hv;
   x.m = m;
   x.su_tile = su_tile;
   x.sv_tile = sv_tile;
@@ -424,11 +447,7 @@ __global__ void __launch_bounds__(TX* TY)
   x.i0 = i0;
   x.j0 = j0;
   x.d = d;
-  x.p = p;
-  x.um = um;
-  x.cor_u = k.cor_u;
-  x.cor_v = k.cor_v;
-  x.fric = k.fric;
+  x.k = k;
 
   // sea-surface height at T (continuity_kern.c:90-117, then bc_ssh)
   double ssh = sn[c];
@@ -438,7 +457,7 @@ __global__ void __launch_bounds__(TX* TY)
     double r2 = (su_tile[q - 1] + f.hu[w]) * un[w];
     double r3 = (sv_tile[q] + f.hv[c]) * vn[c];
     double r4 = (sv_tile[q - SX] + f.hv[s]) * vn[s];
-    ssh = sn[c] + (r2 - r1 + r4 - r3) * p.rdt / um.area_t;
+    ssh = sn[c] + dvc((r2 - r1 + r4 - r3) * k.rdt, k.area_t, k.r_area_t, k.fast_div);
     if (m[c] > 0 && (m[c - W] < 0 || m[c + W] < 0 || m[c + 1] < 0 || m[c - 1] < 0))
       ssh = tide_table ? tide_table[tide_index] : tide;
   }
@@ -473,6 +492,7 @@ __global__ void __launch_bounds__(TX* TY)
     }
   }
   fs.vn_out[c] = va;
+  }  // rows of this thread
 #undef A
 #undef B
 }
@@ -502,6 +522,7 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
   k.cor_u = 2. * s.omega * um.sin_u;
   k.cor_v = 2. * s.omega * um.sin_v;
   k.neg_g = -s.g;
+  k.g = s.g;
   k.rdt = s.rdt;
   k.visc = s.visc;
   const double divisors[8] = {k.area_t, k.area_u, k.area_v, k.dx_t, k.dy_t,
@@ -515,7 +536,7 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
   k.r_fric = 1.0 / k.fric;
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   const dim3 grid((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_fused_step<<<grid, dim3(TX, TY), kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
+  k_fused_step<<<grid, dim3(TX, ROWS_PER_PASS), kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
                                                        tide_index, tide);
 }
 
