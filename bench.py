@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--size", type=int, default=NPTS, help="interior cells per side")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the mixed-precision (config 2) measurement")
     return ap.parse_args()
 
 
@@ -183,6 +185,62 @@ def time_cpu(m, nsteps, target_s=None):
     return done, time.perf_counter() - t0, kind, desc
 
 
+BATHY_RDT = 5.0  # s, for the 50-500 m bathymetry configurations
+MIXED_BYTES_PER_CELL = 48  # read ssh pair 8 + un 4 + vn 4 + ht/hu/hv 12 + mask 4; write 16
+
+
+def measure_form(lib, n, precision, steps, warmup, seed=2):
+    """Config 2: the 4096^2 domain on a seeded Fourier bathymetry, advanced
+    warmup + steps steps in one precision; returns (ms per timed step,
+    final fields)."""
+    import nl2d_testlib as T
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300.workloads import fourier_depth
+    m = make_problem(n)
+    ht, hu, hv = fourier_depth(m.width, m.height, seed)
+    m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = ht, hu, hv
+    # 500 m deep water carries gravity waves at sqrt(g h) = 70 m/s: the
+    # explicit step needs rdt well below dx / 70 m/s = 14 s.
+    m.rdt = BATHY_RDT
+    T.gpu_register(lib, m)
+    lib.nl2d_set_precision(precision)
+    ms = ctypes.c_double(0.0)
+    P.check(lib.nl2d_timed_run(1, warmup, ctypes.byref(ms)), "form warm-up")
+    P.check(lib.nl2d_timed_run(1 + warmup, steps, ctypes.byref(ms)), "form run")
+    out = {}
+    for k in ("sshn_t", "un", "vn"):
+        a = m.f[k]
+        lib.c_read_from_device(a.ctypes.data, a.ctypes.data, 1, 1, m.width, m.height, True)
+        x0, x1, y0, y1 = T.regions(m)["t" if k == "sshn_t" else ("u" if k == "un" else "v")]
+        out[k] = a[y0:y1 + 1, x0:x1 + 1].copy()
+    P.check(None, "form read")
+    lib.nl2d_set_precision(0)
+    lib.nl2d_finalize()
+    return ms.value / steps, out
+
+
+def run_forms(lib, n, steps=1000, warmup=3):
+    fp64_ms, ref = measure_form(lib, n, 0, steps, warmup)
+    mix_ms, mix = measure_form(lib, n, 1, steps, warmup)
+    cells = n * n
+    hbm, _ = peaks()
+    err = {}
+    for k, name in (("sshn_t", "ssh"), ("un", "u"), ("vn", "v")):
+        d = mix[k] - ref[k]
+        err[name] = {"rms": float(np.sqrt(np.mean(d * d))), "max": float(np.abs(d).max()),
+                     "field_max": float(np.abs(ref[k]).max())}
+    ach = MIXED_BYTES_PER_CELL * cells / (mix_ms * 1e-3) / 1e9
+    return {"mixed": {
+        "workload": "nemolite2d_mixed_%dx%d_fourier_bathymetry_seed2_rdt5_%d_steps" % (
+            n, n, steps + warmup),
+        "value": cells / (mix_ms * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+        "fp64_value_same_inputs": cells / (fp64_ms * 1e-3) / 1e6,
+        "speedup_vs_fp64": fp64_ms / mix_ms,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "alg_bytes_per_cell": MIXED_BYTES_PER_CELL},
+        "error_vs_fp64": err, "dtype": "f32 + compensated-f32 ssh"}}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -282,6 +340,10 @@ def run_ours(args, rank, world, local):
             "peak_gops": prof.get("fp64_peak_gops"),
         }
 
+    forms = None
+    if rank == 0 and not args.no_forms:
+        forms = run_forms(lib, n)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
@@ -307,6 +369,7 @@ def run_ours(args, rank, world, local):
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
             "checksums": {"ssh": sums[0], "u": sums[1], "v": sums[2]},
+            "forms": forms,
         }
         print(json.dumps(line))
     if world > 1:

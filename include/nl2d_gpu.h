@@ -101,8 +101,18 @@ void nl2d_finalize(void);
 /* Selects the step path; returns the previous mode. */
 int nl2d_set_mode(int mode);
 
-/* Which path the last step took: 0 none, 1 reference-structured, 2 fused. */
+/* Which path the last step took: 0 none, 1 reference-structured, 2 fused
+ * FP64, 3 mixed precision. */
 int nl2d_last_path(void);
+
+/* Precision of later steps (the survey's nl2d_set_precision): 0 = FP64,
+ * the reference's arithmetic (default); 1 = mixed: velocities, fluxes and
+ * momentum in FP32 and the sea-surface height as a compensated FP32 pair.
+ * The mixed form applies to problems the fused path accepts; it is not
+ * bit-identical to the reference.  Reading a field (c_read_from_device)
+ * returns the FP64 image of the mixed state; switching back to 0 continues
+ * from that image.  Returns the previous precision. */
+int nl2d_set_precision(int precision);
 
 /* Registers and uploads a problem without stepping (same arguments as
  * c_invoke_time_step minus istep).  Returns a status code. */

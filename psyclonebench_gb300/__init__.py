@@ -41,6 +41,7 @@ EXPORTS = {
     "nl2d_finalize": (None, []),
     "nl2d_set_mode": (ctypes.c_int, [ctypes.c_int]),
     "nl2d_last_path": (ctypes.c_int, []),
+    "nl2d_set_precision": (ctypes.c_int, [ctypes.c_int]),
     "nl2d_register": (ctypes.c_int, REGISTER_ARGTYPES),
     "nl2d_run_steps": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP]),
     "nl2d_timed_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP]),

@@ -21,7 +21,10 @@ SOURCES = [
     "nl2d_fused.cu",
     "nl2d_checksum.cu",
     "nl2d_capi.cu",
+    "nl2d_mixed.cu",
 ]
+# The mixed-precision form has no bit-exactness contract: FMA contraction on.
+PER_FILE_FLAGS = {"nl2d_mixed.cu": ["-fmad=true"]}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -62,7 +65,9 @@ def build(force=False, verbose=False):
         o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+            flags = [f for f in NVCC_FLAGS
+                     if not (src in PER_FILE_FLAGS and f.startswith("-fmad"))]
+            jobs.append([nvcc()] + flags + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o])
 
     def run(cmd):
         if verbose:

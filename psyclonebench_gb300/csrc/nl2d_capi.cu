@@ -43,7 +43,16 @@ struct State {
   double* tide_table = nullptr;
   int tide_cap = 0;
   cudaGraphExec_t graph = nullptr;
-  int graph_key[4] = {-1, -1, -1, -1};
+  int graph_key[5] = {-1, -1, -1, -1, -1};
+  // mixed-precision form
+  int precision = 0;           // 0 FP64, 1 mixed
+  MixedFields mix{};
+  float2* msn[2] = {};
+  float* mun[2] = {};
+  float* mvn[2] = {};
+  int mcur = 0;
+  bool mixed_valid = false;    // mixed buffers hold the current state
+  bool mixed_ahead = false;    // ... and it is newer than the FP64 arrays
   int status = NL2D_OK;
   char msg[512] = {0};
 };
@@ -93,6 +102,20 @@ void free_device() {
     cudaFree(s.dev.r_hu);
     cudaFree(s.dev.r_hv);
     for (double* p : s.shadow) cudaFree(p);
+    for (int b = 0; b < 2; b++) {
+      cudaFree(s.msn[b]);
+      cudaFree(s.mun[b]);
+      cudaFree(s.mvn[b]);
+      s.msn[b] = nullptr;
+      s.mun[b] = s.mvn[b] = nullptr;
+    }
+    cudaFree(s.mix.ht);
+    cudaFree(s.mix.hu);
+    cudaFree(s.mix.hv);
+    cudaFree(s.mix.rhu);
+    cudaFree(s.mix.rhv);
+    s.mix = MixedFields{};
+    s.mixed_valid = s.mixed_ahead = false;
   }
   s.dev = Fields{};
   for (double*& p : s.shadow) p = nullptr;
@@ -259,10 +282,14 @@ double* cur_sshn() { return g_state.cur ? g_state.shadow[0] : g_state.dev.sshn_t
 double* cur_un() { return g_state.cur ? g_state.shadow[1] : g_state.dev.un; }
 double* cur_vn() { return g_state.cur ? g_state.shadow[2] : g_state.dev.vn; }
 
+bool sync_from_mixed();
+
 // Brings the primary device arrays to exactly what the reference would hold
-// after the steps taken so far.
+// after the steps taken so far (for the mixed form: the FP64 image of its
+// state).
 bool materialize() {
   State& s = g_state;
+  if (!sync_from_mixed()) return false;
   if (s.materialized) return true;
   if (s.cur) {  // the current state lives in the shadows: swap the roles
     std::swap(s.dev.sshn_t, s.shadow[0]);
@@ -299,6 +326,7 @@ bool sync_shadows() {
 
 bool can_fuse() {
   const State& s = g_state;
+  if (s.precision == 1) return s.mode == NL2D_MODE_AUTO && s.fused_ok;
   return s.mode == NL2D_MODE_AUTO && s.fused_ok && s.consistent;
 }
 
@@ -307,6 +335,7 @@ bool reference_step(int istep) {
   if (!materialize()) return false;
   launch_reference_step(s.dev, dims(), s.sc, istep, s.chain_u, s.chain_v, s.stream);
   if (!CK(cudaGetLastError())) return false;
+  s.mixed_valid = false;
   s.consistent = true;
   s.shadows_synced = false;
   s.last_path = 1;
@@ -315,6 +344,20 @@ bool reference_step(int istep) {
 
 void fused_launch(const double* tide_table, int tide_index, double tide) {
   State& s = g_state;
+  if (s.precision == 1) {  // mixed form: ping-pong of the FP32 buffers
+    MixedState ms;
+    ms.sn_in = s.msn[s.mcur];
+    ms.un_in = s.mun[s.mcur];
+    ms.vn_in = s.mvn[s.mcur];
+    ms.sn_out = s.msn[1 - s.mcur];
+    ms.un_out = s.mun[1 - s.mcur];
+    ms.vn_out = s.mvn[1 - s.mcur];
+    launch_mixed_step(s.mix, ms, s.dev, dims(), s.sc, s.um, tide, tide_table, tide_index,
+                      s.stream);
+    s.mcur = 1 - s.mcur;
+    return;
+  }
+  s.mixed_valid = false;
   FusedState fs;
   fs.sshn_in = cur_sshn();
   fs.un_in = cur_un();
@@ -327,17 +370,89 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
   s.cur = nxt;
 }
 
-bool fused_step(int istep) {
+// Converts the current FP64 state into the mixed buffers (both ping-pong
+// partners, so cells no step writes agree) unless they already hold it.
+bool ensure_mixed() {
   State& s = g_state;
-  if (!sync_shadows()) return false;
-  fused_launch(nullptr, 0, tide_value(istep, s.sc.rdt));
+  const size_t n = (size_t)s.reg.width * s.reg.height;
+  if (!s.msn[0]) {
+    for (int b = 0; b < 2; b++) {
+      if (!CK(cudaMalloc(&s.msn[b], n * sizeof(float2))) ||
+          !CK(cudaMalloc(&s.mun[b], n * sizeof(float))) ||
+          !CK(cudaMalloc(&s.mvn[b], n * sizeof(float))))
+        return false;
+    }
+    if (!CK(cudaMalloc(&s.mix.ht, n * 4)) || !CK(cudaMalloc(&s.mix.hu, n * 4)) ||
+        !CK(cudaMalloc(&s.mix.hv, n * 4)) || !CK(cudaMalloc(&s.mix.rhu, n * 4)) ||
+        !CK(cudaMalloc(&s.mix.rhv, n * 4)))
+      return false;
+    s.mixed_valid = false;
+  }
+  if (s.mixed_valid) return true;
+  if (!materialize()) return false;
+  const Dims d = dims();
+  for (int b = 0; b < 2; b++) {
+    MixedState ms{};
+    ms.sn_out = s.msn[b];
+    ms.un_out = s.mun[b];
+    ms.vn_out = s.mvn[b];
+    launch_to_mixed(s.dev.sshn_t, s.dev.un, s.dev.vn, s.dev, s.mix, ms, d, b == 0, s.stream);
+  }
   if (!CK(cudaGetLastError())) return false;
-  s.materialized = false;
-  s.last_path = 2;
+  s.mcur = 0;
+  s.mixed_valid = true;
+  s.mixed_ahead = false;
+  invalidate_graph();
   return true;
 }
 
-bool one_step(int istep) { return can_fuse() ? fused_step(istep) : reference_step(istep); }
+// Writes the mixed state back into the FP64 arrays (sshn_t, un, vn; the
+// derived arrays follow in materialize()).  The FP64 path then restarts
+// with a reference-structured step.
+bool sync_from_mixed() {
+  State& s = g_state;
+  if (!s.mixed_valid || !s.mixed_ahead) return true;
+  if (s.cur) {
+    std::swap(s.dev.sshn_t, s.shadow[0]);
+    std::swap(s.dev.un, s.shadow[1]);
+    std::swap(s.dev.vn, s.shadow[2]);
+    s.cur = 0;
+    invalidate_graph();
+  }
+  launch_from_mixed(s.msn[s.mcur], s.mun[s.mcur], s.mvn[s.mcur], s.dev.sshn_t, s.dev.un,
+                    s.dev.vn, dims(), s.stream);
+  if (!CK(cudaGetLastError())) return false;
+  s.mixed_ahead = false;
+  s.materialized = false;
+  s.shadows_synced = false;
+  s.consistent = false;
+  return true;
+}
+
+bool fused_step(int istep) {
+  State& s = g_state;
+  if (s.precision == 1) {
+    if (!ensure_mixed()) return false;
+  } else if (!sync_shadows()) {
+    return false;
+  }
+  fused_launch(nullptr, 0, tide_value(istep, s.sc.rdt));
+  if (!CK(cudaGetLastError())) return false;
+  if (s.precision == 1) {
+    s.mixed_ahead = true;
+    s.last_path = 3;
+  } else {
+    s.materialized = false;
+    s.last_path = 2;
+  }
+  return true;
+}
+
+bool one_step(int istep) {
+  const State& s = g_state;
+  if (s.precision == 1) return s.fused_ok ? fused_step(istep) : reference_step(istep);
+  return can_fuse() ? fused_step(istep) : reference_step(istep);
+}
 
 bool ensure_sums(int n) {
   State& s = g_state;
@@ -354,6 +469,15 @@ bool ensure_sums(int n) {
 void enqueue_checksums(double* out3) {
   State& s = g_state;
   const Registration& r = s.reg;
+  if (s.precision == 1 && s.mixed_valid) {
+    launch_checksum_f2(s.msn[s.mcur], r.width, r.xs, r.xe, r.ys, r.ye, s.partials, out3,
+                       s.stream);
+    launch_checksum_f32(s.mun[s.mcur], r.width, r.xs, r.xe - 1, r.ys, r.ye, s.partials,
+                        out3 + 1, s.stream);
+    launch_checksum_f32(s.mvn[s.mcur], r.width, r.xs, r.xe, r.ys, r.ye - 1, s.partials,
+                        out3 + 2, s.stream);
+    return;
+  }
   launch_checksum(cur_sshn(), r.width, r.xs, r.xe, r.ys, r.ye, s.partials, out3, s.stream);
   launch_checksum(cur_un(), r.width, r.xs, r.xe - 1, r.ys, r.ye, s.partials, out3 + 1,
                   s.stream);
@@ -391,7 +515,7 @@ struct CallScope {
 void invalidate_graph() {
   if (g_state.graph) cudaGraphExecDestroy(g_state.graph);
   g_state.graph = nullptr;
-  for (int k = 0; k < 4; k++) g_state.graph_key[k] = -1;
+  for (int k = 0; k < 5; k++) g_state.graph_key[k] = -1;
 }
 
 // Uploads the tidal values of steps istep0 .. istep0+rest-1 and makes
@@ -400,7 +524,7 @@ void invalidate_graph() {
 // the cached one matches.  Nothing is launched; s.cur is left unchanged.
 bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
   State& s = g_state;
-  if (!sync_shadows()) return false;
+  if (s.precision == 1 ? !ensure_mixed() : !sync_shadows()) return false;
   if (s.tide_cap < rest) {
     invalidate_graph();  // it holds the old table address
     if (s.tide_table) cudaFree(s.tide_table);
@@ -416,10 +540,11 @@ bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
     return false;
   // pageable source: the copy is staged before the call returns
   const int phase = checksum_every > 0 ? done_before % checksum_every : 0;
-  const int key[4] = {rest, checksum_every, phase, s.cur};
+  const int key[5] = {rest, checksum_every, phase, s.precision == 1 ? s.mcur : s.cur,
+                      s.precision};
   if (s.graph && memcmp(key, s.graph_key, sizeof key) == 0) return true;
   invalidate_graph();
-  const int cur0 = s.cur;
+  const int cur0 = s.cur, mcur0 = s.mcur;
   cudaGraph_t graph;
   if (!CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal))) return false;
   for (int q = 0; q < rest; q++) {
@@ -429,12 +554,27 @@ bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
       enqueue_checksums(s.sums + 3 * (done / checksum_every - 1));
   }
   s.cur = cur0;
+  s.mcur = mcur0;
   if (!CK(cudaStreamEndCapture(s.stream, &graph))) return false;
   const bool ok = CK(cudaGraphInstantiate(&s.graph, graph, 0));
   cudaGraphDestroy(graph);
   if (!ok) return false;
   memcpy(s.graph_key, key, sizeof key);
   return true;
+}
+
+// Bookkeeping after a launched graph of n steps.
+void advance_after_graph(int n) {
+  State& s = g_state;
+  if (s.precision == 1) {
+    s.mcur = (s.mcur + n) & 1;
+    s.mixed_ahead = true;
+    s.last_path = 3;
+  } else {
+    s.cur = (s.cur + n) & 1;
+    s.materialized = false;
+    s.last_path = 2;
+  }
 }
 
 }  // namespace
@@ -594,6 +734,21 @@ int nl2d_set_mode(int mode) {
 
 int nl2d_last_path(void) { return g_state.last_path; }
 
+int nl2d_set_precision(int precision) {
+  State& s = g_state;
+  const int old = s.precision;
+  if (precision != 0 && precision != 1) {
+    set_error(NL2D_ERR_ARGS, "nl2d_set_precision: unknown precision %d", precision);
+    return old;
+  }
+  if (precision != old) {
+    if (old == 1) sync_from_mixed();  // keep the mixed state, now in FP64
+    s.precision = precision;
+    invalidate_graph();
+  }
+  return old;
+}
+
 int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums_out) {
   State& s = g_state;
   CallScope scope;
@@ -624,9 +779,7 @@ int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums
   if (rest > 0) {
     if (!prepare_graph(istep0 + k, rest, checksum_every, k)) return scope.rc();
     if (!CK(cudaGraphLaunch(s.graph, s.stream))) return scope.rc();
-    s.cur = (s.cur + rest) & 1;
-    s.materialized = false;
-    s.last_path = 2;
+    advance_after_graph(rest);
   }
   if (nsums > 0) {
     if (!CK(cudaMemcpyAsync(checksums_out, s.sums, sizeof(double) * 3 * nsums,
@@ -667,9 +820,7 @@ int nl2d_timed_run(int istep0, int nsteps, double* ms_out) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     if (ms_out) *ms_out = ms;
-    s.cur = (s.cur + nsteps) & 1;
-    s.materialized = false;
-    s.last_path = 2;
+    advance_after_graph(nsteps);
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

@@ -34,8 +34,13 @@ __device__ __forceinline__ double block_sum(double v, double* warp_partials) {
   return v;
 }
 
+__device__ __forceinline__ double as_f64(double v) { return v; }
+__device__ __forceinline__ double as_f64(float v) { return (double)v; }
+__device__ __forceinline__ double as_f64(float2 v) { return (double)v.x + (double)v.y; }
+
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_abs_sum_partial(const double* __restrict__ f, int W, int x0, int nx, int y0, int ny,
+    k_abs_sum_partial(const T* __restrict__ f, int W, int x0, int nx, int y0, int ny,
                       double* __restrict__ partials) {
   __shared__ double wp[kThreads / 32];
   double acc = 0.0;
@@ -43,7 +48,7 @@ __global__ void __launch_bounds__(kThreads)
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int j = (int)(t / nx), i = (int)(t - (long long)j * nx);
-    acc += fabs(f[(long long)(y0 + j) * W + (x0 + i)]);
+    acc += fabs(as_f64(f[(long long)(y0 + j) * W + (x0 + i)]));
   }
   acc = block_sum(acc, wp);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
@@ -64,6 +69,20 @@ int checksum_partials_needed() { return kBlocks; }
 
 void launch_checksum(const double* f, int width, int x0, int x1, int y0, int y1,
                      double* partials, double* out, cudaStream_t st) {
+  const int nx = x1 >= x0 ? x1 - x0 + 1 : 0, ny = y1 >= y0 ? y1 - y0 + 1 : 0;
+  k_abs_sum_partial<<<kBlocks, kThreads, 0, st>>>(f, width, x0, nx, y0, ny, partials);
+  k_abs_sum_final<<<1, kThreads, 0, st>>>(partials, kBlocks, out);
+}
+
+void launch_checksum_f32(const float* f, int width, int x0, int x1, int y0, int y1,
+                         double* partials, double* out, cudaStream_t st) {
+  const int nx = x1 >= x0 ? x1 - x0 + 1 : 0, ny = y1 >= y0 ? y1 - y0 + 1 : 0;
+  k_abs_sum_partial<<<kBlocks, kThreads, 0, st>>>(f, width, x0, nx, y0, ny, partials);
+  k_abs_sum_final<<<1, kThreads, 0, st>>>(partials, kBlocks, out);
+}
+
+void launch_checksum_f2(const float2* f, int width, int x0, int x1, int y0, int y1,
+                        double* partials, double* out, cudaStream_t st) {
   const int nx = x1 >= x0 ? x1 - x0 + 1 : 0, ny = y1 >= y0 ? y1 - y0 + 1 : 0;
   k_abs_sum_partial<<<kBlocks, kThreads, 0, st>>>(f, width, x0, nx, y0, ny, partials);
   k_abs_sum_final<<<1, kThreads, 0, st>>>(partials, kBlocks, out);

@@ -77,6 +77,30 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
 // Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.
 void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
 
+// ---- mixed-precision step (nl2d_mixed.cu) ----
+struct MixedFields {  // static FP32 copies of the depths and the
+  float *ht, *hu, *hv;  // reciprocal momentum denominators
+  float *rhu, *rhv;
+};
+struct MixedState {  // ssh as (hi, lo) float pairs; velocities FP32
+  const float2* sn_in;
+  const float *un_in, *vn_in;
+  float2* sn_out;
+  float *un_out, *vn_out;
+};
+void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields& f,
+                       const Dims& d, const Scalars& s, const UniformMetrics& um,
+                       double tide, const double* tide_table, int tide_index,
+                       cudaStream_t st);
+// FP64 (sshn, un, vn) -> ms.{sn,un,vn}_out; with `statics`, also the FP32
+// depths mf.{ht,hu,hv} from f.
+void launch_to_mixed(const double* sn, const double* un, const double* vn,
+                     const Fields& f, const MixedFields& mf, const MixedState& ms,
+                     const Dims& d, bool statics, cudaStream_t st);
+void launch_from_mixed(const float2* sn2, const float* un_f, const float* vn_f,
+                       double* sn, double* un, double* vn, const Dims& d,
+                       cudaStream_t st);
+
 // ---- checksums (nl2d_checksum.cu) ----
 // Sum of |f| over [x0,x1] x [y0,y1]; per-block partial sums go to
 // `partials` (at least checksum_partials_needed() doubles) and the final
@@ -84,5 +108,10 @@ void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
 int checksum_partials_needed();
 void launch_checksum(const double* f, int width, int x0, int x1, int y0,
                      int y1, double* partials, double* out, cudaStream_t st);
+// The same sums over FP32 fields and over (hi, lo) pairs (hi + lo in FP64).
+void launch_checksum_f32(const float* f, int width, int x0, int x1, int y0,
+                         int y1, double* partials, double* out, cudaStream_t st);
+void launch_checksum_f2(const float2* f, int width, int x0, int x1, int y0,
+                        int y1, double* partials, double* out, cudaStream_t st);
 
 }  // namespace nl2d

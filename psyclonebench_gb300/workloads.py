@@ -1,0 +1,54 @@
+"""Synthetic NEMOLite2D inputs beyond the reference's constant-depth
+namelist configuration (the reference publishes no dataset).
+
+* ``fourier_depth``: seeded smooth bathymetry, the sum of 16 Fourier modes
+  about a mean depth, clipped to [50, 500] m and then to at least 20 m,
+  evaluated at T, U (x + dx/2) and V (y + dy/2) points so that every form
+  sees identical inputs.
+* ``ensemble_domains``: seeded descriptions of many independent domains
+  (sizes log-uniform per axis, bathymetry seed, tidal amplitude and period,
+  which side is open).
+"""
+import math
+
+import numpy as np
+
+
+def fourier_depth(width, height, seed, mean=275.0, nmodes=16, dx=1000.0, dy=1000.0):
+    """(ht, hu, hv) as [height][width] FP64 arrays."""
+    rng = np.random.default_rng(seed)
+    lx, ly = width * dx, height * dy
+    m = rng.integers(-6, 7, size=nmodes)
+    n = rng.integers(-6, 7, size=nmodes)
+    zero = (m == 0) & (n == 0)
+    m[zero] = 1
+    a = rng.uniform(10.0, 35.0, size=nmodes)
+    ph = rng.uniform(0.0, 2.0 * math.pi, size=nmodes)
+    jj, ii = np.mgrid[0:height, 0:width].astype(np.float64)
+
+    def depth(x, y):
+        h = np.full(x.shape, mean)
+        for k in range(nmodes):
+            h += a[k] * np.cos(2.0 * math.pi * (m[k] * x / lx + n[k] * y / ly) + ph[k])
+        return np.maximum(np.clip(h, 50.0, 500.0), 20.0)
+
+    x_t, y_t = ii * dx, jj * dy
+    return depth(x_t, y_t), depth(x_t + 0.5 * dx, y_t), depth(x_t, y_t + 0.5 * dy)
+
+
+def ensemble_domains(count, seed, lo=64, hi=1024):
+    """List of dicts: nx, ny (interior cells), depth_seed, tide_amp (m),
+    tide_period_h, open_side in {"S", "N", "E", "W"}."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        nx = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        ny = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        out.append({
+            "nx": nx, "ny": ny,
+            "depth_seed": int(rng.integers(0, 2 ** 31 - 1)),
+            "tide_amp": float(rng.uniform(0.05, 0.5)),
+            "tide_period_h": float(rng.uniform(10.0, 14.0)),
+            "open_side": "SNEW"[int(rng.integers(0, 4))],
+        })
+    return out

@@ -1,0 +1,66 @@
+"""The mixed-precision form (FP32 momentum, compensated-FP32 ssh) against
+the FP64 path, which the parity tests pin bit for bit to the reference.
+Bar (stated per field): ssh RMS error <= 1e-6 m after 1000 steps on a
+seeded Fourier bathymetry."""
+import numpy as np
+import pytest
+
+import nl2d_testlib as T
+
+pytestmark = pytest.mark.gpu
+
+
+def bathy_model(n, seed, oracle):
+    from psyclonebench_gb300.workloads import fourier_depth
+    m = T.make_model(n + 2, n + 2, 1, width=((n + 3 + 7) // 8) * 8, oracle=oracle)
+    ht, hu, hv = fourier_depth(m.width, m.height, seed)
+    m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = ht, hu, hv
+    m.rdt = 5.0  # gravity-wave CFL at 500 m depth (sqrt(g h) = 70 m/s, dx = 1 km)
+    return m
+
+
+def run_form(gpulib, m, nsteps, precision):
+    import psyclonebench_gb300 as P
+    T.gpu_register(gpulib, m)
+    gpulib.nl2d_set_precision(precision)
+    out = np.zeros(3)
+    P.check(gpulib.nl2d_run_steps(1, nsteps, 0, T.dptr(out)), "run")
+    T.gpu_read_all(gpulib, m)
+    gpulib.nl2d_set_precision(0)
+    return m
+
+
+def test_mixed_error_vs_fp64(gpulib, oracle):
+    base = bathy_model(256, 42, oracle)
+    ref = run_form(gpulib, base.copy(), 1000, 0)
+    mix = run_form(gpulib, base.copy(), 1000, 1)
+    assert gpulib.nl2d_last_path() in (3, 0)
+    report = {}
+    for k, (x0, x1, y0, y1) in (("sshn_t", T.regions(ref)["t"]), ("un", T.regions(ref)["u"]),
+                                ("vn", T.regions(ref)["v"])):
+        a = mix.f[k][y0:y1 + 1, x0:x1 + 1]
+        b = ref.f[k][y0:y1 + 1, x0:x1 + 1]
+        report[k] = (float(np.sqrt(np.mean((a - b) ** 2))), float(np.abs(a - b).max()),
+                     float(np.abs(b).max()))
+    print("mixed vs fp64 after 1000 steps (rms, max, field max):", report)
+    assert report["sshn_t"][0] <= 1e-6
+    assert report["un"][0] <= 1e-4 * report["un"][2]
+    assert report["vn"][0] <= 1e-4 * report["vn"][2]
+
+
+def test_mixed_checksums_and_roundtrip(gpulib, oracle):
+    """In-graph checksums of the mixed state agree with the FP64 image that
+    c_read_from_device returns, and switching back to FP64 continues."""
+    import psyclonebench_gb300 as P
+    m = bathy_model(64, 3, oracle)
+    T.gpu_register(gpulib, m)
+    gpulib.nl2d_set_precision(1)
+    sums = np.zeros(6)
+    P.check(gpulib.nl2d_run_steps(1, 100, 50, T.dptr(sums)), "run mixed")
+    T.gpu_read_all(gpulib, m)
+    cs = T.model_checksums(m, oracle)
+    np.testing.assert_allclose(sums[3:], [cs["sshn_t"], cs["un"], cs["vn"]], rtol=1e-10)
+    gpulib.nl2d_set_precision(0)
+    P.check(gpulib.nl2d_run_steps(101, 20, 0, T.dptr(sums)), "run fp64 after mixed")
+    T.gpu_read_all(gpulib, m)
+    assert np.isfinite(m.f["sshn_t"]).all()
