@@ -27,6 +27,7 @@ namespace {
 
 constexpr int TX = 32, TY = 8, HALO = 2;
 constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, S0 = SX * SY;
+constexpr int P1X = TX + 2, P1Y = TY + 2, S1 = P1X * P1Y;
 
 struct MixConst {
   float area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t;
@@ -187,7 +188,11 @@ __global__ void __launch_bounds__(TX* TY)
     k_mixed_step(MixedFields mf, MixedState ms, Fields f, Dims d, MixConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
   __shared__ float s_sn[S0], s_su[S0], s_sv[S0];
+  __shared__ float s_un[S0], s_vn[S0], s_hu[S0], s_hv[S0], s_Hu[S0], s_Hv[S0];
   __shared__ int s_m[S0];
+  // terms shared by neighbouring updates (halo 1), as in the FP64 step
+  __shared__ float b_flxu[S1], b_flxv[S1], b_gx[S1], b_gy[S1], b_fxu[S1], b_fyv[S1];
+  __shared__ float b_vsc[S1], b_fyu[S1], b_qy[S1], b_uwc[S1], b_fxv[S1], b_qx[S1];
   const int W = d.width, H = d.height;
   const int i0 = d.xs - 1 + blockIdx.x * TX;
   const int j0 = d.ys - 1 + blockIdx.y * TY;
@@ -196,12 +201,16 @@ __global__ void __launch_bounds__(TX* TY)
 
   for (int t = tid; t < S0; t += TX * TY) {
     const int i = i0 - HALO + t % SX, j = j0 - HALO + t / SX;
-    float vsn = 0.f, su = 0.f, sv = 0.f;
+    float vsn = 0.f, su = 0.f, sv = 0.f, vun = 0.f, vvn = 0.f, vhu = 0.f, vhv = 0.f;
     int mm = 0;
     if (i >= 0 && i < W && j >= 0 && j < H) {
       const int c = j * W + i;
       const int* m = f.tmask;
       vsn = sn2[c].x;
+      vun = ms.un_in[c];
+      vvn = ms.vn_in[c];
+      vhu = mf.hu[c];
+      vhv = mf.hv[c];
       mm = m[c];
       bool su_static = true, sv_static = true;
       if (j >= d.ys && j <= d.ye && i >= d.xs && i <= d.xe - 1) {
@@ -235,7 +244,45 @@ __global__ void __launch_bounds__(TX* TY)
     s_sn[t] = vsn;
     s_su[t] = su;
     s_sv[t] = sv;
+    s_un[t] = vun;
+    s_vn[t] = vvn;
+    s_hu[t] = vhu;
+    s_hv[t] = vhv;
+    s_Hu[t] = vhu + su;
+    s_Hv[t] = vhv + sv;
     s_m[t] = mm;
+  }
+  __syncthreads();
+
+  for (int t = tid; t < S1; t += TX * TY) {
+    const int ti = t % P1X, tj = t / P1X;
+    const int i = i0 - 1 + ti, j = j0 - 1 + tj;
+    const int q = (tj + 1) * SX + (ti + 1);
+    const int qw = q - 1, qs = q - SX, qse = qs + 1, qwn = qw + SX;
+    const float ht = (i >= 0 && i < W && j >= 0 && j < H) ? mf.ht[j * W + i] : 0.f;
+    const float D = ht + s_sn[q];
+    const float u_c = s_un[q], u_w = s_un[qw], u_s = s_un[qs], u_wn = s_un[qwn];
+    const float v_c = s_vn[q], v_w = s_vn[qw], v_s = s_vn[qs], v_se = s_vn[qse];
+    b_flxu[t] = s_Hu[q] * u_c;
+    b_flxv[t] = s_Hv[q] * v_c;
+    b_gx[t] = (u_c - u_w) * k.r_dx_t * D;
+    b_gy[t] = (v_c - v_s) * k.r_dy_t * D;
+    const float U = 0.5f * (u_c + u_w) * k.dy_t;
+    b_fxu[t] = (U < 0.f ? u_c : u_w) * U * D;
+    const float V = 0.5f * (v_c + v_s) * k.dx_t;
+    b_fyv[t] = (V < 0.f ? v_c : v_s) * V * D;
+    const float vsc = 0.5f * (v_s + v_se);
+    b_vsc[t] = vsc;
+    const float Vs = 0.5f * vsc * k.dxv2;
+    const float deps = 0.5f * (s_Hv[qs] + s_hv[qse] + s_sv[qse]);
+    b_fyu[t] = (Vs < 0.f ? u_c : u_s) * Vs * deps;
+    b_qy[t] = (u_c - u_s) * k.r_dyu2;
+    const float uwc = 0.5f * (u_w + u_wn);
+    b_uwc[t] = uwc;
+    const float Uw = 0.5f * uwc * k.dyu2;
+    const float depw = 0.5f * (s_Hu[qw] + s_hu[qwn] + s_su[qwn]);
+    b_fxv[t] = (Uw < 0.f ? v_c : v_w) * Uw * depw;
+    b_qx[t] = (v_c - v_w) * k.r_dxv2;
   }
   __syncthreads();
 
@@ -263,6 +310,44 @@ __global__ void __launch_bounds__(TX* TY)
   x.k = k;
   const int t = x.slot(i, j);
   const int* m = s_m;
+
+  bool regular = i >= d.xs && i <= d.xe - 1 && j >= d.ys && j <= d.ye - 1;
+  if (regular) {
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+      for (int di = -1; di <= 1; di++) regular &= m[t + dj * SX + di] > 0;
+  }
+  if (regular) {
+    // Wet cell with a wet 3x3 neighbourhood: no boundary condition applies.
+    const int r = (threadIdx.y + 1) * P1X + (threadIdx.x + 1);
+    const float snc = s_sn[t], Hu = s_Hu[t], Hv = s_Hv[t];
+    const float div = ((b_flxu[r - 1] - b_flxu[r]) + b_flxv[r - P1X]) - b_flxv[r];
+    ms.sn_out[c] = dd_add(sn2[c], div * k.rdt * k.r_area_t);
+    {
+      const float adv = ((b_fxu[r] - b_fxu[r + 1]) + b_fyu[r]) - b_fyu[r + P1X];
+      const float dudy_s = b_qy[r] * (Hu + s_hu[t - SX] + s_su[t - SX]);
+      const float dudy_n = b_qy[r + P1X] * (Hu + s_hu[t + SX] + s_su[t + SX]);
+      const float vis =
+          k.visc * ((b_gx[r + 1] - b_gx[r]) * k.dy_u + 0.5f * (dudy_n - dudy_s) * k.dx_u);
+      const float cor = 0.5f * (k.cor_u * (b_vsc[r] + b_vsc[r + P1X])) * k.area_u * Hu;
+      const float hpg = -k.g * Hu * k.dy_u * (s_sn[t + 1] - snc);
+      ms.un_out[c] = (s_un[t] * Hu + k.rdt * (adv + vis + cor + hpg) * k.r_area_u) *
+                     mf.rhu[c] * k.r_fric;
+    }
+    {
+      const float adv = ((b_fxv[r] - b_fxv[r + 1]) + b_fyv[r]) - b_fyv[r + P1X];
+      const float dvdx_w = b_qx[r] * (Hv + s_hv[t - 1] + s_sv[t - 1]);
+      const float dvdx_e = b_qx[r + 1] * (Hv + s_hv[t + 1] + s_sv[t + 1]);
+      const float vis =
+          k.visc * ((b_gy[r + P1X] - b_gy[r]) * k.dx_v + 0.5f * (dvdx_e - dvdx_w) * k.dy_v);
+      const float cor = -0.5f * (k.cor_v * (b_uwc[r + 1] + b_uwc[r])) * k.area_v * Hv;
+      const float hpg = -k.g * Hv * k.dx_v * (s_sn[t + SX] - snc);
+      ms.vn_out[c] = (s_vn[t] * Hv + k.rdt * (adv + vis + cor + hpg) * k.r_area_v) *
+                     mf.rhv[c] * k.r_fric;
+    }
+    return;
+  }
 
   // ssh: continuity (FP32 flux divergence) + compensated update, bc_ssh
   float2 ssh = sn2[c];
