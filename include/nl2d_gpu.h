@@ -173,6 +173,42 @@ int nl2d_field_checksum_noalloc(const double *d_field, int width, int x0,
                                 int x1, int y0, int y1, double *d_out,
                                 void *stream);
 
+/* ---- ensemble of independent domains (no counterpart in the reference,
+ *      which runs one domain per executable) ----
+ * Domains start from rest; each has its own extents, T-mask, depths, grid
+ * spacing, latitude and tide (bc_ssh of boundary_conditions_kern.c:178-203
+ * with amplitude amp and period period_h; 0.2 m / 12.42 h is the
+ * reference).  One persistent kernel launch advances every domain by one
+ * step; a run of steps is one captured CUDA graph.  FP64 results are
+ * bit-identical to the reference step of each domain. */
+
+/* dims6[6k..6k+5] = width, height, xs, xe, ys, ye (0-based internal
+ * region); geo3[3k..] = dx, dy, latitude (deg); tide2[2k..] = amp (m),
+ * period (h); phys6 = rdt, cbfr, visc, omega, d2r, g. */
+int nl2d_ens_create(int ndom, const int *dims6, const double *geo3,
+                    const double *tide2, const double *phys6);
+/* Static inputs of domain `dom` (width x height each).  Rejects masks with
+ * chained Flather faces and non-positive depths. */
+int nl2d_ens_set_domain(int dom, const int *tmask, const double *ht,
+                        const double *hu, const double *hv);
+/* Schedule knobs the autotuner searches: persistent CTAs per SM (1, 2),
+ * tile assignment (0 contiguous cost-balanced chunks, 1 longest processing
+ * time first) and the cost weight of a boundary-tile edge cell. */
+int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight);
+/* Advances every domain nsteps steps (istep = istep0 ...); per-domain
+ * ssh / u / v checksums after every checksum_every-th step go to
+ * checksums_out[(s * ndom + dom) * 3 + f].  *ms_out: device time. */
+int nl2d_ens_run(int istep0, int nsteps, int checksum_every,
+                 double *checksums_out, double *ms_out);
+/* Current sshn_t, un, vn of one domain (width x height host arrays; any may
+ * be NULL). */
+int nl2d_ens_read(int dom, double *sshn_t, double *un, double *vn);
+/* Puts every domain back at rest (step 0). */
+int nl2d_ens_reset(void);
+/* Interior cells over all domains, tiles, persistent CTAs. */
+int nl2d_ens_info(long long *cells, int *ntiles, int *nctas);
+void nl2d_ens_destroy(void);
+
 /* Test hook: over n sampled doubles x (seeded), counts where the exact
  * FP64 helpers of the fused step differ from the IEEE expressions they
  * stand for — x / d (d in [2^-100, 2^100]), 0.5 * x, and the upwind pick

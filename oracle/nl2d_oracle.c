@@ -28,6 +28,7 @@ typedef struct {
         *dy_v, *dy_t, *gphiu, *gphiv;
     int istep, w;
     double rdt, cbfr, visc, omega, d2r, g;
+    double tide_amp, tide_period_h;  /* 0.2 m and 12.42 h in the reference */
 } step_t;
 
 /* ---- kernels ----------------------------------------------------------- */
@@ -193,12 +194,14 @@ static void k_momentum_v(const step_t *s, int i, int j)
 /* Tidal sea-surface height at wet cells next to an open (-1) cell:
  * kernels/c_family/boundary_conditions_kern.c:178-203 (amplitude 0.2 m,
  * period 12.42 h, the literal 3.14159; neighbour priority S, N, E, W). */
+/* The ensemble form parametrises amplitude and period; with 0.2 m and
+ * 12.42 h the operations, and so the bits, are the reference's. */
 static void k_bc_ssh(const step_t *s, int i, int j)
 {
     const int c = j * s->w + i;
     const int *m = s->tmask;
-    double amp_tide = 0.2;
-    double omega_tide = 2.0 * 3.14159 / (12.42 * 3600.0);
+    double amp_tide = s->tide_amp;
+    double omega_tide = 2.0 * 3.14159 / (s->tide_period_h * 3600.0);
     double rtime = s->istep * s->rdt;
     if (m[c] <= 0) return;
     if (m[c - s->w] < 0 || m[c + s->w] < 0 || m[c + 1] < 0 || m[c - 1] < 0)
@@ -318,7 +321,7 @@ static void psy_step(const step_t *s, int xs, int xe, int ys, int ye, int par)
     step_t s = {ssha_t, sshn_t, sshn_u, sshn_v, hu, hv, un, vn, ua, ht,       \
                 ssha_u, va, ssha_v, tmask, area_t, area_u, area_v, dx_u,      \
                 dx_v, dx_t, dy_u, dy_v, dy_t, gphiu, gphiv, istep, width,    \
-                rdt, cbfr, visc, omega, d2r, g};                              \
+                rdt, cbfr, visc, omega, d2r, g, 0.2, 12.42};                  \
     (void)height
 
 void oracle_invoke_time_step(NL2D_ORACLE_STEP_ARGS)
@@ -333,6 +336,16 @@ void oracle_invoke_time_step_omp(NL2D_ORACLE_STEP_ARGS)
     FILL_STEP(s);
     psy_step(&s, internal_xstart, internal_xstop, internal_ystart,
              internal_ystop, 1);
+}
+
+void oracle_invoke_time_step_tide(NL2D_ORACLE_STEP_ARGS, double tide_amp,
+                                  double tide_period_h)
+{
+    FILL_STEP(s);
+    s.tide_amp = tide_amp;
+    s.tide_period_h = tide_period_h;
+    psy_step(&s, internal_xstart, internal_xstop, internal_ystart,
+             internal_ystop, 0);
 }
 
 /* ---- driver pieces ------------------------------------------------------ */

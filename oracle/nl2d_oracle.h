@@ -40,6 +40,12 @@ void oracle_invoke_time_step(NL2D_ORACLE_STEP_ARGS);
  * psykal_cpp/time_step_omp.cpp:57-146 (bc_flather_v stays serial). */
 void oracle_invoke_time_step_omp(NL2D_ORACLE_STEP_ARGS);
 
+/* The serial step with the tidal amplitude (m) and period (h) of bc_ssh
+ * as parameters (the reference hard-codes 0.2 m and 12.42 h,
+ * boundary_conditions_kern.c:185-186); used for the ensemble's domains. */
+void oracle_invoke_time_step_tide(NL2D_ORACLE_STEP_ARGS, double tide_amp,
+                                  double tide_period_h);
+
 /* &namctl reader (common/gocean2d_io_mod.f90:22-80).  ints = {jpiglo,
  * jpjglo, jphgr_msh, nit000, nitend, irecord}; dbls = {dx, dy, dep_const,
  * rdt, cbfr, visc}.  Returns 0, or -1 if the file cannot be read, or -2 on

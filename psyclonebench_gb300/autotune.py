@@ -1,0 +1,79 @@
+"""Autotuner for the ensemble's persistent-kernel schedule.
+
+The search space is the schedule the kernel exposes: persistent CTAs per SM
+(1 or 2), tile assignment (contiguous cost-balanced chunks, or longest
+processing time first) and the cost weight given to the edge cells of
+boundary tiles (which take the general per-cell path).  Each candidate is
+timed on a few steps of the actual ensemble (after one untimed step), the
+domains are put back at rest, and the fastest candidate is kept.  Results
+are cached on disk per (domain size histogram, precision), so a repeated
+ensemble of the same shape skips the search.
+"""
+import hashlib
+import json
+import os
+
+CANDIDATES = [(cps, pol, bw) for cps in (1, 2) for pol in (0, 1) for bw in (0.0, 4.0, 16.0)]
+
+
+def cache_path():
+    base = os.environ.get("NL2D_TUNE_CACHE") or os.path.join(
+        os.environ.get("XDG_CACHE_HOME", os.path.expanduser("~/.cache")), "psyclonebench_gb300")
+    return os.path.join(base, "ensemble_schedule.json")
+
+
+def signature(domains, precision="fp64"):
+    """Histogram of interior sizes (log2 bins per axis) plus precision."""
+    hist = {}
+    for d in domains:
+        w, h, xs, xe, ys, ye = d["dims"]
+        key = "%d:%d" % ((xe - xs + 1).bit_length(), (ye - ys + 1).bit_length())
+        hist[key] = hist.get(key, 0) + 1
+    blob = json.dumps([precision, sorted(hist.items())])
+    return hashlib.sha1(blob.encode()).hexdigest()[:16]
+
+
+def _load():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _store(db):
+    p = cache_path()
+    try:
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        with open(p, "w") as f:
+            json.dump(db, f, indent=1)
+    except OSError:
+        pass
+
+
+def tune(ens, steps=4, precision="fp64", use_cache=True):
+    """Picks and applies the fastest schedule for `ens`; returns a dict with
+    the choice and the timings.  Leaves the ensemble at rest."""
+    sig = signature(ens.domains, precision)
+    db = _load() if use_cache else {}
+    if sig in db:
+        c = db[sig]
+        ens.schedule(c["ctas_per_sm"], c["policy"], c["boundary_weight"])
+        return dict(c, cached=True)
+    timings = []
+    for cps, pol, bw in CANDIDATES:
+        ens.schedule(cps, pol, bw)
+        ens.run(1, 1)  # untimed: builds the schedule and graph
+        ms, _ = ens.run(2, steps)
+        timings.append((ms / steps, cps, pol, bw))
+        ens.reset()
+    best = min(timings)
+    choice = {"ctas_per_sm": best[1], "policy": best[2], "boundary_weight": best[3],
+              "ms_per_step": best[0],
+              "timings": [{"ms_per_step": t[0], "ctas_per_sm": t[1], "policy": t[2],
+                           "boundary_weight": t[3]} for t in timings]}
+    ens.schedule(best[1], best[2], best[3])
+    db[sig] = choice
+    if use_cache:
+        _store(db)
+    return dict(choice, cached=False)

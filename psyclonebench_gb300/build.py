@@ -22,6 +22,7 @@ SOURCES = [
     "nl2d_checksum.cu",
     "nl2d_capi.cu",
     "nl2d_mixed.cu",
+    "nl2d_ensemble.cu",
 ]
 # The mixed-precision form has no bit-exactness contract: FMA contraction on.
 PER_FILE_FLAGS = {"nl2d_mixed.cu": ["-fmad=true"]}

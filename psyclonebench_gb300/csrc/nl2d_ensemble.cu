@@ -1,0 +1,509 @@
+// Ensemble of independent NEMOLite2D domains (uneven sizes, bathymetries,
+// tidal forcings and open sides) advanced by ONE persistent launch per step.
+//
+// Every domain keeps its own dl_esm_inf-style arrays, packed back to back
+// in large device allocations.  The copy region of each domain is cut into
+// TX x TY tiles; a persistent grid of (SM count x CTAs per SM) blocks walks
+// a static tile schedule (contiguous cost-balanced chunks, or a
+// longest-processing-time assignment) chosen by the autotuner.  Each tile
+// is the fused step's tile function (nl2d_fused_tile.cuh), so a domain
+// advanced here is bit-identical to the reference step with its tide
+// parameters.  Steps are separate graph nodes: no grid-wide barrier inside
+// a step, as tiles of a step are independent.
+//
+// Domains start from rest (ssh = u = v = 0), where the state is already
+// step-consistent, so every step takes the fused path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "../../include/nl2d_gpu.h"
+#include "nl2d_fused_tile.cuh"
+
+namespace nl2d {
+namespace {
+
+// Ensemble: a persistent grid walks a tile list spanning many independent
+// domains; CTA b takes tiles [first[b], first[b+1]).  `tides` holds this
+// step's bc_ssh value per domain.
+__global__ void __launch_bounds__(NTHREADS)
+    k_ensemble_step(const EnsDomain* __restrict__ doms, const int4* __restrict__ tiles,
+                    const int* __restrict__ first, int parity,
+                    const double* __restrict__ tides) {
+  extern __shared__ double smem[];
+  const int t1 = first[blockIdx.x + 1];
+  for (int t = first[blockIdx.x]; t < t1; t++) {
+    const int4 tl = tiles[t];
+    const EnsDomain& D = doms[tl.x];
+    __syncthreads();  // the previous tile's last readers are done with smem
+    fused_tile(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
+  }
+}
+
+// Per-domain checksums: block (dom, field) sums |f| over the domain's
+// region for that field (T interior, u region, v region) in a fixed order.
+__global__ void __launch_bounds__(256)
+    k_ensemble_checksums(const EnsDomain* __restrict__ doms, int parity, int ndom,
+                         double* __restrict__ out) {
+  const int dom = blockIdx.x, fld = blockIdx.y;
+  const EnsDomain& D = doms[dom];
+  const FusedState& st = D.fs[parity];  // buffers read at this parity hold the state
+  const double* f = fld == 0 ? st.sshn_in : (fld == 1 ? st.un_in : st.vn_in);
+  const int x0 = D.d.xs, y0 = D.d.ys;
+  const int x1 = fld == 1 ? D.d.xe - 1 : D.d.xe, y1 = fld == 2 ? D.d.ye - 1 : D.d.ye;
+  const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < nx * ny; t += blockDim.x) {
+    const int j = t / nx, i = t - j * nx;
+    acc += fabs(f[(size_t)(y0 + j) * D.d.width + (x0 + i)]);
+  }
+  __shared__ double wp[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) wp[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < 8 ? wp[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[(size_t)dom * 3 + fld] = acc;
+  }
+}
+
+struct DomainHost {
+  int W, H, xs, xe, ys, ye;
+  double dx, dy, gphi, amp, period_h;
+  size_t off;  // element offset of this domain in every packed array
+  bool ready = false;
+};
+
+struct Ens {
+  int ndom = 0;
+  Scalars sc{};
+  std::vector<DomainHost> dom;
+  size_t total = 0;  // packed elements
+  double *sn[2] = {}, *un[2] = {}, *vn[2] = {};
+  double *ht = nullptr, *hu = nullptr, *hv = nullptr, *zero = nullptr;
+  double *r_hu = nullptr, *r_hv = nullptr;
+  int* tmask = nullptr;
+  EnsDomain* d_desc = nullptr;
+  int4* d_tiles = nullptr;
+  int* d_first = nullptr;
+  int ntiles = 0, nctas = 0, ctas_per_sm = 2, policy = 0;
+  double boundary_weight = 4.0;
+  double* d_tides = nullptr;
+  size_t tides_cap = 0;
+  double* d_sums = nullptr;
+  size_t sums_cap = 0;
+  int parity = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_key[5] = {-1, -1, -1, -1, -1};
+  bool built = false;
+};
+
+Ens g_ens;
+
+bool ck(cudaError_t e) { return e == cudaSuccess; }
+
+void ens_free() {
+  Ens& e = g_ens;
+  if (e.graph) cudaGraphExecDestroy(e.graph);
+  e.graph = nullptr;
+  for (int b = 0; b < 2; b++) {
+    cudaFree(e.sn[b]);
+    cudaFree(e.un[b]);
+    cudaFree(e.vn[b]);
+    e.sn[b] = e.un[b] = e.vn[b] = nullptr;
+  }
+  for (double** p : {&e.ht, &e.hu, &e.hv, &e.zero, &e.r_hu, &e.r_hv, &e.d_tides, &e.d_sums}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(e.tmask);
+  cudaFree(e.d_desc);
+  cudaFree(e.d_tiles);
+  cudaFree(e.d_first);
+  e.tmask = nullptr;
+  e.d_desc = nullptr;
+  e.d_tiles = nullptr;
+  e.d_first = nullptr;
+  if (e.stream) cudaStreamDestroy(e.stream);
+  e.stream = nullptr;
+  e.tides_cap = e.sums_cap = 0;
+  e.built = false;
+  e.ndom = 0;
+  e.dom.clear();
+}
+
+// Flather chains or reads outside the array exclude a domain (the one-launch
+// update equals the reference's serial Flather loops only without them).
+bool mask_ok(const DomainHost& D, const int* m) {
+  const int W = D.W;
+  auto writes = [&](int c, int step) {
+    return m[c] + m[c + step] > -1 && (m[c] < 0 || m[c + step] < 0);
+  };
+  for (int j = D.ys - 1; j <= D.ye + 1; j++)
+    for (int i = D.xs - 1; i <= D.xe; i++) {
+      const int c = j * W + i;
+      if (!writes(c, 1)) continue;
+      const int nb = m[c] < 0 ? i + 1 : i - 1;
+      if (nb < 0) return false;
+      if (nb >= D.xs - 1 && nb <= D.xe && writes(j * W + nb, 1)) return false;
+    }
+  for (int j = D.ys - 1; j <= D.ye; j++)
+    for (int i = D.xs - 1; i <= D.xe + 1; i++) {
+      const int c = j * W + i;
+      if (!writes(c, W)) continue;
+      const int nb = m[c] < 0 ? j + 1 : j - 1;
+      if (nb < 0) return false;
+      if (nb >= D.ys - 1 && nb <= D.ye && writes(nb * W + i, W)) return false;
+    }
+  return true;
+}
+
+double tide_at(const DomainHost& D, int istep, double rdt) {
+  // bc_ssh_code (boundary_conditions_kern.c:183-192) with this domain's
+  // amplitude and period; 0.2 m and 12.42 h give the reference's bits.
+  const double omega_tide = 2.0 * 3.14159 / (D.period_h * 3600.0);
+  const double rtime = istep * rdt;
+  return D.amp * std::sin(omega_tide * rtime);
+}
+
+// Tile list and static schedule.
+bool build_schedule() {
+  Ens& e = g_ens;
+  struct T {
+    int dom, i0, j0;
+    double cost;
+  };
+  std::vector<T> tiles;
+  for (int k = 0; k < e.ndom; k++) {
+    const DomainHost& D = e.dom[k];
+    const int nx = D.xe - D.xs + 3, ny = D.ye - D.ys + 2;
+    const int ntx = (nx + TX - 1) / TX, nty = (ny + TY - 1) / TY;
+    for (int by = 0; by < nty; by++)
+      for (int bx = 0; bx < ntx; bx++) {
+        const int cx = std::min(TX, nx - bx * TX), cy = std::min(TY, ny - by * TY);
+        // boundary tiles run the general per-cell path on their edge cells
+        double edge = 0.0;
+        if (bx == 0 || bx == ntx - 1) edge += cy;
+        if (by == 0 || by == nty - 1) edge += cx;
+        tiles.push_back({k, D.xs - 1 + bx * TX, D.ys - 1 + by * TY,
+                         (double)(cx * cy) + e.boundary_weight * edge});
+      }
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e.nctas = std::max(1, sms * e.ctas_per_sm);
+  std::vector<int4> order;
+  std::vector<int> first(e.nctas + 1, 0);
+  if (e.policy == 1) {
+    // longest processing time first: biggest tile to the least-loaded CTA
+    std::vector<int> idx(tiles.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int a, int b) { return tiles[a].cost > tiles[b].cost; });
+    std::vector<double> load(e.nctas, 0.0);
+    std::vector<std::vector<int>> bins(e.nctas);
+    for (int t : idx) {
+      const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      load[b] += tiles[t].cost;
+      bins[b].push_back(t);
+    }
+    for (int b = 0; b < e.nctas; b++) {
+      std::sort(bins[b].begin(), bins[b].end());  // keep each CTA's tiles in memory order
+      first[b + 1] = first[b] + (int)bins[b].size();
+      for (int t : bins[b]) order.push_back(make_int4(tiles[t].dom, tiles[t].i0, tiles[t].j0, 0));
+    }
+  } else {
+    // contiguous chunks of (nearly) equal cost, in domain order
+    double total = 0.0;
+    for (const T& t : tiles) total += t.cost;
+    double acc = 0.0;
+    int b = 0;
+    for (size_t t = 0; t < tiles.size(); t++) {
+      while (b < e.nctas - 1 && acc >= total * (b + 1) / e.nctas) first[++b] = (int)t;
+      acc += tiles[t].cost;
+      order.push_back(make_int4(tiles[t].dom, tiles[t].i0, tiles[t].j0, 0));
+    }
+    while (b < e.nctas) first[++b] = (int)tiles.size();
+  }
+  e.ntiles = (int)order.size();
+  cudaFree(e.d_tiles);
+  cudaFree(e.d_first);
+  e.d_tiles = nullptr;
+  e.d_first = nullptr;
+  if (!ck(cudaMalloc(&e.d_tiles, sizeof(int4) * std::max<size_t>(1, order.size()))) ||
+      !ck(cudaMalloc(&e.d_first, sizeof(int) * first.size())))
+    return false;
+  if (!ck(cudaMemcpy(e.d_tiles, order.data(), sizeof(int4) * order.size(),
+                     cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.d_first, first.data(), sizeof(int) * first.size(),
+                     cudaMemcpyHostToDevice)))
+    return false;
+  if (e.graph) cudaGraphExecDestroy(e.graph);
+  e.graph = nullptr;
+  return true;
+}
+
+bool build_descriptors() {
+  Ens& e = g_ens;
+  std::vector<EnsDomain> desc(e.ndom);
+  for (int k = 0; k < e.ndom; k++) {
+    const DomainHost& D = e.dom[k];
+    EnsDomain& x = desc[k];
+    memset(&x, 0, sizeof x);
+    const size_t o = D.off;
+    x.f.ht = e.ht + o;
+    x.f.hu = e.hu + o;
+    x.f.hv = e.hv + o;
+    x.f.tmask = e.tmask + o;
+    // rest start: sshn_u / sshn_v, ua / va and ssha_u / ssha_v are zero where
+    // no step writes them
+    x.f.sshn_u = x.f.sshn_v = x.f.ua = x.f.va = x.f.ssha_u = x.f.ssha_v = e.zero + o;
+    x.f.r_hu = e.r_hu + o;
+    x.f.r_hv = e.r_hv + o;
+    for (int p = 0; p < 2; p++) {
+      x.fs[p].sshn_in = e.sn[p] + o;
+      x.fs[p].un_in = e.un[p] + o;
+      x.fs[p].vn_in = e.vn[p] + o;
+      x.fs[p].sshn_out = e.sn[1 - p] + o;
+      x.fs[p].un_out = e.un[1 - p] + o;
+      x.fs[p].vn_out = e.vn[1 - p] + o;
+    }
+    x.d = Dims{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
+    x.p = e.sc;
+    UniformMetrics um{};
+    um.area_t = um.area_u = um.area_v = D.dx * D.dy;
+    um.dx_u = um.dx_v = um.dx_t = D.dx;
+    um.dy_u = um.dy_v = um.dy_t = D.dy;
+    um.sin_u = um.sin_v = std::sin(D.gphi * e.sc.d2r);
+    x.um = um;
+    x.k = make_fast_const(e.sc, um);
+  }
+  cudaFree(e.d_desc);
+  e.d_desc = nullptr;
+  if (!ck(cudaMalloc(&e.d_desc, sizeof(EnsDomain) * e.ndom))) return false;
+  return ck(cudaMemcpy(e.d_desc, desc.data(), sizeof(EnsDomain) * e.ndom,
+                       cudaMemcpyHostToDevice));
+}
+
+__global__ void k_recip(const double* __restrict__ h, double* __restrict__ r, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const double dd = h[t] + 0.0;  // ssha_u / ssha_v are zero at rest
+    r[t] = (dd >= 0x1p-100 && dd <= 0x1p100) ? 1.0 / dd : 0.0;
+  }
+}
+
+}  // namespace
+}  // namespace nl2d
+
+using namespace nl2d;
+
+extern "C" {
+
+int nl2d_ens_create(int ndom, const int* dims6, const double* geo3, const double* tide2,
+                    const double* phys6) {
+  ens_free();
+  Ens& e = g_ens;
+  if (ndom < 1 || !dims6 || !geo3 || !tide2 || !phys6) return NL2D_ERR_ARGS;
+  e.sc = Scalars{phys6[0], phys6[1], phys6[2], phys6[3], phys6[4], phys6[5]};
+  e.dom.resize(ndom);
+  size_t off = 0;
+  for (int k = 0; k < ndom; k++) {
+    DomainHost& D = e.dom[k];
+    D.W = dims6[6 * k], D.H = dims6[6 * k + 1];
+    D.xs = dims6[6 * k + 2], D.xe = dims6[6 * k + 3];
+    D.ys = dims6[6 * k + 4], D.ye = dims6[6 * k + 5];
+    if (D.xs < 1 || D.ys < 1 || D.xe < D.xs || D.ye < D.ys || D.xe > D.W - 2 ||
+        D.ye > D.H - 2) {
+      e.dom.clear();
+      return NL2D_ERR_ARGS;
+    }
+    D.dx = geo3[3 * k], D.dy = geo3[3 * k + 1], D.gphi = geo3[3 * k + 2];
+    D.amp = tide2[2 * k], D.period_h = tide2[2 * k + 1];
+    D.off = off;
+    off += ((size_t)D.W * D.H + 31) / 32 * 32;  // 256-byte aligned domain starts
+  }
+  e.ndom = ndom;
+  e.total = off;
+  const size_t bytes = off * sizeof(double);
+  if (!ck(cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking))) return NL2D_ERR_CUDA;
+  for (int b = 0; b < 2; b++)
+    if (!ck(cudaMalloc(&e.sn[b], bytes)) || !ck(cudaMalloc(&e.un[b], bytes)) ||
+        !ck(cudaMalloc(&e.vn[b], bytes)))
+      return NL2D_ERR_CUDA;
+  for (double** p : {&e.ht, &e.hu, &e.hv, &e.zero, &e.r_hu, &e.r_hv})
+    if (!ck(cudaMalloc(p, bytes))) return NL2D_ERR_CUDA;
+  if (!ck(cudaMalloc(&e.tmask, off * sizeof(int)))) return NL2D_ERR_CUDA;
+  for (double* p : {e.sn[0], e.sn[1], e.un[0], e.un[1], e.vn[0], e.vn[1], e.zero})
+    if (!ck(cudaMemset(p, 0, bytes))) return NL2D_ERR_CUDA;
+  if (!ck(cudaMemset(e.tmask, 0, off * sizeof(int)))) return NL2D_ERR_CUDA;
+  e.parity = 0;
+  return NL2D_OK;
+}
+
+int nl2d_ens_set_domain(int dom, const int* tmask, const double* ht, const double* hu,
+                        const double* hv) {
+  Ens& e = g_ens;
+  if (dom < 0 || dom >= e.ndom || !tmask || !ht || !hu || !hv) return NL2D_ERR_ARGS;
+  DomainHost& D = e.dom[dom];
+  if (!mask_ok(D, tmask)) return NL2D_ERR_ARGS;
+  const size_t n = (size_t)D.W * D.H;
+  for (size_t t = 0; t < n; t++)
+    if (!(hu[t] > 0.0) || !(hv[t] > 0.0)) return NL2D_ERR_ARGS;
+  if (!ck(cudaMemcpy(e.tmask + D.off, tmask, n * sizeof(int), cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.ht + D.off, ht, n * 8, cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.hu + D.off, hu, n * 8, cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.hv + D.off, hv, n * 8, cudaMemcpyHostToDevice)))
+    return NL2D_ERR_CUDA;
+  k_recip<<<64, 256, 0, e.stream>>>(e.hu + D.off, e.r_hu + D.off, n);
+  k_recip<<<64, 256, 0, e.stream>>>(e.hv + D.off, e.r_hv + D.off, n);
+  if (!ck(cudaGetLastError())) return NL2D_ERR_CUDA;
+  D.ready = true;
+  e.built = false;
+  return NL2D_OK;
+}
+
+int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight) {
+  Ens& e = g_ens;
+  if (ctas_per_sm < 1 || ctas_per_sm > 2 || policy < 0 || policy > 1 || boundary_weight < 0)
+    return NL2D_ERR_ARGS;
+  e.ctas_per_sm = ctas_per_sm;
+  e.policy = policy;
+  e.boundary_weight = boundary_weight;
+  e.built = false;
+  return NL2D_OK;
+}
+
+int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_out,
+                 double* ms_out) {
+  Ens& e = g_ens;
+  if (ms_out) *ms_out = 0.0;
+  if (e.ndom < 1 || nsteps < 0 || checksum_every < 0) return NL2D_ERR_ARGS;
+  for (const DomainHost& D : e.dom)
+    if (!D.ready) return NL2D_ERR_STATE;
+  if (!e.built) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_ensemble_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kSmemBytes);
+      attr = true;
+    }
+    if (!build_descriptors() || !build_schedule()) return NL2D_ERR_CUDA;
+    e.built = true;
+  }
+  if (nsteps == 0) return NL2D_OK;
+  const int nsums = checksum_every > 0 ? nsteps / checksum_every : 0;
+  if (nsums > 0 && !checksums_out) return NL2D_ERR_ARGS;
+  // per-step, per-domain tidal values (host libm)
+  const size_t ntide = (size_t)nsteps * e.ndom;
+  if (e.tides_cap < ntide) {
+    cudaFree(e.d_tides);
+    e.d_tides = nullptr;
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    e.graph = nullptr;
+    if (!ck(cudaMalloc(&e.d_tides, ntide * 8))) return NL2D_ERR_CUDA;
+    e.tides_cap = ntide;
+  }
+  std::vector<double> tides(ntide);
+  for (int q = 0; q < nsteps; q++)
+    for (int k = 0; k < e.ndom; k++)
+      tides[(size_t)q * e.ndom + k] = tide_at(e.dom[k], istep0 + q, e.sc.rdt);
+  if (!ck(cudaMemcpyAsync(e.d_tides, tides.data(), ntide * 8, cudaMemcpyHostToDevice,
+                          e.stream)))
+    return NL2D_ERR_CUDA;
+  const size_t nsum_vals = (size_t)std::max(nsums, 1) * e.ndom * 3;
+  if (e.sums_cap < nsum_vals) {
+    cudaFree(e.d_sums);
+    e.d_sums = nullptr;
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    e.graph = nullptr;
+    if (!ck(cudaMalloc(&e.d_sums, nsum_vals * 8))) return NL2D_ERR_CUDA;
+    e.sums_cap = nsum_vals;
+  }
+  const int key[5] = {nsteps, checksum_every, e.parity, e.nctas, e.policy};
+  if (!(e.graph && memcmp(key, e.graph_key, sizeof key) == 0)) {
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    e.graph = nullptr;
+    cudaGraph_t g;
+    if (!ck(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal)))
+      return NL2D_ERR_CUDA;
+    int par = e.parity;
+    for (int q = 0; q < nsteps; q++) {
+      k_ensemble_step<<<e.nctas, NTHREADS, kSmemBytes, e.stream>>>(
+          e.d_desc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
+      par = 1 - par;
+      if (checksum_every > 0 && (q + 1) % checksum_every == 0)
+        k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(
+            e.d_desc, par, e.ndom, e.d_sums + (size_t)((q + 1) / checksum_every - 1) * e.ndom * 3);
+    }
+    if (!ck(cudaStreamEndCapture(e.stream, &g))) return NL2D_ERR_CUDA;
+    const bool ok = ck(cudaGraphInstantiate(&e.graph, g, 0));
+    cudaGraphDestroy(g);
+    if (!ok) return NL2D_ERR_CUDA;
+    memcpy(e.graph_key, key, sizeof key);
+  }
+  cudaEvent_t e0, e1;
+  if (!ck(cudaEventCreate(&e0)) || !ck(cudaEventCreate(&e1))) return NL2D_ERR_CUDA;
+  cudaStreamSynchronize(e.stream);
+  cudaEventRecord(e0, e.stream);
+  const bool launched = ck(cudaGraphLaunch(e.graph, e.stream));
+  cudaEventRecord(e1, e.stream);
+  const bool done = ck(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!launched || !done) return NL2D_ERR_CUDA;
+  if (ms_out) *ms_out = ms;
+  e.parity = (e.parity + nsteps) & 1;
+  if (nsums > 0 && !ck(cudaMemcpy(checksums_out, e.d_sums, (size_t)nsums * e.ndom * 3 * 8,
+                                  cudaMemcpyDeviceToHost)))
+    return NL2D_ERR_CUDA;
+  return NL2D_OK;
+}
+
+int nl2d_ens_read(int dom, double* sshn_t, double* un, double* vn) {
+  Ens& e = g_ens;
+  if (dom < 0 || dom >= e.ndom) return NL2D_ERR_ARGS;
+  const DomainHost& D = e.dom[dom];
+  const size_t n = (size_t)D.W * D.H;
+  cudaStreamSynchronize(e.stream);
+  double* src[3] = {e.sn[e.parity] + D.off, e.un[e.parity] + D.off, e.vn[e.parity] + D.off};
+  double* dst[3] = {sshn_t, un, vn};
+  for (int k = 0; k < 3; k++)
+    if (dst[k] && !ck(cudaMemcpy(dst[k], src[k], n * 8, cudaMemcpyDeviceToHost)))
+      return NL2D_ERR_CUDA;
+  return NL2D_OK;
+}
+
+int nl2d_ens_info(long long* cells, int* ntiles, int* nctas) {
+  const Ens& e = g_ens;
+  long long c = 0;
+  for (const DomainHost& D : e.dom) c += (long long)(D.xe - D.xs + 1) * (D.ye - D.ys + 1);
+  if (cells) *cells = c;
+  if (ntiles) *ntiles = e.ntiles;
+  if (nctas) *nctas = e.nctas;
+  return NL2D_OK;
+}
+
+int nl2d_ens_reset(void) {
+  Ens& e = g_ens;
+  if (e.ndom < 1) return NL2D_ERR_STATE;
+  const size_t bytes = e.total * sizeof(double);
+  cudaStreamSynchronize(e.stream);
+  for (double* p : {e.sn[0], e.sn[1], e.un[0], e.un[1], e.vn[0], e.vn[1]})
+    if (!ck(cudaMemset(p, 0, bytes))) return NL2D_ERR_CUDA;
+  e.parity = 0;
+  return NL2D_OK;
+}
+
+void nl2d_ens_destroy(void) { ens_free(); }
+
+}  // extern "C"

@@ -238,3 +238,36 @@ def gpu_run_graph(lib, m, nsteps, nit000=1, every=0):
     P.check(lib.nl2d_run_steps(nit000, nsteps, every, dptr(out)), "nl2d_run_steps")
     gpu_read_all(lib, m)
     return out[:3 * nsums].reshape(-1, 3)
+
+
+def ensemble_oracle_run(dom, nsteps, rdt=5.0, oracle=None, every=0):
+    """Runs one ensemble domain (a build_domain() dict, at rest) through the
+    oracle with its tide; returns (model, checksums list)."""
+    import ctypes as C
+    lib = oracle or load_oracle()
+    fn = lib.oracle_invoke_time_step_tide
+    fn.argtypes = STEP_ARGTYPES + [C.c_double, C.c_double]
+    fn.restype = None
+    w, h, xs, xe, ys, ye = dom["dims"]
+    m = Model.__new__(Model)
+    m.jpiglo, m.jpjglo = xe + 2, ye + 2
+    m.xs, m.xe, m.ys, m.ye, m.width, m.height = xs, xe, ys, ye, w, h
+    shp = (h, w)
+    m.f = {k: np.zeros(shp, np.float64) for k in FIELDS}
+    m.grid = {k: np.zeros(shp, np.float64) for k in GRID if k != "tmask"}
+    m.grid["tmask"] = np.ascontiguousarray(dom["tmask"], np.int32).copy()
+    for k in ("dx_u", "dx_v", "dx_t", "dy_u", "dy_v", "dy_t"):
+        m.grid[k][:] = 1000.0
+    for k in ("area_t", "area_u", "area_v"):
+        m.grid[k][:] = 1.0e6
+    m.grid["gphiu"][:] = 50.0
+    m.grid["gphiv"][:] = 50.0
+    m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = dom["ht"], dom["hu"], dom["hv"]
+    m.rdt, m.cbfr, m.visc = rdt, 1.5e-4, 0.1
+    amp, per = dom["tide"]
+    sums = []
+    for k in range(nsteps):
+        fn(*(m.step_args(1 + k) + [amp, per]))
+        if every and (k + 1) % every == 0:
+            sums.append(model_checksums(m, lib))
+    return m, sums

@@ -1,0 +1,64 @@
+"""The ensemble form: many domains, one persistent launch per step.  Every
+domain must be bit-identical to the oracle's step with that domain's tide
+(which is the reference's step when amplitude 0.2 m and period 12.42 h)."""
+import numpy as np
+import pytest
+
+import nl2d_testlib as T
+from test_oracle import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def small_specs():
+    specs = []
+    rng = np.random.default_rng(17)
+    for k, side in enumerate("SNEWSNEW"):
+        specs.append({"nx": int(rng.integers(12, 45)), "ny": int(rng.integers(12, 45)),
+                      "depth_seed": 100 + k, "tide_amp": float(rng.uniform(0.05, 0.5)),
+                      "tide_period_h": float(rng.uniform(10.0, 14.0)), "open_side": side})
+    specs[0]["tide_amp"], specs[0]["tide_period_h"] = 0.2, 12.42  # the reference's tide
+    return specs
+
+
+@pytest.fixture(scope="module")
+def domains():
+    from psyclonebench_gb300.ensemble import build_domain
+    return [build_domain(s) for s in small_specs()]
+
+
+@pytest.mark.parametrize("cps,policy", [(2, 0), (1, 1)])
+def test_ensemble_matches_oracle(gpulib, oracle, domains, cps, policy):
+    from psyclonebench_gb300.ensemble import Ensemble
+    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    ens.schedule(cps, policy, 4.0)
+    ms, sums = ens.run(1, 90, checksum_every=30)
+    assert sums.shape == (3, len(domains), 3)
+    for k, d in enumerate(domains):
+        want, want_sums = T.ensemble_oracle_run(d, 90, oracle=oracle, every=30)
+        sn, un, vn = ens.read(k)
+        for name, got in (("sshn_t", sn), ("un", un), ("vn", vn)):
+            x0, x1, y0, y1 = T.regions(want)["t"]
+            assert bits_equal(got[y0 - 1:y1 + 1, x0 - 1:x1 + 2],
+                              want.f[name][y0 - 1:y1 + 1, x0 - 1:x1 + 2]), (k, name)
+        w = np.array([[s["sshn_t"], s["un"], s["vn"]] for s in want_sums])
+        np.testing.assert_allclose(sums[:, k, :], w, rtol=1e-10, atol=1e-300)
+    ens.close()
+
+
+def test_autotuner_picks_a_schedule(gpulib, domains, tmp_path, monkeypatch):
+    from psyclonebench_gb300 import autotune
+    from psyclonebench_gb300.ensemble import Ensemble
+    monkeypatch.setenv("NL2D_TUNE_CACHE", str(tmp_path))
+    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    choice = autotune.tune(ens, steps=2)
+    assert not choice["cached"] and len(choice["timings"]) == len(autotune.CANDIDATES)
+    again = autotune.tune(ens, steps=2)
+    assert again["cached"] and again["policy"] == choice["policy"]
+    # the tuned schedule gives the same bits as any other
+    a_ms, a = ens.run(1, 20, checksum_every=20)
+    ens.reset()
+    ens.schedule(1, 0, 0.0)
+    b_ms, b = ens.run(1, 20, checksum_every=20)
+    assert bits_equal(a, b)
+    ens.close()
