@@ -185,6 +185,7 @@ def time_cpu(m, nsteps, target_s=None):
     return done, time.perf_counter() - t0, kind, desc
 
 
+SEQ_SAMPLE = 32  # domains timed one at a time for the ensemble comparison
 BATHY_RDT = 5.0  # s, for the 50-500 m bathymetry configurations
 MIXED_BYTES_PER_CELL = 48  # read ssh pair 8 + un 4 + vn 4 + ht/hu/hv 12 + mask 4; write 16
 
@@ -239,6 +240,78 @@ def run_forms(lib, n, steps=1000, warmup=3):
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm, "alg_bytes_per_cell": MIXED_BYTES_PER_CELL},
         "error_vs_fp64": err, "dtype": "f32 + compensated-f32 ssh"}}
+
+
+def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
+    """Config 3: 512 seeded domains (log-uniform 64..1024 per axis, Fourier
+    bathymetry 50-500 m, tide 0.05-0.5 m / 10-14 h, random open side), one
+    persistent launch per step; with N ranks each takes a cell-balanced
+    shard of whole domains (weak scaling, no collective)."""
+    from psyclonebench_gb300 import autotune
+    from psyclonebench_gb300.ensemble import Ensemble, build_domain, shard_domains
+    from psyclonebench_gb300.workloads import ensemble_domains
+    specs = ensemble_domains(ndom, seed)
+    mine = shard_domains(specs, world)[rank] if world > 1 else list(range(ndom))
+    doms = [build_domain(specs[k]) for k in mine]
+    ens = Ensemble(doms, rdt=BATHY_RDT, lib=lib)
+    tune = autotune.tune(ens, steps=3)
+    ens.run(1, 1)
+    ms, _ = ens.run(2, steps)
+    cells, ntiles, nctas = ens.info()
+    ens.set_precision(1)
+    ens.run(1, 1)
+    ms_mix, _ = ens.run(2, steps)
+    ens.close()
+    # The same domains one at a time through the single-domain FP64 path (a
+    # sample of SEQ_SAMPLE domains, each timed as one graph launch of
+    # `steps` fused steps): what running the ensemble without the
+    # persistent kernel costs.
+    seq_ms, seq_cells = 0.0, 0
+    import nl2d_testlib as T
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300.ensemble import Ensemble as _E  # noqa: F401
+    sample = doms[:SEQ_SAMPLE]
+    for d in sample:
+        w, h, xs, xe, ys, ye = d["dims"]
+        m = T.Model.__new__(T.Model)
+        m.xs, m.xe, m.ys, m.ye, m.width, m.height = xs, xe, ys, ye, w, h
+        m.f = {k: np.zeros((h, w)) for k in T.FIELDS}
+        m.grid = {k: np.zeros((h, w)) for k in T.GRID if k != "tmask"}
+        m.grid["tmask"] = np.ascontiguousarray(d["tmask"], np.int32)
+        for k in ("dx_u", "dx_v", "dx_t", "dy_u", "dy_v", "dy_t"):
+            m.grid[k][:] = 1000.0
+        for k in ("area_t", "area_u", "area_v"):
+            m.grid[k][:] = 1.0e6
+        m.grid["gphiu"][:] = 50.0
+        m.grid["gphiv"][:] = 50.0
+        m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = d["ht"], d["hu"], d["hv"]
+        m.rdt, m.cbfr, m.visc = BATHY_RDT, 1.5e-4, 0.1
+        T.gpu_register(lib, m)
+        t = ctypes.c_double(0.0)
+        P.check(lib.nl2d_timed_run(1, 2, ctypes.byref(t)), "seq warm-up")
+        P.check(lib.nl2d_timed_run(3, steps, ctypes.byref(t)), "seq run")
+        seq_ms += t.value
+        seq_cells += (xe - xs + 1) * (ye - ys + 1)
+    lib.nl2d_finalize()
+    ens_s = Ensemble(sample, rdt=BATHY_RDT, lib=lib)
+    ens_s.schedule(tune["ctas_per_sm"], tune["policy"], tune["boundary_weight"])
+    ens_s.run(1, 1)
+    ms_s, _ = ens_s.run(2, steps)
+    ens_s.close()
+    return {"workload": "nemolite2d_ensemble_%d_domains_seed%d_rdt5" % (ndom, seed),
+            "domains_this_rank": len(mine), "cells_this_rank": cells, "tiles": ntiles,
+            "persistent_ctas": nctas, "steps": steps,
+            "fp64": {"ms_per_step": ms / steps, "value": cells / (ms / steps * 1e-3) / 1e6},
+            "mixed": {"ms_per_step": ms_mix / steps,
+                      "value": cells / (ms_mix / steps * 1e-3) / 1e6},
+            "unit": "Mcell-steps/s",
+            "one_domain_at_a_time_fp64": {
+                "sample_domains": len(sample), "sample_cells": seq_cells,
+                "value": seq_cells / (seq_ms / steps * 1e-3) / 1e6,
+                "persistent_value_same_sample": seq_cells / (ms_s / steps * 1e-3) / 1e6,
+                "speedup_persistent_vs_sequential": seq_ms / ms_s},
+            "schedule": {k: tune[k] for k in ("ctas_per_sm", "policy", "boundary_weight",
+                                              "cached")}}
 
 
 def run_reference(args, rank, world):
@@ -343,6 +416,10 @@ def run_ours(args, rank, world, local):
     forms = None
     if rank == 0 and not args.no_forms:
         forms = run_forms(lib, n)
+        ens = run_ensemble(lib)
+        ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
+        ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
+        forms["ensemble"] = ens
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

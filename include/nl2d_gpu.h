@@ -203,6 +203,10 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every,
 /* Current sshn_t, un, vn of one domain (width x height host arrays; any may
  * be NULL). */
 int nl2d_ens_read(int dom, double *sshn_t, double *un, double *vn);
+/* Form of later runs: 0 FP64 (bit-identical to the reference), 1 mixed
+ * precision (FP32 momentum, compensated-FP32 ssh).  A change of form
+ * restarts every domain from rest. */
+int nl2d_ens_set_precision(int precision);
 /* Puts every domain back at rest (step 0). */
 int nl2d_ens_reset(void);
 /* Interior cells over all domains, tiles, persistent CTAs. */

@@ -58,6 +58,7 @@ EXPORTS = {
     "nl2d_ens_read": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_ens_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),
     "nl2d_ens_reset": (ctypes.c_int, []),
+    "nl2d_ens_set_precision": (ctypes.c_int, [ctypes.c_int]),
     "nl2d_ens_destroy": (None, []),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),

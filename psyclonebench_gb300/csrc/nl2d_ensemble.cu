@@ -21,9 +21,75 @@
 
 #include "../../include/nl2d_gpu.h"
 #include "nl2d_fused_tile.cuh"
+#include "nl2d_mixed_tile.cuh"
 
 namespace nl2d {
 namespace {
+
+// One domain of a mixed-precision ensemble.
+struct EnsMixDomain {
+  MixedFields mf;
+  MixedState ms[2];
+  Fields f;  // FP64 arrays the mixed step reads where no step writes
+  Dims d;
+  mixk::MixConst k;
+};
+
+__global__ void __launch_bounds__(mixk::TX* mixk::TY)
+    k_ensemble_mixed_step(const EnsMixDomain* __restrict__ doms, const int4* __restrict__ tiles,
+                          const int* __restrict__ first, int parity,
+                          const double* __restrict__ tides) {
+  const int t1 = first[blockIdx.x + 1];
+  for (int t = first[blockIdx.x]; t < t1; t++) {
+    const int4 tl = tiles[t];
+    const EnsMixDomain& D = doms[tl.x];
+    __syncthreads();
+    mixk::mixed_tile(D.mf, D.ms[parity], D.f, D.d, D.k, tides[tl.x], tl.y, tl.z);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_ensemble_mixed_checksums(const EnsMixDomain* __restrict__ doms, int parity,
+                               double* __restrict__ out) {
+  const int dom = blockIdx.x, fld = blockIdx.y;
+  const EnsMixDomain& D = doms[dom];
+  const MixedState& st = D.ms[parity];
+  const int x0 = D.d.xs, y0 = D.d.ys;
+  const int x1 = fld == 1 ? D.d.xe - 1 : D.d.xe, y1 = fld == 2 ? D.d.ye - 1 : D.d.ye;
+  const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < nx * ny; t += blockDim.x) {
+    const int j = t / nx, i = t - j * nx;
+    const size_t c = (size_t)(y0 + j) * D.d.width + (x0 + i);
+    acc += fld == 0 ? fabs((double)st.sn_in[c].x + (double)st.sn_in[c].y)
+                    : fabs((double)(fld == 1 ? st.un_in[c] : st.vn_in[c]));
+  }
+  __shared__ double wp[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) wp[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < 8 ? wp[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[(size_t)dom * 3 + fld] = acc;
+  }
+}
+
+__global__ void k_mixed_statics(const double* __restrict__ ht, const double* __restrict__ hu,
+                                const double* __restrict__ hv, float* __restrict__ fht,
+                                float* __restrict__ fhu, float* __restrict__ fhv,
+                                float* __restrict__ rhu, float* __restrict__ rhv, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x) {
+    fht[t] = (float)ht[t];
+    fhu[t] = (float)hu[t];
+    fhv[t] = (float)hv[t];
+    rhu[t] = (float)(1.0 / hu[t]);  // ssha_u = ssha_v = 0 at rest
+    rhv[t] = (float)(1.0 / hv[t]);
+  }
+}
 
 // Ensemble: a persistent grid walks a tile list spanning many independent
 // domains; CTA b takes tiles [first[b], first[b+1]).  `tides` holds this
@@ -102,6 +168,12 @@ struct Ens {
   cudaGraphExec_t graph = nullptr;
   int graph_key[5] = {-1, -1, -1, -1, -1};
   bool built = false;
+  // mixed-precision form
+  int precision = 0;
+  float2* msn[2] = {};
+  float *mun[2] = {}, *mvn[2] = {};
+  float *mht = nullptr, *mhu = nullptr, *mhv = nullptr, *mrhu = nullptr, *mrhv = nullptr;
+  EnsMixDomain* d_mdesc = nullptr;
 };
 
 Ens g_ens;
@@ -122,6 +194,20 @@ void ens_free() {
     cudaFree(*p);
     *p = nullptr;
   }
+  for (int b = 0; b < 2; b++) {
+    cudaFree(e.msn[b]);
+    cudaFree(e.mun[b]);
+    cudaFree(e.mvn[b]);
+    e.msn[b] = nullptr;
+    e.mun[b] = e.mvn[b] = nullptr;
+  }
+  for (float** p : {&e.mht, &e.mhu, &e.mhv, &e.mrhu, &e.mrhv}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(e.d_mdesc);
+  e.d_mdesc = nullptr;
+  e.precision = 0;
   cudaFree(e.tmask);
   cudaFree(e.d_desc);
   cudaFree(e.d_tiles);
@@ -173,7 +259,7 @@ double tide_at(const DomainHost& D, int istep, double rdt) {
 }
 
 // Tile list and static schedule.
-bool build_schedule() {
+bool build_schedule(int TXv, int TYv) {
   Ens& e = g_ens;
   struct T {
     int dom, i0, j0;
@@ -183,15 +269,15 @@ bool build_schedule() {
   for (int k = 0; k < e.ndom; k++) {
     const DomainHost& D = e.dom[k];
     const int nx = D.xe - D.xs + 3, ny = D.ye - D.ys + 2;
-    const int ntx = (nx + TX - 1) / TX, nty = (ny + TY - 1) / TY;
+    const int ntx = (nx + TXv - 1) / TXv, nty = (ny + TYv - 1) / TYv;
     for (int by = 0; by < nty; by++)
       for (int bx = 0; bx < ntx; bx++) {
-        const int cx = std::min(TX, nx - bx * TX), cy = std::min(TY, ny - by * TY);
+        const int cx = std::min(TXv, nx - bx * TXv), cy = std::min(TYv, ny - by * TYv);
         // boundary tiles run the general per-cell path on their edge cells
         double edge = 0.0;
         if (bx == 0 || bx == ntx - 1) edge += cy;
         if (by == 0 || by == nty - 1) edge += cx;
-        tiles.push_back({k, D.xs - 1 + bx * TX, D.ys - 1 + by * TY,
+        tiles.push_back({k, D.xs - 1 + bx * TXv, D.ys - 1 + by * TYv,
                          (double)(cx * cy) + e.boundary_weight * edge});
       }
   }
@@ -289,6 +375,56 @@ bool build_descriptors() {
   e.d_desc = nullptr;
   if (!ck(cudaMalloc(&e.d_desc, sizeof(EnsDomain) * e.ndom))) return false;
   return ck(cudaMemcpy(e.d_desc, desc.data(), sizeof(EnsDomain) * e.ndom,
+                       cudaMemcpyHostToDevice));
+}
+
+bool build_mixed() {
+  Ens& e = g_ens;
+  const size_t n = e.total;
+  if (!e.msn[0]) {
+    for (int b = 0; b < 2; b++)
+      if (!ck(cudaMalloc(&e.msn[b], n * sizeof(float2))) ||
+          !ck(cudaMalloc(&e.mun[b], n * 4)) || !ck(cudaMalloc(&e.mvn[b], n * 4)))
+        return false;
+    for (float** p : {&e.mht, &e.mhu, &e.mhv, &e.mrhu, &e.mrhv})
+      if (!ck(cudaMalloc(p, n * 4))) return false;
+  }
+  for (int b = 0; b < 2; b++)
+    if (!ck(cudaMemset(e.msn[b], 0, n * sizeof(float2))) || !ck(cudaMemset(e.mun[b], 0, n * 4)) ||
+        !ck(cudaMemset(e.mvn[b], 0, n * 4)))
+      return false;
+  k_mixed_statics<<<152 * 8, 256, 0, e.stream>>>(e.ht, e.hu, e.hv, e.mht, e.mhu, e.mhv, e.mrhu,
+                                                 e.mrhv, n);
+  if (!ck(cudaGetLastError())) return false;
+  std::vector<EnsMixDomain> desc(e.ndom);
+  for (int k = 0; k < e.ndom; k++) {
+    const DomainHost& D = e.dom[k];
+    EnsMixDomain& x = desc[k];
+    memset(&x, 0, sizeof x);
+    const size_t o = D.off;
+    x.mf = MixedFields{e.mht + o, e.mhu + o, e.mhv + o, e.mrhu + o, e.mrhv + o};
+    for (int p = 0; p < 2; p++) {
+      x.ms[p].sn_in = e.msn[p] + o;
+      x.ms[p].un_in = e.mun[p] + o;
+      x.ms[p].vn_in = e.mvn[p] + o;
+      x.ms[p].sn_out = e.msn[1 - p] + o;
+      x.ms[p].un_out = e.mun[1 - p] + o;
+      x.ms[p].vn_out = e.mvn[1 - p] + o;
+    }
+    x.f.tmask = e.tmask + o;
+    x.f.sshn_u = x.f.sshn_v = x.f.ua = x.f.va = x.f.ssha_u = x.f.ssha_v = e.zero + o;
+    x.d = Dims{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
+    UniformMetrics um{};
+    um.area_t = um.area_u = um.area_v = D.dx * D.dy;
+    um.dx_u = um.dx_v = um.dx_t = D.dx;
+    um.dy_u = um.dy_v = um.dy_t = D.dy;
+    um.sin_u = um.sin_v = std::sin(D.gphi * e.sc.d2r);
+    x.k = mixk::make_mix_const(e.sc, um);
+  }
+  cudaFree(e.d_mdesc);
+  e.d_mdesc = nullptr;
+  if (!ck(cudaMalloc(&e.d_mdesc, sizeof(EnsMixDomain) * e.ndom))) return false;
+  return ck(cudaMemcpy(e.d_mdesc, desc.data(), sizeof(EnsMixDomain) * e.ndom,
                        cudaMemcpyHostToDevice));
 }
 
@@ -395,7 +531,12 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
                            (int)kSmemBytes);
       attr = true;
     }
-    if (!build_descriptors() || !build_schedule()) return NL2D_ERR_CUDA;
+    if (e.precision == 1) {
+      if (!build_mixed() || !build_schedule(mixk::TX, mixk::TY)) return NL2D_ERR_CUDA;
+    } else if (!build_descriptors() || !build_schedule(TX, TY)) {
+      return NL2D_ERR_CUDA;
+    }
+    e.parity = 0;
     e.built = true;
   }
   if (nsteps == 0) return NL2D_OK;
@@ -427,7 +568,7 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     if (!ck(cudaMalloc(&e.d_sums, nsum_vals * 8))) return NL2D_ERR_CUDA;
     e.sums_cap = nsum_vals;
   }
-  const int key[5] = {nsteps, checksum_every, e.parity, e.nctas, e.policy};
+  const int key[5] = {nsteps, checksum_every, e.parity, e.nctas, e.policy * 2 + e.precision};
   if (!(e.graph && memcmp(key, e.graph_key, sizeof key) == 0)) {
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
@@ -436,12 +577,23 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
       return NL2D_ERR_CUDA;
     int par = e.parity;
     for (int q = 0; q < nsteps; q++) {
-      k_ensemble_step<<<e.nctas, NTHREADS, kSmemBytes, e.stream>>>(
-          e.d_desc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
-      par = 1 - par;
-      if (checksum_every > 0 && (q + 1) % checksum_every == 0)
-        k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(
-            e.d_desc, par, e.ndom, e.d_sums + (size_t)((q + 1) / checksum_every - 1) * e.ndom * 3);
+      double* sums = e.d_sums + (size_t)((q + 1) / std::max(checksum_every, 1) - 1) * e.ndom * 3;
+      const bool want_sums = checksum_every > 0 && (q + 1) % checksum_every == 0;
+      if (e.precision == 1) {
+        k_ensemble_mixed_step<<<e.nctas, dim3(mixk::TX, mixk::TY), 0, e.stream>>>(
+            e.d_mdesc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
+        par = 1 - par;
+        if (want_sums)
+          k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
+                                                                            sums);
+      } else {
+        k_ensemble_step<<<e.nctas, dim3(TX, ROWS_PER_PASS), kSmemBytes, e.stream>>>(
+            e.d_desc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
+        par = 1 - par;
+        if (want_sums)
+          k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,
+                                                                      sums);
+      }
     }
     if (!ck(cudaStreamEndCapture(e.stream, &g))) return NL2D_ERR_CUDA;
     const bool ok = ck(cudaGraphInstantiate(&e.graph, g, 0));
@@ -475,6 +627,24 @@ int nl2d_ens_read(int dom, double* sshn_t, double* un, double* vn) {
   const DomainHost& D = e.dom[dom];
   const size_t n = (size_t)D.W * D.H;
   cudaStreamSynchronize(e.stream);
+  if (e.precision == 1) {  // FP64 image of the mixed state
+    std::vector<float2> s2(n);
+    std::vector<float> f(n);
+    if (sshn_t) {
+      if (!ck(cudaMemcpy(s2.data(), e.msn[e.parity] + D.off, n * sizeof(float2),
+                         cudaMemcpyDeviceToHost)))
+        return NL2D_ERR_CUDA;
+      for (size_t t = 0; t < n; t++) sshn_t[t] = (double)s2[t].x + (double)s2[t].y;
+    }
+    float* fsrc[2] = {e.mun[e.parity] + D.off, e.mvn[e.parity] + D.off};
+    double* fdst[2] = {un, vn};
+    for (int k = 0; k < 2; k++) {
+      if (!fdst[k]) continue;
+      if (!ck(cudaMemcpy(f.data(), fsrc[k], n * 4, cudaMemcpyDeviceToHost))) return NL2D_ERR_CUDA;
+      for (size_t t = 0; t < n; t++) fdst[k][t] = (double)f[t];
+    }
+    return NL2D_OK;
+  }
   double* src[3] = {e.sn[e.parity] + D.off, e.un[e.parity] + D.off, e.vn[e.parity] + D.off};
   double* dst[3] = {sshn_t, un, vn};
   for (int k = 0; k < 3; k++)
@@ -493,9 +663,26 @@ int nl2d_ens_info(long long* cells, int* ntiles, int* nctas) {
   return NL2D_OK;
 }
 
+int nl2d_ens_set_precision(int precision) {
+  Ens& e = g_ens;
+  if (precision != 0 && precision != 1) return NL2D_ERR_ARGS;
+  if (e.ndom < 1) return NL2D_ERR_STATE;
+  if (precision != e.precision) {
+    e.precision = precision;
+    e.built = false;  // the next run starts this form from rest
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    e.graph = nullptr;
+  }
+  return NL2D_OK;
+}
+
 int nl2d_ens_reset(void) {
   Ens& e = g_ens;
   if (e.ndom < 1) return NL2D_ERR_STATE;
+  if (e.precision == 1) {
+    e.built = false;  // mixed state is re-zeroed when rebuilt
+    return NL2D_OK;
+  }
   const size_t bytes = e.total * sizeof(double);
   cudaStreamSynchronize(e.stream);
   for (double* p : {e.sn[0], e.sn[1], e.un[0], e.un[1], e.vn[0], e.vn[1]})

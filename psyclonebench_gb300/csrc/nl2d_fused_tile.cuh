@@ -233,7 +233,9 @@ constexpr int P1X = TX + 2, P1Y = TY + 2;
 constexpr int S1 = P1X * P1Y;          // 34 x 10 positions
 enum { A_SN, A_UN, A_VN, A_HU, A_HV, A_SU, A_SV, A_HUS, A_HVS, N_A0 };
 enum { B_FLXU, B_FLXV, B_GX, B_GY, B_FXU, B_FYV, B_VSC, B_FYU, B_QY, B_UWC, B_FXV, B_QX, N_B1 };
-constexpr size_t kSmemBytes = sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * S0;
+// + the mask, and the list of the tile's general (non-regular) cells
+constexpr size_t kSmemBytes =
+    sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * (S0 + TX * TY + 1);
 
 // One tile of the fused step: cells [i0, i0+TX) x [j0, j0+TY) of the copy
 // region of one domain.  `tide` is this step's bc_ssh value.
@@ -244,6 +246,8 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   double* a0 = smem;                 // [N_A0][S0]
   double* b1 = smem + N_A0 * S0;     // [N_B1][S1]
   int* mk = (int*)(b1 + N_B1 * S1);  // [S0]
+  int* glist = mk + S0;              // [TX * TY] general cells of this tile
+  int* gcount = glist + TX * TY;
 #define A(q, t) a0[(q) * S0 + (t)]
 #define B(q, t) b1[(q) * S1 + (t)]
 
@@ -254,6 +258,7 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   const double* __restrict__ vn = fs.vn_in;
   const int tid = threadIdx.y * TX + threadIdx.x;
 
+  if (tid == 0) *gcount = 0;
   // ---- phase 0: fields and the sshn_u / sshn_v this step reads ----
   for (int t = tid; t < S0; t += NTHREADS) {
     const int i = i0 - HALO + t % SX, j = j0 - HALO + t / SX;
@@ -369,7 +374,13 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
       for (int di = -1; di <= 1; di++) regular &= mk[q + dj * SX + di] > 0;
   }
 
-  if (regular) {
+  if (!regular) {
+    // queued for the packed general pass below, so that a warp holding a
+    // few boundary cells does not run both paths
+    glist[atomicAdd(gcount, 1)] = row * TX + threadIdx.x;
+    continue;
+  }
+  {
     // Wet cell whose 3x3 neighbourhood is wet: continuity without bc_ssh,
     // unmasked momentum, no solid-wall or Flather change.
     const double snc = A(A_SN, q), Hu = A(A_HUS, q), Hv = A(A_HVS, q);
@@ -413,7 +424,16 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
     continue;
   }
 
-  // ---- general cell: the reference's per-point code, in its order ----
+  }  // rows of this thread
+  __syncthreads();
+
+  // ---- general cells: the reference's per-point code, in its order ----
+  const int ngen = *gcount;
+  for (int g = tid; g < ngen; g += NTHREADS) {
+  const int row = glist[g] / TX, col = glist[g] - (glist[g] / TX) * TX;
+  const int i = i0 + col, j = j0 + row;
+  const int c = j * W + i;
+  const int q = (row + HALO) * SX + (col + HALO);
   double* su_tile = &A(A_SU, 0);
   double* sv_tile = &A(A_SV, 0);
   Ctx x;
@@ -479,7 +499,7 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
     }
   }
   fs.vn_out[c] = va;
-  }  // rows of this thread
+  }  // general cells
 #undef A
 #undef B
 }

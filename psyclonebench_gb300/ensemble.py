@@ -111,7 +111,12 @@ class Ensemble:
         ms = ctypes.c_double(0.0)
         self._check(self.lib.nl2d_ens_run(istep0, nsteps, checksum_every, _dp(out),
                                           ctypes.byref(ms)), "nl2d_ens_run")
-        return ms.value, out[:nsums * len(self.domains) * 3].reshape(nsums, -1, 3)
+        return ms.value, out[:nsums * len(self.domains) * 3].reshape(nsums, len(self.domains), 3)
+
+    def set_precision(self, precision):
+        """0: FP64 (bit-identical to the reference); 1: mixed.  Restarts
+        every domain from rest."""
+        self._check(self.lib.nl2d_ens_set_precision(precision), "nl2d_ens_set_precision")
 
     def reset(self):
         self._check(self.lib.nl2d_ens_reset(), "nl2d_ens_reset")

@@ -24,15 +24,19 @@ def fourier_depth(width, height, seed, mean=275.0, nmodes=16, dx=1000.0, dy=1000
     m[zero] = 1
     a = rng.uniform(10.0, 35.0, size=nmodes)
     ph = rng.uniform(0.0, 2.0 * math.pi, size=nmodes)
-    jj, ii = np.mgrid[0:height, 0:width].astype(np.float64)
+    x_t = np.arange(width, dtype=np.float64) * dx
+    y_t = np.arange(height, dtype=np.float64) * dy
 
     def depth(x, y):
-        h = np.full(x.shape, mean)
+        # cos(A + B) = cos A cos B - sin A sin B with A along x, B along y:
+        # each mode is two outer products of 1-D vectors.
+        h = np.full((y.size, x.size), mean)
         for k in range(nmodes):
-            h += a[k] * np.cos(2.0 * math.pi * (m[k] * x / lx + n[k] * y / ly) + ph[k])
+            A = 2.0 * math.pi * m[k] * x / lx + ph[k]
+            B = 2.0 * math.pi * n[k] * y / ly
+            h += a[k] * (np.outer(np.cos(B), np.cos(A)) - np.outer(np.sin(B), np.sin(A)))
         return np.maximum(np.clip(h, 50.0, 500.0), 20.0)
 
-    x_t, y_t = ii * dx, jj * dy
     return depth(x_t, y_t), depth(x_t + 0.5 * dx, y_t), depth(x_t, y_t + 0.5 * dy)
 
 

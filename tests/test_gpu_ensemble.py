@@ -62,3 +62,26 @@ def test_autotuner_picks_a_schedule(gpulib, domains, tmp_path, monkeypatch):
     b_ms, b = ens.run(1, 20, checksum_every=20)
     assert bits_equal(a, b)
     ens.close()
+
+
+def test_mixed_ensemble_error_vs_fp64(gpulib, domains):
+    """The FP32 form of the ensemble stays within 1e-6 m ssh RMS of the
+    FP64 ensemble (itself bit-identical to the reference) after 300 steps."""
+    from psyclonebench_gb300.ensemble import Ensemble
+    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    ens.run(1, 300)
+    ref = [ens.read(k) for k in range(len(domains))]
+    ens.set_precision(1)
+    _, sums = ens.run(1, 300, checksum_every=300)
+    worst = 0.0
+    for k, d in enumerate(domains):
+        w, h, xs, xe, ys, ye = d["dims"]
+        got = ens.read(k)
+        diff = got[0][ys:ye + 1, xs:xe + 1] - ref[k][0][ys:ye + 1, xs:xe + 1]
+        worst = max(worst, float(np.sqrt(np.mean(diff * diff))))
+        assert np.isfinite(got[1]).all() and np.isfinite(got[2]).all()
+        np.testing.assert_allclose(sums[0, k, 0], np.abs(got[0][ys:ye + 1, xs:xe + 1]).sum(),
+                                   rtol=1e-10)
+    print("mixed ensemble worst per-domain ssh RMS error:", worst)
+    assert worst <= 1e-6
+    ens.close()
