@@ -272,14 +272,15 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
       vhu = f.hu[c];
       vhv = f.hv[c];
       mm = m[c];
-      su = f.sshn_u[c];
-      sv = f.sshn_v[c];
       // next_sshu_code / next_sshv_code (time_update_kern.c:90-155) over
-      // their loop ranges; other faces keep the stored value.
+      // their loop ranges; other faces keep the stored value, which is read
+      // only for them.
+      bool su_stored = true, sv_stored = true;
       if (j >= d.ys && j <= d.ye && i >= d.xs && i <= d.xe - 1) {
-        const int n = c + 1;
-        if (mm + m[n] > 0) {
-          if (mm * m[n] > 0) {
+        const int n = c + 1, mn = m[n];
+        if (mm + mn > 0) {
+          su_stored = false;
+          if (mm * mn > 0) {
             double rtmp1 = k.area_t * vsn + k.area_t * sn[n];
             su = dvc(half(rtmp1), k.area_u, k.r_area_u, k.fast_div);
           } else if (mm <= 0) {
@@ -290,9 +291,10 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
         }
       }
       if (j >= d.ys && j <= d.ye - 1 && i >= d.xs && i <= d.xe) {
-        const int n = c + W;
-        if (mm + m[n] > 0) {
-          if (mm * m[n] > 0) {
+        const int n = c + W, mn = m[n];
+        if (mm + mn > 0) {
+          sv_stored = false;
+          if (mm * mn > 0) {
             double rtmp1 = k.area_t * vsn + k.area_t * sn[n];
             sv = dvc(half(rtmp1), k.area_v, k.r_area_v, k.fast_div);
           } else if (mm <= 0) {
@@ -302,6 +304,8 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
           }
         }
       }
+      if (su_stored) su = f.sshn_u[c];
+      if (sv_stored) sv = f.sshn_v[c];
     }
     A(A_SN, t) = vsn;
     A(A_UN, t) = vun;
