@@ -213,6 +213,19 @@ int nl2d_ens_reset(void);
 int nl2d_ens_info(long long *cells, int *ntiles, int *nctas);
 void nl2d_ens_destroy(void);
 
+/* ---- learned emulator (no counterpart in the reference) ---- */
+
+/* 3x3 convolution (stride 1, zero padding 1) of `batch` NHWC BF16 images
+ * (H x W, cin channels) with weights [9][cout][cin] BF16 (tap = 3*dy+dx) on
+ * the tensor cores (tcgen05, FP32 accumulation); y (BF16) and/or y32
+ * (FP32) receive conv + bias, ReLU'd if relu.  cin in {16,32,48,64}, cout a
+ * multiple of 16 up to 64, W a multiple of 128.  All pointers are device
+ * pointers; err (device int) is set to 1 if the kernel's bounded wait for
+ * its MMAs ran out.  Queued on `stream`. */
+int nl2d_emu_conv3x3(const void *x, const void *w, const float *bias, void *y,
+                     float *y32, int batch, int H, int W, int cin, int cout,
+                     int relu, int *err, void *stream);
+
 /* Test hook: over n sampled doubles x (seeded), counts where the exact
  * FP64 helpers of the fused step differ from the IEEE expressions they
  * stand for — x / d (d in [2^-100, 2^100]), 0.5 * x, and the upwind pick

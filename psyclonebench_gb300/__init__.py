@@ -60,6 +60,8 @@ EXPORTS = {
     "nl2d_ens_reset": (ctypes.c_int, []),
     "nl2d_ens_set_precision": (ctypes.c_int, [ctypes.c_int]),
     "nl2d_ens_destroy": (None, []),
+    "nl2d_emu_conv3x3": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP] + [ctypes.c_int] * 6 +
+                         [_VP, _VP]),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }

@@ -23,6 +23,7 @@ SOURCES = [
     "nl2d_capi.cu",
     "nl2d_mixed.cu",
     "nl2d_ensemble.cu",
+    "nl2d_emu.cu",
 ]
 # The mixed-precision form has no bit-exactness contract: FMA contraction on.
 PER_FILE_FLAGS = {"nl2d_mixed.cu": ["-fmad=true"]}
