@@ -226,6 +226,51 @@ int nl2d_emu_conv3x3(const void *x, const void *w, const float *bias, void *y,
                      float *y32, int batch, int H, int W, int cin, int cout,
                      int relu, int *err, void *stream);
 
+/* wt[8 - tap][ci][cout] = w[tap][co][ci] (BF16): the weights of the
+ * input-gradient convolution. */
+int nl2d_emu_flip_transpose(const void *w, void *wt, int cout, int cin,
+                            void *stream);
+/* Adds the weight and bias gradients of a 3x3 convolution (FP32):
+ * dw[tap][co][ci] += sum_p dy[p][co] x[p + off(tap)][ci], db[co] += sum_p
+ * dy[p][co].  x [batch][H][W][cin], dy [batch][H][W][cout] BF16. */
+int nl2d_emu_conv_wgrad(const void *x, const void *dy, float *dw, float *db,
+                        int batch, int H, int W, int cin, int cout,
+                        void *stream);
+/* out = (y > 0) ? g : 0 (y, out BF16; g FP32), n elements. */
+int nl2d_emu_relu_bwd(const float *g, const void *y, void *out, long long n,
+                      void *stream);
+/* Mean-squared error of the first nc of cpad channels of pred [P][cpad]
+ * against target [P][nc]; grad (BF16, [P][cpad]); loss += mean. */
+int nl2d_emu_mse(const float *pred, const float *target, void *grad,
+                 float *loss, long long P, int nc, int cpad, void *stream);
+/* One Adam step (bias-corrected, step >= 1) on FP32 weights; w16 (BF16
+ * copy) may be NULL. */
+int nl2d_emu_adam(float *w, float *m, float *v, const float *g, void *w16,
+                  int n, float lr, float b1, float b2, float eps, int step,
+                  void *stream);
+
+/* Network inputs (BF16 [batch][HW][cpad]) and, if target != NULL, FP32
+ * targets [batch][HW][3] for snapshot pairs: sample b uses snapshot src[b]
+ * of domain dom[b] (snapshot src[b] + 1 is its successor) from snaps
+ * [n][HW][3] and statics [ndom][HW][2] (depth / 500, open-boundary
+ * indicator); forcing[b] is the tidal ssh at the target time; scale6 =
+ * state scales (3) then increment scales (3), host memory.  Device
+ * pointers otherwise. */
+int nl2d_emu_assemble(const float *snaps, const float *statics, const int *src,
+                      const int *dom, const float *forcing, const float *scale6,
+                      void *x, float *target, int HW, int cpad, int batch,
+                      void *stream);
+/* state[p][0..2] += inc[p][0..2] * inc_scale3[0..2] (inc is [P][cpad]). */
+int nl2d_emu_advance(float *state, const float *inc, const float *inc_scale3,
+                     long long P, int cpad, void *stream);
+/* Interior (ssh, u, v) of every ensemble domain (all the same size) into a
+ * device FP32 array [dom][ny][nx][3]; FP64 form only. */
+int nl2d_ens_export_interior(float *d_out);
+
+/* Sets the interior (ssh, u, v) of every ensemble domain from a device FP32
+ * array [dom][ny][nx][3] (the emulator hands states back to the solver). */
+int nl2d_ens_import_interior(const float *d_in);
+
 /* Test hook: over n sampled doubles x (seeded), counts where the exact
  * FP64 helpers of the fused step differ from the IEEE expressions they
  * stand for — x / d (d in [2^-100, 2^100]), 0.5 * x, and the upwind pick

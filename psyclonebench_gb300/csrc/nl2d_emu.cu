@@ -196,6 +196,177 @@ __global__ void __launch_bounds__(kThreads)
                  "r"(kTmemCols));
 }
 
+// Tap-flipped, channel-transposed weights for the input gradient:
+// wt[8 - tap][ci][co] = w[tap][co][ci].
+__global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w,
+                                 __nv_bfloat16* __restrict__ wt, int cout, int cin) {
+  const int n = 9 * cout * cin;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int tap = t / (cout * cin), rem = t - tap * cout * cin;
+    const int co = rem / cin, ci = rem - co * cin;
+    wt[((size_t)(8 - tap) * cin + ci) * cout + co] = w[t];
+  }
+}
+
+// Weight and bias gradients of a 3x3 convolution, FP32 on the CUDA cores:
+// dw[tap][co][ci] += sum_p dy[p][co] * x[p + off(tap)][ci],
+// db[co] += sum_p dy[p][co].  Block (tap, chunk of rows); each thread owns
+// a fixed set of (co, ci) pairs; a row segment of dy and of the shifted x
+// is staged in shared memory; results are added atomically.
+constexpr int kWgThreads = 256, kWgPix = 64;
+__global__ void __launch_bounds__(kWgThreads)
+    k_conv_wgrad(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
+                 float* __restrict__ dw, float* __restrict__ db, int B, int H, int W, int cin,
+                 int cout, int rows_per_block) {
+  __shared__ float sx[kWgPix][64 + 1];
+  __shared__ float sd[kWgPix][64 + 1];
+  const int tap = blockIdx.x, dyo = tap / 3 - 1, dxo = tap % 3 - 1;
+  const int npairs = cout * cin;
+  float acc[12];
+#pragma unroll
+  for (int q = 0; q < 12; q++) acc[q] = 0.f;
+  float bacc = 0.f;
+  const long long rows_total = (long long)B * H;
+  const long long r0 = (long long)blockIdx.y * rows_per_block;
+  for (long long rr = r0; rr < r0 + rows_per_block && rr < rows_total; rr++) {
+    const int img = (int)(rr / H), row = (int)(rr - (long long)img * H);
+    for (int xb = 0; xb < W; xb += kWgPix) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < kWgPix * 64; t += kWgThreads) {
+        const int p = t >> 6, c = t & 63;
+        const int xx = xb + p;
+        float vd = 0.f, vx = 0.f;
+        if (c < cout) vd = __bfloat162float(dy[(((size_t)img * H + row) * W + xx) * cout + c]);
+        const int ys = row + dyo, xs2 = xx + dxo;
+        if (c < cin && ys >= 0 && ys < H && xs2 >= 0 && xs2 < W)
+          vx = __bfloat162float(x[(((size_t)img * H + ys) * W + xs2) * cin + c]);
+        sd[p][c] = vd;
+        sx[p][c] = vx;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 12; q++) {
+        const int pair = threadIdx.x + q * kWgThreads;
+        if (pair < npairs) {
+          const int co = pair / cin, ci = pair - co * cin;
+          float a = acc[q];
+          for (int p = 0; p < kWgPix; p++) a = fmaf(sd[p][co], sx[p][ci], a);
+          acc[q] = a;
+        }
+      }
+      if (tap == 4 && threadIdx.x < cout)
+        for (int p = 0; p < kWgPix; p++) bacc += sd[p][threadIdx.x];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 12; q++) {
+    const int pair = threadIdx.x + q * kWgThreads;
+    if (pair < npairs) atomicAdd(&dw[(size_t)tap * npairs + pair], acc[q]);
+  }
+  if (tap == 4 && threadIdx.x < cout) atomicAdd(&db[threadIdx.x], bacc);
+}
+
+// dx = (y > 0) ? g : 0 for a ReLU output y (BF16), g FP32 -> BF16.
+__global__ void k_relu_bwd(const float* __restrict__ g, const __nv_bfloat16* __restrict__ y,
+                           __nv_bfloat16* __restrict__ out, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    out[t] = __float2bfloat16(__bfloat162float(y[t]) > 0.f ? g[t] : 0.f);
+}
+
+// Mean-squared error of the first `nc` of `cpad` predicted channels against
+// an FP32 target [p][nc]; grad (BF16, [p][cpad], zero in padded channels)
+// = 2 (pred - target) / (P * nc); loss accumulated into *loss.
+__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target,
+                      __nv_bfloat16* __restrict__ grad, float* __restrict__ loss, long long P,
+                      int nc, int cpad) {
+  __shared__ float red[8];
+  float acc = 0.f;
+  const float scale = 2.f / (float)(P * nc);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < P * cpad;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long p = t / cpad;
+    const int c = (int)(t - p * cpad);
+    float gv = 0.f;
+    if (c < nc) {
+      const float d = pred[t] - target[p * nc + c];
+      acc += d * d;
+      gv = scale * d;
+    }
+    grad[t] = __float2bfloat16(gv);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float s = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += red[k];
+    atomicAdd(loss, s / (float)(P * nc));
+  }
+}
+
+// Adam on FP32 master weights; also writes the BF16 copy the convolution
+// reads (bias: w16 == nullptr).
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, __nv_bfloat16* __restrict__ w16, int n,
+                       float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const float gt = g[t];
+    const float mt = b1 * m[t] + (1.f - b1) * gt;
+    const float vt = b2 * v[t] + (1.f - b2) * gt * gt;
+    m[t] = mt;
+    v[t] = vt;
+    const float wt = w[t] - lr * (mt / c1) / (sqrtf(vt / c2) + eps);
+    w[t] = wt;
+    if (w16) w16[t] = __float2bfloat16(wt);
+  }
+}
+
+// Network input and target for a batch of snapshot pairs.  snaps:
+// [nsnap_total][H][W][3] FP32 states; statics: [ndom][H][W][2] (depth / 500,
+// open-boundary indicator); forcing: [batch] tidal ssh at the target time.
+// x (BF16 [b][H][W][cpad]): state / scale, depth, forcing * indicator, 0.
+// target (FP32 [b][H][W][3], may be NULL): (next - state) / inc_scale.
+__global__ void k_assemble(const float* __restrict__ snaps, const float* __restrict__ statics,
+                           const int* __restrict__ src, const int* __restrict__ dom,
+                           const float* __restrict__ forcing, float3 scale, float3 inc_scale,
+                           __nv_bfloat16* __restrict__ x, float* __restrict__ target, int HW,
+                           int cpad, int batch) {
+  const long long n = (long long)batch * HW;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(t / HW), p = (int)(t - (long long)b * HW);
+    const float* s0 = snaps + ((size_t)src[b] * HW + p) * 3;
+    const float* st = statics + ((size_t)dom[b] * HW + p) * 2;
+    __nv_bfloat16* xo = x + (size_t)t * cpad;
+    xo[0] = __float2bfloat16(s0[0] / scale.x);
+    xo[1] = __float2bfloat16(s0[1] / scale.y);
+    xo[2] = __float2bfloat16(s0[2] / scale.z);
+    xo[3] = __float2bfloat16(st[0]);
+    xo[4] = __float2bfloat16(forcing[b] * st[1] / scale.x);
+    for (int c = 5; c < cpad; c++) xo[c] = __float2bfloat16(0.f);
+    if (target) {
+      const float* s1 = s0 + (size_t)HW * 3;  // the next snapshot of the same domain
+      float* to = target + (size_t)t * 3;
+      to[0] = (s1[0] - s0[0]) / inc_scale.x;
+      to[1] = (s1[1] - s0[1]) / inc_scale.y;
+      to[2] = (s1[2] - s0[2]) / inc_scale.z;
+    }
+  }
+}
+
+// state += increment (first 3 of cpad FP32 output channels) * inc_scale.
+__global__ void k_advance(float* __restrict__ state, const float* __restrict__ inc,
+                          float3 inc_scale, long long P, int cpad) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < P;
+       t += (long long)gridDim.x * blockDim.x) {
+    state[t * 3 + 0] += inc[t * cpad + 0] * inc_scale.x;
+    state[t * 3 + 1] += inc[t * cpad + 1] * inc_scale.y;
+    state[t * 3 + 2] += inc[t * cpad + 2] * inc_scale.z;
+  }
+}
+
 }  // namespace
 }  // namespace emu
 }  // namespace nl2d
@@ -226,6 +397,65 @@ int nl2d_emu_conv3x3(const void* x, const void* w, const float* bias, void* y, f
   k_conv3x3_tc<<<grid, kThreads, smem, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, (const __nv_bfloat16*)w, bias, (__nv_bfloat16*)y, y32, H, W, cin,
       cout, relu, err);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_flip_transpose(const void* w, void* wt, int cout, int cin, void* stream) {
+  if (!w || !wt || cout < 1 || cin < 1) return NL2D_ERR_ARGS;
+  k_flip_transpose<<<64, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)w,
+                                                          (__nv_bfloat16*)wt, cout, cin);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int batch, int H,
+                        int W, int cin, int cout, void* stream) {
+  if (!x || !dy || !dw || !db || cin > 64 || cout > 64 || cin * cout > 12 * kWgThreads ||
+      W % kWgPix)
+    return NL2D_ERR_ARGS;
+  const int rows = batch * H, rows_per_block = 8;
+  const dim3 grid(9, (rows + rows_per_block - 1) / rows_per_block);
+  k_conv_wgrad<<<grid, kWgThreads, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, db, batch, H, W, cin, cout,
+      rows_per_block);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_relu_bwd(const float* g, const void* y, void* out, long long n, void* stream) {
+  k_relu_bwd<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(g, (const __nv_bfloat16*)y,
+                                                         (__nv_bfloat16*)out, n);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_mse(const float* pred, const float* target, void* grad, float* loss, long long P,
+                 int nc, int cpad, void* stream) {
+  k_mse<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(pred, target, (__nv_bfloat16*)grad, loss, P,
+                                                    nc, cpad);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_adam(float* w, float* m, float* v, const float* g, void* w16, int n, float lr,
+                  float b1, float b2, float eps, int step, void* stream) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<64, 256, 0, (cudaStream_t)stream>>>(w, m, v, g, (__nv_bfloat16*)w16, n, lr, b1, b2,
+                                                eps, c1, c2);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_assemble(const float* snaps, const float* statics, const int* src,
+                      const int* dom, const float* forcing, const float* scale6, void* x,
+                      float* target, int HW, int cpad, int batch, void* stream) {
+  if (!snaps || !statics || !src || !dom || !forcing || !scale6 || !x || cpad < 5)
+    return NL2D_ERR_ARGS;
+  k_assemble<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(
+      snaps, statics, src, dom, forcing, make_float3(scale6[0], scale6[1], scale6[2]),
+      make_float3(scale6[3], scale6[4], scale6[5]), (__nv_bfloat16*)x, target, HW, cpad, batch);
+  return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int nl2d_emu_advance(float* state, const float* inc, const float* inc_scale3, long long P,
+                     int cpad, void* stream) {
+  k_advance<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(
+      state, inc, make_float3(inc_scale3[0], inc_scale3[1], inc_scale3[2]), P, cpad);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 

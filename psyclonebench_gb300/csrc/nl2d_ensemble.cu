@@ -428,6 +428,46 @@ bool build_mixed() {
                        cudaMemcpyHostToDevice));
 }
 
+// Interior (ssh, u, v) of every domain, all of size nx x ny, as FP32
+// [dom][ny][nx][3] (the emulator's snapshot layout).
+__global__ void k_export_interior(const EnsDomain* __restrict__ doms, int parity, int ndom,
+                                  int nx, int ny, float* __restrict__ out) {
+  const long long n = (long long)ndom * nx * ny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int dom = (int)(t / ((long long)nx * ny));
+    const int rem = (int)(t - (long long)dom * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    const EnsDomain& D = doms[dom];
+    const size_t c = (size_t)(D.d.ys + j) * D.d.width + (D.d.xs + i);
+    const FusedState& st = D.fs[parity];
+    out[t * 3 + 0] = (float)st.sshn_in[c];
+    out[t * 3 + 1] = (float)st.un_in[c];
+    out[t * 3 + 2] = (float)st.vn_in[c];
+  }
+}
+
+// The inverse: FP32 [dom][ny][nx][3] into the interior of the current FP64
+// state (both ping-pong buffers, so cells no step writes stay consistent).
+__global__ void k_import_interior(const EnsDomain* __restrict__ doms, int ndom, int nx, int ny,
+                                  const float* __restrict__ in) {
+  const long long n = (long long)ndom * nx * ny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int dom = (int)(t / ((long long)nx * ny));
+    const int rem = (int)(t - (long long)dom * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    const EnsDomain& D = doms[dom];
+    const size_t c = (size_t)(D.d.ys + j) * D.d.width + (D.d.xs + i);
+    for (int p = 0; p < 2; p++) {
+      const FusedState& st = D.fs[p];
+      const_cast<double*>(st.sshn_in)[c] = (double)in[t * 3 + 0];
+      const_cast<double*>(st.un_in)[c] = (double)in[t * 3 + 1];
+      const_cast<double*>(st.vn_in)[c] = (double)in[t * 3 + 2];
+    }
+  }
+}
+
 __global__ void k_recip(const double* __restrict__ h, double* __restrict__ r, size_t n) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
        t += (size_t)gridDim.x * blockDim.x) {
@@ -673,6 +713,28 @@ int nl2d_ens_set_precision(int precision) {
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
   }
+  return NL2D_OK;
+}
+
+int nl2d_ens_export_interior(float* d_out) {
+  Ens& e = g_ens;
+  if (e.ndom < 1 || !d_out || e.precision != 0 || !e.built) return NL2D_ERR_STATE;
+  const int nx = e.dom[0].xe - e.dom[0].xs + 1, ny = e.dom[0].ye - e.dom[0].ys + 1;
+  for (const DomainHost& D : e.dom)
+    if (D.xe - D.xs + 1 != nx || D.ye - D.ys + 1 != ny) return NL2D_ERR_ARGS;
+  k_export_interior<<<152 * 8, 256, 0, e.stream>>>(e.d_desc, e.parity, e.ndom, nx, ny, d_out);
+  if (!ck(cudaGetLastError()) || !ck(cudaStreamSynchronize(e.stream))) return NL2D_ERR_CUDA;
+  return NL2D_OK;
+}
+
+int nl2d_ens_import_interior(const float* d_in) {
+  Ens& e = g_ens;
+  if (e.ndom < 1 || !d_in || e.precision != 0 || !e.built) return NL2D_ERR_STATE;
+  const int nx = e.dom[0].xe - e.dom[0].xs + 1, ny = e.dom[0].ye - e.dom[0].ys + 1;
+  for (const DomainHost& D : e.dom)
+    if (D.xe - D.xs + 1 != nx || D.ye - D.ys + 1 != ny) return NL2D_ERR_ARGS;
+  k_import_interior<<<152 * 8, 256, 0, e.stream>>>(e.d_desc, e.ndom, nx, ny, d_in);
+  if (!ck(cudaGetLastError()) || !ck(cudaStreamSynchronize(e.stream))) return NL2D_ERR_CUDA;
   return NL2D_OK;
 }
 
