@@ -260,13 +260,14 @@ def evaluate(ds, net, domains, snaps):
     pairs = [(d, s) for d in domains for s in snaps]
     se_net = se_pers = 0.0
     count = 0
-    for k in range(0, len(pairs) - net.batch + 1, net.batch):
+    for k in range(0, len(pairs), net.batch):
         chunk = pairs[k:k + net.batch]
         ds.batch(chunk, x, tgt)
-        out = net.forward(x)
+        out = net.forward(x, batch=len(chunk))
         torch.cuda.synchronize()
-        d_net = (out[:, 0] - tgt[:, 0]) * ds.inc_scale[0]
-        d_pers = tgt[:, 0] * ds.inc_scale[0]
+        n = len(chunk) * ds.n * ds.n
+        d_net = (out[:n, 0] - tgt[:n, 0]) * ds.inc_scale[0]
+        d_pers = tgt[:n, 0] * ds.inc_scale[0]
         se_net += float(d_net.pow(2).sum())
         se_pers += float(d_pers.pow(2).sum())
         count += d_net.numel()
