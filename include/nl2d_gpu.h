@@ -230,39 +230,58 @@ int nl2d_emu_conv3x3(const void *x, const void *w, const float *bias, void *y,
  * input-gradient convolution. */
 int nl2d_emu_flip_transpose(const void *w, void *wt, int cout, int cin,
                             void *stream);
-/* Adds the weight and bias gradients of a 3x3 convolution (FP32):
+/* Adds the weight and bias gradients of a 3x3 convolution:
  * dw[tap][co][ci] += sum_p dy[p][co] x[p + off(tap)][ci], db[co] += sum_p
- * dy[p][co].  x [batch][H][W][cin], dy [batch][H][W][cout] BF16. */
+ * dy[p][co].  x [batch][H][W][cin], dy [batch][H][W][cout] BF16; dw, db
+ * FP32.  Runs on the tensor cores (tcgen05, FP32 accumulation in tensor
+ * memory, one persistent CTA per SM).  cin a multiple of 16 with 9*cin <=
+ * 512, cout a multiple of 8 up to 128, W a multiple of 128; err (device
+ * int) is set to 1 if a bounded MMA wait ran out. */
 int nl2d_emu_conv_wgrad(const void *x, const void *dy, float *dw, float *db,
-                        int batch, int H, int W, int cin, int cout,
+                        int batch, int H, int W, int cin, int cout, int *err,
                         void *stream);
 /* out = (y > 0) ? g : 0 (y, out BF16; g FP32), n elements. */
 int nl2d_emu_relu_bwd(const float *g, const void *y, void *out, long long n,
                       void *stream);
 /* Mean-squared error of the first nc of cpad channels of pred [P][cpad]
- * against target [P][nc]; grad (BF16, [P][cpad]); loss += mean. */
-int nl2d_emu_mse(const float *pred, const float *target, void *grad,
-                 float *loss, long long P, int nc, int cpad, void *stream);
+ * against target [P][nc], each pixel weighted by weight[p] (FP32 [P], or
+ * NULL for 1); grad (BF16, [P][cpad]) of the mean; loss += mean. */
+int nl2d_emu_mse(const float *pred, const float *target, const float *weight,
+                 void *grad, float *loss, long long P, int nc, int cpad,
+                 void *stream);
 /* One Adam step (bias-corrected, step >= 1) on FP32 weights; w16 (BF16
  * copy) may be NULL. */
 int nl2d_emu_adam(float *w, float *m, float *v, const float *g, void *w16,
                   int n, float lr, float b1, float b2, float eps, int step,
                   void *stream);
 
-/* Network inputs (BF16 [batch][HW][cpad]) and, if target != NULL, FP32
- * targets [batch][HW][3] for snapshot pairs: sample b uses snapshot src[b]
- * of domain dom[b] (snapshot src[b] + 1 is its successor) from snaps
- * [n][HW][3] and statics [ndom][HW][2] (depth / 500, open-boundary
- * indicator); forcing[b] is the tidal ssh at the target time; scale6 =
- * state scales (3) then increment scales (3), host memory.  Device
- * pointers otherwise. */
+/* Network inputs (BF16 [batch][H*W][cpad], cpad >= 15) and, if target !=
+ * NULL, FP32 targets [batch][H*W][3] for snapshot pairs: sample b uses
+ * snapshot src[b] of domain dom[b] (snapshot src[b] + 1 is its successor)
+ * from snaps [n][H][W][3] and statics [ndom][H][W][4] (depth / 500,
+ * open-boundary indicator, east face is a wall, north face is a wall);
+ * forcing[b] is the tidal ssh at the target time.  Channels: ssh minus
+ * that tide, u, v, depth, forcing, the east and north ssh differences and the depth-weighted
+ * flux divergence (formed in FP32), the open-boundary indicator, ssh minus
+ * the tide next to the open side, the two wall indicators, and the low
+ * BF16 parts of the three state channels (value - BF16(value)).  scale12 (host
+ * memory) = state scales (3), increment scales (3), scales of the three
+ * difference channels (3), standard deviations (m, m/s, m/s) of white noise
+ * added to the input state (3; zeros for none), drawn from `seed`; the
+ * target is then the increment from the perturbed state.  Device pointers
+ * otherwise. */
 int nl2d_emu_assemble(const float *snaps, const float *statics, const int *src,
-                      const int *dom, const float *forcing, const float *scale6,
-                      void *x, float *target, int HW, int cpad, int batch,
-                      void *stream);
-/* state[p][0..2] += inc[p][0..2] * inc_scale3[0..2] (inc is [P][cpad]). */
+                      const int *dom, const float *forcing, const float *scale12,
+                      unsigned long long seed, void *x, float *target, int H,
+                      int W, int cpad, int batch, void *stream);
+/* state[p][0..2] += inc[p][0..2] * inc_scale3[0..2] (inc is [P][cpad]).  If
+ * statics is not NULL, sample p / HW belongs to domain dom[p / HW] and the
+ * solver's boundary conditions are applied: velocities on wall faces
+ * (statics channels 2, 3) are zero and the ssh of cells next to the open
+ * side (channel 1) is forcing[p / HW], the tide at the target time. */
 int nl2d_emu_advance(float *state, const float *inc, const float *inc_scale3,
-                     long long P, int cpad, void *stream);
+                     const float *statics, const int *dom, const float *forcing,
+                     long long HW, long long P, int cpad, void *stream);
 /* Interior (ssh, u, v) of every ensemble domain (all the same size) into a
  * device FP32 array [dom][ny][nx][3]; FP64 form only. */
 int nl2d_ens_export_interior(float *d_out);

@@ -63,14 +63,17 @@ EXPORTS = {
     "nl2d_emu_conv3x3": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP] + [ctypes.c_int] * 6 +
                          [_VP, _VP]),
     "nl2d_emu_flip_transpose": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.c_int, _VP]),
-    "nl2d_emu_conv_wgrad": (ctypes.c_int, [_VP, _VP, _VP, _VP] + [ctypes.c_int] * 5 + [_VP]),
+    "nl2d_emu_conv_wgrad": (ctypes.c_int, [_VP, _VP, _VP, _VP] + [ctypes.c_int] * 5 +
+                            [_VP, _VP]),
     "nl2d_emu_relu_bwd": (ctypes.c_int, [_VP, _VP, _VP, ctypes.c_longlong, _VP]),
-    "nl2d_emu_mse": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_longlong, ctypes.c_int,
+    "nl2d_emu_mse": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_longlong, ctypes.c_int,
                                     ctypes.c_int, _VP]),
     "nl2d_emu_adam": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int] +
                       [ctypes.c_float] * 4 + [ctypes.c_int, _VP]),
-    "nl2d_emu_assemble": (ctypes.c_int, [_VP] * 8 + [ctypes.c_int] * 3 + [_VP]),
-    "nl2d_emu_advance": (ctypes.c_int, [_VP, _VP, _VP, ctypes.c_longlong, ctypes.c_int, _VP]),
+    "nl2d_emu_assemble": (ctypes.c_int, [_VP] * 6 + [ctypes.c_ulonglong, _VP, _VP] +
+                          [ctypes.c_int] * 4 + [_VP]),
+    "nl2d_emu_advance": (ctypes.c_int, [_VP] * 6 + [ctypes.c_longlong, ctypes.c_longlong,
+                                                 ctypes.c_int, _VP]),
     "nl2d_ens_export_interior": (ctypes.c_int, [_VP]),
     "nl2d_ens_import_interior": (ctypes.c_int, [_VP]),
     "nl2d_sync": (ctypes.c_int, []),

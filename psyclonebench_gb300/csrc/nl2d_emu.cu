@@ -234,62 +234,165 @@ __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w,
   }
 }
 
-// Weight and bias gradients of a 3x3 convolution, FP32 on the CUDA cores:
-// dw[tap][co][ci] += sum_p dy[p][co] * x[p + off(tap)][ci],
-// db[co] += sum_p dy[p][co].  Block (tap, chunk of rows); each thread owns
-// a fixed set of (co, ci) pairs; a row segment of dy and of the shifted x
-// is staged in shared memory; results are added atomically.
-constexpr int kWgThreads = 256, kWgPix = 64;
-__global__ void __launch_bounds__(kWgThreads)
-    k_conv_wgrad(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
-                 float* __restrict__ dw, float* __restrict__ db, int B, int H, int W, int cin,
-                 int cout, int rows_per_block) {
-  __shared__ float sx[kWgPix][64 + 1];
-  __shared__ float sd[kWgPix][64 + 1];
-  const int tap = blockIdx.x, dyo = tap / 3 - 1, dxo = tap % 3 - 1;
-  const int npairs = cout * cin;
-  float acc[12];
-#pragma unroll
-  for (int q = 0; q < 12; q++) acc[q] = 0.f;
+// Weight and bias gradients on the tensor cores.  For each tap the weight
+// gradient is a GEMM over pixels, D[co][ci] = sum_p dY[p][co] X[p + off][ci],
+// with both operands "MN-major" (channels contiguous per pixel, as the data
+// already is): M = co (padded to 128 with zero rows), N = ci, K = pixels.
+// X is staged exactly as in the forward convolution, so the tap (dy, dx)
+// operand is again a row block started 16 * dx bytes later.  The nine
+// accumulators (9 x ci FP32 columns) stay in tensor memory while a
+// persistent CTA walks its tiles; at the end each CTA adds its partial sums
+// to dw atomically.  db[co] is summed from the staged dY tile.
+constexpr int kWgTmemCols = 512;
+constexpr int kWgGroups = 16;  // 128 M rows = 16 groups of 8 output channels
+constexpr size_t kWgSmem = 120 * 1024;
+
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_conv_wgrad_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
+                    float* __restrict__ dw, float* __restrict__ db, int batch, int H, int W,
+                    int cin, int cout, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t taddr_slot;
+  __shared__ uint32_t s_done;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int kc = cin >> 3, kco = cout >> 3;
+  const uint32_t lbo_y = kTileM * 16;                // next group of 8 output channels
+  const uint32_t lbo_x = kRowPix * 16;               // next group of 8 input channels
+  const uint32_t row_bytes = (uint32_t)kc * lbo_x;
+  unsigned char* a_s = smem;                         // dY tile, kWgGroups x 128 x 16 B
+  unsigned char* b_s = smem + kWgGroups * lbo_y;     // three staged X rows
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&taddr_slot)),
+                 "r"(kWgTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  // rows co >= cout of the M = 128 operand stay zero
+  for (int t = tid; t < kWgGroups * kTileM; t += kThreads)
+    *reinterpret_cast<uint4*>(a_s + t * 16) = make_uint4(0, 0, 0, 0);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t taddr = taddr_slot;
+  const uint32_t idesc = idesc_bf16_mn(cin);
+
+  const int segs = W / kTileM;
+  const long long ntiles = (long long)batch * H * segs;
+  uint32_t phase = 0;
+  bool ok_all = true, any = false;
   float bacc = 0.f;
-  const long long rows_total = (long long)B * H;
-  const long long r0 = (long long)blockIdx.y * rows_per_block;
-  for (long long rr = r0; rr < r0 + rows_per_block && rr < rows_total; rr++) {
-    const int img = (int)(rr / H), row = (int)(rr - (long long)img * H);
-    for (int xb = 0; xb < W; xb += kWgPix) {
-      __syncthreads();
-      for (int t = threadIdx.x; t < kWgPix * 64; t += kWgThreads) {
-        const int p = t >> 6, c = t & 63;
-        const int xx = xb + p;
-        float vd = 0.f, vx = 0.f;
-        if (c < cout) vd = __bfloat162float(dy[(((size_t)img * H + row) * W + xx) * cout + c]);
-        const int ys = row + dyo, xs2 = xx + dxo;
-        if (c < cin && ys >= 0 && ys < H && xs2 >= 0 && xs2 < W)
-          vx = __bfloat162float(x[(((size_t)img * H + ys) * W + xs2) * cin + c]);
-        sd[p][c] = vd;
-        sx[p][c] = vx;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int q = 0; q < 12; q++) {
-        const int pair = threadIdx.x + q * kWgThreads;
-        if (pair < npairs) {
-          const int co = pair / cin, ci = pair - co * cin;
-          float a = acc[q];
-          for (int p = 0; p < kWgPix; p++) a = fmaf(sd[p][co], sx[p][ci], a);
-          acc[q] = a;
+  for (long long tile = blockIdx.x; tile < ntiles && ok_all; tile += gridDim.x) {
+    const int seg = (int)(tile % segs);
+    const long long rr = tile / segs;
+    const int row = (int)(rr % H), img = (int)(rr / H);
+    const int x0 = seg * kTileM;
+    const size_t pix0 = ((size_t)img * H + row) * W + x0;
+    for (int t = tid; t < kco * kTileM; t += kThreads) {
+      const int p = t % kTileM, g = t / kTileM;
+      *reinterpret_cast<uint4*>(a_s + g * lbo_y + p * 16) =
+          *reinterpret_cast<const uint4*>(dy + (pix0 + p) * cout + g * 8);
+    }
+    for (int t = tid; t < 3 * kc * kRowPix; t += kThreads) {
+      const int p = t % kRowPix, rem = t / kRowPix;
+      const int ch = rem % kc, dyr = rem / kc;
+      const int yy = row + dyr - 1, xx = x0 - 1 + p;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+        v = *reinterpret_cast<const uint4*>(x + (((size_t)img * H + yy) * W + xx) * cin +
+                                            ch * 8);
+      *reinterpret_cast<uint4*>(b_s + dyr * row_bytes + ch * lbo_x + p * 16) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid < cout) {  // bias gradient from the staged tile
+      const __nv_bfloat16* col =
+          reinterpret_cast<const __nv_bfloat16*>(a_s + (tid >> 3) * lbo_y) + (tid & 7);
+      for (int p = 0; p < kTileM; p++) bacc += __bfloat162float(col[p * 8]);
+    }
+    if (tid == 0) {
+      for (int tap = 0; tap < 9; tap++) {
+        const int dyr = tap / 3, dx = tap % 3;
+        for (int kq = 0; kq < kTileM / 16; kq++) {
+          const uint32_t aa = smem_u32(a_s) + kq * 256;
+          const uint32_t ba = smem_u32(b_s + dyr * row_bytes) + dx * 16 + kq * 256;
+          // MN-major, no swizzle: LBO steps along K (8 pixels = 128 B), SBO
+          // along M / N (the next 8 channels)
+          const uint64_t ad = smem_desc(aa, 128, lbo_y);
+          const uint64_t bd = smem_desc(ba, 128, lbo_x);
+          const uint32_t acc = (any || kq > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                  taddr + (uint32_t)(tap * cin)),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
         }
       }
-      if (tap == 4 && threadIdx.x < cout)
-        for (int p = 0; p < kWgPix; p++) bacc += sd[p][threadIdx.x];
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar))
+          : "memory");
+      uint32_t ok = 0;
+      const long long t0 = clock64();
+      while (!ok) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_u32(&mbar)), "r"(phase)
+            : "memory");
+        if (!ok && clock64() - t0 > kMaxWaitCycles) break;
+      }
+      if (!ok) atomicExch(err, 1);
+      s_done = ok;
+    }
+    __syncthreads();
+    phase ^= 1u;
+    ok_all = s_done != 0;
+    any = true;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (tid < cout && any) atomicAdd(&db[tid], bacc);
+  if (any && ok_all) {
+    // accumulator row = output channel (lanes 32w .. 32w+31)
+    const int co = warp * 32 + lane;
+    for (int c0 = 0; c0 < 9 * cin; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t ta = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+            "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+            "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(ta));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (co < cout) {
+        const int tap = c0 / cin, ci0 = c0 - tap * cin;
+#pragma unroll
+        for (int q = 0; q < 16; q++)
+          atomicAdd(&dw[((size_t)tap * cout + co) * cin + ci0 + q], __uint_as_float(r[q]));
+      }
     }
   }
-#pragma unroll
-  for (int q = 0; q < 12; q++) {
-    const int pair = threadIdx.x + q * kWgThreads;
-    if (pair < npairs) atomicAdd(&dw[(size_t)tap * npairs + pair], acc[q]);
-  }
-  if (tap == 4 && threadIdx.x < cout) atomicAdd(&db[threadIdx.x], bacc);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr),
+                 "r"(kWgTmemCols));
 }
 
 // dx = (y > 0) ? g : 0 for a ReLU output y (BF16), g FP32 -> BF16.
@@ -304,8 +407,8 @@ __global__ void k_relu_bwd(const float* __restrict__ g, const __nv_bfloat16* __r
 // an FP32 target [p][nc]; grad (BF16, [p][cpad], zero in padded channels)
 // = 2 (pred - target) / (P * nc); loss accumulated into *loss.
 __global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target,
-                      __nv_bfloat16* __restrict__ grad, float* __restrict__ loss, long long P,
-                      int nc, int cpad) {
+                      const float* __restrict__ weight, __nv_bfloat16* __restrict__ grad,
+                      float* __restrict__ loss, long long P, int nc, int cpad) {
   __shared__ float red[8];
   float acc = 0.f;
   const float scale = 2.f / (float)(P * nc);
@@ -316,8 +419,9 @@ __global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ 
     float gv = 0.f;
     if (c < nc) {
       const float d = pred[t] - target[p * nc + c];
-      acc += d * d;
-      gv = scale * d;
+      const float w = weight ? weight[p] : 1.f;
+      acc += w * d * d;
+      gv = scale * w * d;
     }
     grad[t] = __float2bfloat16(gv);
   }
@@ -349,47 +453,139 @@ __global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __re
   }
 }
 
-// Network input and target for a batch of snapshot pairs.  snaps:
-// [nsnap_total][H][W][3] FP32 states; statics: [ndom][H][W][2] (depth / 500,
-// open-boundary indicator); forcing: [batch] tidal ssh at the target time.
-// x (BF16 [b][H][W][cpad]): state / scale, depth, forcing * indicator, 0.
-// target (FP32 [b][H][W][3], may be NULL): (next - state) / inc_scale.
+// Zero-mean, unit-variance noise that depends only on (seed, key): the sum
+// of four uniforms from a 64-bit mix (splitmix64 finaliser), rescaled.
+__device__ __forceinline__ float hash_noise(unsigned long long seed, unsigned long long key) {
+  unsigned long long z = seed ^ (key * 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  float sum = 0.f;
+#pragma unroll
+  for (int q = 0; q < 4; q++) sum += (float)((z >> (16 * q)) & 0xFFFF) * (1.f / 65536.f);
+  return (sum - 2.f) * 1.7320508f;  // variance of the sum is 4/12
+}
+
+// Per-pixel statics of a domain: depth (ht / 500 m), open-boundary
+// indicator (1 on wet cells next to the open side), and 1 where the pixel's
+// east (u) or north (v) face is a wall.
+constexpr int kStatics = 4;
+
+// Network inputs of `batch` domain states (each an H x W image of
+// (ssh, u, v), u / v on the east / north face of the pixel's cell):
+//   0-2  ssh - tidal ssh at the target time, u, v / state scales (ssh as a
+//        departure from the tide keeps BF16's resolution where the level
+//        follows the tide, next to the open side)
+//   3    depth (ht / 500 m)
+//   4    tidal ssh at the target time on cells next to the open side
+//   5    ssh(i+1, j) - ssh(i, j)      (east-face pressure gradient)
+//   6    ssh(i, j+1) - ssh(i, j)      (north-face pressure gradient)
+//   7    sum of face depth x velocity out of the cell (flux divergence)
+//   8    open-boundary indicator
+//   9    ssh - tidal ssh on cells next to the open side (what the Flather
+//        condition radiates out)
+//   10, 11  east / north face is a wall
+//   12-14   low BF16 parts of channels 0-2 (value - BF16(value)): next to
+//        the open side the state is 20-50x its k-step change, so one BF16
+//        (8-bit mantissa) would leave a few per cent of noise in what the
+//        network predicts; high + low carry 16 bits
+// Channels 5-7 and 9 are differences of nearly equal numbers, so they are
+// formed in FP32 before the BF16 rounding; the scales of 5-7 come from the
+// data.  A face outside the image (the closed or open boundary) contributes
+// zero.
+// With noise (training only) the input state is the snapshot plus white
+// noise of the given standard deviations, the same value wherever a cell is
+// read, and the target is the increment from that perturbed state.
+struct Noisy {
+  const float* img;
+  float3 sd;
+  unsigned long long seed, base;
+  __device__ float get(int q, int ch) const {
+    float v = img[(size_t)q * 3 + ch];
+    const float s = ch == 0 ? sd.x : (ch == 1 ? sd.y : sd.z);
+    if (s != 0.f) v += s * hash_noise(seed, (base + (unsigned long long)q) * 3ull + ch);
+    return v;
+  }
+};
+
 __global__ void k_assemble(const float* __restrict__ snaps, const float* __restrict__ statics,
                            const int* __restrict__ src, const int* __restrict__ dom,
                            const float* __restrict__ forcing, float3 scale, float3 inc_scale,
-                           __nv_bfloat16* __restrict__ x, float* __restrict__ target, int HW,
-                           int cpad, int batch) {
+                           float3 dscale, float3 noise, unsigned long long seed,
+                           __nv_bfloat16* __restrict__ x, float* __restrict__ target, int H,
+                           int W, int cpad, int batch) {
+  const long long HW = (long long)H * W;
   const long long n = (long long)batch * HW;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x) {
     const int b = (int)(t / HW), p = (int)(t - (long long)b * HW);
-    const float* s0 = snaps + ((size_t)src[b] * HW + p) * 3;
-    const float* st = statics + ((size_t)dom[b] * HW + p) * 2;
+    const int r = p / W, c = p - r * W;
+    const Noisy img{snaps + (size_t)src[b] * HW * 3, noise, seed,
+                    (unsigned long long)b * (unsigned long long)HW};
+    const float* sti = statics + (size_t)dom[b] * HW * kStatics;
+    const float* st = sti + (size_t)p * kStatics;
+    const int pe = c + 1 < W ? p + 1 : p, pw = c > 0 ? p - 1 : -1;
+    const int pn = r + 1 < H ? p + W : p, ps = r > 0 ? p - W : -1;
+    const float d = st[0];
+    const float e0 = img.get(p, 0), u0 = img.get(p, 1), v0 = img.get(p, 2);
+    const float gx = (pe != p ? img.get(pe, 0) : e0) - e0;
+    const float gy = (pn != p ? img.get(pn, 0) : e0) - e0;
+    float div = 0.5f * (d + sti[(size_t)pe * kStatics]) * u0 +
+                0.5f * (d + sti[(size_t)pn * kStatics]) * v0;
+    if (pw >= 0) div -= 0.5f * (d + sti[(size_t)pw * kStatics]) * img.get(pw, 1);
+    if (ps >= 0) div -= 0.5f * (d + sti[(size_t)ps * kStatics]) * img.get(ps, 2);
     __nv_bfloat16* xo = x + (size_t)t * cpad;
-    xo[0] = __float2bfloat16(s0[0] / scale.x);
-    xo[1] = __float2bfloat16(s0[1] / scale.y);
-    xo[2] = __float2bfloat16(s0[2] / scale.z);
-    xo[3] = __float2bfloat16(st[0]);
+    const float st0[3] = {(e0 - forcing[b]) / scale.x, u0 / scale.y, v0 / scale.z};
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {  // high and low BF16 parts
+      const __nv_bfloat16 hi = __float2bfloat16(st0[ch]);
+      xo[ch] = hi;
+      xo[12 + ch] = __float2bfloat16(st0[ch] - __bfloat162float(hi));
+    }
+    xo[3] = __float2bfloat16(d);
     xo[4] = __float2bfloat16(forcing[b] * st[1] / scale.x);
-    for (int c = 5; c < cpad; c++) xo[c] = __float2bfloat16(0.f);
+    xo[5] = __float2bfloat16(gx / dscale.x);
+    xo[6] = __float2bfloat16(gy / dscale.y);
+    xo[7] = __float2bfloat16(div / dscale.z);
+    xo[8] = __float2bfloat16(st[1]);
+    xo[9] = __float2bfloat16((e0 - forcing[b]) * st[1] / scale.x);
+    xo[10] = __float2bfloat16(st[2]);
+    xo[11] = __float2bfloat16(st[3]);
+    for (int ch = 15; ch < cpad; ch++) xo[ch] = __float2bfloat16(0.f);
     if (target) {
-      const float* s1 = s0 + (size_t)HW * 3;  // the next snapshot of the same domain
+      // the next snapshot of the same domain
+      const float* s1 = img.img + ((size_t)HW + p) * 3;
       float* to = target + (size_t)t * 3;
-      to[0] = (s1[0] - s0[0]) / inc_scale.x;
-      to[1] = (s1[1] - s0[1]) / inc_scale.y;
-      to[2] = (s1[2] - s0[2]) / inc_scale.z;
+      to[0] = (s1[0] - e0) / inc_scale.x;
+      to[1] = (s1[1] - u0) / inc_scale.y;
+      to[2] = (s1[2] - v0) / inc_scale.z;
     }
   }
 }
 
 // state += increment (first 3 of cpad FP32 output channels) * inc_scale.
+// With statics, the solver's boundary conditions are applied as the solver
+// applies them: velocities on wall faces are held at zero, and the ssh of
+// wet cells next to the open side is the tide at the target time.
 __global__ void k_advance(float* __restrict__ state, const float* __restrict__ inc,
-                          float3 inc_scale, long long P, int cpad) {
+                          float3 inc_scale, const float* __restrict__ statics,
+                          const int* __restrict__ dom, const float* __restrict__ forcing,
+                          long long HW, long long P, int cpad) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < P;
        t += (long long)gridDim.x * blockDim.x) {
-    state[t * 3 + 0] += inc[t * cpad + 0] * inc_scale.x;
-    state[t * 3 + 1] += inc[t * cpad + 1] * inc_scale.y;
-    state[t * 3 + 2] += inc[t * cpad + 2] * inc_scale.z;
+    float e = state[t * 3 + 0] + inc[t * cpad + 0] * inc_scale.x;
+    float u = state[t * 3 + 1] + inc[t * cpad + 1] * inc_scale.y;
+    float v = state[t * 3 + 2] + inc[t * cpad + 2] * inc_scale.z;
+    if (statics) {
+      const long long b = t / HW;
+      const float* st = statics + ((size_t)dom[b] * HW + (t - b * HW)) * kStatics;
+      if (st[1] > 0.f) e = forcing[b];
+      if (st[2] > 0.f) u = 0.f;
+      if (st[3] > 0.f) v = 0.f;
+    }
+    state[t * 3 + 0] = e;
+    state[t * 3 + 1] = u;
+    state[t * 3 + 2] = v;
   }
 }
 
@@ -440,15 +636,29 @@ int nl2d_emu_flip_transpose(const void* w, void* wt, int cout, int cin, void* st
 }
 
 int nl2d_emu_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int batch, int H,
-                        int W, int cin, int cout, void* stream) {
-  if (!x || !dy || !dw || !db || cin > 64 || cout > 64 || cin * cout > 12 * kWgThreads ||
-      W % kWgPix)
+                        int W, int cin, int cout, int* err, void* stream) {
+  if (!x || !dy || !dw || !db || !err || cin % 16 || cin < 16 || 9 * cin > kWgTmemCols ||
+      cout % 8 || cout < 8 || cout > 128 || W % kTileM || H < 1 || batch < 1)
     return NL2D_ERR_ARGS;
-  const int rows = batch * H, rows_per_block = 8;
-  const dim3 grid(9, (rows + rows_per_block - 1) / rows_per_block);
-  k_conv_wgrad<<<grid, kWgThreads, 0, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, db, batch, H, W, cin, cout,
-      rows_per_block);
+  // The kernel holds all 512 TMEM columns, so it must be alone on its SM:
+  // asking for more than half an SM's shared memory guarantees that.
+  const size_t need = (size_t)kWgGroups * kTileM * 16 + 3 * (size_t)(cin / 8) * kRowPix * 16;
+  const size_t smem = kWgSmem;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_conv_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kWgSmem) != cudaSuccess)
+      return NL2D_ERR_CUDA;
+    attr = true;
+  }
+  if (need > smem) return NL2D_ERR_ARGS;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (long long)batch * H * (W / kTileM);
+  const int grid = (int)(tiles < sms ? tiles : sms);  // 512 TMEM columns: one CTA per SM
+  k_conv_wgrad_tc<<<grid, kThreads, smem, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, db, batch, H, W, cin, cout, err);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 
@@ -458,10 +668,11 @@ int nl2d_emu_relu_bwd(const float* g, const void* y, void* out, long long n, voi
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 
-int nl2d_emu_mse(const float* pred, const float* target, void* grad, float* loss, long long P,
-                 int nc, int cpad, void* stream) {
-  k_mse<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(pred, target, (__nv_bfloat16*)grad, loss, P,
-                                                    nc, cpad);
+int nl2d_emu_mse(const float* pred, const float* target, const float* weight, void* grad,
+                 float* loss, long long P, int nc, int cpad, void* stream) {
+  if (!pred || !target || !grad || !loss || P < 1 || nc < 1 || cpad < nc) return NL2D_ERR_ARGS;
+  k_mse<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(pred, target, weight, (__nv_bfloat16*)grad,
+                                                    loss, P, nc, cpad);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 
@@ -474,20 +685,30 @@ int nl2d_emu_adam(float* w, float* m, float* v, const float* g, void* w16, int n
 }
 
 int nl2d_emu_assemble(const float* snaps, const float* statics, const int* src,
-                      const int* dom, const float* forcing, const float* scale6, void* x,
-                      float* target, int HW, int cpad, int batch, void* stream) {
-  if (!snaps || !statics || !src || !dom || !forcing || !scale6 || !x || cpad < 5)
+                      const int* dom, const float* forcing, const float* scale12,
+                      unsigned long long seed, void* x, float* target, int H, int W, int cpad,
+                      int batch, void* stream) {
+  if (!snaps || !statics || !src || !dom || !forcing || !scale12 || !x || cpad < 15 || H < 1 ||
+      W < 1 || batch < 1)
     return NL2D_ERR_ARGS;
   k_assemble<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(
-      snaps, statics, src, dom, forcing, make_float3(scale6[0], scale6[1], scale6[2]),
-      make_float3(scale6[3], scale6[4], scale6[5]), (__nv_bfloat16*)x, target, HW, cpad, batch);
+      snaps, statics, src, dom, forcing, make_float3(scale12[0], scale12[1], scale12[2]),
+      make_float3(scale12[3], scale12[4], scale12[5]),
+      make_float3(scale12[6], scale12[7], scale12[8]),
+      make_float3(scale12[9], scale12[10], scale12[11]), seed, (__nv_bfloat16*)x, target, H, W,
+      cpad, batch);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 
-int nl2d_emu_advance(float* state, const float* inc, const float* inc_scale3, long long P,
-                     int cpad, void* stream) {
+int nl2d_emu_advance(float* state, const float* inc, const float* inc_scale3,
+                     const float* statics, const int* dom, const float* forcing, long long HW,
+                     long long P, int cpad, void* stream) {
+  if (!state || !inc || !inc_scale3 || (statics && (!dom || !forcing || HW < 1)) || P < 0 ||
+      cpad < 3)
+    return NL2D_ERR_ARGS;
   k_advance<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(
-      state, inc, make_float3(inc_scale3[0], inc_scale3[1], inc_scale3[2]), P, cpad);
+      state, inc, make_float3(inc_scale3[0], inc_scale3[1], inc_scale3[2]), statics, dom,
+      forcing, HW, P, cpad);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 

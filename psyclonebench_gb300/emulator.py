@@ -3,18 +3,22 @@ reference): a residual CNN that advances (ssh, u, v) by k = 10 solver steps,
 trained only on trajectories the solver itself generates, with the FP64
 solver as judge and fallback during roll-outs.
 
-Network: six 3x3 convolutions, 48 channels, ReLU between them, inputs
-(ssh, u, v, depth, tidal forcing) in BF16, FP32 accumulation; the output is
-the increment of the state, scaled.  Every FLOP of the forward pass, the
-backward pass and inference runs in this library's kernels: the tcgen05
-implicit-GEMM convolution (forward, and the input gradient with flipped,
-transposed weights), the FP32 weight-gradient reduction, the loss and Adam
-kernels.  torch only provides device buffers.
+Network: six 3x3 convolutions, 48 channels, ReLU between them, inputs in
+BF16, FP32 accumulation; the output is the increment of the state, scaled.
+Every FLOP of the forward pass, the backward pass and inference runs in this
+library's kernels: the tcgen05 implicit-GEMM convolution (forward, and the
+input gradient with flipped, transposed weights), the tcgen05 weight-gradient
+GEMM, the loss and Adam kernels.  torch only provides device buffers.
 
 Pixels are the interior T cells of a domain; pixel (i, j) carries sshn_t,
-and un / vn of the east / north faces of that cell.  The forcing channel is
-the tide's bc_ssh value at the target time on wet cells next to the open
-side, zero elsewhere; depth is ht / 500 m.
+and un / vn of the east / north faces of that cell.  Inputs: ssh, u, v,
+depth (ht / 500 m), the tide's bc_ssh value at the target time on wet cells
+next to the open side (zero elsewhere), and three channels formed in FP32
+before the BF16 rounding: the east and north ssh differences (what drives
+the momentum) and the depth-weighted flux divergence (what drives ssh).
+Adjacent cells differ in the fourth significant digit, below BF16's
+resolution, so these differences could not be recovered from the rounded
+state channels.
 """
 import ctypes
 import math
@@ -26,7 +30,8 @@ from . import NL2D_OK, Nl2dError, load_library
 from .ensemble import Ensemble, build_domain
 from .workloads import ensemble_domains
 
-CPAD_IN = 16   # 5 input channels padded for the MMA K granularity
+N_INPUTS = 15  # state (high and low BF16 parts), depth, forcing, differences, geometry
+CPAD_IN = 16   # input channels padded for the MMA K granularity
 CPAD_OUT = 16  # 3 output channels padded (N multiple of 16)
 WIDTH = 48
 LAYERS = [(CPAD_IN, WIDTH, 1)] + [(WIDTH, WIDTH, 1)] * 4 + [(WIDTH, CPAD_OUT, 0)]
@@ -66,10 +71,10 @@ class ConvNet:
         self.w32, self.w16, self.b, self.dw, self.db = [], [], [], [], []
         self.mw, self.vw, self.mb, self.vb, self.wt = [], [], [], [], []
         for cin, cout, _ in LAYERS:
-            fan_in = 9 * (5 if cin == CPAD_IN else cin)
+            fan_in = 9 * (N_INPUTS if cin == CPAD_IN else cin)
             w = torch.randn(9, cout, cin, generator=g) * math.sqrt(2.0 / fan_in)
             if cin == CPAD_IN:
-                w[:, :, 5:] = 0.0
+                w[:, :, N_INPUTS:] = 0.0
             if cout == CPAD_OUT:
                 w *= 0.1  # start near the identity step (zero increment)
             w = w.cuda()
@@ -111,15 +116,17 @@ class ConvNet:
             inp = self.acts[li]
         return self.out32
 
-    def train_step(self, x, target, lr=1e-3):
-        """One Adam step on the batch (x BF16, target FP32 [P, 3]); returns
-        the loss of the batch before the step."""
+    def train_step(self, x, target, lr=1e-3, weight=None):
+        """One Adam step on the batch (x BF16, target FP32 [P, 3], optional
+        per-pixel loss weights FP32 [P]); returns the loss of the batch
+        before the step."""
         torch = _torch()
         P = self.batch * self.H * self.W
         self.forward(x)
         self.loss.zero_()
-        _ck(self.lib.nl2d_emu_mse(_p(self.out32), _p(target), _p(self.gout), _p(self.loss),
-                                  P, 3, CPAD_OUT, None), "nl2d_emu_mse")
+        _ck(self.lib.nl2d_emu_mse(_p(self.out32), _p(target),
+                                  _p(weight) if weight is not None else None, _p(self.gout),
+                                  _p(self.loss), P, 3, CPAD_OUT, None), "nl2d_emu_mse")
         for t in self.dw + self.db:
             t.zero_()
         g = self.gout  # gradient of the loss w.r.t. layer li's pre-activation
@@ -127,7 +134,8 @@ class ConvNet:
             cin, cout, _ = LAYERS[li]
             xin = x if li == 0 else self.acts[li - 1]
             _ck(self.lib.nl2d_emu_conv_wgrad(_p(xin), _p(g), _p(self.dw[li]), _p(self.db[li]),
-                                             self.batch, self.H, self.W, cin, cout, None),
+                                             self.batch, self.H, self.W, cin, cout,
+                                             _p(self.err), None),
                 "nl2d_emu_conv_wgrad")
             if li == 0:
                 break
@@ -165,19 +173,25 @@ def emulator_domain_specs(count, seed, n=256):
 class Dataset:
     """Solver trajectories of `count` seeded domains on the GPU:
     snaps [count * nsnap][n][n][3] FP32 (every K_STEPS steps), statics
-    [count][n][n][2]."""
+    [count][n][n][4] (depth / 500 m, open-boundary indicator, east / north
+    face is a wall).
+
+    The scheme itself goes unstable on a few per cent of the seeded domains
+    (strong tides over shallow banks; the oracle blows up on the same ones),
+    so a few spare domains are generated and the first `count` whose whole
+    trajectory stays finite are kept; `dropped` lists the rest."""
 
     def __init__(self, count=200, nsnap=101, seed=11, n=256, rdt=5.0, lib=None):
         torch = _torch()
         self.lib = lib or load_library()
         self.n, self.nsnap, self.rdt = n, nsnap, rdt
-        self.specs = emulator_domain_specs(count, seed, n)
-        doms = [build_domain(s) for s in self.specs]
-        self.doms = doms
+        total = count + max(2, count // 16)
+        specs = emulator_domain_specs(total, seed, n)
+        doms = [build_domain(s) for s in specs]
         ens = Ensemble(doms, rdt=rdt, lib=self.lib)
         HW = n * n
-        self.snaps = torch.zeros(count, nsnap, HW, 3, device="cuda")
-        buf = torch.zeros(count, HW, 3, device="cuda")
+        snaps = torch.zeros(total, nsnap, HW, 3, device="cuda")
+        buf = torch.zeros(total, HW, 3, device="cuda")
         t0 = time.perf_counter()
         ens.run(1, 0)  # builds the schedule
         solver_ms = 0.0
@@ -186,12 +200,22 @@ class Dataset:
                 ms, _ = ens.run(1 + (s - 1) * K_STEPS, K_STEPS)
                 solver_ms += ms
             _ck(self.lib.nl2d_ens_export_interior(ctypes.c_void_p(buf.data_ptr())), "export")
-            self.snaps[:, s] = buf
+            snaps[:, s] = buf
         self.gen_seconds = time.perf_counter() - t0
         self.solver_ms_per_step = solver_ms / max(1, (nsnap - 1) * K_STEPS)
         ens.close()
-        self.snaps = self.snaps.reshape(count * nsnap, HW, 3)
-        st = np.zeros((count, HW, 2), np.float32)
+        finite = [bool(torch.isfinite(snaps[k]).all()) for k in range(total)]
+        keep = [k for k in range(total) if finite[k]][:count]
+        if len(keep) < count:
+            raise Nl2dError("only %d of %d generated domains stayed finite" % (len(keep), total))
+        self.dropped = [k for k in range(keep[-1] + 1) if not finite[k]]
+        self.specs = [specs[k] for k in keep]
+        self.doms = [doms[k] for k in keep]
+        idx = torch.tensor(keep, device="cuda")
+        self.snaps = snaps.index_select(0, idx).reshape(count * nsnap, HW, 3)
+        del snaps, buf
+        doms = self.doms
+        st = np.zeros((count, HW, 4), np.float32)
         for k, d in enumerate(doms):
             w, h, xs, xe, ys, ye = d["dims"]
             st[k, :, 0] = (d["ht"][ys:ye + 1, xs:xe + 1] / 500.0).reshape(-1)
@@ -200,6 +224,9 @@ class Dataset:
             nb = ((m[ys - 1:ye, xs:xe + 1] < 0) | (m[ys + 1:ye + 2, xs:xe + 1] < 0) |
                   (m[ys:ye + 1, xs - 1:xe] < 0) | (m[ys:ye + 1, xs + 1:xe + 2] < 0))
             st[k, :, 1] = (inner & nb).reshape(-1).astype(np.float32)
+            # a face is a wall where the cell beyond it is land
+            st[k, :, 2] = (m[ys:ye + 1, xs + 1:xe + 2] == 0).reshape(-1)
+            st[k, :, 3] = (m[ys + 1:ye + 2, xs:xe + 1] == 0).reshape(-1)
         self.statics = torch.tensor(st, device="cuda")
         # increment scales from the data (RMS of each channel's k-step change),
         # accumulated domain by domain
@@ -210,31 +237,108 @@ class Dataset:
             acc += inc.double().pow(2).sum(dim=(0, 1))
         rms = (acc / (count * (nsnap - 1) * HW)).sqrt().cpu().numpy()
         self.inc_scale = tuple(float(max(v, 1e-12)) for v in rms)
+        # scales of the difference channels: their RMS over a sample of pairs
+        self.diff_scale = (1.0, 1.0, 1.0)
+        sample = [(d, s) for d in range(0, count, max(1, count // 8))
+                  for s in range(0, nsnap - 1, max(1, (nsnap - 1) // 4))][:32]
+        xs_ = torch.zeros(len(sample) * HW, CPAD_IN, dtype=torch.bfloat16, device="cuda")
+        self.batch(sample, xs_, None)
+        drms = xs_[:, 5:8].float().double().pow(2).mean(dim=0).sqrt().cpu().numpy()
+        self.diff_scale = tuple(float(max(v, 1e-12)) for v in drms)
+
+    def scales(self, noise_frac=0.0):
+        """State, increment and difference-channel scales, then the input
+        noise standard deviations (noise_frac x the increment scales)."""
+        noise = tuple(noise_frac * v for v in self.inc_scale)
+        return (ctypes.c_float * 12)(*(STATE_SCALE + self.inc_scale + self.diff_scale + noise))
 
     def forcing(self, dom, snap):
         """Tide at the target time of pair (dom, snap)."""
         s = self.specs[dom]
         return tide_value(s["tide_amp"], s["tide_period_h"], (snap + 1) * K_STEPS, self.rdt)
 
-    def batch(self, pairs, x, target):
-        """Fills x (BF16) and target (FP32, or None) for (dom, snap) pairs."""
+    def assemble(self, states, src, doms, tsnaps, x, target=None, noise_frac=0.0, seed=0):
+        """Inputs x (BF16) from states[src[b]] (states: FP32 [m][HW][3]) of
+        domain doms[b], with the forcing of snapshot interval tsnaps[b];
+        target (FP32, or None) is the increment to states[src[b] + 1]."""
         torch = _torch()
-        src = torch.tensor([d * self.nsnap + s for d, s in pairs], dtype=torch.int32,
-                           device="cuda")
-        dom = torch.tensor([d for d, _ in pairs], dtype=torch.int32, device="cuda")
-        forcing = torch.tensor([self.forcing(d, s) for d, s in pairs], dtype=torch.float32,
-                               device="cuda")
-        scale6 = (ctypes.c_float * 6)(*(STATE_SCALE + self.inc_scale))
-        _ck(self.lib.nl2d_emu_assemble(_p(self.snaps), _p(self.statics), _p(src), _p(dom),
-                                       _p(forcing), scale6, _p(x),
+        src_t = torch.tensor(list(src), dtype=torch.int32, device="cuda")
+        dom_t = torch.tensor(list(doms), dtype=torch.int32, device="cuda")
+        forcing = torch.tensor([self.forcing(d, t) for d, t in zip(doms, tsnaps)],
+                               dtype=torch.float32, device="cuda")
+        _ck(self.lib.nl2d_emu_assemble(_p(states), _p(self.statics), _p(src_t), _p(dom_t),
+                                       _p(forcing), self.scales(noise_frac), seed, _p(x),
                                        _p(target) if target is not None else None,
-                                       self.n * self.n, CPAD_IN, len(pairs), None),
+                                       self.n, self.n, CPAD_IN, len(src_t), None),
             "nl2d_emu_assemble")
 
+    def advance(self, states, out, doms, tsnaps):
+        """states[b] += the network's increments `out` over snapshot interval
+        tsnaps[b], with the solver's boundary conditions (wall faces at zero
+        velocity, tidal ssh next to the open side); states: FP32
+        [len(doms)][HW][3]."""
+        torch = _torch()
+        dom_t = torch.tensor(list(doms), dtype=torch.int32, device="cuda")
+        forcing = torch.tensor([self.forcing(d, t) for d, t in zip(doms, tsnaps)],
+                               dtype=torch.float32, device="cuda")
+        HW = self.n * self.n
+        _ck(self.lib.nl2d_emu_advance(_p(states), _p(out), (ctypes.c_float * 3)(*self.inc_scale),
+                                      _p(self.statics), _p(dom_t), _p(forcing), HW,
+                                      len(dom_t) * HW, CPAD_OUT, None), "nl2d_emu_advance")
 
-def train(ds, net, iters=2000, lr=1e-3, seed=0, holdout=20):
-    """Trains on pairs of the first count - holdout domains; returns the loss
-    history."""
+    def open_band_weights(self, weight, band=4):
+        """Per-pixel loss weights [count][HW]: `weight` on cells within
+        `band` cells of the open side, where the tide drives the largest
+        and least regular increments, 1 elsewhere."""
+        torch = _torch()
+        n = self.n
+        w = np.ones((len(self.specs), n, n), np.float32)
+        for k, s in enumerate(self.specs):
+            side = s["open_side"]
+            if side == "S":
+                w[k, :band] = weight
+            elif side == "N":
+                w[k, -band:] = weight
+            elif side == "W":
+                w[k, :, :band] = weight
+            else:
+                w[k, :, -band:] = weight
+        return torch.tensor(w.reshape(len(self.specs), n * n), device="cuda")
+
+    def batch(self, pairs, x, target, noise_frac=0.0, seed=0):
+        """Fills x (BF16) and target (FP32, or None) for (dom, snap) pairs;
+        with noise_frac > 0 the input states are perturbed (training)."""
+        self.assemble(self.snaps, [d * self.nsnap + s for d, s in pairs], [d for d, _ in pairs],
+                      [s for _, s in pairs], x, target, noise_frac, seed)
+
+    def pushforward_batch(self, net, pairs, unroll, x, target):
+        """Inputs and targets for the pushforward objective: the state of
+        pair (d, s) is advanced `unroll` steps by the network itself (no
+        gradient), and the target is the increment from that emulated state
+        to snapshot s + unroll + 1 of the solver, so the network learns to
+        correct the errors it makes itself."""
+        torch = _torch()
+        B, HW = len(pairs), self.n * self.n
+        idx = torch.tensor([d * self.nsnap + s for d, s in pairs], device="cuda")
+        doms = [d for d, _ in pairs]
+        cur = self.snaps.index_select(0, idx)
+        for j in range(unroll):
+            self.assemble(cur, range(B), doms, [s + j for _, s in pairs], x)
+            self.advance(cur, net.forward(x, batch=B), doms, [s + j for _, s in pairs])
+        pair_buf = torch.stack((cur, self.snaps.index_select(0, idx + unroll + 1)), dim=1)
+        self.assemble(pair_buf, range(0, 2 * B, 2), doms, [s + unroll for _, s in pairs], x,
+                      target)
+
+
+def train(ds, net, iters=2000, lr=1e-3, seed=0, holdout=20, noise_frac=0.0, pushforward=0.0,
+          max_unroll=1, band_weight=1.0):
+    """Trains on pairs of the first count - holdout domains (cosine learning
+    rate decay) and returns the loss history.  noise_frac perturbs the
+    inputs by that fraction of the increment scales; with probability
+    `pushforward` an iteration (after the first fifth) instead trains on
+    states the network advanced itself by 1..max_unroll steps, which keeps
+    long roll-outs on the solver's trajectories.  band_weight > 1 weights
+    the loss on the cells next to the open side."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     ntrain = len(ds.specs) - holdout
@@ -242,11 +346,24 @@ def train(ds, net, iters=2000, lr=1e-3, seed=0, holdout=20):
     x = torch.zeros(P, CPAD_IN, dtype=torch.bfloat16, device="cuda")
     tgt = torch.zeros(P, 3, device="cuda")
     hist = []
+    weights = ds.open_band_weights(band_weight) if band_weight != 1.0 else None
     for it in range(iters):
-        pairs = [(int(rng.integers(0, ntrain)), int(rng.integers(0, ds.nsnap - 1)))
-                 for _ in range(net.batch)]
-        ds.batch(pairs, x, tgt)
-        hist.append(net.train_step(x, tgt, lr=lr * (0.1 if it > 0.8 * iters else 1.0)))
+        if pushforward and it > iters // 5 and rng.random() < pushforward:
+            unroll = int(rng.integers(1, max_unroll + 1))
+            pairs = [(int(rng.integers(0, ntrain)), int(rng.integers(0, ds.nsnap - 1 - unroll)))
+                     for _ in range(net.batch)]
+            ds.pushforward_batch(net, pairs, unroll, x, tgt)
+        else:
+            pairs = [(int(rng.integers(0, ntrain)), int(rng.integers(0, ds.nsnap - 1)))
+                     for _ in range(net.batch)]
+            ds.batch(pairs, x, tgt, noise_frac=noise_frac,
+                     seed=int(rng.integers(0, 2 ** 63 - 1)) if noise_frac else 0)
+        rate = lr * (0.02 + 0.98 * 0.5 * (1.0 + math.cos(math.pi * it / max(1, iters))))
+        wb = None
+        if weights is not None:
+            idx = torch.tensor([d for d, _ in pairs], device="cuda")
+            wb = weights.index_select(0, idx).reshape(-1)
+        hist.append(net.train_step(x, tgt, lr=rate, weight=wb))
     return hist
 
 
@@ -292,7 +409,7 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     start = state.clone()
     x = torch.zeros(net.batch * HW, CPAD_IN, dtype=torch.bfloat16, device="cuda")
     inc_scale = (ctypes.c_float * 3)(*ds.inc_scale)
-    scale6 = (ctypes.c_float * 6)(*(STATE_SCALE + ds.inc_scale))
+    scale12 = ds.scales()
     src = torch.arange(nd, dtype=torch.int32, device="cuda")
     domt = torch.tensor(list(domains), dtype=torch.int32, device="cuda")
     buf = torch.zeros(nd, HW, 3, device="cuda")
@@ -305,10 +422,11 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
                                            istep + K_STEPS, ds.rdt) for d in domains],
                                dtype=torch.float32, device="cuda")
         _ck(lib.nl2d_emu_assemble(_p(st), _p(ds.statics), _p(src), _p(domt), _p(forcing),
-                                  scale6, _p(x), None, HW, CPAD_IN, nd, None), "assemble")
+                                  scale12, 0, _p(x), None, n, n, CPAD_IN, nd, None),
+            "assemble")
         out = net.forward(x, batch=nd)
-        _ck(lib.nl2d_emu_advance(_p(st), _p(out), inc_scale, nd * HW, CPAD_OUT, None),
-            "advance")
+        _ck(lib.nl2d_emu_advance(_p(st), _p(out), inc_scale, _p(ds.statics), _p(domt),
+                                 _p(forcing), HW, nd * HW, CPAD_OUT, None), "advance")
 
     def solve(st, istep, nsteps):
         _ck(lib.nl2d_ens_import_interior(_p(st)), "import")
@@ -331,7 +449,7 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
         err = float((pred[:, :, 0] - ref[:, :, 0]).pow(2).mean().sqrt())
         report["judge_errors_m"].append(err)
         window = min(judge_every, emu_steps - k)
-        if err > threshold:
+        if not err <= threshold:  # a non-finite error fails the judge too
             state, ms = solve(state, istep, window * K_STEPS)
             sol_ms += ms
             report["windows_solver"] += 1

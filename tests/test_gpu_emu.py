@@ -51,13 +51,15 @@ def test_conv3x3_tcgen05_matches_fp64(gpulib, cin, cout, relu):
     np.testing.assert_allclose(y16.float().cpu().numpy(), want, rtol=1e-2, atol=1e-2 * scale)
 
 
-def test_conv_backward_matches_fp64(gpulib):
+@pytest.mark.parametrize("B,H,W,cin,cout", [(2, 4, 128, 48, 16), (2, 3, 256, 16, 48),
+                                             (1, 5, 128, 48, 48)])
+def test_conv_backward_matches_fp64(gpulib, B, H, W, cin, cout):
     """Input gradient (tcgen05 conv with flipped, transposed weights) and
-    weight / bias gradients (FP32 reduction) of L = sum(y * G) against the
-    FP64 numpy gradients."""
+    weight / bias gradients (tcgen05 GEMM over pixels, FP32 in tensor memory)
+    of L = sum(y * G) against the FP64 numpy gradients, for the layer shapes
+    of the network (16 -> 48, 48 -> 48, 48 -> 16)."""
     import torch
     rng = np.random.default_rng(5)
-    B, H, W, cin, cout = 2, 4, 128, 48, 16
     x = bf16_round(rng.normal(size=(B, H, W, cin)).astype(np.float32))
     w = bf16_round((rng.normal(size=(9, cout, cin)) / 20).astype(np.float32))
     G = bf16_round(rng.normal(size=(B, H, W, cout)).astype(np.float32))
@@ -84,7 +86,8 @@ def test_conv_backward_matches_fp64(gpulib):
     gw = torch.zeros(9, cout, cin, device="cuda")
     gb = torch.zeros(cout, device="cuda")
     assert gpulib.nl2d_emu_conv_wgrad(dxd.data_ptr(), dG.data_ptr(), gw.data_ptr(),
-                                      gb.data_ptr(), B, H, W, cin, cout, None) == 0
+                                      gb.data_ptr(), B, H, W, cin, cout, err.data_ptr(),
+                                      None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     for got, want in ((gx, dx_ref), (gw, dw_ref), (gb, db_ref)):
@@ -113,3 +116,138 @@ def test_training_fits_a_known_convolution(gpulib):
     for _ in range(300):
         last = net.train_step(x, t, lr=3e-3)
     assert last < 0.1 * first, (first, last)
+
+
+@pytest.fixture(scope="module")
+def small_dataset(gpulib):
+    """Solver trajectories of 8 domains of 128 x 128 cells, 21 snapshots
+    (200 FP64 solver steps) each."""
+    from psyclonebench_gb300.emulator import Dataset
+    return Dataset(count=8, nsnap=21, seed=3, n=128, lib=gpulib)
+
+
+def _derived(eta, u, v, d):
+    """East / north ssh differences and depth-weighted flux divergence of
+    one image, zero across the image edge."""
+    gx = np.zeros_like(eta)
+    gx[:, :-1] = eta[:, 1:] - eta[:, :-1]
+    gy = np.zeros_like(eta)
+    gy[:-1] = eta[1:] - eta[:-1]
+    de = d.copy()
+    de[:, :-1] = 0.5 * (d[:, :-1] + d[:, 1:])
+    dn = d.copy()
+    dn[:-1] = 0.5 * (d[:-1] + d[1:])
+    fe, fn = de * u, dn * v
+    div = fe + fn
+    div[:, 1:] -= fe[:, :-1]
+    div[1:] -= fn[:-1]
+    return gx, gy, div
+
+
+@pytest.mark.parametrize("noise_frac", [0.0, 0.5])
+def test_assemble_channels_match_numpy(gpulib, small_dataset, noise_frac):
+    """Every input channel and the target of one assembled pair against the
+    same quantities formed in numpy.  With noise, the perturbed state is
+    recovered from the target (next snapshot minus increment); the noise
+    has the requested standard deviation and every channel is consistent
+    with the same perturbed state."""
+    import torch
+    from psyclonebench_gb300.emulator import CPAD_IN, STATE_SCALE
+    ds = small_dataset
+    n = ds.n
+    dom, snap = 5, 7
+    x = torch.zeros(n * n, CPAD_IN, dtype=torch.bfloat16, device="cuda")
+    tg = torch.zeros(n * n, 3, device="cuda")
+    ds.batch([(dom, snap)], x, tg, noise_frac=noise_frac, seed=1234)
+    torch.cuda.synchronize()
+    s0 = ds.snaps[dom * ds.nsnap + snap].cpu().numpy().reshape(n, n, 3).astype(np.float64)
+    s1 = ds.snaps[dom * ds.nsnap + snap + 1].cpu().numpy().reshape(n, n, 3).astype(np.float64)
+    st = ds.statics[dom].cpu().numpy().reshape(n, n, 4).astype(np.float64)
+    # the solver holds velocities on wall faces at zero
+    assert st[..., 2].any() and st[..., 3].any()
+    assert not s0[..., 1][st[..., 2] > 0].any() and not s0[..., 2][st[..., 3] > 0].any()
+    inc_scale = np.array(ds.inc_scale)
+    tgt = tg.cpu().numpy().reshape(n, n, 3).astype(np.float64)
+    if noise_frac:
+        state = s1 - tgt * inc_scale
+        noise = state - s0
+        for ch in range(3):
+            sd = noise[..., ch].std()
+            assert abs(sd / (noise_frac * inc_scale[ch]) - 1.0) < 0.05
+            assert abs(noise[..., ch].mean()) < 0.05 * sd
+    else:
+        state = s0
+        np.testing.assert_allclose(tgt, (s1 - s0) / inc_scale, rtol=1e-4,
+                                   atol=1e-4 * np.abs((s1 - s0) / inc_scale).max())
+    eta, u, v, d = state[..., 0], state[..., 1], state[..., 2], st[..., 0]
+    gx, gy, div = _derived(eta, u, v, d)
+    want = [(eta - ds.forcing(dom, snap)) / STATE_SCALE[0], u / STATE_SCALE[1], v / STATE_SCALE[2], d,
+            ds.forcing(dom, snap) * st[..., 1] / STATE_SCALE[0],
+            gx / ds.diff_scale[0], gy / ds.diff_scale[1], div / ds.diff_scale[2],
+            st[..., 1], (eta - ds.forcing(dom, snap)) * st[..., 1] / STATE_SCALE[0],
+            st[..., 2], st[..., 3]]
+    got = x.float().cpu().numpy().reshape(n, n, CPAD_IN)
+    for c, w in enumerate(want):
+        np.testing.assert_allclose(got[..., c], w, rtol=2 ** -7, atol=2e-3 * np.abs(w).max(),
+                                   err_msg="channel %d" % c)
+    # low BF16 parts: high + low carries the state channels to ~2^-16
+    for c in range(3):
+        full = got[..., c].astype(np.float64) + got[..., 12 + c]
+        np.testing.assert_allclose(full, want[c], rtol=2 ** -14, atol=1e-6 * np.abs(want[c]).max(),
+                                   err_msg="channel %d high + low" % c)
+    assert not got[..., 15:].any()
+
+
+def test_emulator_beats_persistence_on_held_out_domains(gpulib, small_dataset):
+    """Trained on 6 domains' solver trajectories, the network's 10-step ssh
+    error on the 2 held-out domains is well below that of persistence (the
+    state left unchanged, the method without the network)."""
+    from psyclonebench_gb300.emulator import ConvNet, evaluate, train
+    ds = small_dataset
+    net = ConvNet(4, ds.n, ds.n, seed=2, lib=gpulib)
+    hist = train(ds, net, iters=400, lr=2e-3, holdout=2)
+    assert hist[-1] < 0.5 * hist[0]
+    err_net, err_pers = evaluate(ds, net, [6, 7], list(range(2, ds.nsnap - 1, 3)))
+    assert err_net < 0.5 * err_pers, (err_net, err_pers)
+
+
+def test_hybrid_rollout_judges_and_falls_back(gpulib, small_dataset):
+    """A roll-out with the FP64 solver as judge: with an unreachable error
+    threshold every window falls back to the solver, whose result then
+    equals the pure-solver truth up to the FP32 hand-off of the state
+    between windows; with a loose one the emulator keeps every window."""
+    from psyclonebench_gb300.emulator import ConvNet, rollout
+    ds = small_dataset
+    net = ConvNet(4, ds.n, ds.n, seed=2, lib=gpulib)
+    strict = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=0.0)
+    assert strict["windows_solver"] == 2 and strict["windows_emulator"] == 0
+    assert strict["final_ssh_rms_error_m"] < 1e-6
+    loose = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=1e9)
+    assert loose["windows_emulator"] == 2 and loose["windows_solver"] == 0
+    assert len(loose["judge_errors_m"]) == 2
+
+
+def test_advance_applies_the_solver_boundary_conditions(gpulib, small_dataset):
+    """state + increment x scale everywhere, except: zero velocity on wall
+    faces and the tide at the target time on cells next to the open side."""
+    import torch
+    from psyclonebench_gb300.emulator import CPAD_OUT
+    ds = small_dataset
+    n = ds.n
+    doms, tsnaps = [1, 4], [3, 9]
+    torch.manual_seed(0)
+    state = torch.randn(2, n * n, 3, device="cuda")
+    out = torch.randn(2 * n * n, CPAD_OUT, device="cuda")
+    want = state.cpu().numpy().astype(np.float64) + \
+        out.cpu().numpy()[:, :3].reshape(2, n * n, 3) * np.array(ds.inc_scale)
+    ds.advance(state, out, doms, tsnaps)
+    torch.cuda.synchronize()
+    got = state.cpu().numpy()
+    for q, (d, t) in enumerate(zip(doms, tsnaps)):
+        st = ds.statics[d].cpu().numpy()
+        w = want[q].copy()
+        w[st[:, 1] > 0, 0] = ds.forcing(d, t)
+        w[st[:, 2] > 0, 1] = 0.0
+        w[st[:, 3] > 0, 2] = 0.0
+        assert (st[:, 1] > 0).any()
+        np.testing.assert_allclose(got[q], w, rtol=1e-6, atol=1e-6)
