@@ -60,7 +60,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
-                    help="skip the mixed-precision (config 2) measurement")
+                    help="skip the mixed-precision, ensemble and emulator measurements")
+    ap.add_argument("--no-emulator", action="store_true", help="skip the emulator (config 4)")
+    ap.add_argument("--emu-iters", type=int, default=8000, help="emulator training iterations")
     return ap.parse_args()
 
 
@@ -314,6 +316,68 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
                                               "cached")}}
 
 
+def run_emulator(lib, count=200, nsnap=101, iters=8000, seed=11):
+    """Config 4: the learned emulator.  Solver trajectories of `count`
+    domains of 256^2 cells ((nsnap - 1) x count snapshot pairs, k = 10 FP64
+    steps apart) are generated by the persistent FP64 ensemble; the 6-layer
+    48-channel network trains on them (tcgen05 forward and backward); the
+    report gives the held-out one-step ssh error against persistence, the
+    inference throughput in solver-equivalent cell-steps against the FP64
+    solver on the same domains, and a hybrid roll-out judged by the FP64
+    solver every 50 emulator steps (fallback above 1 mm ssh RMS)."""
+    import torch
+    from psyclonebench_gb300 import emulator as E
+    t0 = time.perf_counter()
+    ds = E.Dataset(count=count, nsnap=nsnap, seed=seed, n=256, lib=lib)
+    gen_s = time.perf_counter() - t0
+    nhold = max(2, count // 10)
+    hold = list(range(count - nhold, count))
+    net = E.ConvNet(16, 256, 256, lib=lib)
+    t0 = time.perf_counter()
+    hist = E.train(ds, net, iters=iters, holdout=nhold, pushforward=0.5, max_unroll=2)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    err_net, err_pers = E.evaluate(ds, net, hold, list(range(10, nsnap - 1, 10)))
+    # inference: one emulator step (k = 10 solver steps) of 16 domains
+    P_ = 16 * 256 * 256
+    x = torch.zeros(P_, E.CPAD_IN, dtype=torch.bfloat16, device="cuda")
+    ds.batch([(hold[q % nhold], 5) for q in range(16)], x, None)
+    for _ in range(3):
+        net.forward(x)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    reps = 50
+    for _ in range(reps):
+        net.forward(x)
+    ev1.record()
+    torch.cuda.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / reps
+    flops = 2 * 9 * sum(ci * co for ci, co, _ in E.LAYERS) * P_
+    emu_value = P_ * E.K_STEPS / (fwd_ms * 1e-3) / 1e6
+    solver_value = count * 256 * 256 / (ds.solver_ms_per_step * 1e-3) / 1e6
+    # 500 emulator steps = 5000 solver steps, judged every 50
+    roll = E.rollout(ds, net, hold[:16], start_snap=10, emu_steps=500, judge_every=50,
+                     threshold=1e-3)
+    return {
+        "workload": "nemolite2d_emulator_%d_domains_256x256_%d_pairs_k10" % (
+            count, count * (nsnap - 1)),
+        "dropped_unstable_domains": len(ds.dropped),
+        "data_generation_s": gen_s,
+        "train": {"iterations": iters, "batch": 16, "seconds": train_s,
+                  "ms_per_step": train_s / iters * 1e3,
+                  "loss_first": hist[0], "loss_last100": sum(hist[-100:]) / 100},
+        "held_out_one_step_ssh_rms_m": {"network": err_net, "persistence": err_pers,
+                                        "gain": err_pers / err_net},
+        "inference": {"forward_ms_16x256x256": fwd_ms,
+                      "tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                      "value": emu_value, "unit": "solver-equivalent Mcell-steps/s",
+                      "fp64_solver_same_domains": solver_value,
+                      "speedup_vs_fp64_solver": emu_value / solver_value},
+        "rollout": roll,
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -420,6 +484,8 @@ def run_ours(args, rank, world, local):
         ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
         ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
         forms["ensemble"] = ens
+        if not args.no_emulator:
+            forms["emulator"] = run_emulator(lib, iters=args.emu_iters)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -37,6 +37,9 @@ extern "C" {
 #define NL2D_ERR_UNKNOWN_FIELD 4 /* pointer is not a registered field        */
 #define NL2D_ERR_NONFINITE 5   /* a checksum found a NaN or an infinity      */
 #define NL2D_ERR_TOO_LARGE 6   /* beyond a fixed capacity (no-alloc entry)   */
+#define NL2D_ERR_IO 7          /* a file could not be opened or written      */
+#define NL2D_ERR_PARSE 8       /* the namelist is not a valid &namctl group  */
+#define NL2D_ERR_UNSUPPORTED 9 /* a configuration the reference also stops on */
 
 /* Step paths (nl2d_set_mode). */
 #define NL2D_MODE_AUTO 0       /* fused one-launch step whenever its preconditions hold */
@@ -301,6 +304,52 @@ int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
 
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
+
+/* ---- host side of the reference executable (no GPU needed) ---- */
+
+/* Reads the &namctl group of a Fortran namelist file
+ * (common/gocean2d_io_mod.f90:22-80 read_namelist): ints = jpiglo, jpjglo,
+ * jphgr_msh, nit000, nitend, irecord; dbls = dx, dy, dep_const, rdt, cbfr,
+ * visc.  Keys the file omits keep the reference's defaults.  NL2D_ERR_IO if
+ * the file cannot be opened, NL2D_ERR_PARSE for a syntax error or a key
+ * outside the group (the reference stops with "err found in reading
+ * namelist file"). */
+int nl2d_read_namelist(const char *path, int *ints, double *dbls);
+
+/* The reference's single-rank start state into caller-owned row-major
+ * [height][width] arrays (width >= jpiglo + 1, height >= jpjglo + 1,
+ * internal T cells 1..jpiglo-2 x 1..jpjglo-2, 0-based): T mask
+ * (common/model_mod.f90:94-249 setup_tpoints_mask, jphgr_msh 1-3), grid
+ * metrics and T-point coordinates (original/nemolite2d.f90:218-290),
+ * depths dep_const and a state at rest
+ * (common/initialisation_mod.f90:7-63).  fields = the 13 field arrays in
+ * c_invoke_time_step's order; metrics = area_t, area_u, area_v, dx_u, dx_v,
+ * dx_t, dy_u, dy_v, dy_t, gphiu, gphiv; xt, yt may be NULL.  jphgr_msh = 0
+ * ("read from file", a STOP in the reference) gives NL2D_ERR_UNSUPPORTED. */
+int nl2d_setup_model(int jphgr_msh, int jpiglo, int jpjglo, double dx,
+                     double dy, double dep_const, int width, int height,
+                     double *const *fields, int *tmask, double *const *metrics,
+                     double *xt, double *yt);
+
+/* Writes dir/go2d_<istp:5>_<rank:5>.dat exactly as model_write
+ * (common/gocean2d_io_mod.f90:97-149) does: per internal T point x, y,
+ * depth, ssh and the velocities averaged to the T point, `(6e16.7)`; an
+ * empty record after each row.  Host arrays [][width]. */
+int nl2d_model_write(const char *dir, int istp, int rank, int width, int xs,
+                     int xe, int ys, int ye, const double *xt, const double *yt,
+                     const double *ht, const double *sshn, const double *un,
+                     const double *vn);
+
+/* Writes dir/tmask_<rank:5>.dat as dump_tmask (common/model_mod.f90:251-291):
+ * raw = every point of the nx x ny mask as `(3(I4,1x))`, else the internal T
+ * points with coordinates as `(2e16.7,1x,I3)`. */
+int nl2d_dump_tmask(const char *dir, int rank, int raw, int width, int nx,
+                    int ny, const int *tmask, int xs, int xe, int ys, int ye,
+                    const double *xt, const double *yt);
+
+/* One value in the Fortran edit descriptor Ew.d (gfortran's layout) into
+ * out (cap >= w + 1 bytes). */
+int nl2d_format_e(double v, int w, int d, char *out, int cap);
 
 /* Device address currently holding a registered field (for callers that
  * share device memory); NULL if unknown.  Valid until the next step. */

@@ -431,8 +431,10 @@ int oracle_read_namelist(const char *path, int ints[6], double dbls[6])
             {
                 char *end;
                 int found = 0;
-                /* Fortran 'd' exponents become 'e' for strtod. */
-                for (q = p; *q && *q != ',' && *q != '/'; q++)
+                /* Fortran 'd' exponents become 'e' for strtod (within
+                 * this value only: it ends at a blank, ',' or '/'). */
+                while (*p && isspace((unsigned char)*p)) p++;
+                for (q = p; *q && *q != ',' && *q != '/' && !isspace((unsigned char)*q); q++)
                     if (*q == 'd') *q = 'e';
                 for (k = 0; k < 6 && !found; k++)
                     if (strcmp(key, ikeys[k]) == 0) {

@@ -18,6 +18,9 @@ NL2D_ERR_STATE = 3
 NL2D_ERR_UNKNOWN_FIELD = 4
 NL2D_ERR_NONFINITE = 5
 NL2D_ERR_TOO_LARGE = 6
+NL2D_ERR_IO = 7
+NL2D_ERR_PARSE = 8
+NL2D_ERR_UNSUPPORTED = 9
 NL2D_MODE_AUTO = 0
 NL2D_MODE_REFERENCE = 1
 
@@ -76,6 +79,15 @@ EXPORTS = {
                                                  ctypes.c_int, _VP]),
     "nl2d_ens_export_interior": (ctypes.c_int, [_VP]),
     "nl2d_ens_import_interior": (ctypes.c_int, [_VP]),
+    "nl2d_read_namelist": (ctypes.c_int, [ctypes.c_char_p, _IP, _DP]),
+    "nl2d_setup_model": (ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 3 +
+                         [ctypes.c_int] * 2 + [ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP),
+                                               _DP, _DP]),
+    "nl2d_model_write": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 7 + [_DP] * 6),
+    "nl2d_dump_tmask": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 5 + [_IP] +
+                        [ctypes.c_int] * 4 + [_DP, _DP]),
+    "nl2d_format_e": (ctypes.c_int, [ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_char_p, ctypes.c_int]),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }

@@ -14,6 +14,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libnl2d_gpu.so")
+# The reference executable's driver around the library (host C++ only).
+DRIVER_SRC = "nl2d_driver_main.cpp"
+DRIVER = os.path.join(OUT_DIR, "nemolite2d_gb300")
 REPO = os.path.dirname(PKG)
 
 SOURCES = [
@@ -24,6 +27,7 @@ SOURCES = [
     "nl2d_mixed.cu",
     "nl2d_ensemble.cu",
     "nl2d_emu.cu",
+    "nl2d_io.cpp",
 ]
 # The mixed-precision form has no bit-exactness contract: FMA contraction on.
 PER_FILE_FLAGS = {"nl2d_mixed.cu": ["-fmad=true"]}
@@ -64,7 +68,7 @@ def build(force=False, verbose=False):
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             flags = [f for f in NVCC_FLAGS
@@ -84,6 +88,11 @@ def build(force=False, verbose=False):
             pass
     if force or jobs or _stale(LIB, objs):
         run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    drv_src = os.path.join(CSRC, DRIVER_SRC)
+    if force or _stale(DRIVER, [drv_src, LIB] + hdrs):
+        run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off",
+             "-I" + os.path.join(REPO, "include"), drv_src, "-o", DRIVER, "-L" + OUT_DIR,
+             "-lnl2d_gpu", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -397,24 +397,53 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     judge_every emulator steps the FP64 solver advances the same state by
     K_STEPS steps and the ssh RMS difference of the two is the judge's error;
     above `threshold` (m) the next window runs on the solver instead.  A
-    pure-solver run from the same start gives the truth.  Returns a report."""
+    pure-solver run from the same start gives the truth; domains on which
+    that run itself goes non-finite (the scheme's own instability) are left
+    out and listed.  Returns a report."""
     torch = _torch()
     lib = ds.lib
-    nd, n = len(domains), ds.n
+    n = ds.n
     HW = n * n
-    assert nd <= net.batch
-    sol = Ensemble([ds.doms[d] for d in domains], rdt=ds.rdt, lib=lib)
-    sol.run(1, 0)
-    state = torch.stack([ds.snaps[d * ds.nsnap + start_snap] for d in domains]).contiguous()
-    start = state.clone()
+    step0 = start_snap * K_STEPS
+    domains = list(domains)
+    assert len(domains) <= net.batch
+
+    def solver_for(doms):
+        e = Ensemble([ds.doms[d] for d in doms], rdt=ds.rdt, lib=lib)
+        e.run(1, 0)
+        return e
+
+    def initial(doms):
+        return torch.stack([ds.snaps[d * ds.nsnap + start_snap] for d in doms]).contiguous()
+
+    # the truth first: a pure-solver run over the whole horizon
+    sol = solver_for(domains)
+    start = initial(domains)
+    _ck(lib.nl2d_ens_import_interior(_p(start)), "import")
+    truth_ms, _ = sol.run(step0 + 1, emu_steps * K_STEPS)
+    truth = torch.zeros(len(domains), HW, 3, device="cuda")
+    _ck(lib.nl2d_ens_export_interior(_p(truth)), "export")
+    finite = [bool(torch.isfinite(truth[q]).all()) for q in range(len(domains))]
+    excluded = [d for d, f in zip(domains, finite) if not f]
+    if excluded:
+        keep = [q for q, f in enumerate(finite) if f]
+        truth = truth[keep].contiguous()
+        domains = [domains[q] for q in keep]
+        sol.close()
+        sol = solver_for(domains)
+    if not domains:
+        sol.close()
+        raise Nl2dError("every roll-out domain went non-finite in the solver itself")
+    nd = len(domains)
+    state = initial(domains)
     x = torch.zeros(net.batch * HW, CPAD_IN, dtype=torch.bfloat16, device="cuda")
     inc_scale = (ctypes.c_float * 3)(*ds.inc_scale)
     scale12 = ds.scales()
     src = torch.arange(nd, dtype=torch.int32, device="cuda")
     domt = torch.tensor(list(domains), dtype=torch.int32, device="cuda")
     buf = torch.zeros(nd, HW, 3, device="cuda")
-    report = {"windows_emulator": 0, "windows_solver": 0, "judge_errors_m": []}
-    step0 = start_snap * K_STEPS
+    report = {"windows_emulator": 0, "windows_solver": 0, "judge_errors_m": [],
+              "domains": nd, "excluded_unstable_in_solver": excluded}
     emu_ms = sol_ms = 0.0
 
     def emu_step(st, istep):
@@ -464,7 +493,6 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
             report["windows_emulator"] += 1
         istep += window * K_STEPS
         k += window
-    truth, truth_ms = solve(start, step0, emu_steps * K_STEPS)
     sol.close()
     d = (state[:, :, 0] - truth[:, :, 0])
     report.update({
