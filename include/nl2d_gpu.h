@@ -290,7 +290,10 @@ int nl2d_emu_advance(float *state, const float *inc, const float *inc_scale3,
 int nl2d_ens_export_interior(float *d_out);
 
 /* Sets the interior (ssh, u, v) of every ensemble domain from a device FP32
- * array [dom][ny][nx][3] (the emulator hands states back to the solver). */
+ * array [dom][ny][nx][3] (the emulator hands states back to the solver).
+ * The velocity on an open boundary face west or south of the interior (the
+ * Flather face, outside the array) is set from the adjacent interior face,
+ * so the imported state does not depend on what the solver held before. */
 int nl2d_ens_import_interior(const float *d_in);
 
 /* Test hook: over n sampled doubles x (seeded), counts where the exact

@@ -449,6 +449,12 @@ __global__ void k_export_interior(const EnsDomain* __restrict__ doms, int parity
 
 // The inverse: FP32 [dom][ny][nx][3] into the interior of the current FP64
 // state (both ping-pong buffers, so cells no step writes stay consistent).
+// The interior leaves out one piece of the solver's state: the velocity on
+// an open boundary face west or south of the interior (the Flather face),
+// which the next step's momentum reads.  It is set from the adjacent
+// interior face (zero normal gradient), so the state after an import
+// depends on the imported interior alone and not on what the solver held
+// before; wall faces stay zero.
 __global__ void k_import_interior(const EnsDomain* __restrict__ doms, int ndom, int nx, int ny,
                                   const float* __restrict__ in) {
   const long long n = (long long)ndom * nx * ny;
@@ -458,12 +464,19 @@ __global__ void k_import_interior(const EnsDomain* __restrict__ doms, int ndom, 
     const int rem = (int)(t - (long long)dom * nx * ny);
     const int j = rem / nx, i = rem - j * nx;
     const EnsDomain& D = doms[dom];
-    const size_t c = (size_t)(D.d.ys + j) * D.d.width + (D.d.xs + i);
+    const int W = D.d.width;
+    const size_t c = (size_t)(D.d.ys + j) * W + (D.d.xs + i);
+    const double e = (double)in[t * 3 + 0], u = (double)in[t * 3 + 1],
+                 v = (double)in[t * 3 + 2];
+    const bool west_open = i == 0 && D.f.tmask[c - 1] < 0;
+    const bool south_open = j == 0 && D.f.tmask[c - W] < 0;
     for (int p = 0; p < 2; p++) {
       const FusedState& st = D.fs[p];
-      const_cast<double*>(st.sshn_in)[c] = (double)in[t * 3 + 0];
-      const_cast<double*>(st.un_in)[c] = (double)in[t * 3 + 1];
-      const_cast<double*>(st.vn_in)[c] = (double)in[t * 3 + 2];
+      const_cast<double*>(st.sshn_in)[c] = e;
+      const_cast<double*>(st.un_in)[c] = u;
+      const_cast<double*>(st.vn_in)[c] = v;
+      if (west_open) const_cast<double*>(st.un_in)[c - 1] = u;
+      if (south_open) const_cast<double*>(st.vn_in)[c - W] = v;
     }
   }
 }

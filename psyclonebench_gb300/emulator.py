@@ -172,48 +172,74 @@ def emulator_domain_specs(count, seed, n=256):
 
 class Dataset:
     """Solver trajectories of `count` seeded domains on the GPU:
-    snaps [count * nsnap][n][n][3] FP32 (every K_STEPS steps), statics
-    [count][n][n][4] (depth / 500 m, open-boundary indicator, east / north
-    face is a wall).
+    snaps [count * nsnap][n][n][3] FP32 (every K_STEPS steps, from rest),
+    statics [count][n][n][4] (depth / 500 m, open-boundary indicator, east /
+    north face is a wall).  Training pairs start at `pair_starts` (all
+    snapshots but the last, or pairs_per_domain starts spread evenly over
+    the trajectory).
 
-    The scheme itself goes unstable on a few per cent of the seeded domains
-    (strong tides over shallow banks; the oracle blows up on the same ones),
-    so a few spare domains are generated and the first `count` whose whole
-    trajectory stays finite are kept; `dropped` lists the rest."""
+    The scheme itself goes unstable on a share of the seeded domains that
+    grows with the horizon (strong tides over shallow banks; the oracle
+    blows up on the same ones), so candidates are generated chunk by chunk
+    and the first `count` whose whole trajectory stays finite are kept;
+    `dropped` lists the candidates left out.  A test set passes its training
+    set as `scales_from` to be normalised the same way."""
 
-    def __init__(self, count=200, nsnap=101, seed=11, n=256, rdt=5.0, lib=None):
+    def __init__(self, count=200, nsnap=101, seed=11, n=256, rdt=5.0, lib=None,
+                 scales_from=None, pairs_per_domain=None, max_candidates=None):
         torch = _torch()
         self.lib = lib or load_library()
         self.n, self.nsnap, self.rdt = n, nsnap, rdt
-        total = count + max(2, count // 16)
-        specs = emulator_domain_specs(total, seed, n)
-        doms = [build_domain(s) for s in specs]
-        ens = Ensemble(doms, rdt=rdt, lib=self.lib)
         HW = n * n
-        snaps = torch.zeros(total, nsnap, HW, 3, device="cuda")
-        buf = torch.zeros(total, HW, 3, device="cuda")
+        max_candidates = max_candidates or 8 * count + 16
+        self.snaps = torch.zeros(count * nsnap, HW, 3, device="cuda")
+        self.specs, self.doms, self.dropped = [], [], []
+        cand = 0
+        chunk = min(96, count + max(2, count // 16))
+        solver_ms, cell_steps = 0.0, 0
         t0 = time.perf_counter()
-        ens.run(1, 0)  # builds the schedule
-        solver_ms = 0.0
-        for s in range(nsnap):
-            if s > 0:
-                ms, _ = ens.run(1 + (s - 1) * K_STEPS, K_STEPS)
-                solver_ms += ms
-            _ck(self.lib.nl2d_ens_export_interior(ctypes.c_void_p(buf.data_ptr())), "export")
-            snaps[:, s] = buf
+        while len(self.specs) < count:
+            if cand >= max_candidates:
+                raise Nl2dError("only %d of %d candidate domains stayed finite for %d steps" % (
+                    len(self.specs), cand, (nsnap - 1) * K_STEPS))
+            specs = emulator_domain_specs(cand + chunk, seed, n)[cand:]
+            doms = [build_domain(sp) for sp in specs]
+            ens = Ensemble(doms, rdt=rdt, lib=self.lib)
+            traj = torch.zeros(len(doms), nsnap, HW, 3, device="cuda")
+            buf = torch.zeros(len(doms), HW, 3, device="cuda")
+            ens.run(1, 0)  # builds the schedule
+            for sn in range(nsnap):
+                if sn > 0:
+                    ms, _ = ens.run(1 + (sn - 1) * K_STEPS, K_STEPS)
+                    solver_ms += ms
+                    cell_steps += len(doms) * HW * K_STEPS
+                _ck(self.lib.nl2d_ens_export_interior(ctypes.c_void_p(buf.data_ptr())), "export")
+                traj[:, sn] = buf
+            ens.close()
+            for q in range(len(doms)):
+                if len(self.specs) == count:
+                    break
+                if not bool(torch.isfinite(traj[q]).all()):
+                    self.dropped.append(cand + q)
+                    continue
+                k = len(self.specs)
+                self.snaps[k * nsnap:(k + 1) * nsnap] = traj[q]
+                self.specs.append(specs[q])
+                self.doms.append(doms[q])
+            del traj, buf
+            cand += len(doms)
+            rate = max(0.2, len(self.specs) / cand)
+            chunk = min(96, int(math.ceil((count - len(self.specs)) / rate * 1.2)) + 1)
         self.gen_seconds = time.perf_counter() - t0
-        self.solver_ms_per_step = solver_ms / max(1, (nsnap - 1) * K_STEPS)
-        ens.close()
-        finite = [bool(torch.isfinite(snaps[k]).all()) for k in range(total)]
-        keep = [k for k in range(total) if finite[k]][:count]
-        if len(keep) < count:
-            raise Nl2dError("only %d of %d generated domains stayed finite" % (len(keep), total))
-        self.dropped = [k for k in range(keep[-1] + 1) if not finite[k]]
-        self.specs = [specs[k] for k in keep]
-        self.doms = [doms[k] for k in keep]
-        idx = torch.tensor(keep, device="cuda")
-        self.snaps = snaps.index_select(0, idx).reshape(count * nsnap, HW, 3)
-        del snaps, buf
+        self.candidates = cand
+        # FP64 ensemble throughput while generating (cell-steps per second)
+        self.solver_mcells = cell_steps / max(solver_ms * 1e-3, 1e-9) / 1e6
+        self.solver_ms_per_step = count * HW / self.solver_mcells / 1e3
+        if pairs_per_domain:
+            self.pair_starts = sorted(set(int(round(v)) for v in np.linspace(
+                0, nsnap - 2, pairs_per_domain)))
+        else:
+            self.pair_starts = list(range(nsnap - 1))
         doms = self.doms
         st = np.zeros((count, HW, 4), np.float32)
         for k, d in enumerate(doms):
@@ -237,6 +263,11 @@ class Dataset:
             acc += inc.double().pow(2).sum(dim=(0, 1))
         rms = (acc / (count * (nsnap - 1) * HW)).sqrt().cpu().numpy()
         self.inc_scale = tuple(float(max(v, 1e-12)) for v in rms)
+        if scales_from is not None:
+            # a test set: normalised as the network's training data was
+            self.inc_scale = scales_from.inc_scale
+            self.diff_scale = scales_from.diff_scale
+            return
         # scales of the difference channels: their RMS over a sample of pairs
         self.diff_scale = (1.0, 1.0, 1.0)
         sample = [(d, s) for d in range(0, count, max(1, count // 8))
@@ -350,11 +381,13 @@ def train(ds, net, iters=2000, lr=1e-3, seed=0, holdout=20, noise_frac=0.0, push
     for it in range(iters):
         if pushforward and it > iters // 5 and rng.random() < pushforward:
             unroll = int(rng.integers(1, max_unroll + 1))
-            pairs = [(int(rng.integers(0, ntrain)), int(rng.integers(0, ds.nsnap - 1 - unroll)))
+            starts = [s for s in ds.pair_starts if s + unroll + 1 <= ds.nsnap - 1]
+            pairs = [(int(rng.integers(0, ntrain)), starts[int(rng.integers(0, len(starts)))])
                      for _ in range(net.batch)]
             ds.pushforward_batch(net, pairs, unroll, x, tgt)
         else:
-            pairs = [(int(rng.integers(0, ntrain)), int(rng.integers(0, ds.nsnap - 1)))
+            starts = ds.pair_starts
+            pairs = [(int(rng.integers(0, ntrain)), starts[int(rng.integers(0, len(starts)))])
                      for _ in range(net.batch)]
             ds.batch(pairs, x, tgt, noise_frac=noise_frac,
                      seed=int(rng.integers(0, 2 ** 63 - 1)) if noise_frac else 0)
@@ -392,21 +425,24 @@ def evaluate(ds, net, domains, snaps):
 
 
 def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, threshold=1e-3):
-    """Hybrid roll-out of `domains` (indices into ds) from snapshot
-    start_snap: the emulator advances K_STEPS solver steps per step; every
-    judge_every emulator steps the FP64 solver advances the same state by
-    K_STEPS steps and the ssh RMS difference of the two is the judge's error;
-    above `threshold` (m) the next window runs on the solver instead.  A
-    pure-solver run from the same start gives the truth; domains on which
-    that run itself goes non-finite (the scheme's own instability) are left
-    out and listed.  Returns a report."""
+    """Hybrid roll-out from snapshot start_snap.  The emulator advances
+    K_STEPS solver steps per step, in windows of judge_every steps; at the
+    end of each window the FP64 solver judges it: one emulator step against
+    K_STEPS solver steps from the window's end state, the ssh RMS difference
+    being the judge's error.  Above `threshold` (m), or if anything is
+    non-finite, the window is rolled back to its checkpoint and redone by
+    the solver.  A pure-solver run from the same start gives the truth.
+
+    `domains` are candidates (indices into ds): those on which the pure
+    solver run itself goes non-finite (the scheme's own instability) are
+    left out and listed, and the first net.batch of the rest are rolled
+    out.  Returns a report."""
     torch = _torch()
     lib = ds.lib
     n = ds.n
     HW = n * n
     step0 = start_snap * K_STEPS
     domains = list(domains)
-    assert len(domains) <= net.batch
 
     def solver_for(doms):
         e = Ensemble([ds.doms[d] for d in doms], rdt=ds.rdt, lib=lib)
@@ -418,22 +454,24 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
 
     # the truth first: a pure-solver run over the whole horizon
     sol = solver_for(domains)
-    start = initial(domains)
-    _ck(lib.nl2d_ens_import_interior(_p(start)), "import")
+    _ck(lib.nl2d_ens_import_interior(_p(initial(domains))), "import")
     truth_ms, _ = sol.run(step0 + 1, emu_steps * K_STEPS)
     truth = torch.zeros(len(domains), HW, 3, device="cuda")
     _ck(lib.nl2d_ens_export_interior(_p(truth)), "export")
     finite = [bool(torch.isfinite(truth[q]).all()) for q in range(len(domains))]
     excluded = [d for d, f in zip(domains, finite) if not f]
-    if excluded:
-        keep = [q for q, f in enumerate(finite) if f]
+    keep = [q for q, f in enumerate(finite) if f][:net.batch]
+    if not keep:
+        sol.close()
+        raise Nl2dError("every roll-out domain went non-finite in the solver itself")
+    if len(keep) != len(domains):
         truth = truth[keep].contiguous()
         domains = [domains[q] for q in keep]
         sol.close()
         sol = solver_for(domains)
-    if not domains:
-        sol.close()
-        raise Nl2dError("every roll-out domain went non-finite in the solver itself")
+        # the truth's solver time, for the kept domains only
+        _ck(lib.nl2d_ens_import_interior(_p(initial(domains))), "import")
+        truth_ms, _ = sol.run(step0 + 1, emu_steps * K_STEPS)
     nd = len(domains)
     state = initial(domains)
     x = torch.zeros(net.batch * HW, CPAD_IN, dtype=torch.bfloat16, device="cuda")
@@ -443,7 +481,8 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     domt = torch.tensor(list(domains), dtype=torch.int32, device="cuda")
     buf = torch.zeros(nd, HW, 3, device="cuda")
     report = {"windows_emulator": 0, "windows_solver": 0, "judge_errors_m": [],
-              "domains": nd, "excluded_unstable_in_solver": excluded}
+              "domains": nd, "candidates": len(finite),
+              "excluded_unstable_in_solver": excluded}
     emu_ms = sol_ms = 0.0
 
     def emu_step(st, istep):
@@ -466,30 +505,26 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     istep = step0
     k = 0
     while k < emu_steps:
-        # judge: one emulator step against K_STEPS solver steps from this state
-        pred = state.clone()
+        window = min(judge_every, emu_steps - k)
+        ckpt = state.clone()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        emu_step(pred, istep)
+        for q in range(window):
+            emu_step(state, istep + q * K_STEPS)
+        # judge: one more emulator step against K_STEPS solver steps
+        pred = state.clone()
+        emu_step(pred, istep + window * K_STEPS)
         torch.cuda.synchronize()
         emu_ms += (time.perf_counter() - t0) * 1e3
-        ref, ms = solve(state, istep, K_STEPS)
+        ref, ms = solve(state, istep + window * K_STEPS, K_STEPS)
         sol_ms += ms
         err = float((pred[:, :, 0] - ref[:, :, 0]).pow(2).mean().sqrt())
         report["judge_errors_m"].append(err)
-        window = min(judge_every, emu_steps - k)
         if not err <= threshold:  # a non-finite error fails the judge too
-            state, ms = solve(state, istep, window * K_STEPS)
+            state, ms = solve(ckpt, istep, window * K_STEPS)
             sol_ms += ms
             report["windows_solver"] += 1
         else:
-            state = pred
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for q in range(1, window):
-                emu_step(state, istep + q * K_STEPS)
-            torch.cuda.synchronize()
-            emu_ms += (time.perf_counter() - t0) * 1e3
             report["windows_emulator"] += 1
         istep += window * K_STEPS
         k += window
