@@ -39,7 +39,6 @@ extern "C" {
 #define NL2D_ERR_TOO_LARGE 6   /* beyond a fixed capacity (no-alloc entry)   */
 #define NL2D_ERR_IO 7          /* a file could not be opened or written      */
 #define NL2D_ERR_PARSE 8       /* the namelist is not a valid &namctl group  */
-#define NL2D_ERR_UNSUPPORTED 9 /* a configuration the reference also stops on */
 
 /* Step paths (nl2d_set_mode). */
 #define NL2D_MODE_AUTO 0       /* fused one-launch step whenever its preconditions hold */
@@ -328,7 +327,8 @@ int nl2d_read_namelist(const char *path, int *ints, double *dbls);
  * (common/initialisation_mod.f90:7-63).  fields = the 13 field arrays in
  * c_invoke_time_step's order; metrics = area_t, area_u, area_v, dx_u, dx_v,
  * dx_t, dy_u, dy_v, dy_t, gphiu, gphiv; xt, yt may be NULL.  jphgr_msh = 0
- * ("read from file", a STOP in the reference) gives NL2D_ERR_UNSUPPORTED. */
+ * (grid "read from file", a STOP in the reference) keeps the caller's tmask
+ * as it is (see nl2d_read_grid_file) and sets up everything else. */
 int nl2d_setup_model(int jphgr_msh, int jpiglo, int jpjglo, double dx,
                      double dy, double dep_const, int width, int height,
                      double *const *fields, int *tmask, double *const *metrics,
@@ -349,6 +349,19 @@ int nl2d_model_write(const char *dir, int istp, int rank, int width, int xs,
 int nl2d_dump_tmask(const char *dir, int rank, int raw, int width, int nx,
                     int ny, const int *tmask, int xs, int xe, int ys, int ye,
                     const double *xt, const double *yt);
+
+/* Reads a grid file of whitespace-separated "i j value" triples, one per
+ * point of the nx x ny mask (1-based; any order; the raw layout of
+ * dump_tmask, so a dumped mask reads back) into row-major [][width] `out`:
+ * ints if is_int (a T mask), else doubles (T-point depths).
+ * NL2D_ERR_PARSE unless every point appears exactly once. */
+int nl2d_read_grid_file(const char *path, int nx, int ny, int width,
+                        int is_int, void *out);
+
+/* Face depths from T-point depths: hu = mean of the two T cells across the
+ * east face, hv across the north face; the last column / row copies ht. */
+int nl2d_face_depths(int width, int height, const double *ht, double *hu,
+                     double *hv);
 
 /* One value in the Fortran edit descriptor Ew.d (gfortran's layout) into
  * out (cap >= w + 1 bytes). */

@@ -20,7 +20,6 @@ NL2D_ERR_NONFINITE = 5
 NL2D_ERR_TOO_LARGE = 6
 NL2D_ERR_IO = 7
 NL2D_ERR_PARSE = 8
-NL2D_ERR_UNSUPPORTED = 9
 NL2D_MODE_AUTO = 0
 NL2D_MODE_REFERENCE = 1
 
@@ -86,6 +85,8 @@ EXPORTS = {
     "nl2d_model_write": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 7 + [_DP] * 6),
     "nl2d_dump_tmask": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 5 + [_IP] +
                         [ctypes.c_int] * 4 + [_DP, _DP]),
+    "nl2d_read_grid_file": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_int] * 4 + [_VP]),
+    "nl2d_face_depths": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_format_e": (ctypes.c_int, [ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_char_p, ctypes.c_int]),
     "nl2d_sync": (ctypes.c_int, []),

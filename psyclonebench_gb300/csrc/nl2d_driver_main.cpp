@@ -86,11 +86,35 @@ int main(int argc, char** argv) {
   double* gp[11];
   for (int k = 0; k < 13; k++) fp[k] = f[k].data();
   for (int k = 0; k < 11; k++) gp[k] = g[k].data();
+  if (jphgr_msh == 0) {
+    // The grid from files (a STOP in the reference): the T mask from
+    // tmask_in.dat in dump_tmask's raw layout ("i j mask" for every point of
+    // the jpiglo x jpjglo mask); points past it stay land.
+    rc = nl2d_read_grid_file("tmask_in.dat", jpiglo, jpjglo, width, 1, tmask.data());
+    if (rc != NL2D_OK) {
+      std::fprintf(stderr, "jphgr_msh = 0 reads the T mask from tmask_in.dat: %s\n",
+                   rc == NL2D_ERR_IO ? "file not found" : "not one \"i j mask\" per point");
+      return 1;
+    }
+  }
   rc = nl2d_setup_model(jphgr_msh, jpiglo, jpjglo, dx, dy, dep_const, width, height, fp,
                         tmask.data(), gp, xt.data(), yt.data());
-  if (rc == NL2D_ERR_UNSUPPORTED) {
-    std::fprintf(stderr, "Reading the grid definition from file is not yet supported!\n");
-    return 1;
+  if (rc == NL2D_OK && jphgr_msh == 0) {
+    // optional T-point depths from depth_in.dat ("i j depth"); the column
+    // and row past the mask copy their neighbours; face depths are averages
+    std::vector<double> ht(cells, dep_const);
+    const int drc = nl2d_read_grid_file("depth_in.dat", jpiglo, jpjglo, width, 0, ht.data());
+    if (drc == NL2D_OK) {
+      for (int j = 0; j < height; j++)
+        for (int i = 0; i < width; i++) {
+          const int si = i < jpiglo ? i : jpiglo - 1, sj = j < jpjglo ? j : jpjglo - 1;
+          f[HT][(size_t)j * width + i] = ht[(size_t)sj * width + si];
+        }
+      nl2d_face_depths(width, height, f[HT].data(), f[HU].data(), f[HV].data());
+    } else if (drc != NL2D_ERR_IO) {
+      std::fprintf(stderr, "depth_in.dat is not one \"i j depth\" per point\n");
+      return 1;
+    }
   }
   if (rc != NL2D_OK) {
     std::fprintf(stderr, "Wrong grid definition type (jphgr_msh must be 0, 1, 2 or 3), "

@@ -222,6 +222,278 @@ __global__ void __launch_bounds__(kThreads)
                  "r"(kTmemCols));
 }
 
+// ---- pipelined convolution ----------------------------------------------
+//
+// Warp-specialised form of the same implicit GEMM.  A CTA walks strips of
+// kStripRows output rows of one 128-pixel column segment.  Input rows pass
+// through a ring of kSlots shared-memory slots (each input row is staged
+// once per strip instead of three times), the accumulator alternates
+// between two TMEM buffers, and the three roles overlap:
+//   warps 0-3  epilogue: TMEM -> bias, ReLU -> BF16 / FP32 stores
+//   warp 4     one thread issues the MMAs of an output row once its three
+//              input rows are staged and its TMEM buffer is free
+//   warps 5-7  stage input rows into the ring
+// Hand-offs are mbarriers: full[slot] (stagers -> MMA), empty[slot] (MMA
+// completion -> stagers), done[buf] (MMA completion -> epilogue),
+// drained[buf] (epilogue -> MMA).  Every wait is bounded (kMaxWaitCycles);
+// one that runs out sets the error flag and a shared abort flag that ends
+// every role's loop, and the MMA thread waits for its last commit before the
+// tensor memory is freed.
+constexpr int kStripRows = 8;
+constexpr int kSlots = 4;
+constexpr int kPipeThreads = 256;
+constexpr int kEpiWarps = 4;
+constexpr int kStageThreads = 96;  // warps 5-7
+constexpr int kPipeTmemCols = 128;  // two accumulators of up to 64 columns
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+// Waits for the phase with the given parity to complete; false if the wait
+// ran out (flag and error set) or another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort_flag, int* err) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kMaxWaitCycles) {
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+}
+
+struct StripWalk {  // work unit u -> (image, first row, rows, column segment)
+  int img, y0, rows, x0;
+  __device__ StripWalk(long long u, int H, int segs) {
+    const int strips = (H + kStripRows - 1) / kStripRows;
+    const int seg = (int)(u % segs);
+    const long long r = u / segs;
+    const int st = (int)(r % strips);
+    img = (int)(r / strips);
+    y0 = st * kStripRows;
+    rows = min(kStripRows, H - y0);
+    x0 = seg * kTileM;
+  }
+};
+
+__global__ void __launch_bounds__(kPipeThreads)
+    k_conv3x3_pipe(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ w,
+                   const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
+                   float* __restrict__ y32, int batch, int H, int W, int cin, int cout,
+                   int relu, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full_bar[kSlots], empty_bar[kSlots];
+  __shared__ __align__(8) uint64_t done_bar[2], drained_bar[2], last_bar;
+  __shared__ uint32_t taddr_slot;
+  __shared__ int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int kc = cin >> 3;
+  const uint32_t lbo_a = kRowPix * 16;
+  const uint32_t row_bytes = (uint32_t)kc * lbo_a;
+  const uint32_t b_bytes = (uint32_t)cout * cin * 2;
+  unsigned char* b_s = smem;
+  unsigned char* ring = smem + ((9 * b_bytes + 1023) & ~1023u);
+  volatile int* abort_v = &abort_flag;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&taddr_slot)),
+                 "r"(kPipeTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < kSlots; q++) {
+      mbar_init(&full_bar[q], kStageThreads);
+      mbar_init(&empty_bar[q], 1);
+    }
+    for (int q = 0; q < 2; q++) {
+      mbar_init(&done_bar[q], 1);
+      mbar_init(&drained_bar[q], kEpiWarps * 32);
+    }
+    mbar_init(&last_bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  for (int t = tid; t < 9 * cout * kc; t += kPipeThreads) {
+    const int tap = t / (cout * kc), rem = t - tap * cout * kc;
+    const int n = rem / kc, ch = rem - n * kc;
+    const uint4 v =
+        *reinterpret_cast<const uint4*>(w + ((size_t)tap * cout + n) * cin + ch * 8);
+    *reinterpret_cast<uint4*>(b_s + tap * b_bytes + core_off(n, ch * 8, cin)) = v;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t taddr = taddr_slot;
+  const int segs = W / kTileM;
+  const long long units = (long long)batch * ((H + kStripRows - 1) / kStripRows) * segs;
+
+  if (warp >= 5) {
+    // ---- stagers: input rows y0-1 .. y0+rows of every strip, in order ----
+    const int st = tid - 5 * 32;
+    long long q = 0;  // input rows staged so far (ring sequence)
+    for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+      const StripWalk sw(u, H, segs);
+      for (int a = 0; a < sw.rows + 2 && !*abort_v; a++, q++) {
+        const int slot = (int)(q % kSlots);
+        if (q >= kSlots &&
+            !mbar_wait(&empty_bar[slot], (uint32_t)((q / kSlots - 1) & 1), abort_v, err))
+          break;
+        const int yy = sw.y0 - 1 + a;
+        unsigned char* dst = ring + slot * row_bytes;
+        for (int t = st; t < kc * kRowPix; t += kStageThreads) {
+          const int p = t % kRowPix, ch = t / kRowPix;
+          const int xx = sw.x0 - 1 + p;
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+            v = *reinterpret_cast<const uint4*>(x + (((size_t)sw.img * H + yy) * W + xx) * cin +
+                                                ch * 8);
+          *reinterpret_cast<uint4*>(dst + ch * lbo_a + p * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&full_bar[slot]);
+      }
+    }
+  } else if (warp == 4) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(cout);
+      long long q = 0, p = 0;  // input rows consumed (sequence base), output rows issued
+      bool issued = false;
+      for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+        const StripWalk sw(u, H, segs);
+        const long long qb = q;  // sequence number of this strip's first input row
+        // its first two input rows
+        bool ok = mbar_wait(&full_bar[qb % kSlots], (uint32_t)((qb / kSlots) & 1), abort_v,
+                            err) &&
+                  mbar_wait(&full_bar[(qb + 1) % kSlots], (uint32_t)(((qb + 1) / kSlots) & 1),
+                            abort_v, err);
+        for (int o = 0; o < sw.rows && ok; o++, p++) {
+          const long long qn = qb + o + 2;  // the new input row this output needs
+          const int buf = (int)(p & 1);
+          ok = mbar_wait(&full_bar[qn % kSlots], (uint32_t)((qn / kSlots) & 1), abort_v, err);
+          if (ok && p >= 2)
+            ok = mbar_wait(&drained_bar[buf], (uint32_t)((p / 2 - 1) & 1), abort_v, err);
+          if (!ok) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t dcol = taddr + (uint32_t)(buf * 64);
+          int first = 1;
+          for (int tap = 0; tap < 9; tap++) {
+            const int dy = tap / 3, dx = tap % 3;
+            const int slot = (int)((qb + o + dy) % kSlots);
+            for (int kq = 0; kq < cin / 16; kq++) {
+              const uint64_t ad = smem_desc(
+                  smem_u32(ring + slot * row_bytes) + 2 * kq * lbo_a + dx * 16, lbo_a, 128);
+              const uint64_t bd =
+                  smem_desc(smem_u32(b_s + tap * b_bytes) + kq * 256, 128, (uint32_t)cin * 16);
+              const uint32_t acc = first ? 0u : 1u;
+              asm volatile(
+                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dcol),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+              first = 0;
+            }
+          }
+          issued = true;
+          tc_commit(&done_bar[buf]);
+          // input row o is not read by later outputs of this strip
+          tc_commit(&empty_bar[(qb + o) % kSlots]);
+        }
+        q = qb + sw.rows + 2;
+        if (ok) {  // the strip's last two input rows are free too
+          tc_commit(&empty_bar[(q - 2) % kSlots]);
+          tc_commit(&empty_bar[(q - 1) % kSlots]);
+        } else {
+          break;
+        }
+      }
+      if (issued) {  // nothing may be in flight when the tensor memory is freed
+        tc_commit(&last_bar);
+        volatile int never = 0;
+        if (!mbar_wait(&last_bar, 0, &never, err)) atomicExch(err, 1);
+      }
+    }
+  } else {
+    // ---- epilogue: warp w owns accumulator lanes (pixels) 32w .. 32w+31 ----
+    long long p = 0;
+    for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+      const StripWalk sw(u, H, segs);
+      for (int o = 0; o < sw.rows; o++, p++) {
+        const int buf = (int)(p & 1);
+        // warp-uniform outcome: tcgen05.ld below needs the whole warp
+        const bool ok = mbar_wait(&done_bar[buf], (uint32_t)((p / 2) & 1), abort_v, err);
+        if (!__all_sync(0xffffffffu, ok)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int m = warp * 32 + lane;
+        const size_t pix = ((size_t)sw.img * H + sw.y0 + o) * W + sw.x0 + m;
+        for (int n0 = 0; n0 < cout; n0 += 16) {
+          uint32_t r[16];
+          const uint32_t ta =
+              taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * 64 + n0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+              "%12,%13,%14,%15}, [%16];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+              : "r"(ta));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          __align__(16) __nv_bfloat16 out[16];
+          float v[16];
+#pragma unroll
+          for (int k = 0; k < 16; k++) {
+            v[k] = __uint_as_float(r[k]) + (bias ? bias[n0 + k] : 0.f);
+            if (relu) v[k] = fmaxf(v[k], 0.f);
+            out[k] = __float2bfloat16(v[k]);
+          }
+          if (y) {
+            uint4* dst = reinterpret_cast<uint4*>(y + pix * cout + n0);
+            dst[0] = reinterpret_cast<const uint4*>(out)[0];
+            dst[1] = reinterpret_cast<const uint4*>(out)[1];
+          }
+          if (y32) {
+            float4* dst = reinterpret_cast<float4*>(y32 + pix * cout + n0);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+              dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(&drained_bar[buf]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr),
+                 "r"(kPipeTmemCols));
+}
+
 // Tap-flipped, channel-transposed weights for the input gradient:
 // wt[8 - tap][ci][co] = w[tap][co][ci].
 __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w,
@@ -608,21 +880,24 @@ int nl2d_emu_conv3x3(const void* x, const void* w, const float* bias, void* y, f
       batch < 1 || !x || !w || !err || (!y && !y32))
     return NL2D_ERR_ARGS;
   const size_t wbytes = ((9 * (size_t)cout * cin * 2) + 1023) & ~(size_t)1023;
-  const size_t smem = wbytes + 3 * (size_t)(cin / 8) * kRowPix * 16;
-  static int attr_bytes = 0;
-  if ((int)smem > attr_bytes) {
-    if (cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             96 * 1024) != cudaSuccess)
+  const size_t smem = wbytes + kSlots * (size_t)(cin / 8) * kRowPix * 16;
+  constexpr int kMaxSmem = 200 * 1024;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_conv3x3_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kMaxSmem) != cudaSuccess)
       return NL2D_ERR_CUDA;
-    attr_bytes = 96 * 1024;
+    attr = true;
   }
-  if (smem > 96 * 1024) return NL2D_ERR_ARGS;
+  if (smem > kMaxSmem) return NL2D_ERR_ARGS;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (long long)batch * H * (W / kTileM);
-  const int grid = (int)(tiles < 2LL * sms ? tiles : 2LL * sms);  // two CTAs per SM
-  k_conv3x3_tc<<<grid, kThreads, smem, (cudaStream_t)stream>>>(
+  const long long units =
+      (long long)batch * ((H + kStripRows - 1) / kStripRows) * (W / kTileM);
+  const long long per_sm = smem <= 110 * 1024 ? 2 : 1;  // CTAs that fit an SM's shared memory
+  const int grid = (int)(units < per_sm * sms ? units : per_sm * sms);
+  k_conv3x3_pipe<<<grid, kPipeThreads, smem, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, (const __nv_bfloat16*)w, bias, (__nv_bfloat16*)y, y32, batch, H,
       W, cin, cout, relu, err);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;

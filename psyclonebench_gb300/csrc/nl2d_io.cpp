@@ -190,10 +190,12 @@ int nl2d_read_namelist(const char* path, int* ints, double* dbls) {
 //    column; yt likewise (original/nemolite2d.f90:236-246).
 //  * state: depths dep_const, everything else zero; sshn_u / sshn_v of a
 //    zero sshn_t are zero (initialisation_mod.f90:24-62).
+//  * jphgr_msh = 0 (a STOP upstream: "read from a file" was never written)
+//    keeps the caller's tmask as it is, e.g. one read by
+//    nl2d_read_grid_file; everything else is set up as above.
 int nl2d_setup_model(int jphgr_msh, int jpiglo, int jpjglo, double dx, double dy,
                      double dep_const, int width, int height, double* const* fields,
                      int* tmask, double* const* metrics, double* xt, double* yt) {
-  if (jphgr_msh == 0) return NL2D_ERR_UNSUPPORTED;  // "read from file" is a STOP upstream
   if (jphgr_msh < 0 || jphgr_msh > 3 || jpiglo < 4 || jpjglo < 4 || width < jpiglo + 1 ||
       height < jpjglo + 1 || !fields || !tmask || !metrics)
     return NL2D_ERR_ARGS;
@@ -205,7 +207,7 @@ int nl2d_setup_model(int jphgr_msh, int jpiglo, int jpjglo, double dx, double dy
   const size_t cells = (size_t)width * height;
   const bool east_open = jphgr_msh == 2 || jphgr_msh == 3;
   const bool south_open = jphgr_msh == 1 || jphgr_msh == 3;
-  for (int j = 0; j < height; j++)
+  for (int j = 0; j < height && jphgr_msh != 0; j++)
     for (int i = 0; i < width; i++) {
       int m = (i >= xs && i <= xe && j >= ys && j <= ye) ? 1 : 0;
       if (i < xs) m = 0;
@@ -248,6 +250,71 @@ int nl2d_setup_model(int jphgr_msh, int jpiglo, int jpjglo, double dx, double dy
     std::free(colx);
     std::free(rowy);
   }
+  return NL2D_OK;
+}
+
+// A grid file: whitespace-separated triples "i j value" (1-based i in
+// 1..nx, j in 1..ny), one per point of the nx x ny mask, in any order, blank
+// lines ignored: the layout dump_tmask writes raw (model_mod.f90:268-274),
+// so a dumped mask reads back.  is_int: int values into `out` (a T mask),
+// else doubles (a depth).  Row-major [][width] output, 0-based.  Every point
+// must appear exactly once.
+int nl2d_read_grid_file(const char* path, int nx, int ny, int width, int is_int, void* out) {
+  if (!path || !out || nx < 1 || ny < 1 || width < nx) return NL2D_ERR_ARGS;
+  FILE* fp = std::fopen(path, "r");
+  if (!fp) return NL2D_ERR_IO;
+  std::string seen((size_t)nx * ny, '\0');
+  long long count = 0;
+  int rc = NL2D_OK;
+  for (;;) {
+    long i, j;
+    int got = std::fscanf(fp, "%ld %ld", &i, &j);
+    if (got == EOF) break;
+    if (got != 2 || i < 1 || i > nx || j < 1 || j > ny) {
+      rc = NL2D_ERR_PARSE;
+      break;
+    }
+    const size_t c = (size_t)(j - 1) * width + (size_t)(i - 1);
+    const size_t key = (size_t)(j - 1) * nx + (size_t)(i - 1);
+    if (seen[key]) {
+      rc = NL2D_ERR_PARSE;
+      break;
+    }
+    seen[key] = 1;
+    if (is_int) {
+      long v;
+      if (std::fscanf(fp, "%ld", &v) != 1) {
+        rc = NL2D_ERR_PARSE;
+        break;
+      }
+      static_cast<int*>(out)[c] = (int)v;
+    } else {
+      double v;
+      if (std::fscanf(fp, "%lf", &v) != 1) {
+        rc = NL2D_ERR_PARSE;
+        break;
+      }
+      static_cast<double*>(out)[c] = v;
+    }
+    count++;
+  }
+  std::fclose(fp);
+  if (rc == NL2D_OK && count != (long long)nx * ny) rc = NL2D_ERR_PARSE;
+  return rc;
+}
+
+// Face depths from T-point depths: hu = (ht(i) + ht(i+1)) / 2 on the east
+// face, hv = (ht(j) + ht(j+1)) / 2 on the north face; the last column / row
+// copies ht.  (The reference sets all three to dep_const; a depth read from a
+// file needs face values and this is the plain average.)
+int nl2d_face_depths(int width, int height, const double* ht, double* hu, double* hv) {
+  if (!ht || !hu || !hv || width < 1 || height < 1) return NL2D_ERR_ARGS;
+  for (int j = 0; j < height; j++)
+    for (int i = 0; i < width; i++) {
+      const size_t c = (size_t)j * width + i;
+      hu[c] = i + 1 < width ? 0.5 * (ht[c] + ht[c + 1]) : ht[c];
+      hv[c] = j + 1 < height ? 0.5 * (ht[c] + ht[c + width]) : ht[c];
+    }
   return NL2D_OK;
 }
 

@@ -25,11 +25,17 @@ def conv_ref(x, w, b, relu):
     return np.maximum(out, 0) if relu else out
 
 
-@pytest.mark.parametrize("cin,cout,relu", [(16, 48, 1), (48, 48, 1), (48, 16, 0), (16, 16, 0)])
-def test_conv3x3_tcgen05_matches_fp64(gpulib, cin, cout, relu):
+@pytest.mark.parametrize("cin,cout,relu,B,H", [
+    (16, 48, 1, 2, 5), (48, 48, 1, 2, 5), (48, 16, 0, 2, 5), (16, 16, 0, 2, 5),
+    # several strips per image, a partial last strip, more units than CTAs;
+    # 64 channels take one CTA per SM
+    (48, 48, 1, 3, 19), (64, 64, 1, 2, 17), (32, 16, 0, 100, 9)])
+def test_conv3x3_tcgen05_matches_fp64(gpulib, cin, cout, relu, B, H):
+    """The pipelined tcgen05 convolution (strips of rows, ring of staged
+    input rows, two TMEM accumulators) against an FP64 convolution."""
     import torch
-    rng = np.random.default_rng(cin * 100 + cout)
-    B, H, W = 2, 5, 256
+    rng = np.random.default_rng(cin * 100 + cout + H)
+    W = 256
     x = bf16_round(rng.normal(size=(B, H, W, cin)).astype(np.float32))
     w = bf16_round((rng.normal(size=(9, cout, cin)) / np.sqrt(9 * cin)).astype(np.float32))
     b = rng.normal(size=cout).astype(np.float32)

@@ -116,11 +116,63 @@ def test_setup_matches_the_reference_start_state(jphgr, oracle):
     assert yt[3, 0] == 550.0 + 2 * 1100.0
 
 
-def test_setup_rejects_read_from_file():
+def test_setup_from_file_keeps_the_callers_mask(tmp_path):
+    """jphgr_msh = 0 (a STOP in the reference) sets up everything but the
+    mask, which comes from a grid file; a raw dump_tmask reads back."""
     import psyclonebench_gb300 as P
     lib = _lib()
-    assert _setup(lib, 0, 34, 27)[0] == P.NL2D_ERR_UNSUPPORTED
+    rc, f, g, tm, xt, yt = _setup(lib, 3, 20, 14)
+    assert rc == 0
+    tm[5:8, 6:9] = 0  # an island
+    d = str(tmp_path).encode()
+    assert lib.nl2d_dump_tmask(d, 0, 1, 21, 20, 14, iptr(tm), 1, 18, 1, 12, dptr(xt),
+                               dptr(yt)) == 0
+    back = np.full_like(tm, 42)
+    assert lib.nl2d_read_grid_file(str(tmp_path / "tmask_00000.dat").encode(), 20, 14, 21, 1,
+                                   back.ctypes.data) == 0
+    np.testing.assert_array_equal(back[:14, :20], tm[:14, :20])
+    assert (back[:, 20] == 42).all() and (back[14] == 42).all()  # outside the mask: untouched
+    rc2, f2, g2, tm2, _, _ = _setup(lib, 0, 20, 14)
+    assert rc2 == 0 and (tm2 == 99).all()  # the caller's mask is kept as it is
+    np.testing.assert_array_equal(f2["ht"], f["ht"])
     assert _setup(lib, 4, 34, 27)[0] == P.NL2D_ERR_ARGS
+
+
+@pytest.mark.parametrize("text", [
+    "1 1 0\n2 1 0\n1 2 0\n",                 # a point missing
+    "1 1 0\n2 1 0\n1 2 0\n1 2 1\n",         # a point twice
+    "1 1 0\n2 1 0\n1 2 0\n3 2 1\n",         # out of range
+    "1 1 0\n2 1 0\n1 2 0\n2 2 x\n",         # not a number
+])
+def test_grid_file_errors(tmp_path, text):
+    import psyclonebench_gb300 as P
+    lib = _lib()
+    p = tmp_path / "g.dat"
+    p.write_text(text)
+    out = np.zeros((2, 2), np.int32)
+    assert lib.nl2d_read_grid_file(str(p).encode(), 2, 2, 2, 1, out.ctypes.data) == \
+        P.NL2D_ERR_PARSE
+    assert lib.nl2d_read_grid_file(str(tmp_path / "none").encode(), 2, 2, 2, 1,
+                                   out.ctypes.data) == P.NL2D_ERR_IO
+
+
+def test_grid_file_depths_and_face_depths(tmp_path):
+    lib = _lib()
+    rng = np.random.default_rng(1)
+    ht = rng.uniform(50, 150, size=(3, 4))
+    lines = ["%d %d %.17g" % (i + 1, j + 1, ht[j, i]) for j in range(3) for i in range(4)]
+    rng.shuffle(lines)
+    (tmp_path / "d.dat").write_text("\n".join(lines) + "\n")
+    out = np.zeros((3, 5))
+    assert lib.nl2d_read_grid_file(str(tmp_path / "d.dat").encode(), 4, 3, 5, 0,
+                                   out.ctypes.data) == 0
+    np.testing.assert_array_equal(out[:, :4], ht)
+    hu, hv = np.zeros_like(out), np.zeros_like(out)
+    assert lib.nl2d_face_depths(5, 3, dptr(out), dptr(hu), dptr(hv)) == 0
+    np.testing.assert_array_equal(hu[:, :4], 0.5 * (out[:, :4] + out[:, 1:]))
+    np.testing.assert_array_equal(hu[:, 4], out[:, 4])
+    np.testing.assert_array_equal(hv[:2], 0.5 * (out[:2] + out[1:]))
+    np.testing.assert_array_equal(hv[2], out[2])
 
 
 def _fmt(lib, v, w=16, d=7):
