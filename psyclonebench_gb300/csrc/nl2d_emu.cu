@@ -31,8 +31,7 @@ namespace emu {
 namespace {
 
 constexpr int kTileM = 128;       // pixels per CTA (one row segment)
-constexpr int kThreads = 128;     // 4 warps: loaders, then the epilogue
-constexpr int kTmemCols = 64;     // >= Cout (<= 64), a power of two >= 32
+constexpr int kThreads = 128;     // weight gradient: 4 warps, loaders then the epilogue
 constexpr long long kMaxWaitCycles = 1LL << 31;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -66,166 +65,15 @@ __device__ __forceinline__ uint32_t core_off(int row, int k, int cin) {
 // rounded up to a multiple of 8 (one core-matrix column of pixels).
 constexpr int kRowPix = 136;
 
-// Persistent 3x3 convolution.  Each CTA keeps the 9 weight taps in shared
-// memory and walks tiles (image, row, 128-pixel segment) with a grid
-// stride.  For a tile it stages the three input rows it needs once, in a
-// layout where pixels of one 8-channel group are 16 bytes apart, so the
-// tap (dy, dx) operand is the dy-th row block started dx pixels (16 * dx
-// bytes) later: no per-tap copies.
-__global__ void __launch_bounds__(kThreads)
-    k_conv3x3_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ w,
-                 const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
-                 float* __restrict__ y32, int batch, int H, int W, int cin, int cout, int relu,
-                 int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t mbar;
-  __shared__ uint32_t taddr_slot;
-  __shared__ uint32_t s_done;
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int kc = cin >> 3;                                   // 8-channel groups
-  const uint32_t lbo_a = kRowPix * 16;                       // next channel group
-  const uint32_t row_bytes = (uint32_t)kc * lbo_a;           // one staged row
-  const uint32_t b_bytes = (uint32_t)cout * cin * 2;         // one weight tap
-  unsigned char* b_s = smem;
-  unsigned char* a_s = smem + ((9 * b_bytes + 1023) & ~1023u);
-
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&taddr_slot)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-  }
-  for (int t = tid; t < 9 * cout * kc; t += kThreads) {
-    const int tap = t / (cout * kc), rem = t - tap * cout * kc;
-    const int n = rem / kc, ch = rem - n * kc;
-    const uint4 v =
-        *reinterpret_cast<const uint4*>(w + ((size_t)tap * cout + n) * cin + ch * 8);
-    *reinterpret_cast<uint4*>(b_s + tap * b_bytes + core_off(n, ch * 8, cin)) = v;
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t taddr = taddr_slot;
-  const uint32_t idesc = idesc_bf16(cout);
-
-  const int segs = W / kTileM;
-  const long long ntiles = (long long)batch * H * segs;
-  uint32_t phase = 0;
-  bool ok_all = true;
-  for (long long tile = blockIdx.x; tile < ntiles && ok_all; tile += gridDim.x) {
-    const int seg = (int)(tile % segs);
-    const long long rr = tile / segs;
-    const int row = (int)(rr % H), img = (int)(rr / H);
-    const int x0 = seg * kTileM;
-    // stage rows row-1 .. row+1, pixels x0-1 .. x0-1+kRowPix-1 (zero outside)
-    for (int t = tid; t < 3 * kc * kRowPix; t += kThreads) {
-      const int p = t % kRowPix, rem = t / kRowPix;
-      const int ch = rem % kc, dy = rem / kc;
-      const int yy = row + dy - 1, xx = x0 - 1 + p;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-        v = *reinterpret_cast<const uint4*>(x + (((size_t)img * H + yy) * W + xx) * cin +
-                                            ch * 8);
-      *reinterpret_cast<uint4*>(a_s + dy * row_bytes + ch * lbo_a + p * 16) = v;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid == 0) {
-      int first = 1;
-      for (int tap = 0; tap < 9; tap++) {
-        const int dy = tap / 3, dx = tap % 3;
-        for (int q = 0; q < cin / 16; q++) {
-          const uint64_t ad =
-              smem_desc(smem_u32(a_s + dy * row_bytes) + 2 * q * lbo_a + dx * 16, lbo_a, 128);
-          const uint64_t bd =
-              smem_desc(smem_u32(b_s + tap * b_bytes) + q * 256, 128, (uint32_t)cin * 16);
-          const uint32_t acc = first ? 0u : 1u;
-          asm volatile(
-              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(taddr),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-          first = 0;
-        }
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&mbar))
-          : "memory");
-      // bounded wait (~1 s) for this tile's MMAs
-      uint32_t ok = 0;
-      const long long t0 = clock64();
-      while (!ok) {
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            "selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(ok)
-            : "r"(smem_u32(&mbar)), "r"(phase)
-            : "memory");
-        if (!ok && clock64() - t0 > kMaxWaitCycles) break;
-      }
-      if (!ok) atomicExch(err, 1);
-      s_done = ok;
-    }
-    __syncthreads();
-    phase ^= 1u;
-    ok_all = s_done != 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok_all) {
-      // epilogue: warp w owns accumulator rows (pixels) 32w .. 32w+31
-      const int m = warp * 32 + lane;
-      const size_t pix = ((size_t)img * H + row) * W + x0 + m;
-      for (int n0 = 0; n0 < cout; n0 += 16) {
-        uint32_t r[16];
-        const uint32_t ta = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-            "%13,%14,%15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(ta));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        __align__(16) __nv_bfloat16 out[16];
-        float v[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          v[q] = __uint_as_float(r[q]) + (bias ? bias[n0 + q] : 0.f);
-          if (relu) v[q] = fmaxf(v[q], 0.f);
-          out[q] = __float2bfloat16(v[q]);
-        }
-        if (y) {
-          uint4* dst = reinterpret_cast<uint4*>(y + pix * cout + n0);
-          dst[0] = reinterpret_cast<const uint4*>(out)[0];
-          dst[1] = reinterpret_cast<const uint4*>(out)[1];
-        }
-        if (y32) {
-          float4* dst = reinterpret_cast<float4*>(y32 + pix * cout + n0);
-#pragma unroll
-          for (int q = 0; q < 4; q++)
-            dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-        }
-      }
-    }
-    // the next tile overwrites the staged rows and the accumulator
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-  }
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr),
-                 "r"(kTmemCols));
-}
-
-// ---- pipelined convolution ----------------------------------------------
+// ---- 3x3 convolution ------------------------------------------------------
 //
-// Warp-specialised form of the same implicit GEMM.  A CTA walks strips of
-// kStripRows output rows of one 128-pixel column segment.  Input rows pass
+// Implicit GEMM on the tensor cores: M = 128 pixels of one image row,
+// N = cout, K = 9 taps x cin.  The 9 weight taps stay in shared memory for
+// the CTA's lifetime.  A staged input row keeps each 8-channel group of its
+// pixels 16 bytes apart, so the operand of tap (dy, dx) is the dy-th row of
+// the window started dx pixels (16 * dx bytes) later: a descriptor offset,
+// no per-tap copies.  Warp-specialised and persistent: a CTA walks strips
+// of kStripRows output rows of one 128-pixel column segment.  Input rows pass
 // through a ring of kSlots shared-memory slots (each input row is staged
 // once per strip instead of three times), the accumulator alternates
 // between two TMEM buffers, and the three roles overlap:

@@ -431,7 +431,10 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     K_STEPS solver steps from the window's end state, the ssh RMS difference
     being the judge's error.  Above `threshold` (m), or if anything is
     non-finite, the window is rolled back to its checkpoint and redone by
-    the solver.  A pure-solver run from the same start gives the truth.
+    the solver; if that redo goes non-finite (the scheme is only marginally
+    stable on these domains), the solver recomputes from the last state it
+    produced on its own.  A pure-solver run from the same start gives the
+    truth.
 
     `domains` are candidates (indices into ds): those on which the pure
     solver run itself goes non-finite (the scheme's own instability) are
@@ -502,11 +505,16 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
         _ck(lib.nl2d_ens_export_interior(_p(buf)), "export")
         return buf.clone(), ms
 
+    # the last state the solver produced on its own from the start: a redo
+    # that goes non-finite (the scheme is only marginally stable on these
+    # domains, and an emulated state can push it over) is recomputed from it
+    clean, clean_step, state_clean = state.clone(), step0, True
     istep = step0
     k = 0
     while k < emu_steps:
         window = min(judge_every, emu_steps - k)
         ckpt = state.clone()
+        ckpt_clean = state_clean
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for q in range(window):
@@ -524,8 +532,16 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
             state, ms = solve(ckpt, istep, window * K_STEPS)
             sol_ms += ms
             report["windows_solver"] += 1
+            if ckpt_clean or not bool(torch.isfinite(state).all()):
+                if not ckpt_clean:
+                    state, ms = solve(clean, clean_step, istep + window * K_STEPS - clean_step)
+                    sol_ms += ms
+                    report["recomputed_from_clean"] = report.get("recomputed_from_clean", 0) + 1
+                clean, clean_step = state.clone(), istep + window * K_STEPS
+                state_clean = True
         else:
             report["windows_emulator"] += 1
+            state_clean = False
         istep += window * K_STEPS
         k += window
     sol.close()
