@@ -31,7 +31,6 @@ namespace emu {
 namespace {
 
 constexpr int kTileM = 128;       // pixels per CTA (one row segment)
-constexpr int kThreads = 128;     // weight gradient: 4 warps, loaders then the epilogue
 constexpr long long kMaxWaitCycles = 1LL << 31;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -92,6 +91,10 @@ constexpr int kSlots = 4;
 constexpr int kPipeThreads = 256;
 constexpr int kEpiWarps = 4;
 constexpr int kStageThreads = 96;  // warps 5-7
+// 16-byte loads per staging thread per row: 8 channel groups x 136 pixels
+// (cin = 64, the widest) fit in 96 x 12
+constexpr int kStageBatch = 12;
+static_assert(8 * kRowPix <= kStageThreads * kStageBatch, "a staged row must fit one batch");
 constexpr int kPipeTmemCols = 128;  // two accumulators of up to 64 columns
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -207,19 +210,32 @@ __global__ void __launch_bounds__(kPipeThreads)
       const StripWalk sw(u, H, segs);
       for (int a = 0; a < sw.rows + 2 && !*abort_v; a++, q++) {
         const int slot = (int)(q % kSlots);
+        const int yy = sw.y0 - 1 + a;
+        // the whole row's loads in flight before waiting for the slot
+        uint4 v[kStageBatch];
+#pragma unroll
+        for (int b = 0; b < kStageBatch; b++) {
+          const int t = st + b * kStageThreads;
+          v[b] = make_uint4(0, 0, 0, 0);
+          if (t < kc * kRowPix) {
+            const int p = t % kRowPix, ch = t / kRowPix;
+            const int xx = sw.x0 - 1 + p;
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+              v[b] = *reinterpret_cast<const uint4*>(
+                  x + (((size_t)sw.img * H + yy) * W + xx) * cin + ch * 8);
+          }
+        }
         if (q >= kSlots &&
             !mbar_wait(&empty_bar[slot], (uint32_t)((q / kSlots - 1) & 1), abort_v, err))
           break;
-        const int yy = sw.y0 - 1 + a;
         unsigned char* dst = ring + slot * row_bytes;
-        for (int t = st; t < kc * kRowPix; t += kStageThreads) {
-          const int p = t % kRowPix, ch = t / kRowPix;
-          const int xx = sw.x0 - 1 + p;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-            v = *reinterpret_cast<const uint4*>(x + (((size_t)sw.img * H + yy) * W + xx) * cin +
-                                                ch * 8);
-          *reinterpret_cast<uint4*>(dst + ch * lbo_a + p * 16) = v;
+#pragma unroll
+        for (int b = 0; b < kStageBatch; b++) {
+          const int t = st + b * kStageThreads;
+          if (t < kc * kRowPix) {
+            const int p = t % kRowPix, ch = t / kRowPix;
+            *reinterpret_cast<uint4*>(dst + ch * lbo_a + p * 16) = v[b];
+          }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&full_bar[slot]);
@@ -354,15 +370,14 @@ __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w,
   }
 }
 
-// Weight and bias gradients on the tensor cores.  For each tap the weight
-// gradient is a GEMM over pixels, D[co][ci] = sum_p dY[p][co] X[p + off][ci],
-// with both operands "MN-major" (channels contiguous per pixel, as the data
-// already is): M = co (padded to 128 with zero rows), N = ci, K = pixels.
-// X is staged exactly as in the forward convolution, so the tap (dy, dx)
-// operand is again a row block started 16 * dx bytes later.  The nine
-// accumulators (9 x ci FP32 columns) stay in tensor memory while a
-// persistent CTA walks its tiles; at the end each CTA adds its partial sums
-// to dw atomically.  db[co] is summed from the staged dY tile.
+// Weight gradient on the tensor cores.  For each tap it is a GEMM over
+// pixels, D[co][ci] = sum_p dY[p][co] X[p + off][ci], with both operands
+// "MN-major" (channels contiguous per pixel, as the data already is):
+// M = co (padded to 128 with zero rows), N = ci, K = pixels.  X is staged as
+// in the convolution, so the tap (dy, dx) operand is again a row block
+// started 16 * dx bytes later.  The nine accumulators (9 x ci FP32 columns)
+// stay in tensor memory for the CTA's lifetime; at the end each CTA adds its
+// partial sums to dw atomically.
 constexpr int kWgTmemCols = 512;
 constexpr int kWgGroups = 16;  // 128 M rows = 16 groups of 8 output channels
 constexpr size_t kWgSmem = 120 * 1024;
@@ -372,22 +387,37 @@ __host__ __device__ constexpr uint32_t idesc_bf16_mn(int n) {
          ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
 }
 
-__global__ void __launch_bounds__(kThreads)
-    k_conv_wgrad_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
-                    float* __restrict__ dw, float* __restrict__ db, int batch, int H, int W,
-                    int cin, int cout, int* __restrict__ err) {
+// Laid out like the convolution: a CTA (alone on its SM: it holds all 512
+// TMEM columns) walks strips of kStripRows rows of one 128-pixel segment:
+//   warps 5-7  stage input rows (X) into a ring of kSlots slots
+//   warps 0-3  stage gradient rows (dY) into a ring of 2 slots, then, at
+//              the end, move the nine accumulators out of TMEM into dw
+//   warp 4     one thread issues, per row, the 9 taps x 8 pixel chunks of
+//              MMAs into the accumulators, which stay in TMEM throughout
+// The bias gradient is a separate reduction (k_bias_grad).
+constexpr int kWgYSlots = 2;
+constexpr int kWgYThreads = 128;   // warps 0-3
+constexpr int kWgYBatch = 16;      // 16-byte loads per thread per dY row (cout <= 128)
+
+__global__ void __launch_bounds__(kPipeThreads)
+    k_conv_wgrad_pipe(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
+                      float* __restrict__ dw, int batch, int H, int W, int cin, int cout,
+                      int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t xfull[kSlots], xempty[kSlots];
+  __shared__ __align__(8) uint64_t yfull[kWgYSlots], yempty[kWgYSlots], last_bar;
   __shared__ uint32_t taddr_slot;
-  __shared__ uint32_t s_done;
+  __shared__ int abort_flag, s_issued;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int kc = cin >> 3, kco = cout >> 3;
-  const uint32_t lbo_y = kTileM * 16;                // next group of 8 output channels
-  const uint32_t lbo_x = kRowPix * 16;               // next group of 8 input channels
+  const uint32_t lbo_y = kTileM * 16;  // next group of 8 output channels (M)
+  const uint32_t lbo_x = kRowPix * 16; // next group of 8 input channels (N)
   const uint32_t row_bytes = (uint32_t)kc * lbo_x;
-  unsigned char* a_s = smem;                         // dY tile, kWgGroups x 128 x 16 B
-  unsigned char* b_s = smem + kWgGroups * lbo_y;     // three staged X rows
+  const uint32_t yslot_bytes = (uint32_t)kWgGroups * lbo_y;
+  unsigned char* yring = smem;                               // kWgYSlots x 32 KB
+  unsigned char* xring = smem + kWgYSlots * yslot_bytes;     // kSlots staged X rows
+  volatile int* abort_v = &abort_flag;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -396,123 +426,211 @@ __global__ void __launch_bounds__(kThreads)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+    for (int q = 0; q < kSlots; q++) {
+      mbar_init(&xfull[q], kStageThreads);
+      mbar_init(&xempty[q], 1);
+    }
+    for (int q = 0; q < kWgYSlots; q++) {
+      mbar_init(&yfull[q], kWgYThreads);
+      mbar_init(&yempty[q], 1);
+    }
+    mbar_init(&last_bar, 1);
+    abort_flag = 0;
+    s_issued = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  // rows co >= cout of the M = 128 operand stay zero
-  for (int t = tid; t < kWgGroups * kTileM; t += kThreads)
-    *reinterpret_cast<uint4*>(a_s + t * 16) = make_uint4(0, 0, 0, 0);
+  // rows co >= cout of the M = 128 operand stay zero in both dY slots
+  for (int t = tid; t < kWgYSlots * kWgGroups * kTileM; t += kPipeThreads)
+    *reinterpret_cast<uint4*>(yring + t * 16) = make_uint4(0, 0, 0, 0);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t taddr = taddr_slot;
-  const uint32_t idesc = idesc_bf16_mn(cin);
-
   const int segs = W / kTileM;
-  const long long ntiles = (long long)batch * H * segs;
-  uint32_t phase = 0;
-  bool ok_all = true, any = false;
-  float bacc = 0.f;
-  for (long long tile = blockIdx.x; tile < ntiles && ok_all; tile += gridDim.x) {
-    const int seg = (int)(tile % segs);
-    const long long rr = tile / segs;
-    const int row = (int)(rr % H), img = (int)(rr / H);
-    const int x0 = seg * kTileM;
-    const size_t pix0 = ((size_t)img * H + row) * W + x0;
-    for (int t = tid; t < kco * kTileM; t += kThreads) {
-      const int p = t % kTileM, g = t / kTileM;
-      *reinterpret_cast<uint4*>(a_s + g * lbo_y + p * 16) =
-          *reinterpret_cast<const uint4*>(dy + (pix0 + p) * cout + g * 8);
+  const long long units = (long long)batch * ((H + kStripRows - 1) / kStripRows) * segs;
+
+  if (warp >= 5) {
+    // ---- X stagers: input rows y0-1 .. y0+rows of every strip ----
+    const int st = tid - 5 * 32;
+    long long q = 0;
+    for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+      const StripWalk sw(u, H, segs);
+      for (int a = 0; a < sw.rows + 2 && !*abort_v; a++, q++) {
+        const int slot = (int)(q % kSlots);
+        const int yy = sw.y0 - 1 + a;
+        uint4 v[kStageBatch];
+#pragma unroll
+        for (int b = 0; b < kStageBatch; b++) {
+          const int t = st + b * kStageThreads;
+          v[b] = make_uint4(0, 0, 0, 0);
+          if (t < kc * kRowPix) {
+            const int p = t % kRowPix, ch = t / kRowPix;
+            const int xx = sw.x0 - 1 + p;
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+              v[b] = *reinterpret_cast<const uint4*>(
+                  x + (((size_t)sw.img * H + yy) * W + xx) * cin + ch * 8);
+          }
+        }
+        if (q >= kSlots &&
+            !mbar_wait(&xempty[slot], (uint32_t)((q / kSlots - 1) & 1), abort_v, err))
+          break;
+        unsigned char* dst = xring + slot * row_bytes;
+#pragma unroll
+        for (int b = 0; b < kStageBatch; b++) {
+          const int t = st + b * kStageThreads;
+          if (t < kc * kRowPix) {
+            const int p = t % kRowPix, ch = t / kRowPix;
+            *reinterpret_cast<uint4*>(dst + ch * lbo_x + p * 16) = v[b];
+          }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&xfull[slot]);
+      }
     }
-    for (int t = tid; t < 3 * kc * kRowPix; t += kThreads) {
-      const int p = t % kRowPix, rem = t / kRowPix;
-      const int ch = rem % kc, dyr = rem / kc;
-      const int yy = row + dyr - 1, xx = x0 - 1 + p;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-        v = *reinterpret_cast<const uint4*>(x + (((size_t)img * H + yy) * W + xx) * cin +
-                                            ch * 8);
-      *reinterpret_cast<uint4*>(b_s + dyr * row_bytes + ch * lbo_x + p * 16) = v;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid < cout) {  // bias gradient from the staged tile
-      const __nv_bfloat16* col =
-          reinterpret_cast<const __nv_bfloat16*>(a_s + (tid >> 3) * lbo_y) + (tid & 7);
-      for (int p = 0; p < kTileM; p++) bacc += __bfloat162float(col[p * 8]);
-    }
-    if (tid == 0) {
-      for (int tap = 0; tap < 9; tap++) {
-        const int dyr = tap / 3, dx = tap % 3;
-        for (int kq = 0; kq < kTileM / 16; kq++) {
-          const uint32_t aa = smem_u32(a_s) + kq * 256;
-          const uint32_t ba = smem_u32(b_s + dyr * row_bytes) + dx * 16 + kq * 256;
-          // MN-major, no swizzle: LBO steps along K (8 pixels = 128 B), SBO
-          // along M / N (the next 8 channels)
-          const uint64_t ad = smem_desc(aa, 128, lbo_y);
-          const uint64_t bd = smem_desc(ba, 128, lbo_x);
-          const uint32_t acc = (any || kq > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-                  taddr + (uint32_t)(tap * cin)),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+  } else if (warp == 4) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_mn(cin);
+      long long q = 0, p = 0;
+      bool issued = false, ok = true;
+      for (long long u = blockIdx.x; u < units && ok && !*abort_v; u += gridDim.x) {
+        const StripWalk sw(u, H, segs);
+        const long long qb = q;
+        ok = mbar_wait(&xfull[qb % kSlots], (uint32_t)((qb / kSlots) & 1), abort_v, err) &&
+             mbar_wait(&xfull[(qb + 1) % kSlots], (uint32_t)(((qb + 1) / kSlots) & 1),
+                       abort_v, err);
+        for (int o = 0; o < sw.rows && ok; o++, p++) {
+          const long long qn = qb + o + 2;
+          const int ys = (int)(p % kWgYSlots);
+          ok = mbar_wait(&xfull[qn % kSlots], (uint32_t)((qn / kSlots) & 1), abort_v, err) &&
+               mbar_wait(&yfull[ys], (uint32_t)((p / kWgYSlots) & 1), abort_v, err);
+          if (!ok) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t ya = smem_u32(yring + ys * yslot_bytes);
+          for (int tap = 0; tap < 9; tap++) {
+            const int dyr = tap / 3, dx = tap % 3;
+            const uint32_t xa =
+                smem_u32(xring + (int)((qb + o + dyr) % kSlots) * row_bytes) + dx * 16;
+            for (int kq = 0; kq < kTileM / 16; kq++) {
+              // MN-major, no swizzle: LBO steps along K (8 pixels = 128 B),
+              // SBO along M / N (the next 8 channels)
+              const uint64_t ad = smem_desc(ya + kq * 256, 128, lbo_y);
+              const uint64_t bd = smem_desc(xa + kq * 256, 128, lbo_x);
+              const uint32_t acc = (issued || kq > 0) ? 1u : 0u;
+              asm volatile(
+                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                      taddr + (uint32_t)(tap * cin)),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+          }
+          issued = true;
+          tc_commit(&yempty[ys]);
+          tc_commit(&xempty[(qb + o) % kSlots]);
+        }
+        q = qb + sw.rows + 2;
+        if (ok) {
+          tc_commit(&xempty[(q - 2) % kSlots]);
+          tc_commit(&xempty[(q - 1) % kSlots]);
         }
       }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&mbar))
-          : "memory");
-      uint32_t ok = 0;
-      const long long t0 = clock64();
-      while (!ok) {
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            "selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(ok)
-            : "r"(smem_u32(&mbar)), "r"(phase)
-            : "memory");
-        if (!ok && clock64() - t0 > kMaxWaitCycles) break;
-      }
-      if (!ok) atomicExch(err, 1);
-      s_done = ok;
+      s_issued = (issued && ok) ? 1 : 0;
+      __threadfence_block();
+      if (issued)
+        tc_commit(&last_bar);  // arrives once every MMA above has completed
+      else
+        mbar_arrive(&last_bar);
     }
-    __syncthreads();
-    phase ^= 1u;
-    ok_all = s_done != 0;
-    any = true;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  }
-  if (tid < cout && any) atomicAdd(&db[tid], bacc);
-  if (any && ok_all) {
-    // accumulator row = output channel (lanes 32w .. 32w+31)
-    const int co = warp * 32 + lane;
-    for (int c0 = 0; c0 < 9 * cin; c0 += 16) {
-      uint32_t r[16];
-      const uint32_t ta = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-          "%13,%14,%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-            "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-            "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(ta));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (co < cout) {
-        const int tap = c0 / cin, ci0 = c0 - tap * cin;
+  } else {
+    // ---- dY stagers, then the epilogue ----
+    long long p = 0;
+    for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+      const StripWalk sw(u, H, segs);
+      for (int o = 0; o < sw.rows && !*abort_v; o++, p++) {
+        const int ys = (int)(p % kWgYSlots);
+        const size_t pix0 = ((size_t)sw.img * H + sw.y0 + o) * W + sw.x0;
+        uint4 v[kWgYBatch];
 #pragma unroll
-        for (int q = 0; q < 16; q++)
-          atomicAdd(&dw[((size_t)tap * cout + co) * cin + ci0 + q], __uint_as_float(r[q]));
+        for (int b = 0; b < kWgYBatch; b++) {
+          const int t = tid + b * kWgYThreads;  // pixel t % 128, group t / 128
+          if (t < kco * kTileM)
+            v[b] = *reinterpret_cast<const uint4*>(dy + (pix0 + (t % kTileM)) * cout +
+                                                   (t / kTileM) * 8);
+        }
+        if (p >= kWgYSlots &&
+            !mbar_wait(&yempty[ys], (uint32_t)((p / kWgYSlots - 1) & 1), abort_v, err))
+          break;
+        unsigned char* dst = yring + ys * yslot_bytes;
+#pragma unroll
+        for (int b = 0; b < kWgYBatch; b++) {
+          const int t = tid + b * kWgYThreads;
+          if (t < kco * kTileM)
+            *reinterpret_cast<uint4*>(dst + (t / kTileM) * lbo_y + (t % kTileM) * 16) = v[b];
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&yfull[ys]);
+      }
+    }
+    // the accumulators: row co (lanes 32w .. 32w+31), 9 x cin columns
+    volatile int never = 0;
+    const bool done = mbar_wait(&last_bar, 0, &never, err);
+    if (__all_sync(0xffffffffu, done) && s_issued && !*abort_v) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int co = warp * 32 + lane;
+      for (int c0 = 0; c0 < 9 * cin; c0 += 16) {
+        uint32_t r[16];
+        const uint32_t ta = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+            "%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (co < cout) {
+          const int tap = c0 / cin, ci0 = c0 - tap * cin;
+#pragma unroll
+          for (int k = 0; k < 16; k++)
+            atomicAdd(&dw[((size_t)tap * cout + co) * cin + ci0 + k], __uint_as_float(r[k]));
+        }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr),
                  "r"(kWgTmemCols));
+}
+
+// db[co] += sum over pixels of dy[p][co] (FP32 partial sums per block,
+// atomics per channel).
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, float* __restrict__ db,
+                            long long P, int cout) {
+  __shared__ float part[128];
+  for (int c = threadIdx.x; c < cout; c += blockDim.x) part[c] = 0.f;
+  __syncthreads();
+  // thread -> one channel pair, rows strided over the grid
+  const int pairs = cout >> 1;
+  const int lanes_per_row = pairs;  // <= 64
+  const int rows_per_block = blockDim.x / lanes_per_row;
+  const int c2 = threadIdx.x % lanes_per_row, r0 = threadIdx.x / lanes_per_row;
+  if (r0 < rows_per_block) {
+    float s0 = 0.f, s1 = 0.f;
+    for (long long pix = (long long)blockIdx.x * rows_per_block + r0; pix < P;
+         pix += (long long)gridDim.x * rows_per_block) {
+      const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(dy + pix * cout)[c2];
+      s0 += __low2float(v);
+      s1 += __high2float(v);
+    }
+    atomicAdd(&part[2 * c2], s0);
+    atomicAdd(&part[2 * c2 + 1], s1);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cout; c += blockDim.x) atomicAdd(&db[c], part[c]);
 }
 
 // dx = (y > 0) ? g : 0 for a ReLU output y (BF16), g FP32 -> BF16.
@@ -765,23 +883,29 @@ int nl2d_emu_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int
     return NL2D_ERR_ARGS;
   // The kernel holds all 512 TMEM columns, so it must be alone on its SM:
   // asking for more than half an SM's shared memory guarantees that.
-  const size_t need = (size_t)kWgGroups * kTileM * 16 + 3 * (size_t)(cin / 8) * kRowPix * 16;
-  const size_t smem = kWgSmem;
+  const size_t need = (size_t)kWgYSlots * kWgGroups * kTileM * 16 +
+                      (size_t)kSlots * (cin / 8) * kRowPix * 16;
+  const size_t smem = need > kWgSmem ? need : kWgSmem;
+  constexpr size_t kMaxSmem = 200 * 1024;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(k_conv_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kWgSmem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_conv_wgrad_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kMaxSmem) != cudaSuccess)
       return NL2D_ERR_CUDA;
     attr = true;
   }
-  if (need > smem) return NL2D_ERR_ARGS;
+  if (smem > kMaxSmem) return NL2D_ERR_ARGS;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (long long)batch * H * (W / kTileM);
-  const int grid = (int)(tiles < sms ? tiles : sms);  // 512 TMEM columns: one CTA per SM
-  k_conv_wgrad_tc<<<grid, kThreads, smem, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, db, batch, H, W, cin, cout, err);
+  const long long units =
+      (long long)batch * ((H + kStripRows - 1) / kStripRows) * (W / kTileM);
+  const int grid = (int)(units < sms ? units : sms);  // 512 TMEM columns: one CTA per SM
+  k_conv_wgrad_pipe<<<grid, kPipeThreads, smem, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, batch, H, W, cin, cout, err);
+  if (cudaGetLastError() != cudaSuccess) return NL2D_ERR_CUDA;
+  k_bias_grad<<<152 * 8, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)dy, db,
+                                                         (long long)batch * H * W, cout);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 

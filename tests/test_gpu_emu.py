@@ -58,10 +58,14 @@ def test_conv3x3_tcgen05_matches_fp64(gpulib, cin, cout, relu, B, H):
 
 
 @pytest.mark.parametrize("B,H,W,cin,cout", [(2, 4, 128, 48, 16), (2, 3, 256, 16, 48),
-                                             (1, 5, 128, 48, 48)])
+                                             (1, 5, 128, 48, 48),
+                                             # several strips per image; more strips
+                                             # than CTAs, so TMEM accumulates across them
+                                             (3, 19, 256, 48, 48), (60, 17, 128, 16, 48)])
 def test_conv_backward_matches_fp64(gpulib, B, H, W, cin, cout):
     """Input gradient (tcgen05 conv with flipped, transposed weights) and
-    weight / bias gradients (tcgen05 GEMM over pixels, FP32 in tensor memory)
+    weight gradient (pipelined tcgen05 GEMM over pixels, FP32 in tensor
+    memory) and bias gradient
     of L = sum(y * G) against the FP64 numpy gradients, for the layer shapes
     of the network (16 -> 48, 48 -> 48, 48 -> 16)."""
     import torch
