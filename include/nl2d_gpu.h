@@ -367,6 +367,37 @@ int nl2d_face_depths(int width, int height, const double *ht, double *hu,
  * out (cap >= w + 1 bytes). */
 int nl2d_format_e(double v, int w, int d, char *out, int cap);
 
+/* ---- tracer advection (benchmarks/nemo/tracer_advection) ---- */
+
+/* One iteration of the tracer-advection benchmark on the GPU, bit-identical
+ * to the reference's operations.  Replaces tra_adv_compute
+ * (compute_in_subroutine/tra_adv_compute.F90:12-14): same arrays in the
+ * same order, Fortran layout a(ji, jj, jk) (ji fastest), extents by value.
+ * The first call with a given set of arrays and extents uploads them and
+ * starts a new run (the reference's work arrays start as fresh, zeroed
+ * pages); later calls with the same arrays advance the device copy of
+ * mydomain, which tra_adv_read copies back (the inputs are assumed
+ * unchanged while registered).  jpi, jpj >= 3, jpk >= 2.  Errors are
+ * recorded for tra_adv_last_error. */
+void tra_adv_compute(const double *ztfreez, const double *pun,
+                     const double *pvn, const double *pwn, const double *umask,
+                     const double *vmask, const double *tmask,
+                     const double *rnfmsk, const double *rnfmsk_z,
+                     const double *upsmsk, double *mydomain, const double *tsn,
+                     int jpi, int jpj, int jpk);
+/* niter more iterations on the registered state; *ms = their device time
+ * (CUDA events on the library's stream). */
+int tra_adv_run(int niter, double *ms);
+/* Copies the current mydomain (all jpi x jpj x jpk values) to the host. */
+int tra_adv_read(double *mydomain);
+/* The benchmark's checksum (tra_adv.F90:263-270): the sum of mydomain over
+ * jk < jpk and the interior columns, in the reference's loop order. */
+int tra_adv_checksum(double *out);
+/* Sticky status of the tracer entry points (cleared by the call). */
+int tra_adv_last_error(char *buf, int len);
+/* Frees the device copies. */
+void tra_adv_finalize(void);
+
 /* Device address currently holding a registered field (for callers that
  * share device memory); NULL if unknown.  Valid until the next step. */
 void *nl2d_device_ptr(const void *field);

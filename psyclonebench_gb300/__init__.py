@@ -89,6 +89,12 @@ EXPORTS = {
     "nl2d_face_depths": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_format_e": (ctypes.c_int, [ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_char_p, ctypes.c_int]),
+    "tra_adv_compute": (None, [_DP] * 12 + [ctypes.c_int] * 3),
+    "tra_adv_run": (ctypes.c_int, [ctypes.c_int, _DP]),
+    "tra_adv_read": (ctypes.c_int, [_DP]),
+    "tra_adv_checksum": (ctypes.c_int, [_DP]),
+    "tra_adv_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "tra_adv_finalize": (None, []),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }

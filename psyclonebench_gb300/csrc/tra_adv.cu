@@ -1,0 +1,399 @@
+// Tracer advection (the NEMO tra_adv benchmark,
+// benchmarks/nemo/tracer_advection/original/tra_adv.F90:107-257, in the
+// per-iteration form of compute_in_subroutine/tra_adv_compute.F90:12-) on
+// the GPU, bit-identical to the reference's operations (built with
+// -fmad=false; SIGN is copysign, MAX / MIN pairwise left to right).
+//
+// Layout: Fortran a(ji, jj, jk) is a[(k * J + j) * I + i], 0-based.
+//
+// One iteration is two kernels:
+//  * k_tra_horizontal: for every interior point (1 <= i <= I-2,
+//    1 <= j <= J-2, k <= K-2) the x / y differences, MUSCL slopes with their
+//    limiter, the upstream fluxes and the flux-divergence update, from the
+//    previous iteration's field (ping-pong buffers: the update of one point
+//    never sees another point's new value, as in the reference's separate
+//    loops).
+//  * k_tra_vertical: one thread per interior column marches up in k through
+//    the vertical differences, slopes, fluxes and the final assignment.
+// Work arrays are never stored: each value is recomputed where it is used.
+// Two of the reference's work-array entries are read before the iteration
+// writes them, so they come from earlier calls:
+//  * zwx(jpi, :, :) (the x difference east of the last interior column)
+//    holds the previous iteration's vertical differences of that column,
+//    whose field never changes: tmask (m(k-1) - m(k)), pwn m at k = 1; on
+//    the first iteration after registration it is zero (fresh pages).
+//  * zwy(jpi, :, :) and zwy(:, jpj, :) are never written: zero.
+// zind depends only on inputs, so it is computed once at registration.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/nl2d_gpu.h"
+
+namespace {
+
+__device__ __forceinline__ double max2(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double min3(double a, double b, double c) {
+  const double m = a < b ? a : b;
+  return m < c ? m : c;
+}
+// (a + b) (0.25 + SIGN(0.25, a b))
+__device__ __forceinline__ double slope_raw(double a, double b) {
+  return (a + b) * (0.25 + copysign(0.25, a * b));
+}
+// SIGN(1, s) MIN(|s|, 2 |p|, 2 |q|)
+__device__ __forceinline__ double limit(double s, double p, double q) {
+  return copysign(1.0, s) * min3(fabs(s), 2.0 * fabs(p), 2.0 * fabs(q));
+}
+// The upstream flux of tra_adv.F90:163-169 (x) / :171-177 (y): vel at the
+// face, the field on the far (f1) and near (f0) side, their slopes.
+__device__ __forceinline__ double upstream(double vel, double f1, double f0, double zind,
+                                           double s1, double s0) {
+  const double z0 = copysign(0.5, vel);
+  const double zalpha = 0.5 - z0;
+  const double zu = z0 - 0.5 * vel * 1.0;
+  const double zzwx = f1 + zind * (zu * s1);
+  const double zzwy = f0 + zind * (zu * s0);
+  return vel * (zalpha * zzwx + (1.0 - zalpha) * zzwy);
+}
+
+struct TraDev {
+  const double *pun, *pvn, *pwn, *umask, *vmask, *tmask, *zind;
+  int I, J, K;
+};
+
+__global__ void k_tra_zind(const double* __restrict__ tsn, const double* __restrict__ ztfreez,
+                           const double* __restrict__ rnfmsk, const double* __restrict__ upsmsk,
+                           const double* __restrict__ rnfmsk_z,
+                           const double* __restrict__ tmask, double* __restrict__ zind, int I,
+                           int J, int K) {
+  const long long n = (long long)I * J * K;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t / ((long long)I * J));
+    const long long p2 = t - (long long)k * I * J;
+    const double zice = tsn[t] <= ztfreez[p2] + 0.1 ? 1.0 : 0.0;
+    double z = max2(max2(rnfmsk[p2] * rnfmsk_z[k], upsmsk[p2]), zice) * tmask[t];
+    zind[t] = 1 - z;
+  }
+}
+
+// zwx of the reference before its flux loop, at (i, j, k) with k <= K-2:
+// the x difference (i <= I-2), or the entry east of the last interior
+// column (i = I-1) that the previous iteration's vertical part left there.
+__device__ __forceinline__ double xdiff(const double* __restrict__ m, const TraDev& d, int i,
+                                        size_t c, int k, bool first) {
+  if (i <= d.I - 2) return d.umask[c] * (m[c + 1] - m[c]);
+  if (first) return 0.0;
+  if (k == 0) return d.pwn[c] * m[c];
+  return d.tmask[c] * (m[c - (size_t)d.I * d.J] - m[c]);
+}
+// zwy before the flux loop at (i, j, k), i <= I-2: the y difference, or
+// zero on the row j = J-1 the reference never writes.
+__device__ __forceinline__ double ydiff(const double* __restrict__ m, const TraDev& d, int j,
+                                        size_t c) {
+  if (j <= d.J - 2) return d.vmask[c] * (m[c + d.I] - m[c]);
+  return 0.0;
+}
+
+// tra_adv.F90:122-194 for the interior points; `mo` the field before the
+// iteration, `mn` receives the updated interior (other points of `mn`
+// already hold their unchanging values).
+__global__ void __launch_bounds__(256)
+    k_tra_horizontal(const double* __restrict__ mo, double* __restrict__ mn, TraDev d,
+                     int first) {
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > d.I - 2 || j > d.J - 2) return;
+  const size_t c = ((size_t)k * d.J + j) * d.I + i;
+  const bool f = first != 0;
+  // x direction: differences at i-2 .. i+1, slopes at i-1 .. i+1
+  const double dm1 = xdiff(mo, d, i - 1, c - 1, k, f);
+  const double d0 = xdiff(mo, d, i, c, k, f);
+  const double dp1 = xdiff(mo, d, i + 1, c + 1, k, f);
+  const double sx0 = limit(slope_raw(d0, dm1), dm1, d0);
+  const double sxp = limit(slope_raw(dp1, d0), d0, dp1);
+  const double fx = upstream(d.pun[c], mo[c + 1], mo[c], d.zind[c], sxp, sx0);
+  double fxm;
+  if (i == 1) {
+    fxm = dm1;  // the reference's flux loop starts at ji = 2: zwx(1) is still the difference
+  } else {
+    const double dm2 = xdiff(mo, d, i - 2, c - 2, k, f);
+    const double sxm = limit(slope_raw(dm1, dm2), dm2, dm1);
+    fxm = upstream(d.pun[c - 1], mo[c], mo[c - 1], d.zind[c - 1], sx0, sxm);
+  }
+  // y direction
+  const size_t I = d.I;
+  const double em1 = ydiff(mo, d, j - 1, c - I);
+  const double e0 = ydiff(mo, d, j, c);
+  const double ep1 = ydiff(mo, d, j + 1, c + I);
+  const double sy0 = limit(slope_raw(e0, em1), em1, e0);
+  const double syp = limit(slope_raw(ep1, e0), e0, ep1);
+  const double fy = upstream(d.pvn[c], mo[c + I], mo[c], d.zind[c], syp, sy0);
+  double fym;
+  if (j == 1) {
+    fym = em1;
+  } else {
+    const double em2 = ydiff(mo, d, j - 2, c - 2 * I);
+    const double sym = limit(slope_raw(em1, em2), em2, em1);
+    fym = upstream(d.pvn[c - I], mo[c], mo[c - I], d.zind[c - I], sy0, sym);
+  }
+  const double ztra = -(1.0 * (fx - fxm + fy - fym));
+  mn[c] = mo[c] + ztra;
+}
+
+// tra_adv.F90:196-251 for one interior column, in place on m (the field
+// after the horizontal update).
+__global__ void __launch_bounds__(256) k_tra_vertical(double* __restrict__ m, TraDev d) {
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > d.I - 2 || j > d.J - 2) return;
+  const size_t s = (size_t)d.I * d.J;
+  const size_t c0 = (size_t)j * d.I + i;
+  const int K = d.K;
+  double mk = m[c0];
+  double mk1 = m[c0 + s];  // K >= 2
+  double zd1 = (1 <= K - 2) ? d.tmask[c0 + s] * (mk - mk1) : 0.0;
+  double slk = 0.0;               // zslpx(:,:,1) = 0
+  double fwk = d.pwn[c0] * mk;    // zwx(:,:,1) = pwn m
+  for (int k = 0; k <= K - 2; k++) {
+    const size_t c = c0 + (size_t)k * s;
+    double mk2 = 0.0, zd2 = 0.0;
+    if (k + 2 <= K - 1) mk2 = m[c + 2 * s];
+    if (k + 2 <= K - 2) zd2 = d.tmask[c + 2 * s] * (mk1 - mk2);
+    const double slk1 = (k + 1 <= K - 2) ? limit(slope_raw(zd1, zd2), zd2, zd1) : 0.0;
+    const double p1 = d.pwn[c + s];
+    const double z0w = copysign(0.5, p1);
+    const double zalpha = 0.5 + z0w;
+    const double zw = z0w - 0.5 * p1 * 1.0 * 1.0;
+    const double zind = d.zind[c];
+    const double zzwx = mk1 + zind * (zw * slk1);
+    const double zzwy = mk + zind * (zw * slk);
+    const double fwk1 = p1 * (zalpha * zzwx + (1. - zalpha) * zzwy);
+    m[c] = -(1.0 * (fwk - fwk1));
+    mk = mk1;
+    mk1 = mk2;
+    zd1 = zd2;
+    slk = slk1;
+    fwk = fwk1;
+  }
+}
+
+}  // namespace
+
+// ---- host side ---------------------------------------------------------------
+
+namespace {
+
+struct TraState {
+  // registration key: the caller's arrays and extents
+  const void* key[12] = {};
+  int I = 0, J = 0, K = 0;
+  bool registered = false;
+  double* m[2] = {nullptr, nullptr};  // ping-pong copies of mydomain
+  double *pun = nullptr, *pvn = nullptr, *pwn = nullptr, *umask = nullptr, *vmask = nullptr,
+         *tmask = nullptr, *zind = nullptr;
+  int cur = 0;                 // buffer holding the current field
+  long long iters = 0;         // iterations since registration
+  cudaStream_t stream = nullptr;
+  int status = NL2D_OK;
+  char msg[256] = "";
+};
+TraState g_tra;
+
+void tra_fail(int code, const char* fmt, ...) {
+  if (g_tra.status != NL2D_OK) return;  // keep the first error
+  g_tra.status = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_tra.msg, sizeof g_tra.msg, fmt, ap);
+  va_end(ap);
+}
+
+bool tra_ck(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  tra_fail(NL2D_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+
+void tra_release() {
+  TraState& s = g_tra;
+  for (double** p : {&s.m[0], &s.m[1], &s.pun, &s.pvn, &s.pwn, &s.umask, &s.vmask, &s.tmask,
+                     &s.zind}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  s.registered = false;
+}
+
+TraDev tra_dev() {
+  const TraState& s = g_tra;
+  return TraDev{s.pun, s.pvn, s.pwn, s.umask, s.vmask, s.tmask, s.zind, s.I, s.J, s.K};
+}
+
+// One iteration's two launches on the library's stream.
+void tra_launch_iteration(int cur, bool first) {
+  TraState& s = g_tra;
+  const dim3 blk(32, 8);
+  const dim3 grd((s.I - 2 + 31) / 32, (s.J - 2 + 7) / 8, s.K - 1);
+  k_tra_horizontal<<<grd, blk, 0, s.stream>>>(s.m[cur], s.m[cur ^ 1], tra_dev(), first ? 1 : 0);
+  const dim3 grd2(grd.x, grd.y, 1);
+  k_tra_vertical<<<grd2, blk, 0, s.stream>>>(s.m[cur ^ 1], tra_dev());
+}
+
+bool tra_register(const double* ztfreez, const double* pun, const double* pvn, const double* pwn,
+                  const double* umask, const double* vmask, const double* tmask,
+                  const double* rnfmsk, const double* rnfmsk_z, const double* upsmsk,
+                  const double* mydomain, const double* tsn, int I, int J, int K) {
+  TraState& s = g_tra;
+  const void* key[12] = {ztfreez, pun, pvn, pwn, umask, vmask, tmask, rnfmsk, rnfmsk_z,
+                         upsmsk, mydomain, tsn};
+  if (s.registered && s.I == I && s.J == J && s.K == K && !memcmp(key, s.key, sizeof key))
+    return true;
+  tra_release();
+  if (!s.stream && !tra_ck(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking),
+                           "cudaStreamCreateWithFlags"))
+    return false;
+  const size_t n3 = (size_t)I * J * K, b3 = n3 * sizeof(double);
+  const size_t b2 = (size_t)I * J * sizeof(double);
+  for (double** p : {&s.m[0], &s.m[1], &s.pun, &s.pvn, &s.pwn, &s.umask, &s.vmask, &s.tmask,
+                     &s.zind})
+    if (!tra_ck(cudaMalloc(p, b3), "cudaMalloc")) return false;
+  double *d_tsn = nullptr, *d2[3] = {nullptr, nullptr, nullptr}, *d_rz = nullptr;
+  bool ok = tra_ck(cudaMalloc(&d_tsn, b3), "cudaMalloc") &&
+            tra_ck(cudaMalloc(&d_rz, K * sizeof(double)), "cudaMalloc");
+  for (int q = 0; q < 3 && ok; q++) ok = tra_ck(cudaMalloc(&d2[q], b2), "cudaMalloc");
+  const struct {
+    double* dst;
+    const double* src;
+    size_t bytes;
+  } up[] = {{s.m[0], mydomain, b3}, {s.pun, pun, b3},     {s.pvn, pvn, b3},
+            {s.pwn, pwn, b3},       {s.umask, umask, b3}, {s.vmask, vmask, b3},
+            {s.tmask, tmask, b3},   {d_tsn, tsn, b3},     {d2[0], ztfreez, b2},
+            {d2[1], rnfmsk, b2},    {d2[2], upsmsk, b2},  {d_rz, rnfmsk_z, K * sizeof(double)}};
+  for (const auto& u : up)
+    if (ok) ok = tra_ck(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s.stream),
+                        "upload");
+  if (ok) {
+    ok = tra_ck(cudaMemcpyAsync(s.m[1], s.m[0], b3, cudaMemcpyDeviceToDevice, s.stream),
+                "copy");
+    k_tra_zind<<<152 * 8, 256, 0, s.stream>>>(d_tsn, d2[0], d2[1], d2[2], d_rz, s.tmask, s.zind,
+                                              I, J, K);
+    ok = ok && tra_ck(cudaGetLastError(), "k_tra_zind") &&
+         tra_ck(cudaStreamSynchronize(s.stream), "registration");
+  }
+  cudaFree(d_tsn);
+  cudaFree(d_rz);
+  for (double* p : d2) cudaFree(p);
+  if (!ok) {
+    tra_release();
+    return false;
+  }
+  memcpy(s.key, key, sizeof key);
+  s.I = I;
+  s.J = J;
+  s.K = K;
+  s.cur = 0;
+  s.iters = 0;
+  s.registered = true;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tra_adv_compute(const double* ztfreez, const double* pun, const double* pvn,
+                     const double* pwn, const double* umask, const double* vmask,
+                     const double* tmask, const double* rnfmsk, const double* rnfmsk_z,
+                     const double* upsmsk, double* mydomain, const double* tsn, int jpi, int jpj,
+                     int jpk) {
+  if (!ztfreez || !pun || !pvn || !pwn || !umask || !vmask || !tmask || !rnfmsk || !rnfmsk_z ||
+      !upsmsk || !mydomain || !tsn || jpi < 3 || jpj < 3 || jpk < 2 ||
+      (double)jpi * jpj * jpk > 4.0e9) {
+    tra_fail(NL2D_ERR_ARGS, "tra_adv_compute: bad arrays or extents (%d x %d x %d)", jpi, jpj,
+             jpk);
+    return;
+  }
+  if (!tra_register(ztfreez, pun, pvn, pwn, umask, vmask, tmask, rnfmsk, rnfmsk_z, upsmsk,
+                    mydomain, tsn, jpi, jpj, jpk))
+    return;
+  TraState& s = g_tra;
+  tra_launch_iteration(s.cur, s.iters == 0);
+  if (!tra_ck(cudaGetLastError(), "tra_adv iteration")) return;
+  s.cur ^= 1;
+  s.iters++;
+}
+
+int tra_adv_run(int niter, double* ms) {
+  TraState& s = g_tra;
+  if (!s.registered) return NL2D_ERR_STATE;
+  if (niter < 0) return NL2D_ERR_ARGS;
+  cudaEvent_t e0, e1;
+  if (!tra_ck(cudaEventCreate(&e0), "cudaEventCreate") ||
+      !tra_ck(cudaEventCreate(&e1), "cudaEventCreate"))
+    return NL2D_ERR_CUDA;
+  cudaEventRecord(e0, s.stream);
+  for (int t = 0; t < niter; t++) {
+    tra_launch_iteration(s.cur, s.iters == 0);
+    s.cur ^= 1;
+    s.iters++;
+  }
+  cudaEventRecord(e1, s.stream);
+  bool ok = tra_ck(cudaGetLastError(), "tra_adv_run") &&
+            tra_ck(cudaEventSynchronize(e1), "tra_adv_run");
+  float t = 0.f;
+  if (ok) cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = t;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ok ? NL2D_OK : NL2D_ERR_CUDA;
+}
+
+int tra_adv_read(double* mydomain) {
+  TraState& s = g_tra;
+  if (!s.registered) return NL2D_ERR_STATE;
+  if (!mydomain) return NL2D_ERR_ARGS;
+  const size_t b3 = (size_t)s.I * s.J * s.K * sizeof(double);
+  if (!tra_ck(cudaMemcpyAsync(mydomain, s.m[s.cur], b3, cudaMemcpyDeviceToHost, s.stream),
+              "tra_adv_read") ||
+      !tra_ck(cudaStreamSynchronize(s.stream), "tra_adv_read"))
+    return NL2D_ERR_CUDA;
+  return NL2D_OK;
+}
+
+int tra_adv_checksum(double* out) {
+  TraState& s = g_tra;
+  if (!s.registered) return NL2D_ERR_STATE;
+  if (!out) return NL2D_ERR_ARGS;
+  std::vector<double> h((size_t)s.I * s.J * s.K);
+  const int rc = tra_adv_read(h.data());
+  if (rc != NL2D_OK) return rc;
+  // tra_adv.F90:264-270, in the reference's loop order
+  double sum = 0.0;
+  for (int k = 0; k <= s.K - 2; k++)
+    for (int j = 1; j <= s.J - 2; j++)
+      for (int i = 1; i <= s.I - 2; i++) sum = sum + h[((size_t)k * s.J + j) * s.I + i];
+  *out = sum;
+  return NL2D_OK;
+}
+
+int tra_adv_last_error(char* buf, int len) {
+  if (buf && len > 0) snprintf(buf, (size_t)len, "%s", g_tra.msg);
+  const int st = g_tra.status;
+  g_tra.status = NL2D_OK;
+  g_tra.msg[0] = '\0';
+  return st;
+}
+
+void tra_adv_finalize(void) {
+  tra_release();
+  if (g_tra.stream) cudaStreamDestroy(g_tra.stream);
+  g_tra.stream = nullptr;
+}
+
+}  // extern "C"
