@@ -391,6 +391,78 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
     }
 
 
+def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
+    """The tracer-advection benchmark (benchmarks/nemo/tracer_advection) at
+    the largest size of the reference's problem-size sweep
+    (scripts/problemsize.sh: JPI = JPJ = 512, JPK = 75, IT = 500), from the
+    benchmark's own initial values.  value: Mpoint-iterations/s of `iters`
+    iterations on the device-resident state (CUDA events); e2e: the same
+    iterations through tra_adv_compute from host arrays, with the upload of
+    the first call and the final read-back; roofline: 72 algorithmic bytes
+    per point-iteration (read mydomain, pun, pvn, pwn, umask, vmask, tmask
+    and the precomputed zind; write mydomain); cpu_baseline: the oracle's
+    OpenMP port on all host cores for `cpu_iters` iterations."""
+    import tra_adv_numpy as TN
+    from test_tra_oracle import oracle_run, tra_lib, zero_work
+    f = TN.init(jpi, jpj, jpk)
+    D = ctypes.POINTER(ctypes.c_double)
+
+    def p(a):
+        return a.ctypes.data_as(D)
+
+    args = [p(f[n]) for n in ("ztfreez", "pun", "pvn", "pwn", "umask", "vmask", "tmask",
+                              "rnfmsk", "rnfmsk_z", "upsmsk", "mydomain", "tsn")] + \
+        [jpi, jpj, jpk]
+    points = jpi * jpj * jpk
+    # e2e: host arrays in, result out
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        lib.tra_adv_compute(*args)
+    out = np.empty_like(f["mydomain"])
+    rc = lib.tra_adv_read(p(out))
+    e2e_s = time.perf_counter() - t0
+    buf = ctypes.create_string_buffer(256)
+    if rc != 0 or lib.tra_adv_last_error(buf, 256) != 0:
+        raise RuntimeError("tra_adv failed: %s" % buf.value.decode())
+    csum = ctypes.c_double(0.0)
+    lib.tra_adv_checksum(ctypes.byref(csum))
+    # value: resident state, after warm-up
+    ms = ctypes.c_double(0.0)
+    lib.tra_adv_run(3, ctypes.byref(ms))
+    lib.tra_adv_run(iters, ctypes.byref(ms))
+    lib.tra_adv_finalize()
+    value = points * iters / (ms.value * 1e-3) / 1e6
+    hbm, peak_kind = peaks()
+    ach = 72.0 * points * iters / (ms.value * 1e-3) / 1e9
+    in_bytes = sum(f[n].nbytes for n in f)
+    # CPU: the oracle's OpenMP port on a bounded sample of the same workload
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    lib_o = tra_lib()
+    g = {n: v.copy() for n, v in f.items()}
+    w = zero_work(g["mydomain"].shape)
+    t0 = time.perf_counter()
+    oracle_run(lib_o, g, w, cpu_iters, omp=True)
+    cpu_s = time.perf_counter() - t0
+    return {
+        "workload": "tra_adv_%dx%dx%d_%d_iterations" % (jpi, jpj, jpk, iters),
+        "metric": "Mpoint-iterations/s", "value": value, "ms_per_iteration": ms.value / iters,
+        "checksum_after_first_run": csum.value,
+        "e2e": {"value": points * iters / e2e_s / 1e6, "unit": "Mpoint-iterations/s",
+                "h2d_bytes_per_step": in_bytes / iters,
+                "d2h_bytes_per_step": out.nbytes / iters, "seconds": e2e_s},
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "peak_kind": peak_kind,
+                     "alg_bytes_per_point": 72, "kernels": ["k_tra_horizontal",
+                                                            "k_tra_vertical"]},
+        "cpu_baseline": {"value": points * cpu_iters / cpu_s / 1e6,
+                         "unit": "Mpoint-iterations/s",
+                         "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                         "sample": "%d iterations of the same domain (oracle OpenMP port)" %
+                                   cpu_iters},
+        "dtype": "f64",
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -497,6 +569,7 @@ def run_ours(args, rank, world, local):
         ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
         ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
         forms["ensemble"] = ens
+        forms["tra_adv"] = run_tra_adv(lib)
         if not args.no_emulator:
             forms["emulator"] = run_emulator(lib, count=args.emu_domains,
                                              horizon=args.emu_horizon, iters=args.emu_iters)
