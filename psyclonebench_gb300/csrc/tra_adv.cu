@@ -7,7 +7,7 @@
 // Layout: Fortran a(ji, jj, jk) is a[(k * J + j) * I + i], 0-based.
 //
 // One iteration is two kernels:
-//  * k_tra_horizontal: for every interior point (1 <= i <= I-2,
+//  * k_tra_horizontal_tiled: for every interior point (1 <= i <= I-2,
 //    1 <= j <= J-2, k <= K-2) the x / y differences, MUSCL slopes with their
 //    limiter, the upstream fluxes and the flux-divergence update, from the
 //    previous iteration's field (ping-pong buffers: the update of one point
@@ -81,69 +81,107 @@ __global__ void k_tra_zind(const double* __restrict__ tsn, const double* __restr
   }
 }
 
-// zwx of the reference before its flux loop, at (i, j, k) with k <= K-2:
-// the x difference (i <= I-2), or the entry east of the last interior
-// column (i = I-1) that the previous iteration's vertical part left there.
-__device__ __forceinline__ double xdiff(const double* __restrict__ m, const TraDev& d, int i,
-                                        size_t c, int k, bool first) {
-  if (i <= d.I - 2) return d.umask[c] * (m[c + 1] - m[c]);
-  if (first) return 0.0;
-  if (k == 0) return d.pwn[c] * m[c];
-  return d.tmask[c] * (m[c - (size_t)d.I * d.J] - m[c]);
-}
-// zwy before the flux loop at (i, j, k), i <= I-2: the y difference, or
-// zero on the row j = J-1 the reference never writes.
-__device__ __forceinline__ double ydiff(const double* __restrict__ m, const TraDev& d, int j,
-                                        size_t c) {
-  if (j <= d.J - 2) return d.vmask[c] * (m[c + d.I] - m[c]);
-  return 0.0;
-}
+// tra_adv.F90:122-194 for the interior points, from `mo` (the field before
+// the iteration) into `mn` (whose other points already hold their
+// unchanging values).  A CTA of kTx x kTy threads owns kTx x kTy interior
+// points of one level and stages, in shared memory, the field with a
+// 2-point halo, then the x / y differences, the limited slopes and the
+// fluxes its points need, each once, shared by the neighbours.  The
+// x difference east of the last interior column (i = I-1) is the entry the
+// previous iteration's vertical part left in the reference's zwx (zero on
+// the first iteration); y differences on the row j = J-1 are zero (never
+// written there).
+constexpr int kTx = 32, kTy = 16;
 
-// tra_adv.F90:122-194 for the interior points; `mo` the field before the
-// iteration, `mn` receives the updated interior (other points of `mn`
-// already hold their unchanging values).
-__global__ void __launch_bounds__(256)
-    k_tra_horizontal(const double* __restrict__ mo, double* __restrict__ mn, TraDev d,
-                     int first) {
-  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i > d.I - 2 || j > d.J - 2) return;
-  const size_t c = ((size_t)k * d.J + j) * d.I + i;
+__global__ void __launch_bounds__(kTx * kTy)
+    k_tra_horizontal_tiled(const double* __restrict__ mo, double* __restrict__ mn, TraDev d,
+                           int first) {
+  __shared__ double sm[kTy + 4][kTx + 4];   // m at (j0-2+r, i0-2+c)
+  __shared__ double dx_[kTy][kTx + 3];      // x difference at i0-2+c
+  __shared__ double dy_[kTy + 3][kTx];      // y difference at j0-2+r
+  __shared__ double sx_[kTy][kTx + 2];      // x slope at i0-1+c
+  __shared__ double sy_[kTy + 2][kTx];      // y slope at j0-1+r
+  __shared__ double fx_[kTy][kTx + 1];      // x flux at i0-1+c
+  __shared__ double fy_[kTy + 1][kTx];      // y flux at j0-1+r
+  const int tid = threadIdx.y * kTx + threadIdx.x, nt = kTx * kTy;
+  const int i0 = 1 + blockIdx.x * kTx, j0 = 1 + blockIdx.y * kTy, k = blockIdx.z;
+  const int I = d.I, J = d.J;
+  const size_t lev = (size_t)k * J * I;
   const bool f = first != 0;
-  // x direction: differences at i-2 .. i+1, slopes at i-1 .. i+1
-  const double dm1 = xdiff(mo, d, i - 1, c - 1, k, f);
-  const double d0 = xdiff(mo, d, i, c, k, f);
-  const double dp1 = xdiff(mo, d, i + 1, c + 1, k, f);
-  const double sx0 = limit(slope_raw(d0, dm1), dm1, d0);
-  const double sxp = limit(slope_raw(dp1, d0), d0, dp1);
-  const double fx = upstream(d.pun[c], mo[c + 1], mo[c], d.zind[c], sxp, sx0);
-  double fxm;
-  if (i == 1) {
-    fxm = dm1;  // the reference's flux loop starts at ji = 2: zwx(1) is still the difference
-  } else {
-    const double dm2 = xdiff(mo, d, i - 2, c - 2, k, f);
-    const double sxm = limit(slope_raw(dm1, dm2), dm2, dm1);
-    fxm = upstream(d.pun[c - 1], mo[c], mo[c - 1], d.zind[c - 1], sx0, sxm);
+
+  for (int t = tid; t < (kTy + 4) * (kTx + 4); t += nt) {
+    const int r = t / (kTx + 4), c = t - r * (kTx + 4);
+    const int i = i0 - 2 + c, j = j0 - 2 + r;
+    sm[r][c] = (i >= 0 && i < I && j >= 0 && j < J) ? mo[lev + (size_t)j * I + i] : 0.0;
   }
-  // y direction
-  const size_t I = d.I;
-  const double em1 = ydiff(mo, d, j - 1, c - I);
-  const double e0 = ydiff(mo, d, j, c);
-  const double ep1 = ydiff(mo, d, j + 1, c + I);
-  const double sy0 = limit(slope_raw(e0, em1), em1, e0);
-  const double syp = limit(slope_raw(ep1, e0), e0, ep1);
-  const double fy = upstream(d.pvn[c], mo[c + I], mo[c], d.zind[c], syp, sy0);
-  double fym;
-  if (j == 1) {
-    fym = em1;
-  } else {
-    const double em2 = ydiff(mo, d, j - 2, c - 2 * I);
-    const double sym = limit(slope_raw(em1, em2), em2, em1);
-    fym = upstream(d.pvn[c - I], mo[c], mo[c - I], d.zind[c - I], sy0, sym);
+  __syncthreads();
+  for (int t = tid; t < kTy * (kTx + 3); t += nt) {  // x differences
+    const int r = t / (kTx + 3), c = t - r * (kTx + 3);
+    const int i = i0 - 2 + c, j = j0 + r;
+    double v = 0.0;
+    if (i >= 0 && j < J) {
+      const size_t g = lev + (size_t)j * I + i;
+      if (i <= I - 2) v = d.umask[g] * (sm[r + 2][c + 1] - sm[r + 2][c]);
+      else if (i == I - 1 && !f)
+        v = (k == 0) ? d.pwn[g] * sm[r + 2][c] : d.tmask[g] * (mo[g - (size_t)I * J] - sm[r + 2][c]);
+    }
+    dx_[r][c] = v;
   }
-  const double ztra = -(1.0 * (fx - fxm + fy - fym));
-  mn[c] = mo[c] + ztra;
+  for (int t = tid; t < (kTy + 3) * kTx; t += nt) {  // y differences
+    const int r = t / kTx, c = t - r * kTx;
+    const int i = i0 + c, j = j0 - 2 + r;
+    double v = 0.0;
+    if (j >= 0 && j <= J - 2 && i < I) {
+      const size_t g = lev + (size_t)j * I + i;
+      v = d.vmask[g] * (sm[r + 1][c + 2] - sm[r][c + 2]);
+    }
+    dy_[r][c] = v;
+  }
+  __syncthreads();
+  for (int t = tid; t < kTy * (kTx + 2); t += nt) {  // x slopes at i0-1+c
+    const int r = t / (kTx + 2), c = t - r * (kTx + 2);
+    const double a = dx_[r][c + 1], b = dx_[r][c];
+    sx_[r][c] = limit(slope_raw(a, b), b, a);
+  }
+  for (int t = tid; t < (kTy + 2) * kTx; t += nt) {  // y slopes at j0-1+r
+    const int r = t / kTx, c = t - r * kTx;
+    const double a = dy_[r + 1][c], b = dy_[r][c];
+    sy_[r][c] = limit(slope_raw(a, b), b, a);
+  }
+  __syncthreads();
+  for (int t = tid; t < kTy * (kTx + 1); t += nt) {  // x fluxes at i0-1+c
+    const int r = t / (kTx + 1), c = t - r * (kTx + 1);
+    const int i = i0 - 1 + c, j = j0 + r;
+    double v = 0.0;
+    if (i == 0) {
+      v = dx_[r][c + 1];  // the flux loop starts at ji = 2: zwx(1) is still the difference
+    } else if (i <= I - 2 && j < J) {
+      const size_t g = lev + (size_t)j * I + i;
+      v = upstream(d.pun[g], sm[r + 2][c + 2], sm[r + 2][c + 1], d.zind[g], sx_[r][c + 1],
+                   sx_[r][c]);
+    }
+    fx_[r][c] = v;
+  }
+  for (int t = tid; t < (kTy + 1) * kTx; t += nt) {  // y fluxes at j0-1+r
+    const int r = t / kTx, c = t - r * kTx;
+    const int i = i0 + c, j = j0 - 1 + r;
+    double v = 0.0;
+    if (j == 0) {
+      v = dy_[r + 1][c];
+    } else if (j <= J - 2 && i < I) {
+      const size_t g = lev + (size_t)j * I + i;
+      v = upstream(d.pvn[g], sm[r + 2][c + 2], sm[r + 1][c + 2], d.zind[g], sy_[r + 1][c],
+                   sy_[r][c]);
+    }
+    fy_[r][c] = v;
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  if (i <= I - 2 && j <= J - 2) {
+    const int r = threadIdx.y, c = threadIdx.x;
+    const double ztra = -(1.0 * (fx_[r][c + 1] - fx_[r][c] + fy_[r + 1][c] - fy_[r][c]));
+    mn[lev + (size_t)j * I + i] = sm[r + 2][c + 2] + ztra;
+  }
 }
 
 // tra_adv.F90:196-251 for one interior column, in place on m (the field
@@ -238,11 +276,13 @@ TraDev tra_dev() {
 // One iteration's two launches on the library's stream.
 void tra_launch_iteration(int cur, bool first) {
   TraState& s = g_tra;
-  const dim3 blk(32, 8);
-  const dim3 grd((s.I - 2 + 31) / 32, (s.J - 2 + 7) / 8, s.K - 1);
-  k_tra_horizontal<<<grd, blk, 0, s.stream>>>(s.m[cur], s.m[cur ^ 1], tra_dev(), first ? 1 : 0);
-  const dim3 grd2(grd.x, grd.y, 1);
-  k_tra_vertical<<<grd2, blk, 0, s.stream>>>(s.m[cur ^ 1], tra_dev());
+  const dim3 blk(kTx, kTy);
+  const dim3 grd((s.I - 2 + kTx - 1) / kTx, (s.J - 2 + kTy - 1) / kTy, s.K - 1);
+  k_tra_horizontal_tiled<<<grd, blk, 0, s.stream>>>(s.m[cur], s.m[cur ^ 1], tra_dev(),
+                                                     first ? 1 : 0);
+  const dim3 vblk(32, 8);
+  const dim3 vgrd((s.I - 2 + 31) / 32, (s.J - 2 + 7) / 8, 1);
+  k_tra_vertical<<<vgrd, vblk, 0, s.stream>>>(s.m[cur ^ 1], tra_dev());
 }
 
 bool tra_register(const double* ztfreez, const double* pun, const double* pvn, const double* pwn,
