@@ -32,32 +32,110 @@
 #include <vector>
 
 #include "../../include/nl2d_gpu.h"
+#include "nl2d_exact.cuh"  // bits, from_bits
 
+// On GB300 the FP64 pipe issues about 2 thread-operations per clock per SM,
+// ~30x fewer than the integer pipe, and this iteration is FP64-bound.  The
+// helpers below return the same bits as the IEEE expressions of the
+// reference (named in each comment) for every input, with fewer FP64
+// instructions.  Operands the integer forms do not cover (non-finite values,
+// subnormal halves, overflowing doubles) take the IEEE expression itself in
+// a separate, non-inlined function: as a real branch it costs nothing when
+// not taken, whereas inlined, the compiler may predicate it and issue its
+// FP64 instructions for every operand.
 namespace {
 
+using nl2d::bits;
+using nl2d::from_bits;
+
+constexpr long long kMag = 0x7fffffffffffffffLL;
+constexpr long long kSign = (long long)0x8000000000000000ULL;
+__device__ __forceinline__ bool finite(long long b) { return ((b >> 52) & 0x7ff) != 0x7ff; }
+
 __device__ __forceinline__ double max2(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double min3(double a, double b, double c) {
-  const double m = a < b ? a : b;
-  return m < c ? m : c;
-}
-// (a + b) (0.25 + SIGN(0.25, a b))
-__device__ __forceinline__ double slope_raw(double a, double b) {
+
+__device__ __noinline__ double half_ieee(double x) { return 0.5 * x; }
+__device__ __noinline__ double pick_ieee(double a, double z) { return a + 0.0 * z; }
+__device__ __noinline__ long long twice_abs_ieee(double x) { return bits(2.0 * fabs(x)); }
+__device__ __noinline__ double slope_ieee(double a, double b) {
   return (a + b) * (0.25 + copysign(0.25, a * b));
 }
-// SIGN(1, s) MIN(|s|, 2 |p|, 2 |q|)
-__device__ __forceinline__ double limit(double s, double p, double q) {
-  return copysign(1.0, s) * min3(fabs(s), 2.0 * fabs(p), 2.0 * fabs(q));
+__device__ __noinline__ double limit_ieee(double s, double p, double q) {
+  const double a = fabs(s), b = 2.0 * fabs(p), c = 2.0 * fabs(q);
+  const double m = a < b ? a : b;
+  return copysign(1.0, s) * (m < c ? m : c);
 }
+
+// 0.5 x: the exponent minus one for a normal x (biased exponent >= 2); a
+// zero keeps its bits.
+__device__ __forceinline__ double half(double x) {
+  const long long b = bits(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex >= 2 && ex <= 2046) return from_bits(b - (1LL << 52));
+  if ((b & kMag) == 0) return x;
+  return half_ieee(x);
+}
+
+// a + (+0) z: a itself unless a is a zero, then a zero whose sign is the AND
+// of the two signs (z finite).
+__device__ __forceinline__ double pick(double a, double z) {
+  const long long ab = bits(a), zb = bits(z);
+  if (!finite(zb)) return pick_ieee(a, z);
+  if ((ab & kMag) != 0) return a;
+  return from_bits(ab & (zb | kMag));
+}
+
+// 2 |x| for finite x: one more in the exponent of a normal value, the
+// magnitude shifted left for a subnormal one (the encoding is continuous
+// across the boundary); the largest binade (2 |x| overflows) multiplies.
+__device__ __forceinline__ long long twice_abs_bits(double x) {
+  const long long m = bits(x) & kMag;
+  const int ex = (int)(m >> 52);
+  if (ex == 0) return m << 1;
+  if (ex <= 2045) return m + (1LL << 52);
+  return twice_abs_ieee(x);
+}
+
+// (a + b) (0.25 + SIGN(0.25, a b)) (tra_adv.F90:138-141, :210-211).  For
+// finite a, b the product's sign is the XOR of theirs (also when it
+// underflows or overflows), so the second factor is 0.5 or +0: the result
+// is half(a + b), or a zero with the sign of a + b (if a + b is finite).
+__device__ __forceinline__ double slope_raw(double a, double b) {
+  const long long ab = bits(a), bb = bits(b);
+  if (!finite(ab) || !finite(bb)) return slope_ieee(a, b);
+  const double s = a + b;
+  const long long sb = bits(s);
+  if (!finite(sb)) return slope_ieee(a, b);
+  if ((ab ^ bb) < 0) return from_bits(sb & kSign);  // factor 0.25 + (-0.25) = +0
+  return half(s);
+}
+
+// SIGN(1, s) MIN(|s|, 2 |p|, 2 |q|) (tra_adv.F90:150-155, :214-216).  The
+// three candidates are non-negative, so their order is the order of their
+// bit patterns; multiplying the minimum by +-1 only sets its sign.
+__device__ __forceinline__ double limit(double s, double p, double q) {
+  const long long sb = bits(s), pb = bits(p), qb = bits(q);
+  if (!finite(sb) || !finite(pb) || !finite(qb)) return limit_ieee(s, p, q);
+  const long long a = sb & kMag, b = twice_abs_bits(p), c = twice_abs_bits(q);
+  const long long m = a < b ? a : b;
+  return from_bits((m < c ? m : c) | (sb & kSign));
+}
+
+// zu = SIGN(0.5, v) - 0.5 v 1 (tra_adv.F90:165, :173, :231).
+__device__ __forceinline__ double courant(double z0, double v) { return z0 - half(v); }
+
 // The upstream flux of tra_adv.F90:163-169 (x) / :171-177 (y): vel at the
 // face, the field on the far (f1) and near (f0) side, their slopes.
+// zalpha = 0.5 - SIGN(0.5, vel) is exactly 1 or +0, so
+// zalpha zzwx + (1 - zalpha) zzwy is one operand plus a zero-weighted
+// partner: pick().
 __device__ __forceinline__ double upstream(double vel, double f1, double f0, double zind,
                                            double s1, double s0) {
   const double z0 = copysign(0.5, vel);
-  const double zalpha = 0.5 - z0;
-  const double zu = z0 - 0.5 * vel * 1.0;
+  const double zu = courant(z0, vel);
   const double zzwx = f1 + zind * (zu * s1);
   const double zzwy = f0 + zind * (zu * s0);
-  return vel * (zalpha * zzwx + (1.0 - zalpha) * zzwy);
+  return vel * ((bits(vel) < 0) ? pick(zzwx, zzwy) : pick(zzwy, zzwx));
 }
 
 struct TraDev {
@@ -206,12 +284,12 @@ __global__ void __launch_bounds__(256) k_tra_vertical(double* __restrict__ m, Tr
     const double slk1 = (k + 1 <= K - 2) ? limit(slope_raw(zd1, zd2), zd2, zd1) : 0.0;
     const double p1 = d.pwn[c + s];
     const double z0w = copysign(0.5, p1);
-    const double zalpha = 0.5 + z0w;
-    const double zw = z0w - 0.5 * p1 * 1.0 * 1.0;
+    const double zw = courant(z0w, p1);
     const double zind = d.zind[c];
     const double zzwx = mk1 + zind * (zw * slk1);
     const double zzwy = mk + zind * (zw * slk);
-    const double fwk1 = p1 * (zalpha * zzwx + (1. - zalpha) * zzwy);
+    // zalpha = 0.5 + SIGN(0.5, pwn): 1 for pwn >= +0, else +0
+    const double fwk1 = p1 * ((bits(p1) < 0) ? pick(zzwy, zzwx) : pick(zzwx, zzwy));
     m[c] = -(1.0 * (fwk - fwk1));
     mk = mk1;
     mk1 = mk2;

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import tra_adv_numpy as TN
-from test_tra_oracle import oracle_run, random_inputs, tra_lib, zero_work
+from test_tra_oracle import oracle_run, quantized_inputs, random_inputs, tra_lib, zero_work
 
 pytestmark = pytest.mark.gpu
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -46,15 +46,18 @@ def oracle_field(f, niter):
     ((33, 17, 7), "random", 6),
     ((130, 70, 9), "random", 4),     # several blocks in i and j
     ((9, 8, 2), "random", 3),        # a single active level
+    ((47, 35, 6), "quantized", 5),   # signed zeros, zero differences, limiter ties
 ])
 def test_gpu_iteration_is_bit_identical(gpulib, oracle, dims, kind, niter):
     I, J, K = dims
-    f = TN.init(I, J, K) if kind == "benchmark" else random_inputs(I, J, K, seed=I + J + K)
+    f = {"benchmark": lambda: TN.init(I, J, K),
+         "random": lambda: random_inputs(I, J, K, seed=I + J + K),
+         "quantized": lambda: quantized_inputs(I, J, K, seed=I + J + K)}[kind]()
     want = oracle_field(f, niter)
     before = f["mydomain"].copy()
     gpu_compute(gpulib, f, niter)
     got = gpu_field(gpulib, want.shape)
-    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got.view(np.int64), want.view(np.int64))  # every bit
     # the host array stays as it was until the caller reads the result back
     np.testing.assert_array_equal(f["mydomain"], before)
     s = ctypes.c_double(0.0)
