@@ -35,12 +35,19 @@ namespace nl2d {
 
 __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
+// The IEEE expressions the helpers fall back to, kept out of line: inlined,
+// the compiler may predicate them and issue their FP64 instructions on every
+// call, taken or not; as calls behind a branch they cost nothing when not
+// taken.
+static __device__ __noinline__ double div_ieee(double x, double d) { return x / d; }
+static __device__ __noinline__ double half_ieee(double x) { return 0.5 * x; }
+static __device__ __noinline__ double pick_ieee(double a, double z) { return a + 0.0 * z; }
 
 __device__ __forceinline__ double div_rn(double x, double d, double r) {
   const int hi = __double2hiint(x);
   const int ex = (hi >> 20) & 0x7ff;
   const bool zero = ((hi & 0x7fffffff) | __double2loint(x)) == 0;
-  if (!zero && (ex < 124 || ex > 1922)) return x / d;
+  if (!zero && (ex < 124 || ex > 1922)) return div_ieee(x, d);
   const double q0 = x * r;
   const double e0 = fma(q0, d, -x);
   const double q1 = fma(-e0, r, q0);
@@ -53,13 +60,13 @@ __device__ __forceinline__ double half(double x) {
   const int ex = (int)((b >> 52) & 0x7ff);
   if (ex >= 2 && ex <= 2046) return from_bits(b - (1LL << 52));
   if ((b & 0x7fffffffffffffffLL) == 0) return x;
-  return 0.5 * x;
+  return half_ieee(x);
 }
 
 // a + (+0 * z): the operand with weight 1 plus the zero-weighted partner.
 __device__ __forceinline__ double pick(double a, double z) {
   const long long ab = bits(a), zb = bits(z);
-  if (((zb >> 52) & 0x7ff) == 0x7ff) return a + 0.0 * z;
+  if (((zb >> 52) & 0x7ff) == 0x7ff) return pick_ieee(a, z);
   if ((ab & 0x7fffffffffffffffLL) != 0) return a;
   return from_bits(ab & (zb | 0x7fffffffffffffffLL));
 }

@@ -32,7 +32,7 @@
 #include <vector>
 
 #include "../../include/nl2d_gpu.h"
-#include "nl2d_exact.cuh"  // bits, from_bits
+#include "nl2d_exact.cuh"  // bits, from_bits, half, pick
 
 // On GB300 the FP64 pipe issues about 2 thread-operations per clock per SM,
 // ~30x fewer than the integer pipe, and this iteration is FP64-bound.  The
@@ -47,6 +47,8 @@ namespace {
 
 using nl2d::bits;
 using nl2d::from_bits;
+using nl2d::half;  // 0.5 x, exact in integer arithmetic for normal x
+using nl2d::pick;  // a + (+0) z: the operand, or a zero with the AND of both signs
 
 constexpr long long kMag = 0x7fffffffffffffffLL;
 constexpr long long kSign = (long long)0x8000000000000000ULL;
@@ -54,8 +56,6 @@ __device__ __forceinline__ bool finite(long long b) { return ((b >> 52) & 0x7ff)
 
 __device__ __forceinline__ double max2(double a, double b) { return a > b ? a : b; }
 
-__device__ __noinline__ double half_ieee(double x) { return 0.5 * x; }
-__device__ __noinline__ double pick_ieee(double a, double z) { return a + 0.0 * z; }
 __device__ __noinline__ long long twice_abs_ieee(double x) { return bits(2.0 * fabs(x)); }
 __device__ __noinline__ double slope_ieee(double a, double b) {
   return (a + b) * (0.25 + copysign(0.25, a * b));
@@ -64,25 +64,6 @@ __device__ __noinline__ double limit_ieee(double s, double p, double q) {
   const double a = fabs(s), b = 2.0 * fabs(p), c = 2.0 * fabs(q);
   const double m = a < b ? a : b;
   return copysign(1.0, s) * (m < c ? m : c);
-}
-
-// 0.5 x: the exponent minus one for a normal x (biased exponent >= 2); a
-// zero keeps its bits.
-__device__ __forceinline__ double half(double x) {
-  const long long b = bits(x);
-  const int ex = (int)((b >> 52) & 0x7ff);
-  if (ex >= 2 && ex <= 2046) return from_bits(b - (1LL << 52));
-  if ((b & kMag) == 0) return x;
-  return half_ieee(x);
-}
-
-// a + (+0) z: a itself unless a is a zero, then a zero whose sign is the AND
-// of the two signs (z finite).
-__device__ __forceinline__ double pick(double a, double z) {
-  const long long ab = bits(a), zb = bits(z);
-  if (!finite(zb)) return pick_ieee(a, z);
-  if ((ab & kMag) != 0) return a;
-  return from_bits(ab & (zb | kMag));
 }
 
 // 2 |x| for finite x: one more in the exponent of a normal value, the
