@@ -73,9 +73,12 @@ struct Ctx {
 
 // (0.5 - copysign(0.5, w)) * p and (0.5 + copysign(0.5, w)) * p alone (the
 // masked upwind forms): p, or +0 * p.
+// (the IEEE form for a non-finite p is out of line, as for the helpers of
+// nl2d_exact.cuh, so that it is not issued on every call)
+static __device__ __noinline__ double zero_times_ieee(double p) { return 0.0 * p; }
 __device__ __forceinline__ double zero_times(double p) {
   const long long b = bits(p);
-  if (((b >> 52) & 0x7ff) == 0x7ff) return 0.0 * p;
+  if (((b >> 52) & 0x7ff) == 0x7ff) return zero_times_ieee(p);
   return from_bits(b & (long long)0x8000000000000000ULL);
 }
 __device__ __forceinline__ double lo_only(double w, double p) {
