@@ -304,6 +304,12 @@ int nl2d_ens_import_interior(const float *d_in);
 int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
                         long long *out);
 
+/* Test hook (no reference counterpart): counts, over n sampled operand
+ * pairs, where the exact IEEE add and multiply done on the integer pipes
+ * (nl2d_exact.cuh: dadd_i, dmul_i) differ from the FP64 instructions;
+ * out[2] = the two counts.  Returns 0, or 1 on a CUDA error. */
+int nl2d_selftest_intfp(long long n, unsigned long long seed, long long *out);
+
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
 

@@ -53,6 +53,8 @@ EXPORTS = {
     "nl2d_selftest_exact": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong,
                                             ctypes.c_double,
                                             ctypes.POINTER(ctypes.c_longlong)]),
+    "nl2d_selftest_intfp": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong,
+                                            ctypes.POINTER(ctypes.c_longlong)]),
     "nl2d_ens_create": (ctypes.c_int, [ctypes.c_int, _IP, _DP, _DP, _DP]),
     "nl2d_ens_set_domain": (ctypes.c_int, [ctypes.c_int, _IP, _DP, _DP, _DP]),
     "nl2d_ens_schedule": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double]),

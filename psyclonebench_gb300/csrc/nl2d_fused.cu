@@ -27,6 +27,7 @@
 // Built with -fmad=false, as the reference oracle is with
 // -ffp-contract=off: results are bit-identical to the reference serial build.
 #include "nl2d_fused_tile.cuh"
+#include "nl2d_intfp.cuh"
 
 namespace nl2d {
 namespace {
@@ -123,8 +124,74 @@ __global__ void k_selftest_exact(long long n, unsigned long long seed, double d,
   if (nu) atomicAdd(&bad[2], nu);
 }
 
+// Pairs for the integer add / multiply: generic samples (zeros, subnormals,
+// infinities and NaNs included), operands a few binades apart with either
+// sign (alignment shifts of 0..70 bits), near-cancelling pairs (the partner
+// is -a with its low significand bits changed), and products near the
+// bottom and top of the normal range.
+__device__ void intfp_pair(unsigned long long z, double& a, double& b) {
+  a = sample(z);
+  const unsigned long long w = mix64(z + 7);
+  const unsigned mode = (unsigned)(w >> 61);  // 0..7
+  if (mode <= 2) {
+    b = sample(mix64(z + 3));
+    return;
+  }
+  const long long ab = bits(a);
+  const int ea = (int)((ab >> 52) & 0x7ff);
+  long long bb = (long long)(mix64(z + 5) & 0x800fffffffffffffULL);
+  if (mode <= 4) {  // exponent within +-70 of a's
+    int eb = ea + (int)((w >> 20) % 141) - 70;
+    eb = eb < 1 ? 1 : (eb > 2046 ? 2046 : eb);
+    b = from_bits(bb | ((long long)eb << 52));
+  } else if (mode == 5) {  // -a with the low 1..52 significand bits replaced
+    const int k = 1 + (int)((w >> 20) % 52);
+    const long long m = (1LL << k) - 1;
+    b = from_bits(((ab ^ (long long)0x8000000000000000ULL) & ~m) | (bb & m));
+  } else {  // a product near an edge of the normal range
+    const int target = (mode == 6) ? (int)((w >> 20) % 60) - 5 : 2046 - (int)((w >> 20) % 60);
+    int eb = target - ea + 1023;
+    eb = eb < 1 ? 1 : (eb > 2046 ? 2046 : eb);
+    b = from_bits(bb | ((long long)eb << 52));
+  }
+}
+
+__global__ void k_selftest_intfp(long long n, unsigned long long seed,
+                                 unsigned long long* bad) {
+  unsigned long long na = 0, nm = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    double a, b;
+    intfp_pair(mix64(seed ^ (unsigned long long)t), a, b);
+    const double s_ref = a + b, s = dadd_i(a, b);
+    if (bits(s_ref) != bits(s) && !(s_ref != s_ref && s != s)) na++;
+    const double p_ref = a * b, p = dmul_i(a, b);
+    if (bits(p_ref) != bits(p) && !(p_ref != p_ref && p != p)) nm++;
+  }
+  if (na) atomicAdd(&bad[0], na);
+  if (nm) atomicAdd(&bad[1], nm);
+}
+
 }  // namespace
 }  // namespace nl2d
+
+// Test hook (no reference counterpart): counts, over n sampled operand
+// pairs, where the integer-pipe add and multiply (dadd_i, dmul_i) differ
+// from the FP64 instructions; out[2] receives the two counts.
+extern "C" int nl2d_selftest_intfp(long long n, unsigned long long seed, long long* out) {
+  unsigned long long* bad = nullptr;
+  if (!out || n < 0) return 2;
+  if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  nl2d::k_selftest_intfp<<<152 * 16, 256>>>(n, seed, bad);
+  unsigned long long h[2] = {0, 0};
+  const cudaError_t e = cudaMemcpy(h, bad, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return 1;
+  out[0] = (long long)h[0];
+  out[1] = (long long)h[1];
+  return 0;
+}
 
 // Test hook (no reference counterpart): counts, over n sampled doubles x,
 // the inputs where the exact helpers of the fused step differ from the IEEE

@@ -190,3 +190,16 @@ def test_exact_helpers_match_ieee(gpulib, d):
     out = (ctypes.c_longlong * 3)()
     assert gpulib.nl2d_selftest_exact(1 << 24, 12345, d, out) == 0
     assert list(out) == [0, 0, 0], list(out)
+
+
+@pytest.mark.parametrize("seed", [1, 0xC0FFEE])
+def test_integer_pipe_add_and_multiply_match_ieee(gpulib, seed):
+    """dadd_i / dmul_i (exact IEEE add and multiply done on the integer
+    pipes) give the FP64 instructions' bits on 2^27 sampled pairs:
+    alignment shifts of 0..70 bits with either sign, near cancellations,
+    products at both ends of the normal range, zeros, subnormals,
+    infinities and NaNs."""
+    import ctypes
+    out = (ctypes.c_longlong * 2)()
+    assert gpulib.nl2d_selftest_intfp(1 << 27, seed, out) == 0
+    assert list(out) == [0, 0], list(out)
