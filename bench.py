@@ -16,7 +16,8 @@ ours:
          129 MB), and the per-step working set is ~1.3 GB, so no flush is
          needed.
   e2e    the same K steps through the reference-facing C-ABI from HOST
-         buffers: c_invoke_time_step per step (the first call uploads all 25
+         buffers (initialised by writing them, as the reference's driver
+         does): c_invoke_time_step per step (the first call uploads all 25
          arrays), then c_read_from_device of sshn_t, un and vn; host wall
          clock around all of it.
   roofline  HBM: 76 algorithmic bytes per interior cell-step (read sshn_t,
@@ -76,13 +77,22 @@ def dist_env():
     return rank, world, local
 
 
-def make_problem(n):
+def make_problem(n, written=False):
     """The reference's initial state for an n x n interior (jpiglo = n + 2),
-    rows padded to a multiple of 8 doubles."""
+    rows padded to a multiple of 8 doubles.  written: every array written
+    once more, as the reference's driver writes them during set-up
+    (initialisation_mod.f90, the grid and field constructors); numpy's
+    zero-filled arrays are otherwise untouched pages, which the first
+    host-to-device copy must fault in (0.42 s instead of 0.14 s of upload at
+    4096^2): a cost of the test harness, not of a caller."""
     import nl2d_testlib as T
     jp = n + 2
     width = ((jp + 1 + 7) // 8) * 8
-    return T.make_model(jp, jp, 1, width=width)
+    m = T.make_model(jp, jp, 1, width=width)
+    if written:
+        for a in list(m.f.values()) + list(m.grid.values()):
+            a[...] = a.copy()
+    return m
 
 
 def peaks():
@@ -530,7 +540,7 @@ def run_ours(args, rank, world, local):
     # ---- e2e: host buffers through c_invoke_time_step ----
     e2e = None
     if not args.no_e2e:
-        m2 = make_problem(n)
+        m2 = make_problem(n, written=True)
         nbytes_in = sum(a.nbytes for a in m2.f.values()) + sum(a.nbytes for a in m2.grid.values())
         nbytes_out = 3 * m2.f["sshn_t"].nbytes
         torch.cuda.synchronize()

@@ -5,10 +5,15 @@
 #include "nl2d_internal.h"
 #include "../../include/nl2d_gpu.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <memory>
+#include <thread>
 #include <vector>
 
 namespace nl2d {
@@ -127,43 +132,77 @@ Dims dims() {
   return Dims{r.xs, r.xe, r.ys, r.ye, r.width, r.height};
 }
 
-// sin(gphi * d2r) per point with the host libm, reusing the last value for
-// runs of equal latitudes (a uniform grid costs one call).
-void host_sines(const double* gphi, size_t n, double d2r, std::vector<double>& out) {
-  out.resize(n);
-  double last_in = NAN, last_out = 0.0;
-  for (size_t k = 0; k < n; k++) {
-    if (!(gphi[k] == last_in) || std::signbit(gphi[k]) != std::signbit(last_in)) {
-      last_in = gphi[k];
-      last_out = std::sin(gphi[k] * d2r);
-    }
-    out[k] = last_out;
+// Registration scans whole grids (16.8 M points at 4096^2) several times;
+// split over the host's cores they take milliseconds instead of a third of
+// a second.  f(lo, hi) runs on contiguous chunks of [begin, end).
+template <class F>
+void parallel_chunks(long long begin, long long end, F f) {
+  const long long n = end - begin;
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  if (nt > 32) nt = 32;
+  if (n < (1LL << 16) || nt == 1) {
+    f(begin, end);
+    return;
   }
+  std::vector<std::thread> th;
+  const long long chunk = (n + nt - 1) / nt;
+  for (unsigned t = 0; t < nt; t++) {
+    const long long lo = begin + (long long)t * chunk;
+    const long long hi = std::min(end, lo + chunk);
+    if (lo >= hi) break;
+    th.emplace_back(f, lo, hi);
+  }
+  for (std::thread& x : th) x.join();
+}
+
+// sin(gphi * d2r) per point with the host libm, reusing the last value for
+// runs of equal latitudes (a uniform grid costs one call per chunk).
+void host_sines(const double* gphi, size_t n, double d2r, double* out) {
+  parallel_chunks(0, (long long)n, [=](long long lo, long long hi) {
+    double last_in = NAN, last_out = 0.0;
+    for (long long k = lo; k < hi; k++) {
+      if (!(gphi[k] == last_in) || std::signbit(gphi[k]) != std::signbit(last_in)) {
+        last_in = gphi[k];
+        last_out = std::sin(gphi[k] * d2r);
+      }
+      out[k] = last_out;
+    }
+  });
 }
 
 bool upload_sines(double d2r) {
   State& s = g_state;
   const size_t n = (size_t)s.reg.width * s.reg.height;
-  std::vector<double> su, sv;
-  host_sines((const double*)s.reg.host[kNumFields + 10], n, d2r, su);
-  host_sines((const double*)s.reg.host[kNumFields + 11], n, d2r, sv);
-  if (!CK(cudaMemcpy(s.dev.sin_u, su.data(), n * 8, cudaMemcpyHostToDevice))) return false;
-  if (!CK(cudaMemcpy(s.dev.sin_v, sv.data(), n * 8, cudaMemcpyHostToDevice))) return false;
+  std::unique_ptr<double[]> su(new double[n]), sv(new double[n]);
+  host_sines((const double*)s.reg.host[kNumFields + 10], n, d2r, su.get());
+  host_sines((const double*)s.reg.host[kNumFields + 11], n, d2r, sv.get());
+  if (!CK(cudaMemcpy(s.dev.sin_u, su.get(), n * 8, cudaMemcpyHostToDevice))) return false;
+  if (!CK(cudaMemcpy(s.dev.sin_v, sv.get(), n * 8, cudaMemcpyHostToDevice))) return false;
   s.sin_d2r = d2r;
   // Uniform-metric check over every point a step reads them at.
   const Registration& r = s.reg;
-  bool uniform = true;
   const int W = r.width;
   auto uniform_over = [&](const double* a, double& v) {
     v = a[(size_t)(r.ys - 1) * W + (r.xs - 1)];
-    for (int j = r.ys - 1; j <= r.ye + 1; j++)
-      for (int i = r.xs - 1; i <= r.xe + 1; i++) {
-        const double x = a[(size_t)j * W + i];
-        if (memcmp(&x, &v, 8) != 0) return false;
+    uint64_t ref;
+    memcpy(&ref, &v, 8);
+    std::atomic<bool> ok{true};
+    parallel_chunks(r.ys - 1, r.ye + 2, [&, ref](long long j0, long long j1) {
+      for (long long j = j0; j < j1 && ok.load(std::memory_order_relaxed); j++) {
+        const uint64_t* row = reinterpret_cast<const uint64_t*>(a + (size_t)j * W);
+        uint64_t diff = 0;  // bitwise equality, branch-free along the row
+        for (int i = r.xs - 1; i <= r.xe + 1; i++) diff |= row[i] ^ ref;
+        if (diff) {
+          ok.store(false, std::memory_order_relaxed);
+          return;
+        }
       }
-    return true;
+    });
+    return ok.load();
   };
   const double** h = (const double**)(r.host + kNumFields);
+  bool uniform = true;
   uniform &= uniform_over(h[1], s.um.area_t);
   uniform &= uniform_over(h[2], s.um.area_u);
   uniform &= uniform_over(h[3], s.um.area_v);
@@ -173,34 +212,47 @@ bool upload_sines(double d2r) {
   uniform &= uniform_over(h[7], s.um.dy_u);
   uniform &= uniform_over(h[8], s.um.dy_v);
   uniform &= uniform_over(h[9], s.um.dy_t);
-  uniform &= uniform_over(su.data(), s.um.sin_u);
-  uniform &= uniform_over(sv.data(), s.um.sin_v);
+  uniform &= uniform_over(su.get(), s.um.sin_u);
+  uniform &= uniform_over(sv.get(), s.um.sin_v);
   // Flather chains (a Flather face reading another Flather face) and reads
   // that would leave the array make the one-launch update differ from the
   // reference's serial Flather loops.
   const int* m = (const int*)r.host[kNumFields];
-  auto writes = [&](int c, int step) {
+  auto writes = [m](int c, int step) {
     return m[c] + m[c + step] > -1 && (m[c] < 0 || m[c + step] < 0);
   };
-  s.chain_u = s.chain_v = false;
-  bool inside = true;
-  for (int j = r.ys - 1; j <= r.ye + 1; j++)
-    for (int i = r.xs - 1; i <= r.xe; i++) {
-      const int c = j * W + i;
-      if (!writes(c, 1)) continue;
-      const int nb = m[c] < 0 ? i + 1 : i - 1;
-      if (nb < 0) { inside = false; continue; }
-      if (nb >= r.xs - 1 && nb <= r.xe && writes(j * W + nb, 1)) s.chain_u = true;
-    }
-  for (int j = r.ys - 1; j <= r.ye; j++)
-    for (int i = r.xs - 1; i <= r.xe + 1; i++) {
-      const int c = j * W + i;
-      if (!writes(c, W)) continue;
-      const int nb = m[c] < 0 ? j + 1 : j - 1;
-      if (nb < 0) { inside = false; continue; }
-      if (nb >= r.ys - 1 && nb <= r.ye && writes(nb * W + i, W)) s.chain_v = true;
-    }
-  s.fused_ok = uniform && inside && !s.chain_u && !s.chain_v;
+  std::atomic<bool> chain_u{false}, chain_v{false}, outside{false};
+  parallel_chunks(r.ys - 1, r.ye + 2, [&](long long j0, long long j1) {
+    for (long long j = j0; j < j1; j++)
+      for (int i = r.xs - 1; i <= r.xe; i++) {
+        const int c = (int)j * W + i;
+        if (!writes(c, 1)) continue;
+        const int nb = m[c] < 0 ? i + 1 : i - 1;
+        if (nb < 0) {
+          outside.store(true, std::memory_order_relaxed);
+          continue;
+        }
+        if (nb >= r.xs - 1 && nb <= r.xe && writes((int)j * W + nb, 1))
+          chain_u.store(true, std::memory_order_relaxed);
+      }
+  });
+  parallel_chunks(r.ys - 1, r.ye + 1, [&](long long j0, long long j1) {
+    for (long long j = j0; j < j1; j++)
+      for (int i = r.xs - 1; i <= r.xe + 1; i++) {
+        const int c = (int)j * W + i;
+        if (!writes(c, W)) continue;
+        const int nb = m[c] < 0 ? (int)j + 1 : (int)j - 1;
+        if (nb < 0) {
+          outside.store(true, std::memory_order_relaxed);
+          continue;
+        }
+        if (nb >= r.ys - 1 && nb <= r.ye && writes(nb * W + i, W))
+          chain_v.store(true, std::memory_order_relaxed);
+      }
+  });
+  s.chain_u = chain_u.load();
+  s.chain_v = chain_v.load();
+  s.fused_ok = uniform && !outside.load() && !s.chain_u && !s.chain_v;
   return true;
 }
 
