@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=NPTS, help="interior cells per side")
+    ap.add_argument("--state", default="rest", choices=["rest", "active"],
+                    help="rest: the reference's start (default); active: every cell in "
+                         "motion on a Fourier bathymetry (rdt 5 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
@@ -92,6 +95,22 @@ def make_problem(n, written=False):
     if written:
         for a in list(m.f.values()) + list(m.grid.values()):
             a[...] = a.copy()
+    return m
+
+
+def make_active(m, seed=3):
+    """Puts every cell of m in motion: the seeded Fourier bathymetry
+    (50-500 m, rdt 5 s) and a random start, sea-surface height within
+    +-0.1 m and velocities within +-0.05 m/s everywhere.  From rest the tide
+    enters through the open south row only, so within a few hundred steps
+    most cells still hold zeros; here (almost) no operand is zero."""
+    from psyclonebench_gb300.workloads import fourier_depth
+    ht, hu, hv = fourier_depth(m.width, m.height, seed)
+    m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = ht, hu, hv
+    rng = np.random.default_rng(seed)
+    for k, a in (("sshn_t", 0.1), ("un", 0.05), ("vn", 0.05)):
+        m.f[k][:] = rng.uniform(-a, a, size=m.f[k].shape)
+    m.rdt = BATHY_RDT
     return m
 
 
@@ -255,6 +274,27 @@ def run_forms(lib, n, steps=1000, warmup=3):
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm, "alg_bytes_per_cell": MIXED_BYTES_PER_CELL},
         "error_vs_fp64": err, "dtype": "f32 + compensated-f32 ssh"}}
+
+
+def run_active(lib, n, rest_value, steps=200, warmup=5):
+    """The FP64 step with every cell in motion (make_active): the same
+    kernel and timing as the headline number, on a state where the exact
+    division's zero-dividend shortcut (almost) never applies."""
+    import nl2d_testlib as T
+    import psyclonebench_gb300 as P
+    m = make_active(make_problem(n))
+    T.gpu_register(lib, m)
+    ms = ctypes.c_double(0.0)
+    P.check(lib.nl2d_timed_run(1, warmup, ctypes.byref(ms)), "active warm-up")
+    P.check(lib.nl2d_timed_run(1 + warmup, steps, ctypes.byref(ms)), "active run")
+    sums = np.zeros(3)
+    P.check(lib.nl2d_checksums(T.dptr(sums)), "active checksums")
+    lib.nl2d_finalize()
+    value = n * n * steps / (ms.value * 1e-3) / 1e6
+    return {"workload": "nemolite2d_fp64_%dx%d_active_fourier_bathymetry_seed3_rdt5" % (n, n),
+            "value": value, "unit": "Mcell-steps/s", "ms_per_step": ms.value / steps,
+            "steps": steps, "warmup": warmup, "ratio_to_rest_start": value / rest_value,
+            "checksums": {"ssh": sums[0], "u": sums[1], "v": sums[2]}, "dtype": "f64"}
 
 
 def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
@@ -515,7 +555,10 @@ def run_ours(args, rank, world, local):
     cells = n * n
 
     # ---- value: resident state, one graph launch of K fused steps ----
+    active = args.state == "active"
     m = make_problem(n)
+    if active:
+        make_active(m)
     T.gpu_register(lib, m)
     ms = ctypes.c_double(0.0)
     P.check(lib.nl2d_timed_run(1, 1 + args.warmup, ctypes.byref(ms)), "warm-up")
@@ -541,6 +584,8 @@ def run_ours(args, rank, world, local):
     e2e = None
     if not args.no_e2e:
         m2 = make_problem(n, written=True)
+        if active:
+            make_active(m2)
         nbytes_in = sum(a.nbytes for a in m2.f.values()) + sum(a.nbytes for a in m2.grid.values())
         nbytes_out = 3 * m2.f["sshn_t"].nbytes
         torch.cuda.synchronize()
@@ -560,21 +605,28 @@ def run_ours(args, rank, world, local):
 
     hbm, peak_kind = peaks()
     prof = load_profile_figures()
+    fig = prof.get("states", {}).get(args.state, {})
     achieved = ALG_BYTES_PER_CELL * cells / (ms_step * 1e-3) / 1e9
+    traffic = fig.get("dram_bytes_per_cell")
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_kind": peak_kind,
-            "traffic": prof.get("dram_bytes_per_launch"),
+            "traffic": traffic * cells if traffic else None,
             "kernel": "k_fused_step", "alg_bytes_per_cell": ALG_BYTES_PER_CELL}
-    if prof.get("fp64_ops_per_launch"):
+    if fig.get("fp64_ops_per_cell"):
+        # FP64 thread-instructions per cell from the ncu capture of the same
+        # start state (the count depends on it: zero dividends skip the
+        # division's FP64 work)
         roof["fp64"] = {
-            "achieved_gops": prof["fp64_ops_per_launch"] / (ms_step * 1e-3) / 1e9,
-            "ops_per_cell": prof["fp64_ops_per_launch"] / cells,
+            "achieved_gops": fig["fp64_ops_per_cell"] * cells / (ms_step * 1e-3) / 1e9,
+            "ops_per_cell": fig["fp64_ops_per_cell"],
             "peak_gops": prof.get("fp64_peak_gops"),
+            "profile": fig.get("source"),
         }
 
     forms = None
     if rank == 0 and not args.no_forms:
         forms = run_forms(lib, n)
+        forms["fp64_active"] = run_active(lib, n, value)
         ens = run_ensemble(lib)
         ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
         ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
@@ -600,9 +652,10 @@ def run_ours(args, rank, world, local):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (reference initial state: rest, constant depth)",
-            "config": {"workload": "nemolite2d_fp64_%dx%d" % (n, n), "interior": [n, n],
-                       "jphgr_msh": 1, "rdt": 20.0, "width": m.width,
+            "data": ("synthetic (every cell in motion: Fourier bathymetry, random start)"
+                     if active else "synthetic (reference initial state: rest, constant depth)"),
+            "config": {"workload": "nemolite2d_fp64_%dx%d%s" % (n, n, "_active" if active else ""),
+                       "interior": [n, n], "jphgr_msh": 1, "rdt": m.rdt, "width": m.width,
                        "l2": "inputs larger than L2 (135 MB per field)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,

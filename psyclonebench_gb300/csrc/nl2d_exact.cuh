@@ -7,18 +7,19 @@
 // instructions:
 //
 //  * div_rn(x, d, r): x / d rounded to nearest for a divisor d > 0 whose
-//    reciprocal r = RN(1/d) was computed beforehand (Markstein, "Computation
-//    of elementary functions on the IBM RISC System/6000 processor", IBM J.
-//    Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point
-//    Arithmetic, 2nd ed., Sec. 4.7): a quotient refined once with an exact
-//    FMA remainder is faithful, and a faithful quotient corrected with the
-//    exact remainder and the correctly rounded reciprocal is the correctly
-//    rounded quotient.  1 DMUL + 4 DFMA.  The remainder is formed as
-//    q*d - x and subtracted, which also returns the correctly signed zero
-//    for x = +-0.  Dividends whose magnitude is tiny (below 2^-899, other
-//    than zero), huge (2^900 and above) or not finite use the IEEE divide,
-//    so no intermediate underflows or overflows; divisors are checked on
-//    the host to lie in [2^-100, 2^100].
+//    reciprocal r = RN(1/d) was computed beforehand.  q0 = RN(x * r) is
+//    within 1.5 ulp of x / d; one exact FMA remainder e0 = q0 * d - x,
+//    compared as an integer with half an ulp of q0 times d, picks the
+//    correctly rounded quotient among q0 and its two neighbours.  1 DMUL +
+//    1 DFMA.  When q0 is a power of two (the spacing changes below it) the
+//    quotient takes Markstein's two refinements instead (Markstein,
+//    "Computation of elementary functions on the IBM RISC System/6000
+//    processor", IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of
+//    Floating-Point Arithmetic, 2nd ed., Sec. 4.7), 1 DMUL + 4 DFMA.
+//    x = +-0 returns x.  Dividends whose magnitude is tiny (below 2^-899,
+//    other than zero), huge (2^900 and above) or not finite use the IEEE
+//    divide, so no intermediate underflows or overflows; divisors are
+//    checked on the host to lie in [2^-100, 2^100].
 //  * half(x): 0.5 * x.  For normal x with a biased exponent >= 2 this is
 //    exact, i.e. the exponent minus one, done in integer arithmetic; zero
 //    keeps its bits; subnormal, smallest-normal and non-finite x use DMUL.
@@ -43,16 +44,37 @@ static __device__ __noinline__ double div_ieee(double x, double d) { return x / 
 static __device__ __noinline__ double half_ieee(double x) { return 0.5 * x; }
 static __device__ __noinline__ double pick_ieee(double a, double z) { return a + 0.0 * z; }
 
-__device__ __forceinline__ double div_rn(double x, double d, double r) {
-  const int hi = __double2hiint(x);
-  const int ex = (hi >> 20) & 0x7ff;
-  const bool zero = ((hi & 0x7fffffff) | __double2loint(x)) == 0;
-  if (!zero && (ex < 124 || ex > 1922)) return div_ieee(x, d);
+// Markstein's two refinements: a faithful quotient, then the correctly
+// rounded one.  Out of line: taken only when x * r lands on a power of two.
+static __device__ __noinline__ double div_markstein(double x, double d, double r) {
   const double q0 = x * r;
   const double e0 = fma(q0, d, -x);
   const double q1 = fma(-e0, r, q0);
   const double e1 = fma(q1, d, -x);
   return fma(-e1, r, q1);
+}
+
+__device__ __forceinline__ double div_rn(double x, double d, double r) {
+  const long long xb = bits(x);
+  if ((xb & 0x7fffffffffffffffLL) == 0) return x;  // +-0 / d keeps the sign for d > 0
+  const int ex = (int)((xb >> 52) & 0x7ff);
+  if (ex < 124 || ex > 1922) return div_ieee(x, d);
+  const double q0 = x * r;
+  const long long qb = bits(q0);
+  if ((qb & 0xfffffffffffffLL) == 0) return div_markstein(x, d, r);
+  // q0 is not a power of two, so q = x / d lies in q0's binade and within
+  // 1.5 ulp of it: RN(q) is q0 - ulp, q0 or q0 + ulp.  The remainder
+  // e0 = q0 * d - x = d * (q0 - q) is exact wherever it decides (|e0| <
+  // 2^53 units of its grid), and RN(q) moves off q0 exactly when |e0| >
+  // h = d * ulp(q0) / 2 (a quotient is never a midpoint).  h is d with
+  // its exponent shifted, compared as a bit pattern.
+  const double e0 = fma(q0, d, -x);
+  const long long eb = bits(e0);
+  const int eq = (int)((qb >> 52) & 0x7ff);
+  const long long hb = bits(d) + ((long long)(eq - 1076) << 52);
+  long long k = 0;  // +1: one ulp up in value, -1: one ulp down
+  if ((eb & 0x7fffffffffffffffLL) > hb) k = (eb < 0) ? 1 : -1;
+  return from_bits(qb + (qb < 0 ? -k : k));
 }
 
 __device__ __forceinline__ double half(double x) {

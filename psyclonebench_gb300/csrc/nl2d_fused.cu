@@ -112,6 +112,23 @@ __global__ void k_selftest_exact(long long n, unsigned long long seed, double d,
     // division: finite quotients must agree bit for bit
     const double q_ref = x / d, q = div_rn(x, d, r);
     if (bits(q_ref) != bits(q) && !(q_ref != q_ref && q != q)) nd++;
+    // Quotients within ~2^-53 ulp of a midpoint: RN((Q + ulp(Q)/2) * d) and
+    // its neighbours; quotients at and next to a power of two.
+    {
+      const unsigned long long y = mix64(z + 3);
+      const long long eq = (long long)((y >> 40) % 1201ULL) - 600;  // Q in [2^-600, 2^601)
+      long long qb = (long long)(y & 0x800fffffffffffffULL) | ((eq + 1023) << 52);
+      if ((y >> 38) & 1) qb &= (long long)0x8000000000000000ULL | (0x7ffLL << 52);  // +-2^eq
+      const double Q = from_bits(qb);
+      const double h = d * from_bits((eq - 53 + 1023) << 52);      // d * ulp(Q) / 2, exact
+      const double xm = fma(Q, d, qb < 0 ? -h : h);
+      const long long nudge = (long long)((y >> 32) & 7) - 3;
+      const double cand[3] = {xm, from_bits(bits(xm) + nudge), from_bits(bits(Q * d) + nudge)};
+      for (int c = 0; c < 3; c++) {
+        const double xr = cand[c] / d, xq = div_rn(cand[c], d, r);
+        if (bits(xr) != bits(xq)) nd++;
+      }
+    }
     const double h_ref = 0.5 * x, h = half(x);
     if (bits(h_ref) != bits(h) && !(h_ref != h_ref && h != h)) nh++;
     const double p = sample(mix64(z + 1)), w = sample(mix64(z + 2));

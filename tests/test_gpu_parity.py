@@ -106,6 +106,25 @@ def test_random_masks_and_bathymetry(gpulib, oracle):
         assert_fields_equal(got, want, "trial %d" % trial)
 
 
+def test_benchmark_size_bitwise(gpulib, oracle):
+    """The benchmark's 4096 x 4096 interior (4098 namelist, width padded to
+    4104 as the bench lays it out) with random depths and a random initial
+    state, 12 steps through c_invoke_time_step (the first on the reference
+    path, the rest fused): all 13 fields bit-identical to the oracle's
+    OpenMP build."""
+    rng = np.random.default_rng(5)
+    m = T.make_model(4098, 4098, 1, width=4104, oracle=oracle)
+    for k in ("ht", "hu", "hv"):
+        m.f[k][:] = rng.uniform(50.0, 500.0, size=m.f[k].shape)
+    for k, a in (("sshn_t", 0.1), ("un", 0.05), ("vn", 0.05)):
+        m.f[k][:] = rng.uniform(-a, a, size=m.f[k].shape)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step_omp, want, 12)
+    paths = T.gpu_run_calls(gpulib, m, 12, mode=0)
+    assert paths[0] == 1 and set(paths[1:]) == {2}, paths
+    assert_fields_equal(m, want, "4096^2")
+
+
 def test_chained_flather_mask_uses_reference_path(gpulib, oracle):
     """A one-cell-wide wet column between two open columns makes a Flather
     face read another Flather face; the library then keeps to the ordered

@@ -66,6 +66,25 @@ def test_gpu_iteration_is_bit_identical(gpulib, oracle, dims, kind, niter):
     gpulib.tra_adv_finalize()
 
 
+def test_benchmark_size_is_bit_identical(gpulib, oracle):
+    """The benchmark's own case, 512 x 512 x 75 from its initial values:
+    three iterations through tra_adv_compute and three through the timed
+    run, every bit of the field against the (OpenMP) oracle."""
+    I, J, K = 512, 512, 75
+    f = TN.init(I, J, K)
+    g = {n: v.copy() for n, v in f.items()}
+    oracle_run(tra_lib(), g, zero_work((K, J, I)), 6, omp=True)
+    gpu_compute(gpulib, f, 3)
+    ms = ctypes.c_double(0.0)
+    assert gpulib.tra_adv_run(3, ctypes.byref(ms)) == 0
+    got = gpu_field(gpulib, (K, J, I))
+    np.testing.assert_array_equal(got.view(np.int64), g["mydomain"].view(np.int64))
+    s = ctypes.c_double(0.0)
+    assert gpulib.tra_adv_checksum(ctypes.byref(s)) == 0
+    assert s.value == tra_lib().tra_oracle_checksum(I, J, K, _p(g["mydomain"]))
+    gpulib.tra_adv_finalize()
+
+
 def test_new_arrays_start_a_new_run_and_run_continues(gpulib, oracle):
     """Other arrays register afresh (work arrays zeroed again); the timed
     run continues the registered state."""
