@@ -66,6 +66,10 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the mixed-precision, ensemble and emulator measurements")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator (config 4)")
+    ap.add_argument("--forms", default="mixed,active,ensemble,tra_adv,emulator",
+                    help="comma-separated forms to measure after the headline number")
+    ap.add_argument("--form-steps", type=int, default=1000,
+                    help="timed steps of the mixed-precision form and its FP64 twin")
     ap.add_argument("--emu-iters", type=int, default=8000, help="emulator training iterations")
     ap.add_argument("--emu-domains", type=int, default=200, help="emulator training domains")
     ap.add_argument("--emu-horizon", type=int, default=5000,
@@ -89,9 +93,18 @@ def make_problem(n, written=False):
     host-to-device copy must fault in (0.42 s instead of 0.14 s of upload at
     4096^2): a cost of the test harness, not of a caller."""
     import nl2d_testlib as T
+    import psyclonebench_gb300 as P
     jp = n + 2
     width = ((jp + 1 + 7) // 8) * 8
-    m = T.make_model(jp, jp, 1, width=width)
+    m = T.Model(jp, jp, width=width)
+    # the library's own set-up (setup_tpoints_mask, grid metrics,
+    # initialisation), not the oracle's
+    DPP = ctypes.POINTER(ctypes.c_double)
+    fp = (DPP * 13)(*[T.dptr(m.f[k]) for k in T.FIELDS])
+    gp = (DPP * 11)(*[T.dptr(m.grid[k]) for k in T.GRID[1:]])
+    P.check(P.load_library().nl2d_setup_model(1, jp, jp, 1000.0, 1000.0, 100.0, m.width,
+                                              m.height, fp, T.iptr(m.grid["tmask"]), gp,
+                                              None, None), "nl2d_setup_model")
     if written:
         for a in list(m.f.values()) + list(m.grid.values()):
             a[...] = a.copy()
@@ -452,9 +465,8 @@ def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
     per point-iteration (read mydomain, pun, pvn, pwn, umask, vmask, tmask
     and the precomputed zind; write mydomain); cpu_baseline: the oracle's
     OpenMP port on all host cores for `cpu_iters` iterations."""
-    import tra_adv_numpy as TN
-    from test_tra_oracle import oracle_run, tra_lib, zero_work
-    f = TN.init(jpi, jpj, jpk)
+    from psyclonebench_gb300.workloads import tra_adv_fields
+    f = tra_adv_fields(jpi, jpj, jpk)
     D = ctypes.POINTER(ctypes.c_double)
 
     def p(a):
@@ -486,6 +498,7 @@ def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
     ach = 72.0 * points * iters / (ms.value * 1e-3) / 1e9
     in_bytes = sum(f[n].nbytes for n in f)
     # CPU: the oracle's OpenMP port on a bounded sample of the same workload
+    from test_tra_oracle import oracle_run, tra_lib, zero_work
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     lib_o = tra_lib()
     g = {n: v.copy() for n, v in f.items()}
@@ -624,15 +637,23 @@ def run_ours(args, rank, world, local):
         }
 
     forms = None
+    want = set(args.forms.split(","))
+    if "emulator" in want and args.no_emulator:
+        want.discard("emulator")
     if rank == 0 and not args.no_forms:
-        forms = run_forms(lib, n)
-        forms["fp64_active"] = run_active(lib, n, value)
-        ens = run_ensemble(lib)
-        ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
-        ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
-        forms["ensemble"] = ens
-        forms["tra_adv"] = run_tra_adv(lib)
-        if not args.no_emulator:
+        forms = {}
+        if "mixed" in want:
+            forms.update(run_forms(lib, n, steps=args.form_steps))
+        if "active" in want:
+            forms["fp64_active"] = run_active(lib, n, value)
+        if "ensemble" in want:
+            ens = run_ensemble(lib)
+            ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value
+            ens["mixed"]["speedup_vs_single_4096_domain_fp64"] = ens["mixed"]["value"] / value
+            forms["ensemble"] = ens
+        if "tra_adv" in want:
+            forms["tra_adv"] = run_tra_adv(lib)
+        if "emulator" in want:
             forms["emulator"] = run_emulator(lib, count=args.emu_domains,
                                              horizon=args.emu_horizon, iters=args.emu_iters)
 

@@ -52,6 +52,7 @@ struct State {
   // mixed-precision form
   int precision = 0;           // 0 FP64, 1 mixed
   MixedFields mix{};
+  int* mix_count = nullptr;    // device int for launch_mixed_flags
   float2* msn[2] = {};
   float* mun[2] = {};
   float* mvn[2] = {};
@@ -119,6 +120,10 @@ void free_device() {
     cudaFree(s.mix.hv);
     cudaFree(s.mix.rhu);
     cudaFree(s.mix.rhv);
+    cudaFree(s.mix.reg);
+    cudaFree(s.mix.glist);
+    cudaFree(s.mix_count);
+    s.mix_count = nullptr;
     s.mix = MixedFields{};
     s.mixed_valid = s.mixed_ahead = false;
   }
@@ -436,7 +441,9 @@ bool ensure_mixed() {
     }
     if (!CK(cudaMalloc(&s.mix.ht, n * 4)) || !CK(cudaMalloc(&s.mix.hu, n * 4)) ||
         !CK(cudaMalloc(&s.mix.hv, n * 4)) || !CK(cudaMalloc(&s.mix.rhu, n * 4)) ||
-        !CK(cudaMalloc(&s.mix.rhv, n * 4)))
+        !CK(cudaMalloc(&s.mix.rhv, n * 4)) || !CK(cudaMalloc(&s.mix.reg, n)) ||
+        !CK(cudaMalloc(&s.mix.glist, n * sizeof(int))) ||
+        !CK(cudaMalloc(&s.mix_count, sizeof(int))))
       return false;
     s.mixed_valid = false;
   }
@@ -451,6 +458,14 @@ bool ensure_mixed() {
     launch_to_mixed(s.dev.sshn_t, s.dev.un, s.dev.vn, s.dev, s.mix, ms, d, b == 0, s.stream);
   }
   if (!CK(cudaGetLastError())) return false;
+  // which cells the column march updates (the mask may have been rewritten)
+  const int ng = launch_mixed_flags(s.dev, d, s.mix, s.mix_count, s.stream);
+  if (ng < 0) {
+    CK(cudaGetLastError());
+    set_error(NL2D_ERR_CUDA, "mixed form: cell flags");
+    return false;
+  }
+  s.mix.gcount = ng;
   s.mcur = 0;
   s.mixed_valid = true;
   s.mixed_ahead = false;

@@ -81,6 +81,12 @@ void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
 struct MixedFields {  // static FP32 copies of the depths and the
   float *ht, *hu, *hv;  // reciprocal momentum denominators
   float *rhu, *rhv;
+  // Single domain only (the ensemble leaves them null): per-cell flags of
+  // the cells the column march updates, and the list of the copy region's
+  // other cells (glist[0 .. gcount)), from launch_mixed_flags.
+  unsigned char* reg;
+  int* glist;
+  int gcount;
 };
 struct MixedState {  // ssh as (hi, lo) float pairs; velocities FP32
   const float2* sn_in;
@@ -97,6 +103,12 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
 void launch_to_mixed(const double* sn, const double* un, const double* vn,
                      const Fields& f, const MixedFields& mf, const MixedState& ms,
                      const Dims& d, bool statics, cudaStream_t st);
+// The march flags and the general-cell list of mf (mf.reg and mf.glist
+// allocated for width x height cells); `count` is one device int.  Returns
+// the number of general cells (synchronises the stream), or -1 on a CUDA
+// error.
+int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, int* count,
+                       cudaStream_t st);
 void launch_from_mixed(const float2* sn2, const float* un_f, const float* vn_f,
                        double* sn, double* un, double* vn, const Dims& d,
                        cudaStream_t st);

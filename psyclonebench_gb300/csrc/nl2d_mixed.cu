@@ -20,17 +20,47 @@
 // multiplications with their FP32 reciprocals; FMA contraction is allowed.
 // The same preconditions as the FP64 fused step apply (uniform metrics, no
 // chained Flather faces).
-#include "nl2d_mixed_tile.cuh"
+#include "nl2d_mixed_march.cuh"
 
 namespace nl2d {
 using namespace mixk;
 namespace {
 
-__global__ void __launch_bounds__(TX* TY)
-    k_mixed_step(MixedFields mf, MixedState ms, Fields f, Dims d, MixConst k,
-                 const double* __restrict__ tide_table, int tide_index, double tide) {
-  mixed_tile(mf, ms, f, d, k, tide_table ? tide_table[tide_index] : tide,
-             d.xs - 1 + blockIdx.x * TX, d.ys - 1 + blockIdx.y * TY);
+// The regular cells: one warp per MW columns x MR rows of the copy region.
+__global__ void __launch_bounds__(32 * MARCH_WARPS)
+    k_mixed_march(MixedFields mf, MixedState ms, Dims d, MixConst k, int ncol, int nwarps) {
+  const int warp = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
+  if (warp >= nwarps) return;  // the whole warp leaves together
+  const int gy = warp / ncol, gx = warp - gy * ncol;
+  mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * MR);
+}
+
+// The copy region's other cells, one thread per listed cell.
+__global__ void __launch_bounds__(128)
+    k_mixed_general(MixedFields mf, MixedState ms, Fields f, Dims d, MixConst k,
+                    const double* __restrict__ tide_table, int tide_index, double tide) {
+  const double td = tide_table ? tide_table[tide_index] : tide;
+  GCtx x{mf, ms, f, d, k};
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < mf.gcount;
+       t += gridDim.x * blockDim.x) {
+    const int c = mf.glist[t];
+    const int j = c / d.width;
+    general_cell(x, c - j * d.width, j, td);
+  }
+}
+
+// march flags over the whole array; the copy region's other cells listed
+__global__ void k_mixed_flags(Fields f, Dims d, unsigned char* __restrict__ reg,
+                              int* __restrict__ glist, int* __restrict__ count) {
+  const long long n = (long long)d.width * d.height;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(t / d.width), i = (int)(t - (long long)j * d.width);
+    const bool r = march_regular(f, d, i, j);
+    reg[t] = r ? 1 : 0;
+    if (!r && i >= d.xs - 1 && i <= d.xe + 1 && j >= d.ys - 1 && j <= d.ye)
+      glist[atomicAdd(count, 1)] = (int)t;
+  }
 }
 
 __global__ void k_to_mixed(const double* __restrict__ sn, const double* __restrict__ un,
@@ -76,8 +106,23 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
                        const double* tide_table, int tide_index, cudaStream_t st) {
   const MixConst k = make_mix_const(s, um);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const dim3 grid((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_mixed_step<<<grid, dim3(TX, TY), 0, st>>>(mf, ms, f, d, k, tide_table, tide_index, tide);
+  const int ncol = (nx + MW - 1) / MW, nrow = (ny + MR - 1) / MR, nwarps = ncol * nrow;
+  k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
+      mf, ms, d, k, ncol, nwarps);
+  if (mf.gcount > 0)
+    k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
+                                                             tide_index, tide);
+}
+
+int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, int* count,
+                       cudaStream_t st) {
+  if (cudaMemsetAsync(count, 0, sizeof(int), st) != cudaSuccess) return -1;
+  k_mixed_flags<<<152 * 8, 256, 0, st>>>(f, d, mf.reg, mf.glist, count);
+  int h = 0;
+  if (cudaMemcpyAsync(&h, count, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return -1;
+  return h;
 }
 
 void launch_to_mixed(const double* sn, const double* un, const double* vn, const Fields& f,

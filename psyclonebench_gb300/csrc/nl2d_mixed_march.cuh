@@ -1,0 +1,442 @@
+// The single-domain mixed-precision step as a column march (device code).
+//
+// The tile form (nl2d_mixed_tile.cuh) stages a 2-cell halo of every field
+// in shared memory for a 32 x 8 tile: 1.7x the cells in loads, index
+// arithmetic and terms, ~930 instructions per cell, far from the HBM bound.
+// Here one warp owns MW = 30 consecutive columns (one lane per column, plus
+// one halo lane on each side) and marches down a strip of MR rows.  Each
+// lane keeps rows j-1, j, j+1 of its column in registers, takes its x
+// neighbours by warp shuffles, and forms every term that two neighbouring
+// updates share once per position, as the tile form does.  No shared
+// memory, no block barrier; the redundancy is 32/30 in x and (MR+3)/MR in
+// loads along y.
+//
+// The march writes the REGULAR cells only: xs+1 <= i <= xe-1,
+// ys+1 <= j <= ye-1, 3x3 mask neighbourhood wet (the byte flags `reg`).
+// For them every sshn_u / sshn_v face the update reads takes next_ssh's
+// two-sided formula, and no momentum mask, bc_ssh, solid-wall or Flather
+// rule applies: the arithmetic is the tile form's regular path.  Every
+// other cell of the copy region (a precomputed list, ~0.1 % of a 4096^2
+// domain) is updated by k_mixed_general with the tile form's general code
+// on global memory.  Both kernels read the same input buffers and write
+// disjoint cells of the output buffers.
+#pragma once
+#include "nl2d_mixed_tile.cuh"
+
+namespace nl2d {
+namespace mixk {
+namespace {
+
+constexpr int MW = 30;  // output columns per warp
+constexpr int MR = 32;  // output rows per warp
+constexpr int MARCH_WARPS = 4;
+constexpr unsigned FULL = 0xffffffffu;
+
+// One loaded row of one column.
+struct MRow {
+  float u, v, sn, lo, hu, hv, ht;
+  float su;  // east face: next_sshu's two-sided formula
+  float sv;  // north face: formed once the next row is loaded
+};
+
+// The terms at one position that neighbouring updates share, and the row
+// values the update at that position reads.
+struct MTerm {
+  float flxu, flxv, gx, gy, fxu, fyv, vsc, fyu, qy, uwc, fxv, qx;
+  float hu, su, hv, sv, sn, lo, u, v;
+};
+
+__device__ __forceinline__ float shd(float x) { return __shfl_down_sync(FULL, x, 1); }
+__device__ __forceinline__ float shu(float x) { return __shfl_up_sync(FULL, x, 1); }
+
+__device__ __forceinline__ float face_ssh(const MixConst& k, float a, float b, float r_area) {
+  return 0.5f * (k.area_t * a + k.area_t * b) * r_area;
+}
+
+// The loaded values of row j of column i (zeros outside the array),
+// issued ahead of their use.
+struct MRaw {
+  float2 s;
+  float u, v, hu, hv, ht;
+};
+
+__device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int i,
+                                         int j, int W, int H) {
+  MRaw r;
+  const bool ok = i >= 0 && i < W && j >= 0 && j < H;
+  const size_t c = ok ? (size_t)j * W + i : 0;
+  r.s = ok ? __ldg(ms.sn_in + c) : make_float2(0.f, 0.f);
+  r.u = ok ? __ldg(ms.un_in + c) : 0.f;
+  r.v = ok ? __ldg(ms.vn_in + c) : 0.f;
+  r.hu = ok ? __ldg(mf.hu + c) : 0.f;
+  r.hv = ok ? __ldg(mf.hv + c) : 0.f;
+  r.ht = ok ? __ldg(mf.ht + c) : 0.f;
+  return r;
+}
+
+// A loaded row and its east face's sshn_u; the east neighbour's ssh comes
+// from lane + 1 (lane 31's su is not used).
+__device__ __forceinline__ MRow finish_row(const MRaw& a, const MixConst& k) {
+  MRow r;
+  r.sn = a.s.x;
+  r.lo = a.s.y;
+  r.u = a.u;
+  r.v = a.v;
+  r.hu = a.hu;
+  r.hv = a.hv;
+  r.ht = a.ht;
+  r.su = face_ssh(k, r.sn, shd(r.sn), k.r_area_u);
+  r.sv = 0.f;
+  return r;
+}
+
+// What the update of output row j reads besides the terms, issued a row
+// ahead.
+struct MOut {
+  float rhu, rhv;
+  unsigned char reg;
+};
+
+__device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int i, int j, int W,
+                                         int jend) {
+  MOut o{0.f, 0.f, 0};
+  if (col && j < jend) {
+    const size_t c = (size_t)j * W + i;
+    o.reg = __ldg(mf.reg + c);
+    o.rhu = __ldg(mf.rhu + c);
+    o.rhv = __ldg(mf.rhv + c);
+  }
+  return o;
+}
+
+// The shared terms at (i, r) from rows r-1 (P), r (C), r+1 (N): the tile
+// form's phase 1, operation for operation.
+__device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const MRow& N,
+                                           const MixConst& k) {
+  MTerm t;
+  const float Hu = C.hu + C.su, Hv = C.hv + C.sv;
+  const float uW = shu(C.u), vW = shu(C.v), HuW = shu(Hu);
+  const float vE_P = shd(P.v), hvE_P = shd(P.hv), svE_P = shd(P.sv);
+  const float uW_N = shu(N.u), huW_N = shu(N.hu), suW_N = shu(N.su);
+  const float D = C.ht + C.sn;
+  t.flxu = Hu * C.u;
+  t.flxv = Hv * C.v;
+  t.gx = (C.u - uW) * k.r_dx_t * D;
+  t.gy = (C.v - P.v) * k.r_dy_t * D;
+  const float U = 0.5f * (C.u + uW) * k.dy_t;
+  t.fxu = (U < 0.f ? C.u : uW) * U * D;
+  const float V = 0.5f * (C.v + P.v) * k.dx_t;
+  t.fyv = (V < 0.f ? C.v : P.v) * V * D;
+  const float vsc = 0.5f * (P.v + vE_P);
+  t.vsc = vsc;
+  const float Vs = 0.5f * vsc * k.dxv2;
+  const float deps = 0.5f * ((P.hv + P.sv) + hvE_P + svE_P);
+  t.fyu = (Vs < 0.f ? C.u : P.u) * Vs * deps;
+  t.qy = (C.u - P.u) * k.r_dyu2;
+  const float uwc = 0.5f * (uW + uW_N);
+  t.uwc = uwc;
+  const float Uw = 0.5f * uwc * k.dyu2;
+  const float depw = 0.5f * (HuW + huW_N + suW_N);
+  t.fxv = (Uw < 0.f ? C.v : vW) * Uw * depw;
+  t.qx = (C.v - vW) * k.r_dxv2;
+  t.hu = C.hu;
+  t.su = C.su;
+  t.hv = C.hv;
+  t.sv = C.sv;
+  t.sn = C.sn;
+  t.lo = C.lo;
+  t.u = C.u;
+  t.v = C.v;
+  return t;
+}
+
+// One warp: lane L holds column i0-1+L; output rows j0 .. j0+MR-1 of the
+// copy region, regular cells only.
+__device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedState& ms,
+                                            const Dims& d, const MixConst& k, int i0, int j0) {
+  const int lane = threadIdx.x & 31;
+  const int W = d.width, H = d.height;
+  const int i = i0 - 1 + lane;
+  const int jend = min(j0 + MR, d.ye + 1);
+  const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
+  MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H), k);
+  MRow C = finish_row(load_raw(mf, ms, i, j0, W, H), k);
+  MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H), k);
+  MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H), R2 = load_raw(mf, ms, i, j0 + 3, W, H);
+  MOut O = load_out(mf, out_col, i, j0, W, jend);
+  P.sv = face_ssh(k, P.sn, C.sn, k.r_area_v);
+  C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
+  // row j0-1: what the updates of row j0 read from it
+  float flxv0 = (P.hv + P.sv) * P.v, hu0 = P.hu, su0 = P.su;
+  MTerm T1 = row_terms(P, C, N, k);  // row j0
+  for (int j = j0; j < jend; j++) {
+    P = C;  // row j
+    C = N;  // row j+1
+    N = finish_row(R1, k);  // row j+2, loaded two iterations ago
+    R1 = R2;
+    R2 = load_raw(mf, ms, i, j + 4, W, H);  // in flight for two iterations
+    const MOut Oc = O;
+    O = load_out(mf, out_col, i, j + 1, W, jend);
+    C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
+    const MTerm T2 = row_terms(P, C, N, k);  // row j+1
+    // x neighbours of row j's terms (every lane takes part)
+    const float flxuW = shu(T1.flxu), fxuE = shd(T1.fxu), gxE = shd(T1.gx), snE = shd(T1.sn);
+    const float fxvE = shd(T1.fxv), qxE = shd(T1.qx), uwcE = shd(T1.uwc);
+    const float hvW = shu(T1.hv), svW = shu(T1.sv), hvE = shd(T1.hv), svE = shd(T1.sv);
+    if (out_col && Oc.reg) {
+      const size_t c = (size_t)j * W + i;
+      {
+        const float div = ((flxuW - T1.flxu) + flxv0) - T1.flxv;
+        ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rdt * k.r_area_t);
+        const float Hu = T1.hu + T1.su, Hv = T1.hv + T1.sv;
+        {
+          const float adv = ((T1.fxu - fxuE) + T1.fyu) - T2.fyu;
+          const float dudy_s = T1.qy * (Hu + hu0 + su0);
+          const float dudy_n = T2.qy * (Hu + T2.hu + T2.su);
+          const float vis = k.visc * ((gxE - T1.gx) * k.dy_u + 0.5f * (dudy_n - dudy_s) * k.dx_u);
+          const float cor = 0.5f * (k.cor_u * (T1.vsc + T2.vsc)) * k.area_u * Hu;
+          const float hpg = -k.g * Hu * k.dy_u * (snE - T1.sn);
+          ms.un_out[c] = (T1.u * Hu + k.rdt * (adv + vis + cor + hpg) * k.r_area_u) *
+                         Oc.rhu * k.r_fric;
+        }
+        {
+          const float adv = ((T1.fxv - fxvE) + T1.fyv) - T2.fyv;
+          const float dvdx_w = T1.qx * (Hv + hvW + svW);
+          const float dvdx_e = qxE * (Hv + hvE + svE);
+          const float vis = k.visc * ((T2.gy - T1.gy) * k.dx_v + 0.5f * (dvdx_e - dvdx_w) * k.dy_v);
+          const float cor = -0.5f * (k.cor_v * (uwcE + T1.uwc)) * k.area_v * Hv;
+          const float hpg = -k.g * Hv * k.dx_v * (T2.sn - T1.sn);
+          ms.vn_out[c] = (T1.v * Hv + k.rdt * (adv + vis + cor + hpg) * k.r_area_v) *
+                         Oc.rhv * k.r_fric;
+        }
+      }
+    }
+    flxv0 = T1.flxv;
+    hu0 = T1.hu;
+    su0 = T1.su;
+    T1 = T2;
+  }
+}
+
+// ---- the other cells of the copy region, on global memory ----------------
+
+// Global-memory view of the tile form's staged values: zeros outside the
+// array, sshn_u / sshn_v by next_ssh{u,v}'s rules inside it (the stored
+// value on faces those kernels never update).
+struct GCtx {
+  MixedFields mf;
+  MixedState ms;
+  Fields f;
+  Dims d;
+  MixConst k;
+  __device__ __forceinline__ bool in(int i, int j) const {
+    return i >= 0 && i < d.width && j >= 0 && j < d.height;
+  }
+  __device__ __forceinline__ int ix(int i, int j) const { return j * d.width + i; }
+  __device__ __forceinline__ int m(int i, int j) const { return in(i, j) ? f.tmask[ix(i, j)] : 0; }
+  __device__ __forceinline__ float sn(int i, int j) const {
+    return in(i, j) ? ms.sn_in[ix(i, j)].x : 0.f;
+  }
+  __device__ __forceinline__ float su(int i, int j) const {
+    if (!in(i, j)) return 0.f;
+    const int mm = m(i, j);
+    if (j >= d.ys && j <= d.ye && i >= d.xs && i <= d.xe - 1) {
+      const int mn = m(i + 1, j);
+      if (mm + mn > 0) {
+        if (mm * mn > 0) return face_ssh(k, sn(i, j), sn(i + 1, j), k.r_area_u);
+        return mm <= 0 ? sn(i + 1, j) : sn(i, j);
+      }
+    }
+    return (float)f.sshn_u[ix(i, j)];
+  }
+  __device__ __forceinline__ float sv(int i, int j) const {
+    if (!in(i, j)) return 0.f;
+    const int mm = m(i, j);
+    if (j >= d.ys && j <= d.ye - 1 && i >= d.xs && i <= d.xe) {
+      const int mn = m(i, j + 1);
+      if (mm + mn > 0) {
+        if (mm * mn > 0) return face_ssh(k, sn(i, j), sn(i, j + 1), k.r_area_v);
+        return mm <= 0 ? sn(i, j + 1) : sn(i, j);
+      }
+    }
+    return (float)f.sshn_v[ix(i, j)];
+  }
+  __device__ __forceinline__ bool in_copy(int i, int j) const {
+    return i >= d.xs - 1 && i <= d.xe + 1 && j >= d.ys - 1 && j <= d.ye;
+  }
+};
+
+// momentum_u_kern.c:150-262 in FP32 at (i, j): the tile form's mom_u32.
+__device__ bool gmom_u(const GCtx& x, int i, int j, float& out) {
+  const int W = x.d.width, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
+            se = s + 1;
+  if (x.m(i, j) + x.m(i + 1, j) <= 0) return false;
+  if (x.m(i, j) <= 0 || x.m(i + 1, j) <= 0) return false;
+  const float *un = x.ms.un_in, *vn = x.ms.vn_in, *hu = x.mf.hu, *hv = x.mf.hv, *ht = x.mf.ht;
+  const MixConst& k = x.k;
+  const float sn_c = x.sn(i, j), sn_e = x.sn(i + 1, j);
+  const float u_e = 0.5f * (un[c] + un[e]) * k.dy_t;
+  const float depe = ht[e] + sn_e;
+  const float u_w = 0.5f * (un[c] + un[wst]) * k.dy_t;
+  const float depw = ht[c] + sn_c;
+  const float v_sc = 0.5f * (vn[s] + vn[se]);
+  const float v_s = 0.5f * v_sc * k.dxv2;
+  const float deps = 0.5f * (hv[s] + x.sv(i, j - 1) + hv[se] + x.sv(i + 1, j - 1));
+  const float v_nc = 0.5f * (vn[c] + vn[e]);
+  const float v_n = 0.5f * v_nc * k.dxv2;
+  const float depn = 0.5f * (hv[c] + x.sv(i, j) + hv[e] + x.sv(i + 1, j));
+  const float uu_w = wlo(u_w) * un[c] + whi(u_w) * un[wst];
+  const float uu_e = whi(u_e) * un[c] + wlo(u_e) * un[e];
+  const bool south_dry = x.m(i, j - 1) <= 0 || x.m(i + 1, j - 1) <= 0;
+  const bool north_dry = x.m(i, j + 1) <= 0 || x.m(i + 1, j + 1) <= 0;
+  const float uu_s = south_dry ? wlo(v_s) * un[c] : wlo(v_s) * un[c] + whi(v_s) * un[s];
+  const float uu_n = north_dry ? whi(v_n) * un[c] : whi(v_n) * un[c] + wlo(v_n) * un[n];
+  const float adv = uu_w * u_w * depw - uu_e * u_e * depe + uu_s * v_s * deps -
+                    uu_n * v_n * depn;
+  const float dudx_e = (un[e] - un[c]) * k.r_dx_t * depe;
+  const float dudx_w = (un[c] - un[wst]) * k.r_dx_t * depw;
+  const float Hu = hu[c] + x.su(i, j);
+  const float dudy_s =
+      south_dry ? 0.f : (un[c] - un[s]) * k.r_dyu2 * (Hu + hu[s] + x.su(i, j - 1));
+  const float dudy_n =
+      north_dry ? 0.f : (un[n] - un[c]) * k.r_dyu2 * (Hu + hu[n] + x.su(i, j + 1));
+  const float vis =
+      k.visc * ((dudx_e - dudx_w) * k.dy_u + (dudy_n - dudy_s) * k.dx_u * 0.5f);
+  const float cor = 0.5f * (k.cor_u * (v_sc + v_nc)) * k.area_u * Hu;
+  const float hpg = -k.g * Hu * k.dy_u * (sn_e - sn_c);
+  out = (un[c] * Hu + k.rdt * (adv + vis + cor + hpg) * k.r_area_u) * x.mf.rhu[c] * k.r_fric;
+  return true;
+}
+
+// momentum_v_kern.c:125-241 in FP32 at (i, j): the tile form's mom_v32
+// (its first guard reads the east mask, as the reference kernel does).
+__device__ bool gmom_v(const GCtx& x, int i, int j, float& out) {
+  const int W = x.d.width, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
+            nw = n - 1;
+  if (x.m(i, j) + x.m(i + 1, j) <= 0) return false;
+  if (x.m(i, j) <= 0 || x.m(i, j + 1) <= 0) return false;
+  const float *un = x.ms.un_in, *vn = x.ms.vn_in, *hu = x.mf.hu, *hv = x.mf.hv, *ht = x.mf.ht;
+  const MixConst& k = x.k;
+  const float sn_c = x.sn(i, j), sn_n = x.sn(i, j + 1);
+  const float v_n = 0.5f * (vn[c] + vn[n]) * k.dx_t;
+  const float depn = ht[n] + sn_n;
+  const float v_s = 0.5f * (vn[c] + vn[s]) * k.dx_t;
+  const float deps = ht[c] + sn_c;
+  const float u_wc = 0.5f * (un[wst] + un[nw]);
+  const float u_w = 0.5f * u_wc * k.dyu2;
+  const float depw = 0.5f * (hu[wst] + x.su(i - 1, j) + hu[nw] + x.su(i - 1, j + 1));
+  const float u_ec = 0.5f * (un[c] + un[n]);
+  const float u_e = 0.5f * u_ec * k.dyu2;
+  const float depe = 0.5f * (hu[c] + x.su(i, j) + hu[n] + x.su(i, j + 1));
+  const float vv_s = wlo(v_s) * vn[c] + whi(v_s) * vn[s];
+  const float vv_n = whi(v_n) * vn[c] + wlo(v_n) * vn[n];
+  const bool west_dry = x.m(i - 1, j) <= 0 || x.m(i - 1, j + 1) <= 0;
+  const bool east_dry = x.m(i + 1, j) <= 0 || x.m(i + 1, j + 1) <= 0;
+  const float vv_w = west_dry ? wlo(u_w) * vn[c] : wlo(u_w) * vn[c] + whi(u_w) * vn[wst];
+  const float vv_e = east_dry ? whi(u_e) * vn[c] : whi(u_e) * vn[c] + wlo(u_e) * vn[e];
+  const float adv = vv_w * u_w * depw - vv_e * u_e * depe + vv_s * v_s * deps -
+                    vv_n * v_n * depn;
+  const float dvdy_n = (vn[n] - vn[c]) * k.r_dy_t * depn;
+  const float dvdy_s = (vn[c] - vn[s]) * k.r_dy_t * deps;
+  const float Hv = hv[c] + x.sv(i, j);
+  const float dvdx_w =
+      west_dry ? 0.f : (vn[c] - vn[wst]) * k.r_dxv2 * (Hv + hv[wst] + x.sv(i - 1, j));
+  const float dvdx_e =
+      east_dry ? 0.f : (vn[e] - vn[c]) * k.r_dxv2 * (Hv + hv[e] + x.sv(i + 1, j));
+  const float vis =
+      k.visc * ((dvdy_n - dvdy_s) * k.dx_v + (dvdx_e - dvdx_w) * k.dy_v * 0.5f);
+  const float cor = -0.5f * (k.cor_v * (u_ec + u_wc)) * k.area_v * Hv;
+  const float hpg = -k.g * Hv * k.dx_v * (sn_n - sn_c);
+  out = (vn[c] * Hv + k.rdt * (adv + vis + cor + hpg) * k.r_area_v) * x.mf.rhv[c] * k.r_fric;
+  return true;
+}
+
+// u at face (i, j) before Flather: momentum where it applies, bc_solid_u.
+__device__ float gua_pre(const GCtx& x, int i, int j) {
+  const int c = x.ix(i, j);
+  float ua = x.in_copy(i, j) ? x.ms.un_in[c] : (float)x.f.ua[c];
+  if (i >= x.d.xs && i <= x.d.xe - 1 && j >= x.d.ys && j <= x.d.ye) {
+    float v;
+    if (gmom_u(x, i, j, v)) ua = v;
+  }
+  if (i >= x.d.xs - 1 && i <= x.d.xe && j >= x.d.ys - 1 && j <= x.d.ye + 1 &&
+      x.m(i, j) * x.m(i + 1, j) == 0)
+    ua = 0.f;
+  return ua;
+}
+
+// v at face (i, j) before Flather: momentum where it applies, bc_solid_v.
+__device__ float gva_pre(const GCtx& x, int i, int j) {
+  const int c = x.ix(i, j);
+  float va = x.in_copy(i, j) ? x.ms.vn_in[c] : (float)x.f.va[c];
+  if (i >= x.d.xs && i <= x.d.xe && j >= x.d.ys && j <= x.d.ye - 1) {
+    float v;
+    if (gmom_v(x, i, j, v)) va = v;
+  }
+  if (i >= x.d.xs - 1 && i <= x.d.xe + 1 && j >= x.d.ys - 1 && j <= x.d.ye &&
+      x.m(i, j) * x.m(i, j + 1) == 0)
+    va = 0.f;
+  return va;
+}
+
+// One cell (i, j) of the copy region by the tile form's general path:
+// continuity and bc_ssh, momentum, bc_solid and bc_flather.
+__device__ void general_cell(const GCtx& x, int i, int j, double tide) {
+  const Dims& d = x.d;
+  const MixConst& k = x.k;
+  const int W = d.width, c = x.ix(i, j);
+  float2 ssh = x.ms.sn_in[c];
+  if (i >= d.xs && i <= d.xe && j >= d.ys && j <= d.ye) {
+    const float r1 = (x.su(i, j) + x.mf.hu[c]) * x.ms.un_in[c];
+    const float r2 = (x.su(i - 1, j) + x.mf.hu[c - 1]) * x.ms.un_in[c - 1];
+    const float r3 = (x.sv(i, j) + x.mf.hv[c]) * x.ms.vn_in[c];
+    const float r4 = (x.sv(i, j - 1) + x.mf.hv[c - W]) * x.ms.vn_in[c - W];
+    ssh = dd_add(ssh, (r2 - r1 + r4 - r3) * k.rdt * k.r_area_t);
+    if (x.m(i, j) > 0 && (x.m(i, j - 1) < 0 || x.m(i, j + 1) < 0 || x.m(i + 1, j) < 0 ||
+                          x.m(i - 1, j) < 0)) {
+      const float hi = (float)tide;
+      ssh = make_float2(hi, (float)(tide - (double)hi));
+    }
+  }
+  x.ms.sn_out[c] = ssh;
+
+  float ua = x.ms.un_in[c];
+  if (i <= d.xe) {
+    ua = gua_pre(x, i, j);
+    const int mc = x.m(i, j), me = x.m(i + 1, j);
+    if (mc + me > -1) {
+      if (mc < 0)
+        ua = gua_pre(x, i + 1, j) + sqrtf(k.g / x.mf.hu[c]) * (x.su(i, j) - x.su(i + 1, j));
+      else if (me < 0 && i >= 1)
+        ua = gua_pre(x, i - 1, j) + sqrtf(k.g / x.mf.hu[c]) * (x.su(i, j) - x.su(i - 1, j));
+    }
+  }
+  x.ms.un_out[c] = ua;
+
+  float va = gva_pre(x, i, j);
+  const int mc = x.m(i, j), mn = x.m(i, j + 1);
+  if (mc + mn > -1) {
+    if (mc < 0)
+      va = gva_pre(x, i, j + 1) + sqrtf(k.g / x.mf.hv[c]) * (x.sv(i, j) - x.sv(i, j + 1));
+    else if (mn < 0 && j >= 1)
+      va = gva_pre(x, i, j - 1) + sqrtf(k.g / x.mf.hv[c]) * (x.sv(i, j) - x.sv(i, j - 1));
+  }
+  x.ms.vn_out[c] = va;
+}
+
+// Whether the march updates cell (i, j): interior away from the edges of
+// next_ssh's ranges, 3x3 mask neighbourhood wet.
+__device__ __forceinline__ bool march_regular(const Fields& f, const Dims& d, int i, int j) {
+  if (i < d.xs + 1 || i > d.xe - 1 || j < d.ys + 1 || j > d.ye - 1) return false;
+  const int W = d.width;
+#pragma unroll
+  for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+    for (int di = -1; di <= 1; di++)
+      if (f.tmask[(j + dj) * W + (i + di)] <= 0) return false;
+  return true;
+}
+
+}  // namespace
+}  // namespace mixk
+}  // namespace nl2d

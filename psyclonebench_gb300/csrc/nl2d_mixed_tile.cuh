@@ -44,7 +44,7 @@ __device__ __forceinline__ float whi(float x) { return 0.5f + copysignf(0.5f, x)
 __device__ bool mom_u32(const MCtx& x, int i, int j, float& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             se = s + 1;
-  const int t = x.slot(i, j), te = t + 1, tw = t - 1, ts = t - SX, tn = t + SX, tse = ts + 1,
+  const int t = x.slot(i, j), te = t + 1, ts = t - SX, tn = t + SX, tse = ts + 1,
             tne = tn + 1;
   const int* m = x.m;
   if (m[t] + m[te] <= 0) return false;

@@ -8,22 +8,8 @@ import argparse
 import ctypes
 import sys
 
-import numpy as np
-
 from .. import load_library
-
-
-def benchmark_fields(jpi, jpj, jpk):
-    k, j, i = np.meshgrid(np.arange(1, jpk + 1), np.arange(1, jpj + 1), np.arange(1, jpi + 1),
-                          indexing="ij")
-    v3 = (k * j * i).astype(np.float64) / float(jpi * jpj * jpk)
-    j2, i2 = np.meshgrid(np.arange(1, jpj + 1), np.arange(1, jpi + 1), indexing="ij")
-    v2 = (j2 * i2).astype(np.float64) / float(jpi * jpj)
-    f = {n: v3.copy() for n in ("mydomain", "tsn", "pun", "pvn", "pwn", "umask", "vmask",
-                                "tmask")}
-    f.update({n: v2.copy() for n in ("ztfreez", "rnfmsk", "upsmsk")})
-    f["rnfmsk_z"] = np.array([float(kk // jpk) for kk in range(1, jpk + 1)])
-    return f
+from ..workloads import tra_adv_fields
 
 
 def main():
@@ -33,7 +19,7 @@ def main():
     ap.add_argument("--iters", type=int, default=3)
     a = ap.parse_args()
     lib = load_library()
-    f = benchmark_fields(a.size, a.size, a.levels)
+    f = tra_adv_fields(a.size, a.size, a.levels)
     D = ctypes.POINTER(ctypes.c_double)
     args = [f[n].ctypes.data_as(D) for n in ("ztfreez", "pun", "pvn", "pwn", "umask", "vmask",
                                              "tmask", "rnfmsk", "rnfmsk_z", "upsmsk",

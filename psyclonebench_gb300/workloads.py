@@ -56,3 +56,21 @@ def ensemble_domains(count, seed, lo=64, hi=1024):
             "open_side": "SNEW"[int(rng.integers(0, 4))],
         })
     return out
+
+
+def tra_adv_fields(jpi, jpj, jpk):
+    """The tracer-advection benchmark's initial values
+    (tracer_advection/original/tra_adv.F90:63-98), Fortran layout
+    a(ji, jj, jk) -> a[jk, jj, ji]: the 3-d fields k j i / (jpi jpj jpk),
+    the 2-d ones j i / (jpi jpj), rnfmsk_z(jk) = jk / jpk in integer
+    division."""
+    k, j, i = np.meshgrid(np.arange(1, jpk + 1), np.arange(1, jpj + 1), np.arange(1, jpi + 1),
+                          indexing="ij")
+    v3 = (k * j * i).astype(np.float64) / float(jpi * jpj * jpk)
+    j2, i2 = np.meshgrid(np.arange(1, jpj + 1), np.arange(1, jpi + 1), indexing="ij")
+    v2 = (j2 * i2).astype(np.float64) / float(jpi * jpj)
+    f = {n: v3.copy() for n in ("mydomain", "tsn", "pun", "pvn", "pwn", "umask", "vmask",
+                                "tmask")}
+    f.update({n: v2.copy() for n in ("ztfreez", "rnfmsk", "upsmsk")})
+    f["rnfmsk_z"] = np.array([float(kk // jpk) for kk in range(1, jpk + 1)])
+    return f

@@ -64,3 +64,28 @@ def test_mixed_checksums_and_roundtrip(gpulib, oracle):
     P.check(gpulib.nl2d_run_steps(101, 20, 0, T.dptr(sums)), "run fp64 after mixed")
     T.gpu_read_all(gpulib, m)
     assert np.isfinite(m.f["sshn_t"]).all()
+
+
+def test_mixed_random_land_vs_fp64(gpulib, oracle):
+    """8 % random land cells inside a bathymetry domain: the cells next to
+    land are updated by the mixed step's general path (the column march
+    leaves them out), the rest by the march; after 300 steps the mixed
+    fields stay within the same bar against FP64."""
+    rng = np.random.default_rng(4)
+    base = bathy_model(192, 7, oracle)
+    inner = base.grid["tmask"][base.ys + 1:base.ye, base.xs + 1:base.xe]
+    inner[rng.random(inner.shape) < 0.08] = 0
+    ref = run_form(gpulib, base.copy(), 300, 0)
+    mix = run_form(gpulib, base.copy(), 300, 1)
+    report = {}
+    for k, (x0, x1, y0, y1) in (("sshn_t", T.regions(ref)["t"]), ("un", T.regions(ref)["u"]),
+                                ("vn", T.regions(ref)["v"])):
+        a = mix.f[k][y0:y1 + 1, x0:x1 + 1]
+        b = ref.f[k][y0:y1 + 1, x0:x1 + 1]
+        assert np.isfinite(a).all(), k
+        report[k] = (float(np.sqrt(np.mean((a - b) ** 2))), float(np.abs(a - b).max()),
+                     float(np.abs(b).max()))
+    print("mixed vs fp64 with land, 300 steps (rms, max, field max):", report)
+    assert report["sshn_t"][0] <= 1e-6
+    assert report["un"][0] <= 1e-4 * report["un"][2]
+    assert report["vn"][0] <= 1e-4 * report["vn"][2]
