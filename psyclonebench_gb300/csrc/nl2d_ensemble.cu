@@ -21,19 +21,12 @@
 
 #include "../../include/nl2d_gpu.h"
 #include "nl2d_fused_tile.cuh"
-#include "nl2d_mixed_tile.cuh"
+#include "nl2d_mixed_march.cuh"
 
 namespace nl2d {
 namespace {
 
-// One domain of a mixed-precision ensemble.
-struct EnsMixDomain {
-  MixedFields mf;
-  MixedState ms[2];
-  Fields f;  // FP64 arrays the mixed step reads where no step writes
-  Dims d;
-  mixk::MixConst k;
-};
+using EnsMixDomain = mixk::EnsDom;  // one domain of a mixed-precision ensemble
 
 __global__ void __launch_bounds__(mixk::TX* mixk::TY)
     k_ensemble_mixed_step(const EnsMixDomain* __restrict__ doms, const int4* __restrict__ tiles,
@@ -174,6 +167,15 @@ struct Ens {
   float *mun[2] = {}, *mvn[2] = {};
   float *mht = nullptr, *mhu = nullptr, *mhv = nullptr, *mrhu = nullptr, *mrhv = nullptr;
   EnsMixDomain* d_mdesc = nullptr;
+  // the column march (all domains share the step's constants)
+  bool march = false;
+  mixk::MixConst mk{};
+  unsigned char* mreg = nullptr;
+  int2* mglist = nullptr;
+  int* mcount = nullptr;
+  int mgn = 0;
+  int4* d_units = nullptr;
+  int nunits = 0;
 };
 
 Ens g_ens;
@@ -207,6 +209,16 @@ void ens_free() {
   }
   cudaFree(e.d_mdesc);
   e.d_mdesc = nullptr;
+  cudaFree(e.mreg);
+  cudaFree(e.mglist);
+  cudaFree(e.mcount);
+  cudaFree(e.d_units);
+  e.mreg = nullptr;
+  e.mglist = nullptr;
+  e.mcount = nullptr;
+  e.d_units = nullptr;
+  e.mgn = e.nunits = 0;
+  e.march = false;
   e.precision = 0;
   cudaFree(e.tmask);
   cudaFree(e.d_desc);
@@ -378,6 +390,55 @@ bool build_descriptors() {
                        cudaMemcpyHostToDevice));
 }
 
+// The column march needs one set of step constants for all domains (they
+// are kernel parameters); otherwise the tile kernel runs.  Builds the march
+// flags, the general-cell list and the march units.
+bool build_march(const std::vector<EnsMixDomain>& desc) {
+  Ens& e = g_ens;
+  e.march = false;
+  for (const EnsMixDomain& x : desc)
+    if (memcmp(&x.k, &desc[0].k, sizeof x.k) != 0) return true;
+  if (!e.mreg && (!ck(cudaMalloc(&e.mreg, e.total)) || !ck(cudaMalloc(&e.mcount, sizeof(int)))))
+    return false;
+  // two passes: count the general cells, then list them
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) {
+      cudaFree(e.mglist);
+      e.mglist = nullptr;
+      if (e.mgn > 0 && !ck(cudaMalloc(&e.mglist, sizeof(int2) * e.mgn))) return false;
+    }
+    if (!ck(cudaMemsetAsync(e.mcount, 0, sizeof(int), e.stream))) return false;
+    for (int k = 0; k < e.ndom; k++)
+      launch_ens_mixed_flags(e.d_mdesc, k, e.mreg, pass == 1 ? e.mglist : nullptr, e.mcount,
+                             e.stream);
+    int n = 0;
+    if (!ck(cudaGetLastError()) ||
+        !ck(cudaMemcpyAsync(&n, e.mcount, sizeof(int), cudaMemcpyDeviceToHost, e.stream)) ||
+        !ck(cudaStreamSynchronize(e.stream)))
+      return false;
+    if (pass == 1 && n != e.mgn) return false;
+    e.mgn = n;
+  }
+  std::vector<int4> units;
+  for (const EnsMixDomain& x : desc) {
+    const int nx = x.d.xe - x.d.xs + 3, ny = x.d.ye - x.d.ys + 2;
+    const int dom = (int)(&x - desc.data());
+    for (int gy = 0; gy < (ny + mixk::MR - 1) / mixk::MR; gy++)
+      for (int gx = 0; gx < (nx + mixk::MW - 1) / mixk::MW; gx++)
+        units.push_back(make_int4(dom, x.d.xs - 1 + gx * mixk::MW, x.d.ys - 1 + gy * mixk::MR, 0));
+  }
+  cudaFree(e.d_units);
+  e.d_units = nullptr;
+  if (!ck(cudaMalloc(&e.d_units, sizeof(int4) * units.size())) ||
+      !ck(cudaMemcpy(e.d_units, units.data(), sizeof(int4) * units.size(),
+                     cudaMemcpyHostToDevice)))
+    return false;
+  e.nunits = (int)units.size();
+  e.mk = desc[0].k;
+  e.march = true;
+  return true;
+}
+
 bool build_mixed() {
   Ens& e = g_ens;
   const size_t n = e.total;
@@ -420,12 +481,15 @@ bool build_mixed() {
     um.dy_u = um.dy_v = um.dy_t = D.dy;
     um.sin_u = um.sin_v = std::sin(D.gphi * e.sc.d2r);
     x.k = mixk::make_mix_const(e.sc, um);
+    x.off = o;
   }
   cudaFree(e.d_mdesc);
   e.d_mdesc = nullptr;
-  if (!ck(cudaMalloc(&e.d_mdesc, sizeof(EnsMixDomain) * e.ndom))) return false;
-  return ck(cudaMemcpy(e.d_mdesc, desc.data(), sizeof(EnsMixDomain) * e.ndom,
-                       cudaMemcpyHostToDevice));
+  if (!ck(cudaMalloc(&e.d_mdesc, sizeof(EnsMixDomain) * e.ndom)) ||
+      !ck(cudaMemcpy(e.d_mdesc, desc.data(), sizeof(EnsMixDomain) * e.ndom,
+                     cudaMemcpyHostToDevice)))
+    return false;
+  return build_march(desc);
 }
 
 // Interior (ssh, u, v) of every domain, all of size nx x ny, as FP32
@@ -578,6 +642,9 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
   for (const DomainHost& D : e.dom)
     if (!D.ready) return NL2D_ERR_STATE;
   if (!e.built) {
+    // a rebuild may move every buffer a captured graph refers to
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    e.graph = nullptr;
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_ensemble_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -585,7 +652,8 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
       attr = true;
     }
     if (e.precision == 1) {
-      if (!build_mixed() || !build_schedule(mixk::TX, mixk::TY)) return NL2D_ERR_CUDA;
+      if (!build_mixed() || (!e.march && !build_schedule(mixk::TX, mixk::TY)))
+        return NL2D_ERR_CUDA;
     } else if (!build_descriptors() || !build_schedule(TX, TY)) {
       return NL2D_ERR_CUDA;
     }
@@ -632,7 +700,18 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     for (int q = 0; q < nsteps; q++) {
       double* sums = e.d_sums + (size_t)((q + 1) / std::max(checksum_every, 1) - 1) * e.ndom * 3;
       const bool want_sums = checksum_every > 0 && (q + 1) % checksum_every == 0;
-      if (e.precision == 1) {
+      if (e.precision == 1 && e.march) {
+        const MixedFields mf{e.mht, e.mhu, e.mhv, e.mrhu, e.mrhv, e.mreg, nullptr, 0};
+        const MixedState ms{e.msn[par], e.mun[par], e.mvn[par],
+                            e.msn[1 - par], e.mun[1 - par], e.mvn[1 - par]};
+        launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.stream);
+        launch_ens_mixed_general(e.d_mdesc, e.mglist, e.mgn, par,
+                                 e.d_tides + (size_t)q * e.ndom, e.stream);
+        par = 1 - par;
+        if (want_sums)
+          k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
+                                                                            sums);
+      } else if (e.precision == 1) {
         k_ensemble_mixed_step<<<e.nctas, dim3(mixk::TX, mixk::TY), 0, e.stream>>>(
             e.d_mdesc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
         par = 1 - par;

@@ -109,6 +109,17 @@ void launch_to_mixed(const double* sn, const double* un, const double* vn,
 // error.
 int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, int* count,
                        cudaStream_t st);
+// Ensemble form of the march (nl2d_mixed.cu, built with FMA contraction
+// like the single-domain mixed step).  `doms` is a device array of the
+// ensemble's mixed domain descriptors (mixk::EnsDom), `k` the host copy of
+// the step constants all domains share (mixk::MixConst).
+void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
+                            const MixedFields& mf, const MixedState& ms, const void* k,
+                            cudaStream_t st);
+void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,
+                              const double* tides, cudaStream_t st);
+void launch_ens_mixed_flags(const void* doms, int dom, unsigned char* reg, int2* glist,
+                            int* count, cudaStream_t st);
 void launch_from_mixed(const float2* sn2, const float* un_f, const float* vn_f,
                        double* sn, double* un, double* vn, const Dims& d,
                        cudaStream_t st);

@@ -20,6 +20,8 @@
 // multiplications with their FP32 reciprocals; FMA contraction is allowed.
 // The same preconditions as the FP64 fused step apply (uniform metrics, no
 // chained Flather faces).
+#include <cstring>
+
 #include "nl2d_mixed_march.cuh"
 
 namespace nl2d {
@@ -32,7 +34,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS)
   const int warp = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (warp >= nwarps) return;  // the whole warp leaves together
   const int gy = warp / ncol, gx = warp - gy * ncol;
-  mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * MR);
+  mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * MR, 0);
 }
 
 // The copy region's other cells, one thread per listed cell.
@@ -46,6 +48,51 @@ __global__ void __launch_bounds__(128)
     const int c = mf.glist[t];
     const int j = c / d.width;
     general_cell(x, c - j * d.width, j, td);
+  }
+}
+
+// ---- ensemble: the march over every domain when all share the step's
+// constants (kernel parameters); warp w takes units[w] = (domain, i0, j0)
+// with the packed arrays' base pointers in mf / ms.
+__global__ void __launch_bounds__(32 * MARCH_WARPS)
+    k_ensemble_mixed_march(const EnsDom* __restrict__ doms, const int4* __restrict__ units,
+                           int nunits, MixedFields mf, MixedState ms, MixConst k) {
+  const int w = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
+  if (w >= nunits) return;  // the whole warp leaves together
+  const int4 u = units[w];
+  const Dims d = doms[u.x].d;
+  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off);
+}
+
+// The other cells of every domain's copy region: glist[t] = (domain, cell).
+__global__ void __launch_bounds__(128)
+    k_ensemble_mixed_general(const EnsDom* __restrict__ doms, const int2* __restrict__ glist,
+                             int n, int parity, const double* __restrict__ tides) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int2 g = glist[t];
+    const EnsDom& D = doms[g.x];
+    const GCtx x{D.mf, D.ms[parity], D.f, D.d, D.k};
+    const int j = g.y / D.d.width;
+    general_cell(x, g.y - j * D.d.width, j, tides[g.x]);
+  }
+}
+
+// March flags of domain `dom` and, when glist is not null, its general
+// cells appended as (dom, cell); *count counts them either way.
+__global__ void k_ensemble_mixed_flags(const EnsDom* __restrict__ doms, int dom,
+                                       unsigned char* __restrict__ reg, int2* __restrict__ glist,
+                                       int* __restrict__ count) {
+  const EnsDom& D = doms[dom];
+  const long long n = (long long)D.d.width * D.d.height;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(t / D.d.width), i = (int)(t - (long long)j * D.d.width);
+    const bool r = march_regular(D.f, D.d, i, j);
+    reg[D.off + t] = r ? 1 : 0;
+    if (!r && i >= D.d.xs - 1 && i <= D.d.xe + 1 && j >= D.d.ys - 1 && j <= D.d.ye) {
+      const int slot = atomicAdd(count, 1);
+      if (glist) glist[slot] = make_int2(dom, (int)t);
+    }
   }
 }
 
@@ -112,6 +159,27 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
   if (mf.gcount > 0)
     k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
                                                              tide_index, tide);
+}
+
+void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
+                            const MixedFields& mf, const MixedState& ms, const void* k,
+                            cudaStream_t st) {
+  MixConst kc;
+  memcpy(&kc, k, sizeof kc);
+  k_ensemble_mixed_march<<<(nunits + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
+      (const EnsDom*)doms, units, nunits, mf, ms, kc);
+}
+
+void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,
+                              const double* tides, cudaStream_t st) {
+  if (n > 0)
+    k_ensemble_mixed_general<<<(n + 127) / 128, 128, 0, st>>>((const EnsDom*)doms, glist, n,
+                                                               parity, tides);
+}
+
+void launch_ens_mixed_flags(const void* doms, int dom, unsigned char* reg, int2* glist,
+                            int* count, cudaStream_t st) {
+  k_ensemble_mixed_flags<<<64, 256, 0, st>>>((const EnsDom*)doms, dom, reg, glist, count);
 }
 
 int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, int* count,

@@ -61,10 +61,10 @@ struct MRaw {
 };
 
 __device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int i,
-                                         int j, int W, int H) {
+                                         int j, int W, int H, size_t base) {
   MRaw r;
   const bool ok = i >= 0 && i < W && j >= 0 && j < H;
-  const size_t c = ok ? (size_t)j * W + i : 0;
+  const size_t c = base + (ok ? (size_t)j * W + i : 0);
   r.s = ok ? __ldg(ms.sn_in + c) : make_float2(0.f, 0.f);
   r.u = ok ? __ldg(ms.un_in + c) : 0.f;
   r.v = ok ? __ldg(ms.vn_in + c) : 0.f;
@@ -98,10 +98,10 @@ struct MOut {
 };
 
 __device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int i, int j, int W,
-                                         int jend) {
+                                         int jend, size_t base) {
   MOut o{0.f, 0.f, 0};
   if (col && j < jend) {
-    const size_t c = (size_t)j * W + i;
+    const size_t c = base + (size_t)j * W + i;
     o.reg = __ldg(mf.reg + c);
     o.rhu = __ldg(mf.rhu + c);
     o.rhv = __ldg(mf.rhv + c);
@@ -151,19 +151,21 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
 }
 
 // One warp: lane L holds column i0-1+L; output rows j0 .. j0+MR-1 of the
-// copy region, regular cells only.
+// copy region, regular cells only.  `base`: the domain's first element in
+// the arrays (an ensemble packs its domains back to back; 0 otherwise).
 __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedState& ms,
-                                            const Dims& d, const MixConst& k, int i0, int j0) {
+                                            const Dims& d, const MixConst& k, int i0, int j0,
+                                            size_t base) {
   const int lane = threadIdx.x & 31;
   const int W = d.width, H = d.height;
   const int i = i0 - 1 + lane;
   const int jend = min(j0 + MR, d.ye + 1);
   const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
-  MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H), k);
-  MRow C = finish_row(load_raw(mf, ms, i, j0, W, H), k);
-  MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H), k);
-  MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H), R2 = load_raw(mf, ms, i, j0 + 3, W, H);
-  MOut O = load_out(mf, out_col, i, j0, W, jend);
+  MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H, base), k);
+  MRow C = finish_row(load_raw(mf, ms, i, j0, W, H, base), k);
+  MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H, base), k);
+  MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H, base), R2 = load_raw(mf, ms, i, j0 + 3, W, H, base);
+  MOut O = load_out(mf, out_col, i, j0, W, jend, base);
   P.sv = face_ssh(k, P.sn, C.sn, k.r_area_v);
   C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
   // row j0-1: what the updates of row j0 read from it
@@ -174,9 +176,9 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     C = N;  // row j+1
     N = finish_row(R1, k);  // row j+2, loaded two iterations ago
     R1 = R2;
-    R2 = load_raw(mf, ms, i, j + 4, W, H);  // in flight for two iterations
+    R2 = load_raw(mf, ms, i, j + 4, W, H, base);  // in flight for two iterations
     const MOut Oc = O;
-    O = load_out(mf, out_col, i, j + 1, W, jend);
+    O = load_out(mf, out_col, i, j + 1, W, jend, base);
     C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
     const MTerm T2 = row_terms(P, C, N, k);  // row j+1
     // x neighbours of row j's terms (every lane takes part)
@@ -184,7 +186,7 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     const float fxvE = shd(T1.fxv), qxE = shd(T1.qx), uwcE = shd(T1.uwc);
     const float hvW = shu(T1.hv), svW = shu(T1.sv), hvE = shd(T1.hv), svE = shd(T1.sv);
     if (out_col && Oc.reg) {
-      const size_t c = (size_t)j * W + i;
+      const size_t c = base + (size_t)j * W + i;
       {
         const float div = ((flxuW - T1.flxu) + flxv0) - T1.flxv;
         ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rdt * k.r_area_t);
@@ -423,6 +425,16 @@ __device__ void general_cell(const GCtx& x, int i, int j, double tide) {
   }
   x.ms.vn_out[c] = va;
 }
+
+// One domain of a mixed-precision ensemble (device descriptor).
+struct EnsDom {
+  MixedFields mf;
+  MixedState ms[2];
+  Fields f;  // FP64 arrays the mixed step reads where no step writes
+  Dims d;
+  MixConst k;
+  size_t off;  // the domain's first element in the packed arrays
+};
 
 // Whether the march updates cell (i, j): interior away from the edges of
 // next_ssh's ranges, 3x3 mask neighbourhood wet.

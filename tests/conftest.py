@@ -27,3 +27,15 @@ def gpulib():
     if not torch.cuda.is_available():
         pytest.fail("GPU test run without a CUDA device")
     return P.load_library()
+
+
+@pytest.fixture(autouse=True)
+def _fresh_library(request):
+    """Every test that uses the library starts with no problem registered.
+    The library keys a problem's residency on the caller's host pointers
+    (the reference's driver keeps its arrays for the program's life), so a
+    model whose arrays land at the addresses of an earlier test's freed
+    arrays would otherwise be taken for that earlier registration."""
+    if "gpulib" in request.fixturenames:
+        request.getfixturevalue("gpulib").nl2d_finalize()
+    yield
