@@ -195,7 +195,9 @@ int nl2d_ens_set_domain(int dom, const int *tmask, const double *ht,
                         const double *hu, const double *hv);
 /* Schedule knobs the autotuner searches: persistent CTAs per SM (1, 2),
  * tile assignment (0 contiguous cost-balanced chunks, 1 longest processing
- * time first) and the cost weight of a boundary-tile edge cell. */
+ * time first, 2 one tile per CTA with as many CTAs as tiles, balanced by the
+ * hardware block scheduler; the CTA count then does not apply) and the
+ * cost weight of a boundary-tile edge cell. */
 int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight);
 /* Advances every domain nsteps steps (istep = istep0 ...); per-domain
  * ssh / u / v checksums after every checksum_every-th step go to

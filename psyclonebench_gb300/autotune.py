@@ -1,9 +1,10 @@
 """Autotuner for the ensemble's persistent-kernel schedule.
 
 The search space is the schedule the kernel exposes: persistent CTAs per SM
-(1 or 2), tile assignment (contiguous cost-balanced chunks, or longest
-processing time first) and the cost weight given to the edge cells of
-boundary tiles (which take the general per-cell path).  Each candidate is
+(1 or 2), tile assignment (contiguous cost-balanced chunks, longest
+processing time first, or one tile per CTA left to the hardware block
+scheduler) and the cost weight given to the edge cells of boundary tiles
+(which take the general per-cell path).  Each candidate is
 timed on a few steps of the actual ensemble (after one untimed step), the
 domains are put back at rest, and the fastest candidate is kept.  Results
 are cached on disk per (domain size histogram, precision), so a repeated
@@ -13,7 +14,9 @@ import hashlib
 import json
 import os
 
-CANDIDATES = [(cps, pol, bw) for cps in (1, 2) for pol in (0, 1) for bw in (0.0, 4.0, 16.0)]
+# policy 2 (one tile per CTA) ignores the CTAs per SM and the edge weight
+CANDIDATES = ([(cps, pol, bw) for cps in (1, 2) for pol in (0, 1) for bw in (0.0, 4.0, 16.0)] +
+              [(2, 2, 0.0)])
 
 
 def cache_path():

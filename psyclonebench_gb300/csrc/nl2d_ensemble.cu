@@ -296,10 +296,17 @@ bool build_schedule(int TXv, int TYv) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e.nctas = std::max(1, sms * e.ctas_per_sm);
+  e.nctas = e.policy == 2 ? std::max<int>(1, (int)tiles.size()) : std::max(1, sms * e.ctas_per_sm);
   std::vector<int4> order;
   std::vector<int> first(e.nctas + 1, 0);
-  if (e.policy == 1) {
+  if (e.policy == 2) {
+    // one tile per CTA, in domain order: the hardware block scheduler
+    // balances the load and keeps as many CTAs per SM as fit
+    for (size_t t = 0; t < tiles.size(); t++) {
+      order.push_back(make_int4(tiles[t].dom, tiles[t].i0, tiles[t].j0, 0));
+      first[t + 1] = (int)t + 1;
+    }
+  } else if (e.policy == 1) {
     // longest processing time first: biggest tile to the least-loaded CTA
     std::vector<int> idx(tiles.size());
     std::iota(idx.begin(), idx.end(), 0);
@@ -625,7 +632,7 @@ int nl2d_ens_set_domain(int dom, const int* tmask, const double* ht, const doubl
 
 int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight) {
   Ens& e = g_ens;
-  if (ctas_per_sm < 1 || ctas_per_sm > 2 || policy < 0 || policy > 1 || boundary_weight < 0)
+  if (ctas_per_sm < 1 || ctas_per_sm > 2 || policy < 0 || policy > 2 || boundary_weight < 0)
     return NL2D_ERR_ARGS;
   e.ctas_per_sm = ctas_per_sm;
   e.policy = policy;

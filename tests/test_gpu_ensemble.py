@@ -27,7 +27,7 @@ def domains():
     return [build_domain(s) for s in small_specs()]
 
 
-@pytest.mark.parametrize("cps,policy", [(2, 0), (1, 1)])
+@pytest.mark.parametrize("cps,policy", [(2, 0), (1, 1), (2, 2)])
 def test_ensemble_matches_oracle(gpulib, oracle, domains, cps, policy):
     from psyclonebench_gb300.ensemble import Ensemble
     ens = Ensemble(domains, rdt=5.0, lib=gpulib)
