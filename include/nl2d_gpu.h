@@ -287,7 +287,12 @@ int nl2d_emu_advance(float *state, const float *inc, const float *inc_scale3,
                      const float *statics, const int *dom, const float *forcing,
                      long long HW, long long P, int cpad, void *stream);
 /* Interior (ssh, u, v) of every ensemble domain (all the same size) into a
- * device FP32 array [dom][ny][nx][3]; FP64 form only. */
+ * device FP32 array [dom][ny][nx][3], from the FP64 or the mixed-precision
+ * state (ssh = hi + lo). */
+/* 1 when the built mixed-precision ensemble runs the column march (every
+ * domain shares the step's constants), 0 when it runs the shared-memory
+ * tile form (or nothing is built). */
+int nl2d_ens_uses_march(void);
 int nl2d_ens_export_interior(float *d_out);
 
 /* Sets the interior (ssh, u, v) of every ensemble domain from a device FP32

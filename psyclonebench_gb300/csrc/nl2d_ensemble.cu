@@ -518,6 +518,25 @@ __global__ void k_export_interior(const EnsDomain* __restrict__ doms, int parity
   }
 }
 
+// The same from the mixed-precision state: ssh hi + lo, velocities as held.
+__global__ void k_export_interior_mixed(const EnsMixDomain* __restrict__ doms, int parity,
+                                        int ndom, int nx, int ny, float* __restrict__ out) {
+  const long long n = (long long)ndom * nx * ny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int dom = (int)(t / ((long long)nx * ny));
+    const int rem = (int)(t - (long long)dom * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    const EnsMixDomain& D = doms[dom];
+    const size_t c = (size_t)(D.d.ys + j) * D.d.width + (D.d.xs + i);
+    const MixedState& st = D.ms[parity];
+    const float2 s2 = st.sn_in[c];
+    out[t * 3 + 0] = s2.x + s2.y;
+    out[t * 3 + 1] = st.un_in[c];
+    out[t * 3 + 2] = st.vn_in[c];
+  }
+}
+
 // The inverse: FP32 [dom][ny][nx][3] into the interior of the current FP64
 // state (both ping-pong buffers, so cells no step writes stay consistent).
 // The interior leaves out one piece of the solver's state: the velocity on
@@ -817,11 +836,15 @@ int nl2d_ens_set_precision(int precision) {
 
 int nl2d_ens_export_interior(float* d_out) {
   Ens& e = g_ens;
-  if (e.ndom < 1 || !d_out || e.precision != 0 || !e.built) return NL2D_ERR_STATE;
+  if (e.ndom < 1 || !d_out || !e.built) return NL2D_ERR_STATE;
   const int nx = e.dom[0].xe - e.dom[0].xs + 1, ny = e.dom[0].ye - e.dom[0].ys + 1;
   for (const DomainHost& D : e.dom)
     if (D.xe - D.xs + 1 != nx || D.ye - D.ys + 1 != ny) return NL2D_ERR_ARGS;
-  k_export_interior<<<152 * 8, 256, 0, e.stream>>>(e.d_desc, e.parity, e.ndom, nx, ny, d_out);
+  if (e.precision == 1)
+    k_export_interior_mixed<<<152 * 8, 256, 0, e.stream>>>(e.d_mdesc, e.parity, e.ndom, nx, ny,
+                                                           d_out);
+  else
+    k_export_interior<<<152 * 8, 256, 0, e.stream>>>(e.d_desc, e.parity, e.ndom, nx, ny, d_out);
   if (!ck(cudaGetLastError()) || !ck(cudaStreamSynchronize(e.stream))) return NL2D_ERR_CUDA;
   return NL2D_OK;
 }
@@ -851,6 +874,8 @@ int nl2d_ens_reset(void) {
   e.parity = 0;
   return NL2D_OK;
 }
+
+int nl2d_ens_uses_march(void) { return g_ens.march ? 1 : 0; }
 
 void nl2d_ens_destroy(void) { ens_free(); }
 

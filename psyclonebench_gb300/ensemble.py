@@ -76,7 +76,8 @@ def shard_domains(specs, world):
 
 class Ensemble:
     """A set of domains resident on the GPU.  `domains` are build_domain()
-    dicts; all share rdt, cbfr, visc, dx, dy and latitude."""
+    dicts; all share rdt, cbfr and visc, and dx, dy and latitude unless a
+    domain carries its own as "geo": (dx, dy, gphi)."""
 
     def __init__(self, domains, rdt=5.0, cbfr=1.5e-4, visc=0.1, dx=1000.0, dy=1000.0,
                  gphi=50.0, lib=None):
@@ -84,7 +85,7 @@ class Ensemble:
         self.domains = domains
         n = len(domains)
         dims = np.array([d["dims"] for d in domains], np.int32).reshape(-1)
-        geo = np.array([(dx, dy, gphi)] * n, np.float64).reshape(-1)
+        geo = np.array([d.get("geo", (dx, dy, gphi)) for d in domains], np.float64).reshape(-1)
         tide = np.array([d["tide"] for d in domains], np.float64).reshape(-1)
         phys = np.array([rdt, cbfr, visc, OMEGA, D2R, G], np.float64)
         self._check(self.lib.nl2d_ens_create(n, _ip(dims), _dp(geo), _dp(tide), _dp(phys)),
@@ -99,6 +100,11 @@ class Ensemble:
     def _check(rc, what):
         if rc != NL2D_OK:
             raise Nl2dError("%s failed (%d)" % (what, rc))
+
+    def uses_march(self):
+        """Whether the mixed-precision form runs the column march (all
+        domains share the step's constants) rather than the tile form."""
+        return bool(self.lib.nl2d_ens_uses_march())
 
     def schedule(self, ctas_per_sm=2, policy=0, boundary_weight=4.0):
         self._check(self.lib.nl2d_ens_schedule(ctas_per_sm, policy, boundary_weight),

@@ -73,6 +73,7 @@ def test_mixed_ensemble_error_vs_fp64(gpulib, domains):
     ref = [ens.read(k) for k in range(len(domains))]
     ens.set_precision(1)
     _, sums = ens.run(1, 300, checksum_every=300)
+    assert ens.uses_march()  # every domain shares the step's constants
     worst = 0.0
     for k, d in enumerate(domains):
         w, h, xs, xe, ys, ye = d["dims"]
@@ -83,5 +84,32 @@ def test_mixed_ensemble_error_vs_fp64(gpulib, domains):
         np.testing.assert_allclose(sums[0, k, 0], np.abs(got[0][ys:ye + 1, xs:xe + 1]).sum(),
                                    rtol=1e-10)
     print("mixed ensemble worst per-domain ssh RMS error:", worst)
+    assert worst <= 1e-6
+    ens.close()
+
+
+def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
+    """Domains with their own grid spacing and latitude do not share the
+    step's constants, so the mixed ensemble runs the shared-memory tile form
+    instead of the column march; it stays within the same bar against the
+    FP64 ensemble."""
+    from psyclonebench_gb300.ensemble import Ensemble
+    doms = [dict(d) for d in domains[:4]]
+    doms[1]["geo"] = (900.0, 1100.0, 45.0)
+    doms[3]["geo"] = (1200.0, 800.0, 30.0)
+    ens = Ensemble(doms, rdt=5.0, lib=gpulib)
+    ens.run(1, 300)
+    ref = [ens.read(k) for k in range(len(doms))]
+    ens.set_precision(1)
+    ens.run(1, 300)
+    assert not ens.uses_march()
+    worst = 0.0
+    for k, d in enumerate(doms):
+        w, h, xs, xe, ys, ye = d["dims"]
+        got = ens.read(k)
+        diff = got[0][ys:ye + 1, xs:xe + 1] - ref[k][0][ys:ye + 1, xs:xe + 1]
+        worst = max(worst, float(np.sqrt(np.mean(diff * diff))))
+        assert np.isfinite(got[1]).all() and np.isfinite(got[2]).all()
+    print("tile-form mixed ensemble worst per-domain ssh RMS error:", worst)
     assert worst <= 1e-6
     ens.close()
