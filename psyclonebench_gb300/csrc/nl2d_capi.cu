@@ -43,6 +43,7 @@ struct State {
   int last_path = 0;
   cudaStream_t stream = nullptr;
   double* partials = nullptr;  // checksum scratch
+  double* scan = nullptr;      // registration scan: flags word + reference values
   double* sums = nullptr;      // device checksum results
   int sums_cap = 0;
   double* tide_table = nullptr;
@@ -176,88 +177,154 @@ void host_sines(const double* gphi, size_t n, double d2r, double* out) {
   });
 }
 
-bool upload_sines(double d2r) {
-  State& s = g_state;
-  const size_t n = (size_t)s.reg.width * s.reg.height;
-  std::unique_ptr<double[]> su(new double[n]), sv(new double[n]);
-  host_sines((const double*)s.reg.host[kNumFields + 10], n, d2r, su.get());
-  host_sines((const double*)s.reg.host[kNumFields + 11], n, d2r, sv.get());
-  if (!CK(cudaMemcpy(s.dev.sin_u, su.get(), n * 8, cudaMemcpyHostToDevice))) return false;
-  if (!CK(cudaMemcpy(s.dev.sin_v, sv.get(), n * 8, cudaMemcpyHostToDevice))) return false;
-  s.sin_d2r = d2r;
-  // Uniform-metric check over every point a step reads them at.
-  const Registration& r = s.reg;
-  const int W = r.width;
-  auto uniform_over = [&](const double* a, double& v) {
-    v = a[(size_t)(r.ys - 1) * W + (r.xs - 1)];
-    uint64_t ref;
-    memcpy(&ref, &v, 8);
-    std::atomic<bool> ok{true};
-    parallel_chunks(r.ys - 1, r.ye + 2, [&, ref](long long j0, long long j1) {
-      for (long long j = j0; j < j1 && ok.load(std::memory_order_relaxed); j++) {
-        const uint64_t* row = reinterpret_cast<const uint64_t*>(a + (size_t)j * W);
-        uint64_t diff = 0;  // bitwise equality, branch-free along the row
-        for (int i = r.xs - 1; i <= r.xe + 1; i++) diff |= row[i] ^ ref;
-        if (diff) {
-          ok.store(false, std::memory_order_relaxed);
-          return;
-        }
-      }
-    });
-    return ok.load();
-  };
-  const double** h = (const double**)(r.host + kNumFields);
-  bool uniform = true;
-  uniform &= uniform_over(h[1], s.um.area_t);
-  uniform &= uniform_over(h[2], s.um.area_u);
-  uniform &= uniform_over(h[3], s.um.area_v);
-  uniform &= uniform_over(h[4], s.um.dx_u);
-  uniform &= uniform_over(h[5], s.um.dx_v);
-  uniform &= uniform_over(h[6], s.um.dx_t);
-  uniform &= uniform_over(h[7], s.um.dy_u);
-  uniform &= uniform_over(h[8], s.um.dy_v);
-  uniform &= uniform_over(h[9], s.um.dy_t);
-  uniform &= uniform_over(su.get(), s.um.sin_u);
-  uniform &= uniform_over(sv.get(), s.um.sin_v);
-  // Flather chains (a Flather face reading another Flather face) and reads
-  // that would leave the array make the one-launch update differ from the
-  // reference's serial Flather loops.
-  const int* m = (const int*)r.host[kNumFields];
+// What registration needs to know about the uploaded grid, from the device
+// copies at HBM speed: bit q (0..8) set if metric array q (area_t, area_u,
+// area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t) is not bitwise uniform over
+// [xs-1, xe+1] x [ys-1, ye+1] (every point a step reads it at); bits 9, 10
+// if gphiu / gphiv are not uniform over the whole array; bit 11 / 12 if a
+// Flather face in u / v reads another Flather face; bit 13 if one would read
+// outside the array (time_step.cpp's Flather loops are serial in those
+// cases).  The reference values (the region's first point, gphi's first
+// element) are compared as bit patterns.
+struct ScanIn {
+  const double* metric[9];
+  const double* gphi[2];
+  const int* m;
+  int xs, xe, ys, ye, W, H;
+};
+enum : unsigned { kScanChainU = 1u << 11, kScanChainV = 1u << 12, kScanOutside = 1u << 13 };
+
+__global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
+  const int W = in.W;
+  const size_t o = (size_t)(in.ys - 1) * W + (in.xs - 1);
+  unsigned long long ref[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) ref[q] = __double_as_longlong(in.metric[q][o]);
+  const unsigned long long g0 = __double_as_longlong(in.gphi[0][0]);
+  const unsigned long long g1 = __double_as_longlong(in.gphi[1][0]);
+  const int* m = in.m;
   auto writes = [m](int c, int step) {
     return m[c] + m[c + step] > -1 && (m[c] < 0 || m[c + step] < 0);
   };
-  std::atomic<bool> chain_u{false}, chain_v{false}, outside{false};
-  parallel_chunks(r.ys - 1, r.ye + 2, [&](long long j0, long long j1) {
-    for (long long j = j0; j < j1; j++)
-      for (int i = r.xs - 1; i <= r.xe; i++) {
-        const int c = (int)j * W + i;
-        if (!writes(c, 1)) continue;
-        const int nb = m[c] < 0 ? i + 1 : i - 1;
-        if (nb < 0) {
-          outside.store(true, std::memory_order_relaxed);
-          continue;
+  unsigned f = 0;
+  const int nx = in.xe - in.xs + 3, ny = in.ye - in.ys + 3;
+  const long long nr = (long long)nx * ny;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nr; t += stride) {
+    const int j = in.ys - 1 + (int)(t / nx), i = in.xs - 1 + (int)(t % nx);
+    const int c = j * W + i;
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+      if ((unsigned long long)__double_as_longlong(in.metric[q][c]) != ref[q]) f |= 1u << q;
+    if (i <= in.xe && writes(c, 1)) {  // Flather u over [xs-1, xe] x [ys-1, ye+1]
+      const int nb = m[c] < 0 ? i + 1 : i - 1;
+      if (nb < 0)
+        f |= kScanOutside;
+      else if (nb >= in.xs - 1 && nb <= in.xe && writes(j * W + nb, 1))
+        f |= kScanChainU;
+    }
+    if (j <= in.ye && writes(c, W)) {  // Flather v over [xs-1, xe+1] x [ys-1, ye]
+      const int nb = m[c] < 0 ? j + 1 : j - 1;
+      if (nb < 0)
+        f |= kScanOutside;
+      else if (nb >= in.ys - 1 && nb <= in.ye && writes(nb * W + i, W))
+        f |= kScanChainV;
+    }
+  }
+  const long long n = (long long)W * in.H;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += stride) {
+    if ((unsigned long long)__double_as_longlong(in.gphi[0][t]) != g0) f |= 1u << 9;
+    if ((unsigned long long)__double_as_longlong(in.gphi[1][t]) != g1) f |= 1u << 10;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+__global__ void k_fill(double* __restrict__ a, double v, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x)
+    a[t] = v;
+}
+
+// The Coriolis sines sin(gphi * d2r) on the device and the fused path's
+// preconditions (uniform metrics, no chained Flather faces), from the
+// device copies of the grid.  A latitude uniform over the array takes one
+// host sin per direction (the host libm, as the reference evaluates it);
+// otherwise every point is evaluated on the host.
+bool upload_sines(double d2r) {
+  State& s = g_state;
+  const Registration& r = s.reg;
+  const size_t n = (size_t)r.width * r.height;
+  if (!s.scan && !CK(cudaMalloc(&s.scan, 4 * sizeof(double)))) return false;
+  ScanIn in{};
+  const double* g[11] = {s.dev.area_t, s.dev.area_u, s.dev.area_v, s.dev.dx_u,  s.dev.dx_v,
+                         s.dev.dx_t,   s.dev.dy_u,   s.dev.dy_v,   s.dev.dy_t,  s.dev.gphiu,
+                         s.dev.gphiv};
+  for (int q = 0; q < 9; q++) in.metric[q] = g[q];
+  in.gphi[0] = g[9];
+  in.gphi[1] = g[10];
+  in.m = s.dev.tmask;
+  in.xs = r.xs, in.xe = r.xe, in.ys = r.ys, in.ye = r.ye, in.W = r.width, in.H = r.height;
+  unsigned* d_flags = reinterpret_cast<unsigned*>(s.scan);
+  if (!CK(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s.stream))) return false;
+  k_register_scan<<<152 * 8, 256, 0, s.stream>>>(in, d_flags);
+  if (!CK(cudaGetLastError())) return false;
+  // the reference values: the region's first point of each metric array,
+  // the first element of each latitude array
+  const size_t o = (size_t)(r.ys - 1) * r.width + (r.xs - 1);
+  double refs[11];
+  unsigned flags = 0;
+  for (int q = 0; q < 11; q++)
+    if (!CK(cudaMemcpyAsync(&refs[q], g[q] + (q < 9 ? o : 0), 8, cudaMemcpyDeviceToHost,
+                            s.stream)))
+      return false;
+  if (!CK(cudaMemcpyAsync(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s.stream)) ||
+      !CK(cudaStreamSynchronize(s.stream)))
+    return false;
+  double* um[9] = {&s.um.area_t, &s.um.area_u, &s.um.area_v, &s.um.dx_u, &s.um.dx_v,
+                   &s.um.dx_t,   &s.um.dy_u,   &s.um.dy_v,   &s.um.dy_t};
+  for (int q = 0; q < 9; q++) *um[q] = refs[q];
+  bool uniform = (flags & 0x1ffu) == 0;
+  if ((flags & (3u << 9)) == 0) {
+    s.um.sin_u = std::sin(refs[9] * d2r);
+    s.um.sin_v = std::sin(refs[10] * d2r);
+    k_fill<<<152 * 8, 256, 0, s.stream>>>(s.dev.sin_u, s.um.sin_u, n);
+    k_fill<<<152 * 8, 256, 0, s.stream>>>(s.dev.sin_v, s.um.sin_v, n);
+    if (!CK(cudaGetLastError())) return false;
+  } else {
+    // per-point latitudes: the host libm on every point, the fused path
+    // only if the sines are uniform over the region the step reads
+    std::unique_ptr<double[]> su(new double[n]), sv(new double[n]);
+    host_sines((const double*)r.host[kNumFields + 10], n, d2r, su.get());
+    host_sines((const double*)r.host[kNumFields + 11], n, d2r, sv.get());
+    if (!CK(cudaMemcpy(s.dev.sin_u, su.get(), n * 8, cudaMemcpyHostToDevice)) ||
+        !CK(cudaMemcpy(s.dev.sin_v, sv.get(), n * 8, cudaMemcpyHostToDevice)))
+      return false;
+    const int W = r.width;
+    auto uniform_over = [&](const double* a, double& v) {
+      v = a[o];
+      uint64_t ref;
+      memcpy(&ref, &v, 8);
+      std::atomic<bool> ok{true};
+      parallel_chunks(r.ys - 1, r.ye + 2, [&, ref](long long j0, long long j1) {
+        for (long long j = j0; j < j1 && ok.load(std::memory_order_relaxed); j++) {
+          const uint64_t* row = reinterpret_cast<const uint64_t*>(a + (size_t)j * W);
+          uint64_t diff = 0;  // bitwise equality, branch-free along the row
+          for (int i = r.xs - 1; i <= r.xe + 1; i++) diff |= row[i] ^ ref;
+          if (diff) {
+            ok.store(false, std::memory_order_relaxed);
+            return;
+          }
         }
-        if (nb >= r.xs - 1 && nb <= r.xe && writes((int)j * W + nb, 1))
-          chain_u.store(true, std::memory_order_relaxed);
-      }
-  });
-  parallel_chunks(r.ys - 1, r.ye + 1, [&](long long j0, long long j1) {
-    for (long long j = j0; j < j1; j++)
-      for (int i = r.xs - 1; i <= r.xe + 1; i++) {
-        const int c = (int)j * W + i;
-        if (!writes(c, W)) continue;
-        const int nb = m[c] < 0 ? (int)j + 1 : (int)j - 1;
-        if (nb < 0) {
-          outside.store(true, std::memory_order_relaxed);
-          continue;
-        }
-        if (nb >= r.ys - 1 && nb <= r.ye && writes(nb * W + i, W))
-          chain_v.store(true, std::memory_order_relaxed);
-      }
-  });
-  s.chain_u = chain_u.load();
-  s.chain_v = chain_v.load();
-  s.fused_ok = uniform && !outside.load() && !s.chain_u && !s.chain_v;
+      });
+      return ok.load();
+    };
+    uniform &= uniform_over(su.get(), s.um.sin_u);
+    uniform &= uniform_over(sv.get(), s.um.sin_v);
+  }
+  s.sin_d2r = d2r;
+  s.chain_u = (flags & kScanChainU) != 0;
+  s.chain_v = (flags & kScanChainV) != 0;
+  s.fused_ok = uniform && (flags & kScanOutside) == 0 && !s.chain_u && !s.chain_v;
   return true;
 }
 
@@ -782,7 +849,8 @@ void nl2d_finalize(void) {
   if (s.partials) cudaFree(s.partials);
   if (s.sums) cudaFree(s.sums);
   if (s.tide_table) cudaFree(s.tide_table);
-  s.partials = s.sums = s.tide_table = nullptr;
+  if (s.scan) cudaFree(s.scan);
+  s.partials = s.sums = s.tide_table = s.scan = nullptr;
   s.sums_cap = s.tide_cap = 0;
   if (s.stream) cudaStreamDestroy(s.stream);
   s.stream = nullptr;

@@ -125,6 +125,20 @@ def test_benchmark_size_bitwise(gpulib, oracle):
     assert_fields_equal(m, want, "4096^2")
 
 
+def test_varying_latitude_takes_the_reference_path(gpulib, oracle):
+    """Latitudes that vary over the grid: the Coriolis sines are evaluated
+    per point with the host libm, the fused path does not apply, and the
+    reference-structured steps stay bit-identical to the oracle."""
+    m = T.make_model(40, 33, 1, oracle=oracle)
+    for k in ("gphiu", "gphiv"):
+        m.grid[k][:] = 40.0 + 0.3 * np.arange(m.height)[:, None]
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 30)
+    paths = T.gpu_run_calls(gpulib, m, 30, mode=0)
+    assert set(paths) == {1}, paths
+    assert_fields_equal(m, want, "varying latitude")
+
+
 def test_chained_flather_mask_uses_reference_path(gpulib, oracle):
     """A one-cell-wide wet column between two open columns makes a Flather
     face read another Flather face; the library then keeps to the ordered
