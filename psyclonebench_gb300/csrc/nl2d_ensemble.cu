@@ -87,7 +87,7 @@ __global__ void k_mixed_statics(const double* __restrict__ ht, const double* __r
 // Ensemble: a persistent grid walks a tile list spanning many independent
 // domains; CTA b takes tiles [first[b], first[b+1]).  `tides` holds this
 // step's bc_ssh value per domain.
-__global__ void __launch_bounds__(NTHREADS)
+__global__ void __launch_bounds__(NTHREADS, 2)
     k_ensemble_step(const EnsDomain* __restrict__ doms, const int4* __restrict__ tiles,
                     const int* __restrict__ first, int parity,
                     const double* __restrict__ tides) {

@@ -32,7 +32,7 @@
 namespace nl2d {
 namespace {
 
-__global__ void __launch_bounds__(NTHREADS)
+__global__ void __launch_bounds__(NTHREADS, 2)
     k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
   extern __shared__ double smem[];

@@ -240,6 +240,58 @@ enum { B_FLXU, B_FLXV, B_GX, B_GY, B_FXU, B_FYV, B_VSC, B_FYU, B_QY, B_UWC, B_FX
 constexpr size_t kSmemBytes =
     sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * (S0 + TX * TY + 1);
 
+// A regular cell's new (sshn_t, un, vn) from the tile's staged fields (a0)
+// and shared terms (b1) at its slots q (phase 0) and r (phase 1): continuity
+// (continuity_kern.c:90-117) and unmasked momentum
+// (momentum_u_kern.c:184-261, momentum_v_kern.c:159-239) in the
+// reference's operation order.  sau, rhu, sav, rhv: ssha_u, RN(1 / (hu +
+// ssha_u)), ssha_v, RN(1 / (hv + ssha_v)) at the cell.
+struct RegOut {
+  double ssh, u, v;
+};
+__device__ __forceinline__ RegOut regular_cell(const double* a0, const double* b1, int q, int r,
+                                               double sau, double rhu, double sav, double rhv,
+                                               const FastConst& k) {
+#define A(qq, t) a0[(qq) * S0 + (t)]
+#define B(qq, t) b1[(qq) * S1 + (t)]
+  RegOut o;
+  const double snc = A(A_SN, q), Hu = A(A_HUS, q), Hv = A(A_HVS, q);
+  const double ssh = (((B(B_FLXU, r - 1) - B(B_FLXU, r)) + B(B_FLXV, r - P1X)) - B(B_FLXV, r)) *
+                     k.rdt;
+  o.ssh = snc + dvc(ssh, k.area_t, k.r_area_t, k.fast_div);
+  {
+    const double adv = ((B(B_FXU, r) - B(B_FXU, r + 1)) + B(B_FYU, r)) - B(B_FYU, r + P1X);
+    const double dudy_s = B(B_QY, r) * ((Hu + A(A_HU, q - SX)) + A(A_SU, q - SX));
+    const double dudy_n = B(B_QY, r + P1X) * ((Hu + A(A_HU, q + SX)) + A(A_SU, q + SX));
+    double vis = (B(B_GX, r + 1) - B(B_GX, r)) * k.dy_u + half((dudy_n - dudy_s) * k.dx_u);
+    vis = k.visc * vis;
+    const double cor = (half(k.cor_u * (B(B_VSC, r) + B(B_VSC, r + P1X))) * k.area_u) * Hu;
+    const double hpg = ((k.neg_g * Hu) * k.dy_u) * (A(A_SN, q + 1) - snc);
+    const double num =
+        A(A_UN, q) * Hu +
+        dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_u, k.r_area_u, k.fast_div);
+    const double t1 = dvf(num, A(A_HU, q) + sau, rhu);
+    o.u = dvc(t1, k.fric, k.r_fric, k.fast_div);
+  }
+  {
+    const double adv = ((B(B_FXV, r) - B(B_FXV, r + 1)) + B(B_FYV, r)) - B(B_FYV, r + P1X);
+    const double dvdx_w = B(B_QX, r) * ((Hv + A(A_HV, q - 1)) + A(A_SV, q - 1));
+    const double dvdx_e = B(B_QX, r + 1) * ((Hv + A(A_HV, q + 1)) + A(A_SV, q + 1));
+    double vis = (B(B_GY, r + P1X) - B(B_GY, r)) * k.dx_v + half((dvdx_e - dvdx_w) * k.dy_v);
+    vis = k.visc * vis;
+    const double cor = (-half(k.cor_v * (B(B_UWC, r + 1) + B(B_UWC, r))) * k.area_v) * Hv;
+    const double hpg = ((k.neg_g * Hv) * k.dx_v) * (A(A_SN, q + SX) - snc);
+    const double num =
+        A(A_VN, q) * Hv +
+        dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_v, k.r_area_v, k.fast_div);
+    const double t1 = dvf(num, A(A_HV, q) + sav, rhv);
+    o.v = dvc(t1, k.fric, k.r_fric, k.fast_div);
+  }
+#undef A
+#undef B
+  return o;
+}
+
 // One tile of the fused step: cells [i0, i0+TX) x [j0, j0+TY) of the copy
 // region of one domain.  `tide` is this step's bc_ssh value.
 __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs, const Dims& d,
@@ -366,72 +418,63 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   }
   __syncthreads();
 
-  for (int row = threadIdx.y; row < TY; row += ROWS_PER_PASS) {
-  const int i = i0 + threadIdx.x, j = j0 + row;
-  if (i > d.xe + 1 || j > d.ye) continue;
-  const int c = j * W + i;
-  const int q = (row + HALO) * SX + (threadIdx.x + HALO);
-  const int r = (row + 1) * P1X + (threadIdx.x + 1);
-
-  bool regular = i >= d.xs && i <= d.xe - 1 && j >= d.ys && j <= d.ye - 1;
-  if (regular) {
-#pragma unroll
-    for (int dj = -1; dj <= 1; dj++)
-#pragma unroll
-      for (int di = -1; di <= 1; di++) regular &= mk[q + dj * SX + di] > 0;
-  }
-
-  if (!regular) {
-    // queued for the packed general pass below, so that a warp holding a
-    // few boundary cells does not run both paths
-    glist[atomicAdd(gcount, 1)] = row * TX + threadIdx.x;
-    continue;
-  }
+  // Each thread owns the cells (i, j0 + row) of its rows.  Regular cells
+  // (wet 3x3 neighbourhood: continuity without bc_ssh, unmasked momentum, no
+  // solid-wall or Flather change) are computed here; the others are queued
+  // for the packed general pass below, so that a warp holding a few boundary
+  // cells does not run both paths.  When both of a thread's cells are
+  // regular they are computed in one straight-line block, so the compiler
+  // can interleave two independent FP64 chains; the per-face global inputs
+  // are loaded first and the results stored last, so no store can alias a
+  // later load.
+  static_assert(TY == 2 * ROWS_PER_PASS, "two rows per thread");
   {
-    // Wet cell whose 3x3 neighbourhood is wet: continuity without bc_ssh,
-    // unmasked momentum, no solid-wall or Flather change.
-    const double snc = A(A_SN, q), Hu = A(A_HUS, q), Hv = A(A_HVS, q);
-    double ssh = (((B(B_FLXU, r - 1) - B(B_FLXU, r)) + B(B_FLXV, r - P1X)) - B(B_FLXV, r)) *
-                 k.rdt;
-    fs.sshn_out[c] = snc + dvc(ssh, k.area_t, k.r_area_t, k.fast_div);
-
-    // u-momentum (momentum_u_kern.c:184-261)
-    {
-      const double adv = ((B(B_FXU, r) - B(B_FXU, r + 1)) + B(B_FYU, r)) - B(B_FYU, r + P1X);
-      const double dudy_s =
-          B(B_QY, r) * ((Hu + A(A_HU, q - SX)) + A(A_SU, q - SX));
-      const double dudy_n =
-          B(B_QY, r + P1X) * ((Hu + A(A_HU, q + SX)) + A(A_SU, q + SX));
-      double vis = (B(B_GX, r + 1) - B(B_GX, r)) * k.dy_u + half((dudy_n - dudy_s) * k.dx_u);
-      vis = k.visc * vis;
-      const double cor = (half(k.cor_u * (B(B_VSC, r) + B(B_VSC, r + P1X))) * k.area_u) * Hu;
-      const double hpg = ((k.neg_g * Hu) * k.dy_u) * (A(A_SN, q + 1) - snc);
-      const double num = A(A_UN, q) * Hu +
-                         dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_u, k.r_area_u,
-                             k.fast_div);
-      const double t1 = dvf(num, A(A_HU, q) + f.ssha_u[c], f.r_hu[c]);
-      fs.un_out[c] = dvc(t1, k.fric, k.r_fric, k.fast_div);
+    const int i = i0 + threadIdx.x;
+    int c[2], q[2], r[2];
+    bool reg[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int row = threadIdx.y + e * ROWS_PER_PASS, j = j0 + row;
+      c[e] = j * W + i;
+      q[e] = (row + HALO) * SX + (threadIdx.x + HALO);
+      r[e] = (row + 1) * P1X + (threadIdx.x + 1);
+      const bool live = i <= d.xe + 1 && j <= d.ye;
+      bool regular = live && i >= d.xs && i <= d.xe - 1 && j >= d.ys && j <= d.ye - 1;
+      if (regular) {
+#pragma unroll
+        for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+          for (int di = -1; di <= 1; di++) regular &= mk[q[e] + dj * SX + di] > 0;
+      }
+      reg[e] = regular;
+      if (live && !regular) glist[atomicAdd(gcount, 1)] = row * TX + threadIdx.x;
     }
-    // v-momentum (momentum_v_kern.c:159-239)
-    {
-      const double adv = ((B(B_FXV, r) - B(B_FXV, r + 1)) + B(B_FYV, r)) - B(B_FYV, r + P1X);
-      const double dvdx_w = B(B_QX, r) * ((Hv + A(A_HV, q - 1)) + A(A_SV, q - 1));
-      const double dvdx_e = B(B_QX, r + 1) * ((Hv + A(A_HV, q + 1)) + A(A_SV, q + 1));
-      double vis =
-          (B(B_GY, r + P1X) - B(B_GY, r)) * k.dx_v + half((dvdx_e - dvdx_w) * k.dy_v);
-      vis = k.visc * vis;
-      const double cor = (-half(k.cor_v * (B(B_UWC, r + 1) + B(B_UWC, r))) * k.area_v) * Hv;
-      const double hpg = ((k.neg_g * Hv) * k.dx_v) * (A(A_SN, q + SX) - snc);
-      const double num = A(A_VN, q) * Hv +
-                         dvc(k.rdt * (((adv + vis) + cor) + hpg), k.area_v, k.r_area_v,
-                             k.fast_div);
-      const double t1 = dvf(num, A(A_HV, q) + f.ssha_v[c], f.r_hv[c]);
-      fs.vn_out[c] = dvc(t1, k.fric, k.r_fric, k.fast_div);
+    double sau[2], rhu[2], sav[2], rhv[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+      if (reg[e]) {
+        sau[e] = f.ssha_u[c[e]];
+        rhu[e] = f.r_hu[c[e]];
+        sav[e] = f.ssha_v[c[e]];
+        rhv[e] = f.r_hv[c[e]];
+      }
+    RegOut o[2];
+    if (reg[0] && reg[1]) {
+      o[0] = regular_cell(a0, b1, q[0], r[0], sau[0], rhu[0], sav[0], rhv[0], k);
+      o[1] = regular_cell(a0, b1, q[1], r[1], sau[1], rhu[1], sav[1], rhv[1], k);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        if (reg[e]) o[e] = regular_cell(a0, b1, q[e], r[e], sau[e], rhu[e], sav[e], rhv[e], k);
     }
-    continue;
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+      if (reg[e]) {
+        fs.sshn_out[c[e]] = o[e].ssh;
+        fs.un_out[c[e]] = o[e].u;
+        fs.vn_out[c[e]] = o[e].v;
+      }
   }
-
-  }  // rows of this thread
   __syncthreads();
 
   // ---- general cells: the reference's per-point code, in its order ----

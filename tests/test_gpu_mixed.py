@@ -89,3 +89,28 @@ def test_mixed_random_land_vs_fp64(gpulib, oracle):
     assert report["sshn_t"][0] <= 1e-6
     assert report["un"][0] <= 1e-4 * report["un"][2]
     assert report["vn"][0] <= 1e-4 * report["vn"][2]
+
+
+@pytest.mark.parametrize("jphgr,nx,ny", [(2, 97, 61), (3, 75, 130)])
+def test_mixed_other_masks_vs_fp64(gpulib, oracle, jphgr, nx, ny):
+    """The T masks of jphgr_msh 2 and 3 (model_mod.f90:94-249) on odd-sized
+    grids with a padded width: the column march and its general pass against
+    FP64 after 300 steps, same bar."""
+    from psyclonebench_gb300.workloads import fourier_depth
+    m = T.make_model(nx + 2, ny + 2, jphgr, width=nx + 9, oracle=oracle)
+    ht, hu, hv = fourier_depth(m.width, m.height, 5)
+    m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = ht, hu, hv
+    m.rdt = 5.0
+    ref = run_form(gpulib, m.copy(), 300, 0)
+    mix = run_form(gpulib, m.copy(), 300, 1)
+    assert gpulib.nl2d_last_path() in (3, 0)  # the mixed form ran
+    for k, (x0, x1, y0, y1) in (("sshn_t", T.regions(ref)["t"]), ("un", T.regions(ref)["u"]),
+                                ("vn", T.regions(ref)["v"])):
+        a = mix.f[k][y0:y1 + 1, x0:x1 + 1]
+        b = ref.f[k][y0:y1 + 1, x0:x1 + 1]
+        assert np.isfinite(a).all(), k
+        rms = float(np.sqrt(np.mean((a - b) ** 2)))
+        if k == "sshn_t":
+            assert rms <= 1e-6, (k, rms)
+        else:
+            assert rms <= 1e-4 * max(float(np.abs(b).max()), 1e-12), (k, rms)
