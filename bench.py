@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the mixed-precision, ensemble and emulator measurements")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator (config 4)")
-    ap.add_argument("--forms", default="mixed,active,ensemble,tra_adv,emulator",
+    ap.add_argument("--forms", default="mixed,active,sweep,ensemble,tra_adv,emulator",
                     help="comma-separated forms to measure after the headline number")
     ap.add_argument("--form-steps", type=int, default=1000,
                     help="timed steps of the mixed-precision form and its FP64 twin")
@@ -308,6 +308,34 @@ def run_active(lib, n, rest_value, steps=200, warmup=5):
             "value": value, "unit": "Mcell-steps/s", "ms_per_step": ms.value / steps,
             "steps": steps, "warmup": warmup, "ratio_to_rest_start": value / rest_value,
             "checksums": {"ssh": sums[0], "u": sums[1], "v": sums[2]}, "dtype": "f64"}
+
+
+def run_sweep(lib, sizes=(256, 512, 1024, 2048, 4096, 8192)):
+    """Config 1's sweep of interior sizes (the reference's
+    scripts/problemsize.sh:15-22 edits the namelist's jpiglo / jpjglo): the
+    FP64 step and the mixed form at each size, device-resident, from the
+    reference's rest start, with about the same number of cell-steps per
+    size."""
+    import nl2d_testlib as T
+    import psyclonebench_gb300 as P
+    out = []
+    for n in sizes:
+        m = make_problem(n)
+        T.gpu_register(lib, m)
+        steps = max(20, min(400, int(2e9 / (n * n))))
+        ms = ctypes.c_double(0.0)
+        P.check(lib.nl2d_timed_run(1, 5, ctypes.byref(ms)), "sweep warm-up")
+        P.check(lib.nl2d_timed_run(6, steps, ctypes.byref(ms)), "sweep fp64")
+        fp64 = n * n * steps / (ms.value * 1e-3) / 1e6
+        lib.nl2d_set_precision(1)
+        P.check(lib.nl2d_timed_run(6 + steps, 5, ctypes.byref(ms)), "sweep mixed warm-up")
+        P.check(lib.nl2d_timed_run(11 + steps, steps, ctypes.byref(ms)), "sweep mixed")
+        mixed = n * n * steps / (ms.value * 1e-3) / 1e6
+        lib.nl2d_set_precision(0)
+        lib.nl2d_finalize()
+        del m
+        out.append({"interior": n, "steps": steps, "fp64": fp64, "mixed": mixed})
+    return {"unit": "Mcell-steps/s", "sizes": out}
 
 
 def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
@@ -650,6 +678,8 @@ def run_ours(args, rank, world, local):
             forms.update(run_forms(lib, n, steps=args.form_steps))
         if "active" in want:
             forms["fp64_active"] = run_active(lib, n, value)
+        if "sweep" in want:
+            forms["size_sweep"] = run_sweep(lib)
         if "ensemble" in want:
             ens = run_ensemble(lib)
             ens["fp64"]["speedup_vs_single_4096_domain_fp64"] = ens["fp64"]["value"] / value

@@ -30,11 +30,12 @@ namespace {
 
 // The regular cells: one warp per MW columns x MR rows of the copy region.
 __global__ void __launch_bounds__(32 * MARCH_WARPS)
-    k_mixed_march(MixedFields mf, MixedState ms, Dims d, MixConst k, int ncol, int nwarps) {
+    k_mixed_march(MixedFields mf, MixedState ms, Dims d, MixConst k, int ncol, int nwarps,
+                  int mr) {
   const int warp = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (warp >= nwarps) return;  // the whole warp leaves together
   const int gy = warp / ncol, gx = warp - gy * ncol;
-  mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * MR, 0);
+  mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * mr, 0, mr);
 }
 
 // The copy region's other cells, one thread per listed cell.
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS)
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
   const Dims d = doms[u.x].d;
-  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off);
+  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, MR);
 }
 
 // The other cells of every domain's copy region: glist[t] = (domain, cell).
@@ -153,9 +154,14 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
                        const double* tide_table, int tide_index, cudaStream_t st) {
   const MixConst k = make_mix_const(s, um);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const int ncol = (nx + MW - 1) / MW, nrow = (ny + MR - 1) / MR, nwarps = ncol * nrow;
+  // Strips of MR rows, halved (down to 8) until the grid holds about two
+  // waves of warps: a smaller domain trades halo rows for parallelism.
+  const int ncol = (nx + MW - 1) / MW;
+  int mr = MR;
+  while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 5 * MARCH_WARPS) mr /= 2;
+  const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
   k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-      mf, ms, d, k, ncol, nwarps);
+      mf, ms, d, k, ncol, nwarps, mr);
   if (mf.gcount > 0)
     k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
                                                              tide_index, tide);

@@ -28,7 +28,7 @@ namespace mixk {
 namespace {
 
 constexpr int MW = 30;  // output columns per warp
-constexpr int MR = 32;  // output rows per warp
+constexpr int MR = 32;  // output rows per warp (at most; smaller domains take shorter strips)
 constexpr int MARCH_WARPS = 4;
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -150,16 +150,16 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
   return t;
 }
 
-// One warp: lane L holds column i0-1+L; output rows j0 .. j0+MR-1 of the
+// One warp: lane L holds column i0-1+L; output rows j0 .. j0+mr-1 of the
 // copy region, regular cells only.  `base`: the domain's first element in
 // the arrays (an ensemble packs its domains back to back; 0 otherwise).
 __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedState& ms,
                                             const Dims& d, const MixConst& k, int i0, int j0,
-                                            size_t base) {
+                                            size_t base, int mr) {
   const int lane = threadIdx.x & 31;
   const int W = d.width, H = d.height;
   const int i = i0 - 1 + lane;
-  const int jend = min(j0 + MR, d.ye + 1);
+  const int jend = min(j0 + mr, d.ye + 1);
   const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
   MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H, base), k);
   MRow C = finish_row(load_raw(mf, ms, i, j0, W, H, base), k);
