@@ -574,9 +574,11 @@ def run_reference(args, rank, world):
         "metric": "Mcell-steps/s", "value": val, "unit": "Mcell-steps/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
         "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state)",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (reference initial state: rest, constant depth)",
         "config": {"workload": "nemolite2d_fp64_%dx%d" % (n, n), "interior": [n, n],
-                   "jphgr_msh": 1, "rdt": 20.0, "parallelism": "replicas"},
+                   "jphgr_msh": 1, "rdt": 20.0, "width": m.width,
+                   "parallelism": "single (rank 0, all host cores)"},
         "cpu_baseline": {"value": val, "unit": "Mcell-steps/s", "cores": cores,
                          "kind": kind, "sample": "%d steps of the %dx%d domain (%s)" % (
                              steps, n, n, desc)},
