@@ -189,8 +189,8 @@ class ClockSampler:
 
 
 def load_profile_figures():
-    """Per-launch DRAM traffic and FP64 instruction counts of the fused
-    kernel from the committed ncu summary, if present."""
+    """DRAM bytes and FP64 thread-instructions per cell of the fused kernel,
+    per start state ("rest", "active"), from the committed ncu summary."""
     p = os.path.join(REPO, "profiles", "fused_fp64_step.json")
     try:
         with open(p) as f:

@@ -250,7 +250,7 @@ __global__ void k_fill(double* __restrict__ a, double v, size_t n) {
 // device copies of the grid.  A latitude uniform over the array takes one
 // host sin per direction (the host libm, as the reference evaluates it);
 // otherwise every point is evaluated on the host.
-bool upload_sines(double d2r) {
+bool scan_grid(double d2r) {
   State& s = g_state;
   const Registration& r = s.reg;
   const size_t n = (size_t)r.width * r.height;
@@ -392,7 +392,7 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
     return false;
   if (!CK(cudaStreamSynchronize(s.stream))) return false;
   s.sc = sc;
-  if (!upload_sines(sc.d2r)) return false;
+  if (!scan_grid(sc.d2r)) return false;
   s.cur = 0;
   s.consistent = false;
   s.shadows_synced = false;
@@ -743,7 +743,7 @@ void c_invoke_time_step(double* ssha_t, double* sshn_t, double* sshn_u, double* 
       return;
   } else {
     s.sc = sc;
-    if (!(d2r == s.sin_d2r) && !upload_sines(d2r)) return;
+    if (!(d2r == s.sin_d2r) && !scan_grid(d2r)) return;
   }
   one_step(istep);
 }
@@ -826,7 +826,7 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
     launch_depth_reciprocals(s.dev, dims(), s.stream);
     if (!CK(cudaGetLastError())) return;
   }
-  if (k >= kNumFields && !upload_sines(s.sc.d2r)) return;
+  if (k >= kNumFields && !scan_grid(s.sc.d2r)) return;
   if (blocking) CK(cudaStreamSynchronize(s.stream));
 }
 
