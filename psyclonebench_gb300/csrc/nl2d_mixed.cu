@@ -43,7 +43,17 @@ __global__ void __launch_bounds__(128)
     k_mixed_general(MixedFields mf, MixedState ms, Fields f, Dims d, MixConst k,
                     const double* __restrict__ tide_table, int tide_index, double tide) {
   const double td = tide_table ? tide_table[tide_index] : tide;
-  GCtx x{mf, ms, f, d, k};
+  __shared__ EnsDom sd;  // the kernel's arguments as one descriptor in memory
+  if (threadIdx.x == 0) {
+    sd.mf = mf;
+    sd.ms[0] = ms;
+    sd.f = f;
+    sd.d = d;
+    sd.k = k;
+    sd.off = 0;
+  }
+  __syncthreads();
+  const GCtx x{sd.mf, sd.ms[0], sd.f, sd.d, sd.k};
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < mf.gcount;
        t += gridDim.x * blockDim.x) {
     const int c = mf.glist[t];

@@ -222,15 +222,28 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
 
 // ---- the other cells of the copy region, on global memory ----------------
 
-// Global-memory view of the tile form's staged values: zeros outside the
-// array, sshn_u / sshn_v by next_ssh{u,v}'s rules inside it (the stored
-// value on faces those kernels never update).
-struct GCtx {
+// One domain of a mixed-precision ensemble (device descriptor).
+struct EnsDom {
   MixedFields mf;
-  MixedState ms;
-  Fields f;
+  MixedState ms[2];
+  Fields f;  // FP64 arrays the mixed step reads where no step writes
   Dims d;
   MixConst k;
+  size_t off;  // the domain's first element in the packed arrays
+};
+
+// Global-memory view of the tile form's staged values: zeros outside the
+// array, sshn_u / sshn_v by next_ssh{u,v}'s rules inside it (the stored
+// value on faces those kernels never update).  The members refer to a
+// domain descriptor held in memory (the ensemble's device array, or a
+// single domain's copy in shared memory), so the context passed to the
+// out-of-line helpers is five pointers, not a copy of the descriptor.
+struct GCtx {
+  const MixedFields& mf;
+  const MixedState& ms;
+  const Fields& f;
+  const Dims& d;
+  const MixConst& k;
   __device__ __forceinline__ bool in(int i, int j) const {
     return i >= 0 && i < d.width && j >= 0 && j < d.height;
   }
@@ -425,16 +438,6 @@ __device__ void general_cell(const GCtx& x, int i, int j, double tide) {
   }
   x.ms.vn_out[c] = va;
 }
-
-// One domain of a mixed-precision ensemble (device descriptor).
-struct EnsDom {
-  MixedFields mf;
-  MixedState ms[2];
-  Fields f;  // FP64 arrays the mixed step reads where no step writes
-  Dims d;
-  MixConst k;
-  size_t off;  // the domain's first element in the packed arrays
-};
 
 // Whether the march updates cell (i, j): interior away from the edges of
 // next_ssh's ranges, 3x3 mask neighbourhood wet.
