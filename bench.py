@@ -730,6 +730,12 @@ def run_ours(args, rank, world, local):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    # The CPU legs (the reference arm, the CPU baselines) run OpenMP on every
+    # host core, one thread per core, threads kept close (OpenMP reads these
+    # when the CPU library is first loaded, always after this point).
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:
