@@ -663,10 +663,11 @@ def run_ours(args, rank, world, local):
         # FP64 thread-instructions per cell from the ncu capture of the same
         # start state (the count depends on it: zero dividends skip the
         # division's FP64 work)
+        gops = fig["fp64_ops_per_cell"] * cells / (ms_step * 1e-3) / 1e9
+        peak = prof.get("fp64_peak_gops")
         roof["fp64"] = {
-            "achieved_gops": fig["fp64_ops_per_cell"] * cells / (ms_step * 1e-3) / 1e9,
-            "ops_per_cell": fig["fp64_ops_per_cell"],
-            "peak_gops": prof.get("fp64_peak_gops"),
+            "achieved_gops": gops, "ops_per_cell": fig["fp64_ops_per_cell"],
+            "peak_gops": peak, "frac": gops / peak if peak else None,
             "profile": fig.get("source"),
         }
 
