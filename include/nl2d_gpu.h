@@ -317,6 +317,13 @@ int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
  * out[2] = the two counts.  Returns 0, or 1 on a CUDA error. */
 int nl2d_selftest_intfp(long long n, unsigned long long seed, long long *out);
 
+/* Test hook (no reference counterpart): one thread waits, through the
+ * convolution kernels' bounded mbarrier wait, on a barrier that nothing
+ * arrives on; after max_cycles (1 .. 2^32 clocks) the wait gives up and
+ * sets the error flag.  *status = 1 then (2 would mean the phase completed,
+ * 0 that the flag was not set).  The context stays usable. */
+int nl2d_selftest_wait(long long max_cycles, int *status);
+
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
 

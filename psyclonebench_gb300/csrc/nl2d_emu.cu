@@ -112,9 +112,10 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
       : "memory");
 }
 // Waits for the phase with the given parity to complete; false if the wait
-// ran out (flag and error set) or another role aborted.
+// ran out after max_cycles (flag and error set) or another role aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          volatile int* abort_flag, int* err) {
+                                          volatile int* abort_flag, int* err,
+                                          long long max_cycles = kMaxWaitCycles) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t ok;
@@ -126,12 +127,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
         : "memory");
     if (ok) return true;
     if (*abort_flag) return false;
-    if (clock64() - t0 > kMaxWaitCycles) {
+    if (clock64() - t0 > max_cycles) {
       *abort_flag = 1;
       atomicExch(err, 1);
       return false;
     }
   }
+}
+
+// The failure path of the bounded waits, exercised on purpose: one thread
+// waits on a barrier that nothing arrives on, gives up after max_cycles,
+// sets the error flag and returns (err = 2 would mean the phase completed).
+__global__ void k_selftest_wait(long long max_cycles, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && mbar_wait(&bar, 0, &abort_flag, err, max_cycles)) atomicExch(err, 2);
 }
 
 struct StripWalk {  // work unit u -> (image, first row, rows, column segment)
@@ -834,6 +850,20 @@ __global__ void k_advance(float* __restrict__ state, const float* __restrict__ i
 using namespace nl2d::emu;
 
 extern "C" {
+
+// Test hook (no reference counterpart): runs k_selftest_wait and returns
+// its status in *status: 1 when the wait ran out and reported it, as the
+// convolution kernels' waits do.
+int nl2d_selftest_wait(long long max_cycles, int* status) {
+  if (!status || max_cycles < 1 || max_cycles > (1LL << 32)) return NL2D_ERR_ARGS;
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return NL2D_ERR_CUDA;
+  cudaMemset(d, 0, sizeof(int));
+  k_selftest_wait<<<1, 32>>>(max_cycles, d);
+  const cudaError_t e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
+}
 
 // 3x3 convolution (stride 1, zero padding 1) of a batch of NHWC BF16
 // images on the tensor cores.  cin, cout: multiples of 16, cout <= 64;

@@ -261,3 +261,15 @@ def test_advance_applies_the_solver_boundary_conditions(gpulib, small_dataset):
         w[st[:, 3] > 0, 2] = 0.0
         assert (st[:, 1] > 0).any()
         np.testing.assert_allclose(got[q], w, rtol=1e-6, atol=1e-6)
+
+
+def test_bounded_wait_runs_out_and_reports(gpulib):
+    """The tcgen05 kernels' mbarrier waits are bounded: a wait on a barrier
+    that nothing arrives on gives up after its limit (here 2^22 clocks, about
+    2 ms), sets the error flag the host reads and returns; the context stays
+    usable, so a convolution afterwards still matches its FP64 reference."""
+    import ctypes
+    st = ctypes.c_int(-1)
+    assert gpulib.nl2d_selftest_wait(1 << 22, ctypes.byref(st)) == 0
+    assert st.value == 1
+    test_conv3x3_tcgen05_matches_fp64(gpulib, 16, 16, 0, 2, 5)
