@@ -324,6 +324,19 @@ int nl2d_selftest_intfp(long long n, unsigned long long seed, long long *out);
  * 0 that the flag was not set).  The context stays usable. */
 int nl2d_selftest_wait(long long max_cycles, int *status);
 
+/* Checkpoint / resume (no reference counterpart; the reference keeps no
+ * restart files).  nl2d_checkpoint_write stores the registered problem's 13
+ * fields exactly as c_read_from_device returns them (FP64, row-major
+ * [height][width], c_invoke_time_step's order), the extents and `istep`
+ * (the caller's next step number) in `path`.  nl2d_checkpoint_read loads
+ * such a file into the registered problem (same extents, else
+ * NL2D_ERR_ARGS; not a checkpoint: NL2D_ERR_PARSE; I/O: NL2D_ERR_IO) and
+ * returns the stored istep; the next step is then reference-structured, as
+ * after c_write_to_device, so a resumed run equals the uninterrupted one
+ * bit for bit.  The grid comes from the caller's own set-up. */
+int nl2d_checkpoint_write(const char *path, int istep);
+int nl2d_checkpoint_read(const char *path, int *istep);
+
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
 

@@ -81,6 +81,8 @@ EXPORTS = {
     "nl2d_ens_export_interior": (ctypes.c_int, [_VP]),
     "nl2d_ens_uses_march": (ctypes.c_int, []),
     "nl2d_selftest_wait": (ctypes.c_int, [ctypes.c_longlong, _IP]),
+    "nl2d_checkpoint_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "nl2d_checkpoint_read": (ctypes.c_int, [ctypes.c_char_p, _IP]),
     "nl2d_ens_import_interior": (ctypes.c_int, [_VP]),
     "nl2d_read_namelist": (ctypes.c_int, [ctypes.c_char_p, _IP, _DP]),
     "nl2d_setup_model": (ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 3 +

@@ -830,6 +830,115 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
   if (blocking) CK(cudaStreamSynchronize(s.stream));
 }
 
+// ---- checkpoint / resume (no reference counterpart) ----
+// A checkpoint is the 13 fields exactly as c_read_from_device returns them
+// (FP64, row-major [height][width], in c_invoke_time_step's order) after an
+// 8-byte magic and eleven int32s: version, width, height, xs, xe, ys, ye,
+// istep, field count, two reserved.  The grid (mask, metrics) is not in it:
+// it comes from the namelist and set-up the caller repeats.
+struct CheckpointHeader {
+  char magic[8];
+  int32_t version, width, height, xs, xe, ys, ye, istep, nfields, reserved[2];
+};
+constexpr char kCheckpointMagic[8] = {'N', 'L', '2', 'D', 'C', 'K', 'P', '1'};
+
+int nl2d_checkpoint_write(const char* path, int istep) {
+  State& s = g_state;
+  CallScope scope;
+  if (!s.registered) {
+    set_error(NL2D_ERR_STATE, "nl2d_checkpoint_write: no problem registered");
+    return scope.rc();
+  }
+  if (!path) {
+    set_error(NL2D_ERR_ARGS, "nl2d_checkpoint_write: path is NULL");
+    return scope.rc();
+  }
+  if (!materialize()) return scope.rc();
+  const Registration& r = s.reg;
+  const size_t n = (size_t)r.width * r.height;
+  std::vector<double> buf(n);
+  FILE* f = fopen(path, "wb");
+  if (!f) {
+    set_error(NL2D_ERR_IO, "nl2d_checkpoint_write: cannot open %s", path);
+    return scope.rc();
+  }
+  CheckpointHeader h{};
+  memcpy(h.magic, kCheckpointMagic, 8);
+  h.version = 1, h.width = r.width, h.height = r.height, h.xs = r.xs, h.xe = r.xe;
+  h.ys = r.ys, h.ye = r.ye, h.istep = istep, h.nfields = kNumFields;
+  bool ok = fwrite(&h, sizeof h, 1, f) == 1;
+  for (int k = 0; k < kNumFields && ok; k++) {
+    ok = CK(cudaMemcpyAsync(buf.data(), device_of(k), n * 8, cudaMemcpyDeviceToHost,
+                            s.stream)) &&
+         CK(cudaStreamSynchronize(s.stream));
+    if (ok) ok = fwrite(buf.data(), 8, n, f) == n;
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok && s.status == NL2D_OK)
+    set_error(NL2D_ERR_IO, "nl2d_checkpoint_write: writing %s", path);
+  return scope.rc();
+}
+
+int nl2d_checkpoint_read(const char* path, int* istep) {
+  State& s = g_state;
+  CallScope scope;
+  if (!s.registered) {
+    set_error(NL2D_ERR_STATE, "nl2d_checkpoint_read: no problem registered");
+    return scope.rc();
+  }
+  if (!path || !istep) {
+    set_error(NL2D_ERR_ARGS, "nl2d_checkpoint_read: NULL argument");
+    return scope.rc();
+  }
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_error(NL2D_ERR_IO, "nl2d_checkpoint_read: cannot open %s", path);
+    return scope.rc();
+  }
+  const Registration& r = s.reg;
+  CheckpointHeader h{};
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kCheckpointMagic, 8) != 0 ||
+      h.version != 1 || h.nfields != kNumFields) {
+    fclose(f);
+    set_error(NL2D_ERR_PARSE, "nl2d_checkpoint_read: %s is not a checkpoint", path);
+    return scope.rc();
+  }
+  if (h.width != r.width || h.height != r.height || h.xs != r.xs || h.xe != r.xe ||
+      h.ys != r.ys || h.ye != r.ye) {
+    fclose(f);
+    set_error(NL2D_ERR_ARGS, "nl2d_checkpoint_read: %s holds a %dx%d problem, not %dx%d", path,
+              h.width, h.height, r.width, r.height);
+    return scope.rc();
+  }
+  if (!materialize()) {
+    fclose(f);
+    return scope.rc();
+  }
+  const size_t n = (size_t)r.width * r.height;
+  std::vector<double> buf(n);
+  bool ok = true;
+  for (int k = 0; k < kNumFields && ok; k++) {
+    ok = fread(buf.data(), 8, n, f) == n;
+    if (!ok) {
+      set_error(NL2D_ERR_IO, "nl2d_checkpoint_read: %s is truncated", path);
+      break;
+    }
+    ok = CK(cudaMemcpyAsync(device_of(k), buf.data(), n * 8, cudaMemcpyHostToDevice,
+                            s.stream)) &&
+         CK(cudaStreamSynchronize(s.stream));
+  }
+  fclose(f);
+  if (!ok) return scope.rc();
+  // as after c_write_to_device: the next step is reference-structured
+  s.consistent = false;
+  s.shadows_synced = false;
+  s.mixed_valid = s.mixed_ahead = false;
+  launch_depth_reciprocals(s.dev, dims(), s.stream);
+  if (!CK(cudaGetLastError()) || !CK(cudaStreamSynchronize(s.stream))) return scope.rc();
+  *istep = h.istep;
+  return scope.rc();
+}
+
 int nl2d_last_error(char* msg, int msg_len) {
   State& s = g_state;
   const int st = s.status;

@@ -31,11 +31,15 @@ def gpulib():
 
 @pytest.fixture(autouse=True)
 def _fresh_library(request):
-    """Every test that uses the library starts with no problem registered.
+    """Every test that uses the library starts with no problem registered
+    and no sticky error status left by an earlier test.
     The library keys a problem's residency on the caller's host pointers
     (the reference's driver keeps its arrays for the program's life), so a
     model whose arrays land at the addresses of an earlier test's freed
     arrays would otherwise be taken for that earlier registration."""
     if "gpulib" in request.fixturenames:
-        request.getfixturevalue("gpulib").nl2d_finalize()
+        import ctypes
+        lib = request.getfixturevalue("gpulib")
+        lib.nl2d_finalize()
+        lib.nl2d_last_error(ctypes.create_string_buffer(256), 256)  # no status carried over
     yield

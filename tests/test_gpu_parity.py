@@ -125,6 +125,47 @@ def test_benchmark_size_bitwise(gpulib, oracle):
     assert_fields_equal(m, want, "4096^2")
 
 
+def test_checkpoint_resume_is_bitwise(gpulib, oracle, tmp_path):
+    """A run checkpointed after 40 steps and resumed from the file by a fresh
+    registration (the model rebuilt from its set-up, so its host arrays hold
+    the start state) ends with every field bit-identical to the
+    uninterrupted run; a file of other extents or another kind is refused."""
+    import ctypes
+    import psyclonebench_gb300 as P
+    rng = np.random.default_rng(8)
+    m = T.make_model(61, 47, 1, width=64, oracle=oracle)
+    for k in ("ht", "hu", "hv"):
+        m.f[k][:] = rng.uniform(50.0, 500.0, size=m.f[k].shape)
+    m.rdt = 5.0
+    full = m.copy()
+    T.gpu_run_calls(gpulib, full, 100, mode=0)
+    gpulib.nl2d_finalize()
+    a = m.copy()
+    T.gpu_run_calls(gpulib, a, 40, mode=0)
+    path = str(tmp_path / "ck.bin").encode()
+    assert gpulib.nl2d_checkpoint_write(path, 41) == 0
+    gpulib.nl2d_finalize()
+    b = m.copy()
+    T.gpu_register(gpulib, b)
+    istep = ctypes.c_int(0)
+    assert gpulib.nl2d_checkpoint_read(path, ctypes.byref(istep)) == 0
+    assert istep.value == 41
+    paths = T.gpu_run_calls(gpulib, b, 60, nit000=41, mode=0)
+    assert paths[0] == 1 and set(paths[1:]) == {2}, paths
+    assert_fields_equal(b, full, "resumed")
+    # another problem's extents, and a file that is not a checkpoint
+    gpulib.nl2d_finalize()
+    c = T.make_model(40, 33, 1, oracle=oracle)
+    T.gpu_register(gpulib, c)
+    assert gpulib.nl2d_checkpoint_read(path, ctypes.byref(istep)) == P.NL2D_ERR_ARGS
+    junk = tmp_path / "junk.bin"
+    junk.write_bytes(b"not a checkpoint" * 8)
+    assert gpulib.nl2d_checkpoint_read(str(junk).encode(), ctypes.byref(istep)) == \
+        P.NL2D_ERR_PARSE
+    buf = ctypes.create_string_buffer(256)
+    assert gpulib.nl2d_last_error(buf, 256) == P.NL2D_ERR_PARSE  # the status, then cleared
+
+
 def test_varying_latitude_takes_the_reference_path(gpulib, oracle):
     """Latitudes that vary over the grid: the Coriolis sines are evaluated
     per point with the host libm, the fused path does not apply, and the

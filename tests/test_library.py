@@ -71,3 +71,15 @@ def test_missing_library_fails_loudly(tmp_path):
             P.load_library(str(tmp_path / "nope.so"))
     finally:
         P._lib = saved
+
+
+def test_checkpoint_needs_a_problem(lib, tmp_path):
+    """Without a registered problem both checkpoint calls report
+    NL2D_ERR_STATE and touch no GPU."""
+    import psyclonebench_gb300 as P
+    path = str(tmp_path / "ck.bin").encode()
+    ist = ctypes.c_int(0)
+    assert lib.nl2d_checkpoint_write(path, 1) == P.NL2D_ERR_STATE
+    assert lib.nl2d_checkpoint_read(path, ctypes.byref(ist)) == P.NL2D_ERR_STATE
+    buf = ctypes.create_string_buffer(256)
+    lib.nl2d_last_error(buf, 256)
