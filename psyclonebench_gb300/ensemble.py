@@ -74,6 +74,29 @@ def shard_domains(specs, world):
     return [sorted(p) for p in parts]
 
 
+def gather_results(local, timeout_s=30.0):
+    """Merges every rank's {domain index: result} over the default process
+    group (host side; the domains never exchange data during a run).  A
+    monitored barrier runs first: a rank that died or never reaches the
+    gather makes rank 0 fail within `timeout_s` with Nl2dError naming the
+    ranks that did not report, instead of waiting forever.  Needs the gloo
+    backend (the barrier's failure report is gloo's)."""
+    import datetime
+
+    import torch.distributed as dist
+    try:
+        dist.monitored_barrier(timeout=datetime.timedelta(seconds=timeout_s),
+                               wait_all_ranks=True)
+    except RuntimeError as e:
+        raise Nl2dError("ensemble ranks did not report: %s" % str(e).splitlines()[0]) from e
+    gathered = [None] * dist.get_world_size()
+    dist.all_gather_object(gathered, local)
+    merged = {}
+    for g in gathered:
+        merged.update(g)
+    return merged
+
+
 class Ensemble:
     """A set of domains resident on the GPU.  `domains` are build_domain()
     dicts; all share rdt, cbfr and visc, and dx, dy and latitude unless a

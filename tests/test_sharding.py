@@ -40,12 +40,9 @@ def _rank_main(rank, world, port, out):
     for k in mine:
         _, sums = T.ensemble_oracle_run(build_domain(SPECS[k]), NSTEPS, every=NSTEPS)
         res[k] = [sums[-1]["sshn_t"], sums[-1]["un"], sums[-1]["vn"]]
-    gathered = [None] * world
-    dist.all_gather_object(gathered, res)
+    from psyclonebench_gb300.ensemble import gather_results
+    merged = gather_results(res, timeout_s=60.0)
     if rank == 0:
-        merged = {}
-        for g in gathered:
-            merged.update(g)
         out.put(merged)
     dist.barrier()
     dist.destroy_process_group()
@@ -72,3 +69,45 @@ def test_two_rank_gloo_matches_single_process():
         _, sums = T.ensemble_oracle_run(build_domain(spec), NSTEPS, every=NSTEPS)
         want = [sums[-1]["sshn_t"], sums[-1]["un"], sums[-1]["vn"]]
         assert merged[k] == want
+
+
+def _rank_dies(rank, world, port, out):
+    """Rank 1 fails before the gather (an exception on the host, as a crashed
+    solver process would); rank 0 reports what gather_results raises."""
+    import datetime
+
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=30))
+    from psyclonebench_gb300 import Nl2dError
+    from psyclonebench_gb300.ensemble import gather_results
+    if rank == 1:
+        raise SystemExit(3)
+    try:
+        gather_results({0: [1.0, 2.0, 3.0]}, timeout_s=5.0)
+        out.put("no error")
+    except Nl2dError as e:
+        out.put("Nl2dError: %s" % e)
+
+
+def test_a_dead_rank_is_reported_not_waited_for():
+    """A rank that exits before the gather: the surviving rank gets an
+    Nl2dError naming it within the barrier's timeout (host-side failure
+    detection; no GPU involved)."""
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_dies, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    msg = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+    assert procs[1].exitcode == 3
+    assert msg.startswith("Nl2dError") and "1" in msg, msg
