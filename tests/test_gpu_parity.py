@@ -166,6 +166,28 @@ def test_checkpoint_resume_is_bitwise(gpulib, oracle, tmp_path):
     assert gpulib.nl2d_last_error(buf, 256) == P.NL2D_ERR_PARSE  # the status, then cleared
 
 
+def test_nan_in_a_field_is_reported_by_the_checksums(gpulib, oracle):
+    """A NaN seeded into a host field before upload spreads through the
+    steps (which still run); the checksums then report NL2D_ERR_NONFINITE
+    instead of a number, and a clean problem registered afterwards runs
+    normally."""
+    import ctypes
+    import psyclonebench_gb300 as P
+    m = T.make_model(30, 26, 1, oracle=oracle)
+    m.f["sshn_t"][10, 12] = np.nan
+    T.gpu_register(gpulib, m)
+    out = np.zeros(3)
+    assert gpulib.nl2d_run_steps(1, 5, 0, T.dptr(out)) == 0
+    assert gpulib.nl2d_checksums(T.dptr(out)) == P.NL2D_ERR_NONFINITE
+    buf = ctypes.create_string_buffer(256)
+    assert gpulib.nl2d_last_error(buf, 256) == P.NL2D_ERR_NONFINITE
+    gpulib.nl2d_finalize()
+    c = T.make_model(30, 26, 1, oracle=oracle)
+    T.gpu_register(gpulib, c)
+    assert gpulib.nl2d_run_steps(1, 5, 0, T.dptr(out)) == 0
+    assert gpulib.nl2d_checksums(T.dptr(out)) == 0 and np.isfinite(out).all()
+
+
 def test_varying_latitude_takes_the_reference_path(gpulib, oracle):
     """Latitudes that vary over the grid: the Coriolis sines are evaluated
     per point with the host libm, the fused path does not apply, and the
