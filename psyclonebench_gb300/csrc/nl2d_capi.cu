@@ -733,6 +733,7 @@ void c_invoke_time_step(double* ssha_t, double* sshn_t, double* sshn_u, double* 
                         int internal_xstop, int internal_ystart, int internal_ystop,
                         int width, int height, double rdt, double cbfr, double visc,
                         double omega, double d2r, double g) {
+  nl2d::NvtxRange nvtx_range("c_invoke_time_step");
   NL2D_PTRS;
   State& s = g_state;
   const Scalars sc{rdt, cbfr, visc, omega, d2r, g};
@@ -756,6 +757,7 @@ int nl2d_register(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v
                   int internal_xstart, int internal_xstop, int internal_ystart,
                   int internal_ystop, int width, int height, double rdt, double cbfr,
                   double visc, double omega, double d2r, double g) {
+  nl2d::NvtxRange nvtx_range("nl2d_register");
   NL2D_PTRS;
   CallScope scope;
   const Scalars sc{rdt, cbfr, visc, omega, d2r, g};
@@ -766,6 +768,7 @@ int nl2d_register(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v
 
 void c_read_from_device(void* from, void* to, int startx, int starty, int nx, int ny,
                         bool blocking) {
+  nl2d::NvtxRange nvtx_range("c_read_from_device");
   State& s = g_state;
   const int k = find_field(from);
   if (k < 0) {
@@ -792,6 +795,7 @@ void c_read_from_device(void* from, void* to, int startx, int starty, int nx, in
 
 void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int ny,
                        bool blocking) {
+  nl2d::NvtxRange nvtx_range("c_write_to_device");
   State& s = g_state;
   const int k = find_field(to);
   if (k < 0) {
@@ -843,6 +847,7 @@ struct CheckpointHeader {
 constexpr char kCheckpointMagic[8] = {'N', 'L', '2', 'D', 'C', 'K', 'P', '1'};
 
 int nl2d_checkpoint_write(const char* path, int istep) {
+  nl2d::NvtxRange nvtx_range("nl2d_checkpoint_write");
   State& s = g_state;
   CallScope scope;
   if (!s.registered) {
@@ -880,6 +885,7 @@ int nl2d_checkpoint_write(const char* path, int istep) {
 }
 
 int nl2d_checkpoint_read(const char* path, int* istep) {
+  nl2d::NvtxRange nvtx_range("nl2d_checkpoint_read");
   State& s = g_state;
   CallScope scope;
   if (!s.registered) {
@@ -994,6 +1000,7 @@ int nl2d_set_precision(int precision) {
 }
 
 int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums_out) {
+  nl2d::NvtxRange nvtx_range("nl2d_run_steps");
   State& s = g_state;
   CallScope scope;
   if (!s.registered) {
@@ -1035,6 +1042,7 @@ int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums
 }
 
 int nl2d_timed_run(int istep0, int nsteps, double* ms_out) {
+  nl2d::NvtxRange nvtx_range("nl2d_timed_run");
   State& s = g_state;
   CallScope scope;
   if (ms_out) *ms_out = 0.0;
@@ -1072,6 +1080,7 @@ int nl2d_timed_run(int istep0, int nsteps, double* ms_out) {
 }
 
 int nl2d_checksums(double out[3]) {
+  nl2d::NvtxRange nvtx_range("nl2d_checksums");
   State& s = g_state;
   CallScope scope;
   auto take_status = [&]() { return scope.rc(); };

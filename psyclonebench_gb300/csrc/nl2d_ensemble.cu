@@ -662,6 +662,7 @@ int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight) {
 
 int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_out,
                  double* ms_out) {
+  nl2d::NvtxRange nvtx_range("nl2d_ens_run");
   Ens& e = g_ens;
   if (ms_out) *ms_out = 0.0;
   if (e.ndom < 1 || nsteps < 0 || checksum_every < 0) return NL2D_ERR_ARGS;

@@ -6,9 +6,19 @@
 // the same shape in int32.  The internal T region is [xs,xe] x [ys,ye].
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 
 namespace nl2d {
+
+// An NVTX range for the lifetime of the object: each public entry point
+// names itself in a profiler's timeline (a no-op unless a tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Device copies of the 13 fields and 12 grid arrays that
 // c_invoke_time_step receives (psykal_cpp/time_step.cpp:10-51), plus the

@@ -33,6 +33,7 @@
 
 #include "../../include/nl2d_gpu.h"
 #include "nl2d_exact.cuh"  // bits, from_bits, half, pick
+#include "nl2d_internal.h"  // NvtxRange
 
 // On GB300 the FP64 pipe issues about 2 thread-operations per clock per SM,
 // ~30x fewer than the integer pipe, and this iteration is FP64-bound.  The
@@ -411,6 +412,7 @@ void tra_adv_compute(const double* ztfreez, const double* pun, const double* pvn
                      const double* tmask, const double* rnfmsk, const double* rnfmsk_z,
                      const double* upsmsk, double* mydomain, const double* tsn, int jpi, int jpj,
                      int jpk) {
+  nl2d::NvtxRange nvtx_range("tra_adv_compute");
   if (!ztfreez || !pun || !pvn || !pwn || !umask || !vmask || !tmask || !rnfmsk || !rnfmsk_z ||
       !upsmsk || !mydomain || !tsn || jpi < 3 || jpj < 3 || jpk < 2 ||
       (double)jpi * jpj * jpk > 4.0e9) {
@@ -429,6 +431,7 @@ void tra_adv_compute(const double* ztfreez, const double* pun, const double* pvn
 }
 
 int tra_adv_run(int niter, double* ms) {
+  nl2d::NvtxRange nvtx_range("tra_adv_run");
   TraState& s = g_tra;
   if (!s.registered) return NL2D_ERR_STATE;
   if (niter < 0) return NL2D_ERR_ARGS;
