@@ -261,6 +261,9 @@ __global__ void __launch_bounds__(kPipeThreads)
     // ---- MMA issuer ----
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16(cout);
+      const uint64_t b_desc0 = smem_desc(smem_u32(b_s), 128, (uint32_t)cin * 16);
+      const uint32_t a_kstep = (2 * lbo_a) >> 4;
+      const int kcq = cin / 16;
       long long q = 0, p = 0;  // input rows consumed (sequence base), output rows issued
       bool issued = false;
       for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
@@ -280,21 +283,27 @@ __global__ void __launch_bounds__(kPipeThreads)
           if (!ok) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t dcol = taddr + (uint32_t)(buf * 64);
-          int first = 1;
-          for (int tap = 0; tap < 9; tap++) {
-            const int dy = tap / 3, dx = tap % 3;
-            const int slot = (int)((qb + o + dy) % kSlots);
-            for (int kq = 0; kq < cin / 16; kq++) {
-              const uint64_t ad = smem_desc(
-                  smem_u32(ring + slot * row_bytes) + 2 * kq * lbo_a + dx * 16, lbo_a, 128);
-              const uint64_t bd =
-                  smem_desc(smem_u32(b_s + tap * b_bytes) + kq * 256, 128, (uint32_t)cin * 16);
-              const uint32_t acc = first ? 0u : 1u;
+          // Operand descriptors: built once per input row and for tap 0, then
+          // advanced by adding byte offsets / 16 to their address field
+          // (shared addresses stay below 256 KB, so the field never carries
+          // into the others): + dx for the tap's pixel shift, + 2 lbo / 16
+          // per A K-step, + 256 / 16 per B K-step, + b_bytes / 16 per tap.
+          uint64_t arow[3];
+#pragma unroll
+          for (int dy = 0; dy < 3; dy++)
+            arow[dy] = smem_desc(smem_u32(ring + (int)((qb + o + dy) % kSlots) * row_bytes),
+                                 lbo_a, 128);
+          uint64_t btap = b_desc0;
+          uint32_t acc = 0u;
+#pragma unroll
+          for (int tap = 0; tap < 9; tap++, btap += b_bytes >> 4) {
+            uint64_t ad = arow[tap / 3] + (uint64_t)(tap % 3), bd = btap;
+            for (int kq = 0; kq < kcq; kq++, ad += a_kstep, bd += 256 >> 4) {
               asm volatile(
                   "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dcol),
                   "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-              first = 0;
+              acc = 1u;
             }
           }
           issued = true;
