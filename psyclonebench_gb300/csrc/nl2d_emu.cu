@@ -532,16 +532,22 @@ __global__ void __launch_bounds__(kPipeThreads)
                mbar_wait(&yfull[ys], (uint32_t)((p / kWgYSlots) & 1), abort_v, err);
           if (!ok) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t ya = smem_u32(yring + ys * yslot_bytes);
+          // MN-major, no swizzle: LBO steps along K (8 pixels = 128 B), SBO
+          // along M / N (the next 8 channels).  Descriptors built once per
+          // row and advanced by adding byte offsets / 16 to their address
+          // field (shared addresses stay below 256 KB): + 256 / 16 per
+          // K-step, + dx for the tap's pixel shift.
+          const uint64_t yrow = smem_desc(smem_u32(yring + ys * yslot_bytes), 128, lbo_y);
+          uint64_t xrow[3];
+#pragma unroll
+          for (int dyr = 0; dyr < 3; dyr++)
+            xrow[dyr] = smem_desc(smem_u32(xring + (int)((qb + o + dyr) % kSlots) * row_bytes),
+                                  128, lbo_x);
+#pragma unroll
           for (int tap = 0; tap < 9; tap++) {
-            const int dyr = tap / 3, dx = tap % 3;
-            const uint32_t xa =
-                smem_u32(xring + (int)((qb + o + dyr) % kSlots) * row_bytes) + dx * 16;
-            for (int kq = 0; kq < kTileM / 16; kq++) {
-              // MN-major, no swizzle: LBO steps along K (8 pixels = 128 B),
-              // SBO along M / N (the next 8 channels)
-              const uint64_t ad = smem_desc(ya + kq * 256, 128, lbo_y);
-              const uint64_t bd = smem_desc(xa + kq * 256, 128, lbo_x);
+            uint64_t ad = yrow, bd = xrow[tap / 3] + (uint64_t)(tap % 3);
+#pragma unroll
+            for (int kq = 0; kq < kTileM / 16; kq++, ad += 256 >> 4, bd += 256 >> 4) {
               const uint32_t acc = (issued || kq > 0) ? 1u : 0u;
               asm volatile(
                   "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
