@@ -906,8 +906,15 @@ int nl2d_emu_conv3x3(const void* x, const void* w, const float* bias, void* y, f
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long units =
       (long long)batch * ((H + kStripRows - 1) / kStripRows) * (W / kTileM);
-  const long long per_sm = smem <= 110 * 1024 ? 2 : 1;  // CTAs that fit an SM's shared memory
-  const int grid = (int)(units < per_sm * sms ? units : per_sm * sms);
+  // Persistent CTAs: as many as are resident at once (registers and shared
+  // memory decide; each holds kPipeTmemCols of the SM's 512 TMEM columns).
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_pipe, kPipeThreads,
+                                                    smem) != cudaSuccess ||
+      per_sm < 1)
+    return NL2D_ERR_CUDA;
+  per_sm = per_sm < 512 / kPipeTmemCols ? per_sm : 512 / kPipeTmemCols;
+  const int grid = (int)(units < (long long)per_sm * sms ? units : (long long)per_sm * sms);
   k_conv3x3_pipe<<<grid, kPipeThreads, smem, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, (const __nv_bfloat16*)w, bias, (__nv_bfloat16*)y, y32, batch, H,
       W, cin, cout, relu, err);
