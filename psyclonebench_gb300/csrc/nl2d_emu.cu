@@ -906,14 +906,29 @@ int nl2d_emu_conv3x3(const void* x, const void* w, const float* bias, void* y, f
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long units =
       (long long)batch * ((H + kStripRows - 1) / kStripRows) * (W / kTileM);
-  // Persistent CTAs: as many as are resident at once (registers and shared
-  // memory decide; each holds kPipeTmemCols of the SM's 512 TMEM columns).
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_pipe, kPipeThreads,
-                                                    smem) != cudaSuccess ||
-      per_sm < 1)
-    return NL2D_ERR_CUDA;
+  // Persistent CTAs: as many as are resident at once.  Counted from the
+  // kernel's registers (allocated per warp in units of 256) and shared
+  // memory (dynamic + static + the driver's reserve per block), as the
+  // hardware limits them; each CTA also holds kPipeTmemCols of the SM's 512
+  // TMEM columns.  (cudaOccupancyMaxActiveBlocksPerMultiprocessor answered 1
+  // here where 2 are resident, and the forward pass took 0.78 instead of
+  // 0.51 ms.)
+  static cudaFuncAttributes fa;
+  static bool fa_ok = false;
+  if (!fa_ok) {
+    if (cudaFuncGetAttributes(&fa, k_conv3x3_pipe) != cudaSuccess) return NL2D_ERR_CUDA;
+    fa_ok = true;
+  }
+  int regs_sm = 0, smem_sm = 0, smem_rsv = 0;
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;
+  const int by_regs = regs_sm / (warp_regs * (kPipeThreads / 32));
+  const int by_smem = smem_sm / (int)(smem + fa.sharedSizeBytes + smem_rsv);
+  int per_sm = by_regs < by_smem ? by_regs : by_smem;
   per_sm = per_sm < 512 / kPipeTmemCols ? per_sm : 512 / kPipeTmemCols;
+  per_sm = per_sm < 1 ? 1 : per_sm;
   const int grid = (int)(units < (long long)per_sm * sms ? units : (long long)per_sm * sms);
   k_conv3x3_pipe<<<grid, kPipeThreads, smem, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, (const __nv_bfloat16*)w, bias, (__nv_bfloat16*)y, y32, batch, H,

@@ -29,8 +29,9 @@ using namespace mixk;
 namespace {
 
 // The regular cells: one warp per MW columns x MR rows of the copy region.
-__global__ void __launch_bounds__(32 * MARCH_WARPS)
-    k_mixed_march(MixedFields mf, MixedState ms, Dims d, MixConst k, int ncol, int nwarps,
+// Both march kernels are held to 96 registers, 5 blocks of 4 warps per SM.
+__global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
+    k_mixed_march(MixedFields mf, MixedState ms, Dims d, MarchConst k, int ncol, int nwarps,
                   int mr) {
   const int warp = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (warp >= nwarps) return;  // the whole warp leaves together
@@ -65,9 +66,9 @@ __global__ void __launch_bounds__(128)
 // ---- ensemble: the march over every domain when all share the step's
 // constants (kernel parameters); warp w takes units[w] = (domain, i0, j0)
 // with the packed arrays' base pointers in mf / ms.
-__global__ void __launch_bounds__(32 * MARCH_WARPS)
+__global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
     k_ensemble_mixed_march(const EnsDom* __restrict__ doms, const int4* __restrict__ units,
-                           int nunits, MixedFields mf, MixedState ms, MixConst k) {
+                           int nunits, MixedFields mf, MixedState ms, MarchConst k) {
   const int w = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
@@ -171,7 +172,7 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
   while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 5 * MARCH_WARPS) mr /= 2;
   const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
   k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-      mf, ms, d, k, ncol, nwarps, mr);
+      mf, ms, d, make_march_const(k), ncol, nwarps, mr);
   if (mf.gcount > 0)
     k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
                                                              tide_index, tide);
@@ -183,7 +184,7 @@ void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
   MixConst kc;
   memcpy(&kc, k, sizeof kc);
   k_ensemble_mixed_march<<<(nunits + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-      (const EnsDom*)doms, units, nunits, mf, ms, kc);
+      (const EnsDom*)doms, units, nunits, mf, ms, make_march_const(kc));
 }
 
 void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,

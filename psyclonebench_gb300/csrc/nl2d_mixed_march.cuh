@@ -32,20 +32,6 @@ constexpr int MR = 32;  // output rows per warp (at most; smaller domains take s
 constexpr int MARCH_WARPS = 4;
 constexpr unsigned FULL = 0xffffffffu;
 
-// One loaded row of one column.
-struct MRow {
-  float u, v, sn, lo, hu, hv, ht;
-  float su;  // east face: next_sshu's two-sided formula
-  float sv;  // north face: formed once the next row is loaded
-};
-
-// The terms at one position that neighbouring updates share, and the row
-// values the update at that position reads.
-struct MTerm {
-  float flxu, flxv, gx, gy, fxu, fyv, vsc, fyu, qy, uwc, fxv, qx;
-  float hu, su, hv, sv, sn, lo, u, v;
-};
-
 __device__ __forceinline__ float shd(float x) { return __shfl_down_sync(FULL, x, 1); }
 __device__ __forceinline__ float shu(float x) { return __shfl_up_sync(FULL, x, 1); }
 
@@ -53,11 +39,93 @@ __device__ __forceinline__ float face_ssh(const MixConst& k, float a, float b, f
   return 0.5f * (k.area_t * a + k.area_t * b) * r_area;
 }
 
+// The u and v halves of the update have the same shape, so they run as
+// pairs on the packed FP32 instructions (add / mul / fma .f32x2: one issue
+// slot for two operations); a float2 below is always (u side, v side).  The
+// shared terms (row_terms) use the same pairs with scalar operations: packed
+// there too, the march needed 117 registers instead of 96 (4 blocks of 4
+// warps per SM instead of 5) and ran slower (63.8 k against 71.3 k
+// Mcell-steps/s at 4096^2; packed in the update only: 74.0 k).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b in one rounding: (-1) * b + a
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 add2s(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 mul2s(float2 a, float2 b) {
+  return make_float2(a.x * b.x, a.y * b.y);
+}
+__device__ __forceinline__ float2 sub2s(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+
+// The march's step constants (kernel parameters), pairs as above, with the
+// factors 0.5 of the tile form's face averages and upwind speeds folded in
+// (powers of two: the same values) and the per-step products formed once.
+struct MarchConst {
+  float2 r_dxy;  // (1/dx_t, 1/dy_t): the x / y gradients
+  float2 uu;     // (dy_t / 2, dyu2 / 8): U east-west and the U of the v flux
+  float2 vv;     // (dxv2 / 8, dx_t / 2): the V of the u flux and V north-south
+  float2 r_q;    // (1/dyu2, 1/dxv2): the cross gradients
+  float2 vis1;   // (visc dy_u, visc dx_v)
+  float2 vis2;   // (visc dx_u / 2, visc dy_v / 2)
+  float2 cor;    // (cor_u area_u / 4, -cor_v area_v / 4)
+  float2 hpg;    // (-g dy_u, -g dx_v)
+  float2 rra;    // (rdt / area_u, rdt / area_v)
+  float face_u, face_v;  // area_t / (2 area_u), area_t / (2 area_v): next_ssh's faces
+  float rrat;            // rdt / area_t
+  float r_fric;
+};
+
+inline MarchConst make_march_const(const MixConst& k) {
+  MarchConst c;
+  c.r_dxy = make_float2(k.r_dx_t, k.r_dy_t);
+  c.uu = make_float2(0.5f * k.dy_t, 0.125f * k.dyu2);
+  c.vv = make_float2(0.125f * k.dxv2, 0.5f * k.dx_t);
+  c.r_q = make_float2(k.r_dyu2, k.r_dxv2);
+  c.vis1 = make_float2(k.visc * k.dy_u, k.visc * k.dx_v);
+  c.vis2 = make_float2(0.5f * k.visc * k.dx_u, 0.5f * k.visc * k.dy_v);
+  c.cor = make_float2(0.25f * k.cor_u * k.area_u, -0.25f * k.cor_v * k.area_v);
+  c.hpg = make_float2(-k.g * k.dy_u, -k.g * k.dx_v);
+  c.rra = make_float2(k.rdt * k.r_area_u, k.rdt * k.r_area_v);
+  c.face_u = 0.5f * k.area_t * k.r_area_u;
+  c.face_v = 0.5f * k.area_t * k.r_area_v;
+  c.rrat = k.rdt * k.r_area_t;
+  c.r_fric = k.r_fric;
+  return c;
+}
+
+// One loaded row of one column.
+struct MRow {
+  float2 uv, hh;  // (u, v), (hu, hv)
+  float2 ss;      // (sshn_u of the east face, sshn_v of the north face); the
+                  // north face is formed once the next row is loaded
+  float sn, lo, ht;
+};
+
+// The terms at one position that neighbouring updates share, and the row
+// values the update at that position reads.
+struct MTerm {
+  float2 flx;  // (hu + su) u, (hv + sv) v: the continuity fluxes
+  float2 g;    // x gradient of u, y gradient of v, times the depth
+  float2 fx;   // advective fluxes of u and of v through the west face
+  float2 fy;   // advective fluxes of u and of v through the south face
+  float2 q;    // y gradient of u, x gradient of v
+  float2 vw;   // the v sum of the u Coriolis term, the u sum of the v one
+  float2 H;    // total depths at the u and v faces
+  float2 hh, ss, uv;
+  float sn, lo;
+};
+
 // The loaded values of row j of column i (zeros outside the array),
 // issued ahead of their use.
 struct MRaw {
-  float2 s;
-  float u, v, hu, hv, ht;
+  float2 s, uv, hh;
+  float ht;
 };
 
 __device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int i,
@@ -66,87 +134,74 @@ __device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState
   const bool ok = i >= 0 && i < W && j >= 0 && j < H;
   const size_t c = base + (ok ? (size_t)j * W + i : 0);
   r.s = ok ? __ldg(ms.sn_in + c) : make_float2(0.f, 0.f);
-  r.u = ok ? __ldg(ms.un_in + c) : 0.f;
-  r.v = ok ? __ldg(ms.vn_in + c) : 0.f;
-  r.hu = ok ? __ldg(mf.hu + c) : 0.f;
-  r.hv = ok ? __ldg(mf.hv + c) : 0.f;
+  r.uv = make_float2(ok ? __ldg(ms.un_in + c) : 0.f, ok ? __ldg(ms.vn_in + c) : 0.f);
+  r.hh = make_float2(ok ? __ldg(mf.hu + c) : 0.f, ok ? __ldg(mf.hv + c) : 0.f);
   r.ht = ok ? __ldg(mf.ht + c) : 0.f;
   return r;
 }
 
 // A loaded row and its east face's sshn_u; the east neighbour's ssh comes
 // from lane + 1 (lane 31's su is not used).
-__device__ __forceinline__ MRow finish_row(const MRaw& a, const MixConst& k) {
+__device__ __forceinline__ MRow finish_row(const MRaw& a, const MarchConst& c) {
   MRow r;
   r.sn = a.s.x;
   r.lo = a.s.y;
-  r.u = a.u;
-  r.v = a.v;
-  r.hu = a.hu;
-  r.hv = a.hv;
+  r.uv = a.uv;
+  r.hh = a.hh;
   r.ht = a.ht;
-  r.su = face_ssh(k, r.sn, shd(r.sn), k.r_area_u);
-  r.sv = 0.f;
+  r.ss = make_float2((r.sn + shd(r.sn)) * c.face_u, 0.f);
   return r;
 }
 
 // What the update of output row j reads besides the terms, issued a row
 // ahead.
 struct MOut {
-  float rhu, rhv;
+  float2 rh;  // 1 / (hu + ssha_u), 1 / (hv + ssha_v)
   unsigned char reg;
 };
 
 __device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int i, int j, int W,
                                          int jend, size_t base) {
-  MOut o{0.f, 0.f, 0};
+  MOut o{make_float2(0.f, 0.f), 0};
   if (col && j < jend) {
     const size_t c = base + (size_t)j * W + i;
     o.reg = __ldg(mf.reg + c);
-    o.rhu = __ldg(mf.rhu + c);
-    o.rhv = __ldg(mf.rhv + c);
+    o.rh = make_float2(__ldg(mf.rhu + c), __ldg(mf.rhv + c));
   }
   return o;
 }
 
 // The shared terms at (i, r) from rows r-1 (P), r (C), r+1 (N): the tile
-// form's phase 1, operation for operation.
+// form's phase 1, in (scalar) pairs.
 __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const MRow& N,
-                                           const MixConst& k) {
+                                           const MarchConst& c) {
   MTerm t;
-  const float Hu = C.hu + C.su, Hv = C.hv + C.sv;
-  const float uW = shu(C.u), vW = shu(C.v), HuW = shu(Hu);
-  const float vE_P = shd(P.v), hvE_P = shd(P.hv), svE_P = shd(P.sv);
-  const float uW_N = shu(N.u), huW_N = shu(N.hu), suW_N = shu(N.su);
+  t.H = add2s(C.hh, C.ss);
+  t.flx = mul2s(t.H, C.uv);
+  const float uW = shu(C.uv.x), vW = shu(C.uv.y), HuW = shu(t.H.x);
+  const float vE_P = shd(P.uv.y), hvE_P = shd(P.hh.y), svE_P = shd(P.ss.y);
+  const float uW_N = shu(N.uv.x), huW_N = shu(N.hh.x), suW_N = shu(N.ss.x);
   const float D = C.ht + C.sn;
-  t.flxu = Hu * C.u;
-  t.flxv = Hv * C.v;
-  t.gx = (C.u - uW) * k.r_dx_t * D;
-  t.gy = (C.v - P.v) * k.r_dy_t * D;
-  const float U = 0.5f * (C.u + uW) * k.dy_t;
-  t.fxu = (U < 0.f ? C.u : uW) * U * D;
-  const float V = 0.5f * (C.v + P.v) * k.dx_t;
-  t.fyv = (V < 0.f ? C.v : P.v) * V * D;
-  const float vsc = 0.5f * (P.v + vE_P);
-  t.vsc = vsc;
-  const float Vs = 0.5f * vsc * k.dxv2;
-  const float deps = 0.5f * ((P.hv + P.sv) + hvE_P + svE_P);
-  t.fyu = (Vs < 0.f ? C.u : P.u) * Vs * deps;
-  t.qy = (C.u - P.u) * k.r_dyu2;
-  const float uwc = 0.5f * (uW + uW_N);
-  t.uwc = uwc;
-  const float Uw = 0.5f * uwc * k.dyu2;
-  const float depw = 0.5f * (HuW + huW_N + suW_N);
-  t.fxv = (Uw < 0.f ? C.v : vW) * Uw * depw;
-  t.qx = (C.v - vW) * k.r_dxv2;
-  t.hu = C.hu;
-  t.su = C.su;
-  t.hv = C.hv;
-  t.sv = C.sv;
+  t.g = mul2s(mul2s(sub2s(C.uv, make_float2(uW, P.uv.y)), c.r_dxy), make_float2(D, D));
+  // (u + u_west, u_west + u_west of the next row), (v_south + v_south-east, v + v_south)
+  const float2 sA = add2s(make_float2(C.uv.x, uW), make_float2(uW, uW_N));
+  const float2 sB = add2s(make_float2(P.uv.y, C.uv.y), make_float2(vE_P, P.uv.y));
+  t.vw = make_float2(sB.x, sA.y);
+  const float2 UU = mul2s(sA, c.uu);  // (U, U of the v flux / 2)
+  const float2 VV = mul2s(sB, c.vv);  // (V of the u flux / 2, V)
+  // depths of the v-flux west face and the u-flux south face, times 2
+  const float2 dep = add2s(add2s(make_float2(HuW, P.hh.y + P.ss.y), make_float2(huW_N, hvE_P)),
+                          make_float2(suW_N, svE_P));
+  const float2 selx = make_float2(UU.x < 0.f ? C.uv.x : uW, UU.y < 0.f ? C.uv.y : vW);
+  const float2 sely = make_float2(VV.x < 0.f ? C.uv.x : P.uv.x, VV.y < 0.f ? C.uv.y : P.uv.y);
+  t.fx = mul2s(mul2s(selx, UU), make_float2(D, dep.x));
+  t.fy = mul2s(mul2s(sely, VV), make_float2(dep.y, D));
+  t.q = mul2s(sub2s(C.uv, make_float2(P.uv.x, vW)), c.r_q);
+  t.hh = C.hh;
+  t.ss = C.ss;
+  t.uv = C.uv;
   t.sn = C.sn;
   t.lo = C.lo;
-  t.u = C.u;
-  t.v = C.v;
   return t;
 }
 
@@ -154,7 +209,7 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
 // copy region, regular cells only.  `base`: the domain's first element in
 // the arrays (an ensemble packs its domains back to back; 0 otherwise).
 __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedState& ms,
-                                            const Dims& d, const MixConst& k, int i0, int j0,
+                                            const Dims& d, const MarchConst& k, int i0, int j0,
                                             size_t base, int mr) {
   const int lane = threadIdx.x & 31;
   const int W = d.width, H = d.height;
@@ -166,10 +221,10 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
   MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H, base), k);
   MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H, base), R2 = load_raw(mf, ms, i, j0 + 3, W, H, base);
   MOut O = load_out(mf, out_col, i, j0, W, jend, base);
-  P.sv = face_ssh(k, P.sn, C.sn, k.r_area_v);
-  C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
+  P.ss.y = (P.sn + C.sn) * k.face_v;
+  C.ss.y = (C.sn + N.sn) * k.face_v;
   // row j0-1: what the updates of row j0 read from it
-  float flxv0 = (P.hv + P.sv) * P.v, hu0 = P.hu, su0 = P.su;
+  float flxv0 = (P.hh.y + P.ss.y) * P.uv.y, hu0 = P.hh.x, su0 = P.ss.x;
   MTerm T1 = row_terms(P, C, N, k);  // row j0
   for (int j = j0; j < jend; j++) {
     P = C;  // row j
@@ -179,43 +234,38 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     R2 = load_raw(mf, ms, i, j + 4, W, H, base);  // in flight for two iterations
     const MOut Oc = O;
     O = load_out(mf, out_col, i, j + 1, W, jend, base);
-    C.sv = face_ssh(k, C.sn, N.sn, k.r_area_v);
+    C.ss.y = (C.sn + N.sn) * k.face_v;
     const MTerm T2 = row_terms(P, C, N, k);  // row j+1
     // x neighbours of row j's terms (every lane takes part)
-    const float flxuW = shu(T1.flxu), fxuE = shd(T1.fxu), gxE = shd(T1.gx), snE = shd(T1.sn);
-    const float fxvE = shd(T1.fxv), qxE = shd(T1.qx), uwcE = shd(T1.uwc);
-    const float hvW = shu(T1.hv), svW = shu(T1.sv), hvE = shd(T1.hv), svE = shd(T1.sv);
+    const float flxuW = shu(T1.flx.x), snE = shd(T1.sn);
+    const float2 fxE = make_float2(shd(T1.fx.x), shd(T1.fx.y));
+    const float gxE = shd(T1.g.x), qxE = shd(T1.q.y), uwcE = shd(T1.vw.y);
+    const float hvW = shu(T1.hh.y), svW = shu(T1.ss.y), hvE = shd(T1.hh.y), svE = shd(T1.ss.y);
     if (out_col && Oc.reg) {
       const size_t c = base + (size_t)j * W + i;
-      {
-        const float div = ((flxuW - T1.flxu) + flxv0) - T1.flxv;
-        ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rdt * k.r_area_t);
-        const float Hu = T1.hu + T1.su, Hv = T1.hv + T1.sv;
-        {
-          const float adv = ((T1.fxu - fxuE) + T1.fyu) - T2.fyu;
-          const float dudy_s = T1.qy * (Hu + hu0 + su0);
-          const float dudy_n = T2.qy * (Hu + T2.hu + T2.su);
-          const float vis = k.visc * ((gxE - T1.gx) * k.dy_u + 0.5f * (dudy_n - dudy_s) * k.dx_u);
-          const float cor = 0.5f * (k.cor_u * (T1.vsc + T2.vsc)) * k.area_u * Hu;
-          const float hpg = -k.g * Hu * k.dy_u * (snE - T1.sn);
-          ms.un_out[c] = (T1.u * Hu + k.rdt * (adv + vis + cor + hpg) * k.r_area_u) *
-                         Oc.rhu * k.r_fric;
-        }
-        {
-          const float adv = ((T1.fxv - fxvE) + T1.fyv) - T2.fyv;
-          const float dvdx_w = T1.qx * (Hv + hvW + svW);
-          const float dvdx_e = qxE * (Hv + hvE + svE);
-          const float vis = k.visc * ((T2.gy - T1.gy) * k.dx_v + 0.5f * (dvdx_e - dvdx_w) * k.dy_v);
-          const float cor = -0.5f * (k.cor_v * (uwcE + T1.uwc)) * k.area_v * Hv;
-          const float hpg = -k.g * Hv * k.dx_v * (T2.sn - T1.sn);
-          ms.vn_out[c] = (T1.v * Hv + k.rdt * (adv + vis + cor + hpg) * k.r_area_v) *
-                         Oc.rhv * k.r_fric;
-        }
-      }
+      const float div = ((flxuW - T1.flx.x) + flxv0) - T1.flx.y;
+      ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rrat);
+      const float2 Hf = T1.H;
+      const float2 adv = sub2(add2(sub2(T1.fx, fxE), T1.fy), T2.fy);
+      // (du/dy, dv/dx) times the depth at the south / west and north / east faces
+      const float2 dS = mul2(T1.q, add2(add2(Hf, make_float2(hu0, hvW)), make_float2(su0, svW)));
+      const float2 dN = mul2(make_float2(T2.q.x, qxE),
+                             add2(add2(Hf, make_float2(T2.hh.x, hvE)), make_float2(T2.ss.x, svE)));
+      const float2 vis =
+          fma2(sub2(dN, dS), k.vis2, mul2(sub2(make_float2(gxE, T2.g.y), T1.g), k.vis1));
+      const float2 cor =
+          mul2(mul2(add2(make_float2(T1.vw.x, uwcE), make_float2(T2.vw.x, T1.vw.y)), k.cor), Hf);
+      const float2 hpg =
+          mul2(mul2(Hf, k.hpg), sub2(make_float2(snE, T2.sn), make_float2(T1.sn, T1.sn)));
+      const float2 tend = add2(add2(add2(adv, vis), cor), hpg);
+      const float2 out = mul2(mul2(fma2(tend, k.rra, mul2(T1.uv, Hf)), Oc.rh),
+                              make_float2(k.r_fric, k.r_fric));
+      ms.un_out[c] = out.x;
+      ms.vn_out[c] = out.y;
     }
-    flxv0 = T1.flxv;
-    hu0 = T1.hu;
-    su0 = T1.su;
+    flxv0 = T1.flx.y;
+    hu0 = T1.hh.x;
+    su0 = T1.ss.x;
     T1 = T2;
   }
 }
