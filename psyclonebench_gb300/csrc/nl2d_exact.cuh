@@ -34,8 +34,22 @@
 
 namespace nl2d {
 
-__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
-__device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
+// A double's bit pattern and back.  Moved through inline PTX so the
+// compiler treats the integer work on the bits as integer work: through a
+// plain bitcast it may rewrite bits(x) & 0x7fff... as fabs(x), a sign-bit
+// merge as copysign and a zero test as an FP64 compare, and on GB300 those
+// run on the FP64 pipe the helpers are there to spare.  (The move itself
+// costs nothing: both sides live in the same 64-bit register pair.)
+__device__ __forceinline__ long long bits(double x) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+__device__ __forceinline__ double from_bits(long long b) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(b));
+  return x;
+}
 // The IEEE expressions the helpers fall back to, kept out of line: inlined,
 // the compiler may predicate them and issue their FP64 instructions on every
 // call, taken or not; as calls behind a branch they cost nothing when not

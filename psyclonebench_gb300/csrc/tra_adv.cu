@@ -103,6 +103,12 @@ __device__ __forceinline__ double limit(double s, double p, double q) {
   return from_bits((m < c ? m : c) | (sb & kSign));
 }
 
+// SIGN(0.5, v): 0.5 with v's sign bit (copysign), set in integer
+// arithmetic.
+__device__ __forceinline__ double half_sign(double v) {
+  return from_bits(0x3FE0000000000000LL | (bits(v) & kSign));
+}
+
 // zu = SIGN(0.5, v) - 0.5 v 1 (tra_adv.F90:165, :173, :231).
 __device__ __forceinline__ double courant(double z0, double v) { return z0 - half(v); }
 
@@ -113,7 +119,7 @@ __device__ __forceinline__ double courant(double z0, double v) { return z0 - hal
 // partner: pick().
 __device__ __forceinline__ double upstream(double vel, double f1, double f0, double zind,
                                            double s1, double s0) {
-  const double z0 = copysign(0.5, vel);
+  const double z0 = half_sign(vel);
   const double zu = courant(z0, vel);
   const double zzwx = f1 + zind * (zu * s1);
   const double zzwy = f0 + zind * (zu * s0);
@@ -265,7 +271,7 @@ __global__ void __launch_bounds__(256) k_tra_vertical(double* __restrict__ m, Tr
     if (k + 2 <= K - 2) zd2 = d.tmask[c + 2 * s] * (mk1 - mk2);
     const double slk1 = (k + 1 <= K - 2) ? limit(slope_raw(zd1, zd2), zd2, zd1) : 0.0;
     const double p1 = d.pwn[c + s];
-    const double z0w = copysign(0.5, p1);
+    const double z0w = half_sign(p1);
     const double zw = courant(z0w, p1);
     const double zind = d.zind[c];
     const double zzwx = mk1 + zind * (zw * slk1);
