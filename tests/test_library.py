@@ -83,3 +83,22 @@ def test_checkpoint_needs_a_problem(lib, tmp_path):
     assert lib.nl2d_checkpoint_read(path, ctypes.byref(ist)) == P.NL2D_ERR_STATE
     buf = ctypes.create_string_buffer(256)
     lib.nl2d_last_error(buf, 256)
+
+
+def test_exact_helpers_keep_bit_work_off_the_fp64_pipe():
+    """The exact FP64 helpers move a double's bit pattern through inline
+    PTX, not a bitcast: through a bitcast the compiler rewrote their integer
+    tests as FP64 abs / compare / copysign instructions (on GB300's narrow
+    FP64 pipe: 21-27 % of the FP64 step's and the tracer's time).  A source
+    check, since the bits are identical either way and only the instruction
+    count shows the difference."""
+    csrc = os.path.join(REPO, "psyclonebench_gb300", "csrc")
+    src = open(os.path.join(csrc, "nl2d_exact.cuh")).read()
+    body = lambda name: re.search(r"\b%s\([^)]*\)\s*\{(.*?)\n\}" % name, src, re.S).group(1)
+    for name in ("bits", "from_bits"):
+        b = body(name)
+        assert "mov.b64" in b and "asm(" in b, name
+        assert "__double_as_longlong" not in b and "__longlong_as_double" not in b, name
+    for f in ("nl2d_fused_tile.cuh", "tra_adv.cu", "nl2d_intfp.cuh"):
+        text = open(os.path.join(csrc, f)).read()
+        assert "__double_as_longlong" not in text and "__longlong_as_double" not in text, f
