@@ -45,7 +45,6 @@ import numpy as np
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
-sys.path.insert(0, os.path.join(REPO, "tests"))
 
 ALG_BYTES_PER_CELL = 76  # 6 x 8 B read + 4 B mask + 3 x 8 B write
 NPTS = 4096
@@ -74,6 +73,11 @@ def parse():
     ap.add_argument("--emu-domains", type=int, default=200, help="emulator training domains")
     ap.add_argument("--emu-horizon", type=int, default=5000,
                     help="solver steps of the emulator's trajectories and roll-out")
+    ap.add_argument("--case", default=None,
+                    choices=["fused", "fused_active", "mixed", "tra_adv", "emu"],
+                    help="run one small case of one kernel family and print its device time "
+                         "(for profiler captures; prints no bench line)")
+    ap.add_argument("--batch", type=int, default=24, help="--case emu: images of 256^2")
     return ap.parse_args()
 
 
@@ -85,30 +89,28 @@ def dist_env():
 
 
 def make_problem(n, written=False):
-    """The reference's initial state for an n x n interior (jpiglo = n + 2),
-    rows padded to a multiple of 8 doubles.  written: every array written
-    once more, as the reference's driver writes them during set-up
-    (initialisation_mod.f90, the grid and field constructors); numpy's
-    zero-filled arrays are otherwise untouched pages, which the first
-    host-to-device copy must fault in (0.42 s instead of 0.14 s of upload at
-    4096^2): a cost of the test harness, not of a caller."""
-    import nl2d_testlib as T
-    import psyclonebench_gb300 as P
+    """The reference's initial state for an n x n interior through the
+    library's own set-up (psyclonebench_gb300.model.reference_problem)."""
+    from psyclonebench_gb300.model import reference_problem
+    return reference_problem(n, written=written)
+
+
+def make_problem_oracle(n):
+    """The same initial state through the oracle's set-up, for the CPU legs:
+    they load no library of the product."""
+    from oracle import cpu as O
+    from psyclonebench_gb300.model import Model
     jp = n + 2
-    width = ((jp + 1 + 7) // 8) * 8
-    m = T.Model(jp, jp, width=width)
-    # the library's own set-up (setup_tpoints_mask, grid metrics,
-    # initialisation), not the oracle's
-    DPP = ctypes.POINTER(ctypes.c_double)
-    fp = (DPP * 13)(*[T.dptr(m.f[k]) for k in T.FIELDS])
-    gp = (DPP * 11)(*[T.dptr(m.grid[k]) for k in T.GRID[1:]])
-    P.check(P.load_library().nl2d_setup_model(1, jp, jp, 1000.0, 1000.0, 100.0, m.width,
-                                              m.height, fp, T.iptr(m.grid["tmask"]), gp,
-                                              None, None), "nl2d_setup_model")
-    if written:
-        for a in list(m.f.values()) + list(m.grid.values()):
-            a[...] = a.copy()
-    return m
+    return O.setup_model(Model(jp, jp, width=((jp + 1 + 7) // 8) * 8))
+
+
+def bench_config(n, width, rdt, active=False, world=1):
+    """The config object both arms print (same keys and values)."""
+    return {"workload": "nemolite2d_fp64_%dx%d%s" % (n, n, "_active" if active else ""),
+            "interior": [n, n], "jphgr_msh": 1, "rdt": rdt, "width": width,
+            "l2": "inputs larger than L2 (135 MB per field)" if n >= 4096 else
+                  "working set per step above L2 only from 4096^2",
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 def make_active(m, seed=3):
@@ -199,37 +201,41 @@ def load_profile_figures():
         return {}
 
 
-def cpu_step_fn():
-    """The reference's OpenMP PSy layer where oracle/_ref holds it (compiled
-    from the reference sources on this machine), else the oracle's OpenMP
-    port.  Returns (callable, kind, description)."""
-    import nl2d_testlib as T
-    ref = T.load_ref("omp")
-    if ref is not None:
-        return ref.c_invoke_time_step, "reference", "psykal_cpp/time_step_omp.cpp (-O3 -fopenmp)"
-    o = T.load_oracle()
-    return o.oracle_invoke_time_step_omp, "port", "oracle OpenMP port of time_step_omp.cpp"
-
-
-def time_cpu(m, nsteps, target_s=None):
-    """Times CPU steps; if target_s is given, runs until ~target_s seconds
-    (at least one step) and returns (steps, seconds)."""
-    import nl2d_testlib as T
-    fn, kind, desc = cpu_step_fn()
-    nargs = len(fn.argtypes)
+def time_cpu(m, nsteps, fn, target_s=None, istep0=1):
+    """Times CPU steps of one step function; if target_s is given, runs
+    until ~target_s seconds (at least one step).  Returns (steps, seconds)."""
+    from oracle import cpu as O
     done, t0 = 0, time.perf_counter()
     while True:
-        args = m.step_args(1 + done)
-        if nargs == len(T.REF_ARGTYPES):
-            del args[31]
-        fn(*args)
+        O.call_step(fn, m.step_args(istep0 + done))
         done += 1
         el = time.perf_counter() - t0
         if target_s is None and done >= nsteps:
             break
         if target_s is not None and (el >= target_s or done >= nsteps):
             break
-    return done, time.perf_counter() - t0, kind, desc
+    return done, time.perf_counter() - t0
+
+
+def time_cpu_layers(n, nsteps, warmup, target_s):
+    """The reference's two OpenMP PSy layers (time_step_omp.cpp, worksharing;
+    time_step_ompopt.cpp, partially fused) on the n x n domain from rest,
+    each after `warmup` untimed steps: the reference's own builds where
+    oracle/_ref holds them, else the oracle's ports.  Returns the faster
+    one's (Mcell-steps/s, steps, seconds, kind, description) and every
+    layer's rate."""
+    from oracle import cpu as O
+    best, rates = None, {}
+    for fn, kind, desc in O.cpu_step_fns():
+        m = make_problem_oracle(n)
+        time_cpu(m, max(warmup, 1), fn)
+        steps, secs = time_cpu(m, nsteps, fn, target_s=target_s, istep0=1 + max(warmup, 1))
+        val = n * n * steps / secs / 1e6
+        rates[desc] = val
+        if best is None or val > best[0]:
+            best = (val, steps, secs, kind, desc)
+        del m
+    return best, rates
 
 
 SEQ_SAMPLE = 32  # domains timed one at a time for the ensemble comparison
@@ -241,8 +247,8 @@ def measure_form(lib, n, precision, steps, warmup, seed=2):
     """Config 2: the 4096^2 domain on a seeded Fourier bathymetry, advanced
     warmup + steps steps in one precision; returns (ms per timed step,
     final fields)."""
-    import nl2d_testlib as T
     import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import register
     from psyclonebench_gb300.workloads import fourier_depth
     m = make_problem(n)
     ht, hu, hv = fourier_depth(m.width, m.height, seed)
@@ -250,7 +256,7 @@ def measure_form(lib, n, precision, steps, warmup, seed=2):
     # 500 m deep water carries gravity waves at sqrt(g h) = 70 m/s: the
     # explicit step needs rdt well below dx / 70 m/s = 14 s.
     m.rdt = BATHY_RDT
-    T.gpu_register(lib, m)
+    register(lib, m)
     lib.nl2d_set_precision(precision)
     ms = ctypes.c_double(0.0)
     P.check(lib.nl2d_timed_run(1, warmup, ctypes.byref(ms)), "form warm-up")
@@ -259,7 +265,7 @@ def measure_form(lib, n, precision, steps, warmup, seed=2):
     for k in ("sshn_t", "un", "vn"):
         a = m.f[k]
         lib.c_read_from_device(a.ctypes.data, a.ctypes.data, 1, 1, m.width, m.height, True)
-        x0, x1, y0, y1 = T.regions(m)["t" if k == "sshn_t" else ("u" if k == "un" else "v")]
+        x0, x1, y0, y1 = m.regions()["t" if k == "sshn_t" else ("u" if k == "un" else "v")]
         out[k] = a[y0:y1 + 1, x0:x1 + 1].copy()
     P.check(None, "form read")
     lib.nl2d_set_precision(0)
@@ -293,15 +299,15 @@ def run_active(lib, n, rest_value, steps=200, warmup=5):
     """The FP64 step with every cell in motion (make_active): the same
     kernel and timing as the headline number, on a state where the exact
     division's zero-dividend shortcut (almost) never applies."""
-    import nl2d_testlib as T
     import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import dptr, register
     m = make_active(make_problem(n))
-    T.gpu_register(lib, m)
+    register(lib, m)
     ms = ctypes.c_double(0.0)
     P.check(lib.nl2d_timed_run(1, warmup, ctypes.byref(ms)), "active warm-up")
     P.check(lib.nl2d_timed_run(1 + warmup, steps, ctypes.byref(ms)), "active run")
     sums = np.zeros(3)
-    P.check(lib.nl2d_checksums(T.dptr(sums)), "active checksums")
+    P.check(lib.nl2d_checksums(dptr(sums)), "active checksums")
     lib.nl2d_finalize()
     value = n * n * steps / (ms.value * 1e-3) / 1e6
     return {"workload": "nemolite2d_fp64_%dx%d_active_fourier_bathymetry_seed3_rdt5" % (n, n),
@@ -316,12 +322,12 @@ def run_sweep(lib, sizes=(256, 512, 1024, 2048, 4096, 8192)):
     FP64 step and the mixed form at each size, device-resident, from the
     reference's rest start, with about the same number of cell-steps per
     size."""
-    import nl2d_testlib as T
     import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import register
     out = []
     for n in sizes:
         m = make_problem(n)
-        T.gpu_register(lib, m)
+        register(lib, m)
         steps = max(20, min(400, int(2e9 / (n * n))))
         ms = ctypes.c_double(0.0)
         P.check(lib.nl2d_timed_run(1, 5, ctypes.byref(ms)), "sweep warm-up")
@@ -363,26 +369,16 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
     # `steps` fused steps): what running the ensemble without the
     # persistent kernel costs.
     seq_ms, seq_cells = 0.0, 0
-    import nl2d_testlib as T
     import psyclonebench_gb300 as P
-    from psyclonebench_gb300.ensemble import Ensemble as _E  # noqa: F401
+    from psyclonebench_gb300.model import Model, register
     sample = doms[:SEQ_SAMPLE]
     for d in sample:
         w, h, xs, xe, ys, ye = d["dims"]
-        m = T.Model.__new__(T.Model)
-        m.xs, m.xe, m.ys, m.ye, m.width, m.height = xs, xe, ys, ye, w, h
-        m.f = {k: np.zeros((h, w)) for k in T.FIELDS}
-        m.grid = {k: np.zeros((h, w)) for k in T.GRID if k != "tmask"}
-        m.grid["tmask"] = np.ascontiguousarray(d["tmask"], np.int32)
-        for k in ("dx_u", "dx_v", "dx_t", "dy_u", "dy_v", "dy_t"):
-            m.grid[k][:] = 1000.0
-        for k in ("area_t", "area_u", "area_v"):
-            m.grid[k][:] = 1.0e6
-        m.grid["gphiu"][:] = 50.0
-        m.grid["gphiv"][:] = 50.0
+        m = Model.from_extents(w, h, xs, xe, ys, ye).uniform_metrics()
+        m.grid["tmask"][:] = np.ascontiguousarray(d["tmask"], np.int32)
         m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = d["ht"], d["hu"], d["hv"]
         m.rdt, m.cbfr, m.visc = BATHY_RDT, 1.5e-4, 0.1
-        T.gpu_register(lib, m)
+        register(lib, m)
         t = ctypes.c_double(0.0)
         P.check(lib.nl2d_timed_run(1, 2, ctypes.byref(t)), "seq warm-up")
         P.check(lib.nl2d_timed_run(3, steps, ctypes.byref(t)), "seq run")
@@ -530,13 +526,13 @@ def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
     ach = 72.0 * points * iters / (ms.value * 1e-3) / 1e9
     in_bytes = sum(f[n].nbytes for n in f)
     # CPU: the oracle's OpenMP port on a bounded sample of the same workload
-    from test_tra_oracle import oracle_run, tra_lib, zero_work
+    from oracle import cpu as O
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-    lib_o = tra_lib()
+    lib_o = O.load_oracle()
     g = {n: v.copy() for n, v in f.items()}
-    w = zero_work(g["mydomain"].shape)
+    w = O.tra_zero_work(g["mydomain"].shape)
     t0 = time.perf_counter()
-    oracle_run(lib_o, g, w, cpu_iters, omp=True)
+    O.tra_oracle_run(lib_o, g, w, cpu_iters, omp=True)
     cpu_s = time.perf_counter() - t0
     return {
         "workload": "tra_adv_%dx%dx%d_%d_iterations" % (jpi, jpj, jpk, iters),
@@ -559,29 +555,28 @@ def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU implementation of the step on
+    all host cores, K steps of the same domain after W warm-up steps, built
+    with the oracle's set-up (no library of the product is loaded).  Both
+    OpenMP PSy layers run; the faster one is the line's value."""
     if rank != 0:
         return
-    cores = os.cpu_count()
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
     n = args.size
-    m = make_problem(n)
-    # warm-up steps, then K timed steps (bounded: stop after ~120 s)
-    time_cpu(m, max(args.warmup, 1))
-    steps, secs, kind, desc = time_cpu(m, args.steps, target_s=120.0)
-    cells = n * n
-    val = cells * steps / secs / 1e6
+    best, rates = time_cpu_layers(n, args.steps, args.warmup, target_s=90.0)
+    val, steps, secs, kind, desc = best
+    width = ((n + 3 + 7) // 8) * 8
     line = {
         "metric": "Mcell-steps/s", "value": val, "unit": "Mcell-steps/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
         "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (reference initial state: rest, constant depth)",
-        "config": {"workload": "nemolite2d_fp64_%dx%d" % (n, n), "interior": [n, n],
-                   "jphgr_msh": 1, "rdt": 20.0, "width": m.width,
-                   "parallelism": "single (rank 0, all host cores)"},
+        "config": bench_config(n, width, 20.0, world=world),
         "cpu_baseline": {"value": val, "unit": "Mcell-steps/s", "cores": cores,
                          "kind": kind, "sample": "%d steps of the %dx%d domain (%s)" % (
-                             steps, n, n, desc)},
+                             steps, n, n, desc),
+                         "layers": rates},
         "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -589,10 +584,10 @@ def run_reference(args, rank, world):
 
 
 def run_ours(args, rank, world, local):
-    import nl2d_testlib as T
     import psyclonebench_gb300 as P
     import torch
     import torch.distributed as dist
+    from psyclonebench_gb300.model import dptr, register
 
     if world > 1:
         torch.cuda.set_device(local)
@@ -606,7 +601,7 @@ def run_ours(args, rank, world, local):
     m = make_problem(n)
     if active:
         make_active(m)
-    T.gpu_register(lib, m)
+    register(lib, m)
     ms = ctypes.c_double(0.0)
     P.check(lib.nl2d_timed_run(1, 1 + args.warmup, ctypes.byref(ms)), "warm-up")
     istep = 2 + args.warmup
@@ -622,7 +617,7 @@ def run_ours(args, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         kernel_ms = float(t.item())
     sums = np.zeros(3)
-    P.check(lib.nl2d_checksums(T.dptr(sums)), "checksums")
+    P.check(lib.nl2d_checksums(dptr(sums)), "checksums")
     value = cells * args.steps * world / (kernel_ms * 1e-3) / 1e6
     ms_step = kernel_ms / args.steps
     lib.nl2d_finalize()
@@ -697,12 +692,13 @@ def run_ours(args, rank, world, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-        mc = make_problem(n)
-        steps, secs, kind, desc = time_cpu(mc, 10 ** 6, target_s=15.0)
-        cpu = {"value": cells * steps / secs / 1e6, "unit": "Mcell-steps/s",
+        best, rates = time_cpu_layers(n, 10 ** 6, 2, target_s=10.0)
+        val, steps, secs, kind, desc = best
+        cpu = {"value": val, "unit": "Mcell-steps/s",
                "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": kind,
-               "sample": "%d steps of the %dx%d domain from rest (%s), ~15 s" % (
-                   steps, n, n, desc)}
+               "sample": "%d steps of the %dx%d domain from rest (%s, the faster of the "
+                         "reference's two OpenMP layers), ~10 s each" % (steps, n, n, desc),
+               "layers": rates}
 
     if rank == 0:
         line = {
@@ -712,10 +708,7 @@ def run_ours(args, rank, world, local):
             "vs_baseline": None, "dtype": "f64",
             "data": ("synthetic (every cell in motion: Fourier bathymetry, random start)"
                      if active else "synthetic (reference initial state: rest, constant depth)"),
-            "config": {"workload": "nemolite2d_fp64_%dx%d%s" % (n, n, "_active" if active else ""),
-                       "interior": [n, n], "jphgr_msh": 1, "rdt": m.rdt, "width": m.width,
-                       "l2": "inputs larger than L2 (135 MB per field)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": bench_config(n, m.width, m.rdt, active, world),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
@@ -728,6 +721,69 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def run_case(args):
+    """One small case for a profiler: --size interior (levels 75 for the
+    tracer; --batch images for the emulator), --warmup untimed then --steps
+    timed steps or iterations, device time from the library's CUDA events."""
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import register
+    lib = P.load_library()
+    n, out = args.size, {"case": args.case, "size": args.size, "steps": args.steps}
+    ms = ctypes.c_double(0.0)
+    if args.case in ("fused", "fused_active", "mixed"):
+        m = make_problem(n)
+        if args.case == "fused_active":
+            make_active(m)
+        if args.case == "mixed":
+            from psyclonebench_gb300.workloads import fourier_depth
+            m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = fourier_depth(m.width, m.height, 2)
+            m.rdt = BATHY_RDT
+        register(lib, m)
+        lib.nl2d_set_precision(1 if args.case == "mixed" else 0)
+        P.check(lib.nl2d_timed_run(1, 1 + args.warmup, ctypes.byref(ms)), "case warm-up")
+        P.check(lib.nl2d_timed_run(2 + args.warmup, args.steps, ctypes.byref(ms)), "case run")
+        lib.nl2d_set_precision(0)
+        lib.nl2d_finalize()
+    elif args.case == "tra_adv":
+        from psyclonebench_gb300.workloads import tra_adv_fields
+        f = tra_adv_fields(n, n, 75)
+        D = ctypes.POINTER(ctypes.c_double)
+        targs = [f[k].ctypes.data_as(D) for k in ("ztfreez", "pun", "pvn", "pwn", "umask",
+                                                  "vmask", "tmask", "rnfmsk", "rnfmsk_z",
+                                                  "upsmsk", "mydomain", "tsn")]
+        for _ in range(max(1, args.warmup)):
+            lib.tra_adv_compute(*targs, n, n, 75)
+        rc = lib.tra_adv_run(args.steps, ctypes.byref(ms))
+        buf = ctypes.create_string_buffer(256)
+        if rc or lib.tra_adv_last_error(buf, 256):
+            raise RuntimeError("tra_adv: %s" % buf.value.decode())
+        lib.tra_adv_finalize()
+    elif args.case == "emu":
+        import torch
+        from psyclonebench_gb300 import emulator as E
+        net = E.ConvNet(args.batch, 256, 256, seed=0, lib=lib)
+        npx = args.batch * 256 * 256
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn(npx, E.CPAD_IN, device="cuda", generator=g).to(torch.bfloat16)
+        target = torch.randn(npx, 3, device="cuda", generator=g)
+        for _ in range(max(1, args.warmup)):
+            net.forward(x)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            net.forward(x)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.value = e0.elapsed_time(e1)
+        net.train_step(x, target)
+        torch.cuda.synchronize()
+        if int(net.err.item()) != 0:
+            raise RuntimeError("emulator: a tensor-core wait ran out")
+        out["batch"] = args.batch
+    out["ms_per_step"] = ms.value / max(1, args.steps)
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -737,7 +793,9 @@ def main():
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     os.environ.setdefault("OMP_PROC_BIND", "close")
     os.environ.setdefault("OMP_PLACES", "cores")
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local)

@@ -167,9 +167,13 @@ int nl2d_field_checksum(const void *field, int x0, int x1, int y0, int y1,
  * synchronisation an allocation can cause) and allocates nothing.  Its
  * scratch is a fixed 128 KiB device array inside the library, held by every
  * GPU that loads it until exit; rectangles above 8192 x 8192 cells return
- * NL2D_ERR_TOO_LARGE.  The first call on a device looks up that array (make
- * it before any stream capture); calls that overlap on the GPU race on the
- * shared array.  Returns a status code; errors are not recorded for
+ * NL2D_ERR_TOO_LARGE.  The first call on a device looks up that array's
+ * device address (make it before any stream capture) and keeps it until
+ * nl2d_finalize; a caller that resets the device (cudaDeviceReset) calls
+ * nl2d_finalize before the next call.  Calls that overlap on the GPU race
+ * on the shared array.  A launch error that earlier work left pending in
+ * the calling thread is reported as NL2D_ERR_CUDA and left in place, with
+ * nothing launched.  Returns a status code; errors are not recorded for
  * nl2d_last_error(). */
 int nl2d_field_checksum_noalloc(const double *d_field, int width, int x0,
                                 int x1, int y0, int y1, double *d_out,

@@ -317,6 +317,65 @@ static void psy_step(const step_t *s, int xs, int xe, int ys, int ye, int par)
                        j * W + i, W);
 }
 
+/* The partially fused loop nest of psykal_cpp/time_step_ompopt.cpp:61-150,
+ * the reference's faster OpenMP PSy layer: continuity, bc_ssh, momentum_u
+ * and momentum_v in one loop over the whole internal region (so momentum_u
+ * also runs at i = xe and momentum_v at j = ye, where the serial layer's
+ * ranges stop one short), the boundary kernels and the copies as in the
+ * worksharing layer, and next_sshu / next_sshv in one loop over
+ * [xs, xe-1] x [ys, ye].  Its results need not equal the serial layer's bit
+ * for bit at those edges; it is timed as a CPU baseline and checked against
+ * the reference's own compiled ompopt layer. */
+static void psy_step_ompopt(const step_t *s, int xs, int xe, int ys, int ye)
+{
+    const int W = s->w;
+    int i, j;
+
+#pragma omp parallel for private(i)
+    for (j = ys; j <= ye; j++)
+        for (i = xs; i <= xe; i++) {
+            k_continuity(s, i, j);
+            k_bc_ssh(s, i, j);
+            k_momentum_u(s, i, j);
+            k_momentum_v(s, i, j);
+        }
+
+#pragma omp parallel for private(i)
+    for (j = ys - 1; j <= ye + 1; j++)
+        for (i = xs - 1; i <= xe; i++) k_bc_solid_u(s, i, j);
+
+#pragma omp parallel for private(i)
+    for (j = ys - 1; j <= ye; j++)
+        for (i = xs - 1; i <= xe + 1; i++) k_bc_solid_v(s, i, j);
+
+#pragma omp parallel for private(i)
+    for (j = ys - 1; j <= ye + 1; j++)
+        for (i = xs - 1; i <= xe; i++)
+            k_bc_flather(s->ua, s->hu, s->sshn_u, s->tmask, s->g, j * W + i, 1);
+
+    for (j = ys - 1; j <= ye; j++)
+        for (i = xs - 1; i <= xe + 1; i++)
+            k_bc_flather(s->va, s->hv, s->sshn_v, s->tmask, s->g, j * W + i, W);
+
+#pragma omp parallel for private(i)
+    for (j = ys - 1; j < ye + 1; j++)
+        for (i = xs - 1; i <= xe + 1; i++) {
+            const int c = j * W + i;
+            s->un[c] = s->ua[c];
+            s->vn[c] = s->va[c];
+            s->sshn_t[c] = s->ssha_t[c];
+        }
+
+#pragma omp parallel for private(i)
+    for (j = ys; j <= ye; j++)
+        for (i = xs; i <= xe - 1; i++) {
+            k_next_ssh(s->sshn_u, s->sshn_t, s->tmask, s->area_t, s->area_u,
+                       j * W + i, 1);
+            k_next_ssh(s->sshn_v, s->sshn_t, s->tmask, s->area_t, s->area_v,
+                       j * W + i, W);
+        }
+}
+
 #define FILL_STEP(s)                                                          \
     step_t s = {ssha_t, sshn_t, sshn_u, sshn_v, hu, hv, un, vn, ua, ht,       \
                 ssha_u, va, ssha_v, tmask, area_t, area_u, area_v, dx_u,      \
@@ -336,6 +395,13 @@ void oracle_invoke_time_step_omp(NL2D_ORACLE_STEP_ARGS)
     FILL_STEP(s);
     psy_step(&s, internal_xstart, internal_xstop, internal_ystart,
              internal_ystop, 1);
+}
+
+void oracle_invoke_time_step_ompopt(NL2D_ORACLE_STEP_ARGS)
+{
+    FILL_STEP(s);
+    psy_step_ompopt(&s, internal_xstart, internal_xstop, internal_ystart,
+                    internal_ystop);
 }
 
 void oracle_invoke_time_step_tide(NL2D_ORACLE_STEP_ARGS, double tide_amp,

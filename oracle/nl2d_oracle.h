@@ -39,6 +39,10 @@ void oracle_invoke_time_step(NL2D_ORACLE_STEP_ARGS);
 /* One time step with the loop-level OpenMP worksharing of
  * psykal_cpp/time_step_omp.cpp:57-146 (bc_flather_v stays serial). */
 void oracle_invoke_time_step_omp(NL2D_ORACLE_STEP_ARGS);
+/* One time step with the partially fused loops of
+ * psykal_cpp/time_step_ompopt.cpp:61-150 (continuity, bc_ssh and both
+ * momentum kernels in one loop; next_sshu and next_sshv in one loop). */
+void oracle_invoke_time_step_ompopt(NL2D_ORACLE_STEP_ARGS);
 
 /* The serial step with the tidal amplitude (m) and period (h) of bc_ssh
  * as parameters (the reference hard-codes 0.2 m and 12.42 h,

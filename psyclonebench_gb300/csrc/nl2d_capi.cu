@@ -969,6 +969,7 @@ void nl2d_finalize(void) {
   s.sums_cap = s.tide_cap = 0;
   if (s.stream) cudaStreamDestroy(s.stream);
   s.stream = nullptr;
+  noalloc_forget();
 }
 
 int nl2d_set_mode(int mode) {

@@ -10,6 +10,8 @@
 // relative), not bit for bit; repeated runs are bit-identical.
 #include "nl2d_internal.h"
 
+#include <atomic>
+
 #include "../../include/nl2d_gpu.h"
 
 namespace nl2d {
@@ -106,27 +108,39 @@ constexpr long long kNoAllocCellsPerPartial = 256LL * 16;  // one block, 16 cell
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
 
 constexpr int kMaxDevices = 64;
-double* g_noalloc_addr[kMaxDevices] = {};
+// One cached address per device, filled on that device's first call.  Host
+// threads may make their first calls at the same time; the entries are
+// atomics, and every thread that looks an address up stores the same value.
+std::atomic<double*> g_noalloc_addr[kMaxDevices];
 
 // Device address of g_noalloc_partials on the current device.  In host
 // code the array's name is only a host-side stand-in, so the address comes
 // from cudaGetSymbolAddress, once per device, with that device current.
+// The address stays valid as long as the device's context does: after a
+// cudaDeviceReset, nl2d_noalloc_forget() (called by nl2d_finalize) drops it
+// so that the next call looks it up again.
 cudaError_t noalloc_scratch(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_noalloc_addr[dev]) {
-    double* p = nullptr;
+  double* p = g_noalloc_addr[dev].load(std::memory_order_relaxed);
+  if (!p) {
     e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
     if (e != cudaSuccess) return e;
-    g_noalloc_addr[dev] = p;
+    g_noalloc_addr[dev].store(p, std::memory_order_relaxed);
   }
-  *out = g_noalloc_addr[dev];
+  *out = p;
   return cudaSuccess;
 }
 
 }  // namespace
+
+namespace nl2d {
+void noalloc_forget() {
+  for (auto& a : g_noalloc_addr) a.store(nullptr, std::memory_order_relaxed);
+}
+}  // namespace nl2d
 
 // Sum of |d_field| over a rectangle without allocating: the library's two
 // checksum kernels, with one partial sum per block of 4096 cells kept in
@@ -143,6 +157,10 @@ extern "C" int nl2d_field_checksum_noalloc(const double* d_field, int width, int
   const long long cells = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
   const long long blocks = (cells + kNoAllocCellsPerPartial - 1) / kNoAllocCellsPerPartial;
   if (blocks > kNoAllocMaxPartials) return NL2D_ERR_TOO_LARGE;
+  // A launch error that earlier work left pending in this thread belongs to
+  // its caller: it is left in place (not cleared) and reported, and nothing
+  // is launched, so the status below is this call's own.
+  if (cudaPeekAtLastError() != cudaSuccess) return NL2D_ERR_CUDA;
   double* scratch = nullptr;
   if (noalloc_scratch(&scratch) != cudaSuccess) return NL2D_ERR_CUDA;
   cudaStream_t st = (cudaStream_t)stream;

@@ -139,6 +139,10 @@ void launch_from_mixed(const float2* sn2, const float* un_f, const float* vn_f,
 // `partials` (at least checksum_partials_needed() doubles) and the final
 // FP64 value to *out, both on the device.
 int checksum_partials_needed();
+// Drops the cached device addresses of the allocation-free checksum's
+// scratch array (nl2d_finalize calls it: after a device reset the next call
+// looks the address up again).
+void noalloc_forget();
 void launch_checksum(const double* f, int width, int x0, int x1, int y0,
                      int y1, double* partials, double* out, cudaStream_t st);
 // The same sums over FP32 fields and over (hi, lo) pairs (hi + lo in FP64).

@@ -11,16 +11,36 @@ import sys
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+# Runs bench.py's main() in this interpreter, then reports which of the
+# product's shared libraries the process mapped.
+RUNNER = """
+import runpy, sys
+sys.argv = ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"]
+runpy.run_path("bench.py", run_name="__main__")
+maps = open("/proc/self/maps").read()
+print("MAPPED", sorted(set(l.split()[-1] for l in maps.splitlines()
+                           if l.endswith(".so") and "psyclonebench_gb300" in l)))
+"""
+
+
 def test_reference_arm_prints_its_json_line():
-    out = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference",
-                          "--steps", "1", "--warmup", "3"],
+    out = subprocess.run([sys.executable, "-c", RUNNER],
                          cwd=REPO, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
-    line = json.loads(out.stdout.strip().splitlines()[-1])
+    lines = out.stdout.strip().splitlines()
+    # the reference arm maps no library of the product
+    assert lines[-1] == "MAPPED []", lines[-1]
+    line = json.loads(lines[-2])
     assert line["impl"] == "reference"
     assert line["metric"] == "Mcell-steps/s" and line["unit"] == "Mcell-steps/s"
     assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 3
     assert line["config"]["workload"] == "nemolite2d_fp64_4096x4096"
+    # the same config object as the GPU arm's line
+    sys.path.insert(0, REPO)
+    import bench
+    assert line["config"] == bench.bench_config(4096, 4104, 20.0)
+    assert len(cb_layers := line["cpu_baseline"]["layers"]) == 2
+    assert line["value"] == max(cb_layers.values())
     assert line["value"] > 0
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]

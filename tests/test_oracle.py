@@ -76,6 +76,49 @@ def test_oracle_matches_reference_build_random_masks(oracle):
             assert bits_equal(m.f[k], m2.f[k]), (trial, k)
 
 
+@pytest.mark.parametrize("kind,port", [("omp", "oracle_invoke_time_step_omp"),
+                                       ("ompopt", "oracle_invoke_time_step_ompopt")])
+def test_openmp_ports_match_reference_builds(oracle, kind, port):
+    """The two OpenMP ports timed as CPU baselines (the worksharing layer and
+    the partially fused one) are bit-identical to the reference's own
+    time_step_omp.cpp / time_step_ompopt.cpp compiled here, on the parity
+    namelist and on a random-mask case with open east and south sides."""
+    ref = T.load_ref(kind)
+    if ref is None:
+        pytest.skip("reference not built here (oracle/_ref)")
+    rng = np.random.default_rng(5)
+    cases = [T.make_model(40, 33, 1, oracle=oracle),
+             T.make_model(29, 37, 3, width=33, oracle=oracle)]
+    inner = cases[1].grid["tmask"][2:-4, 2:-4]
+    inner[rng.random(inner.shape) < 0.08] = 0
+    for k in ("ht", "hu", "hv"):
+        cases[1].f[k][:] = rng.uniform(50, 500, size=cases[1].f[k].shape)
+    for m in cases:
+        m2 = m.copy()
+        T.run(getattr(oracle, port), m, 60)
+        T.run(ref.c_invoke_time_step, m2, 60)
+        for k in T.FIELDS:
+            assert bits_equal(m.f[k], m2.f[k]), (kind, k)
+
+
+def test_ompopt_layer_skips_the_east_column_of_next_sshv(oracle):
+    """The reference's partially fused layer runs next_sshv over next_sshu's
+    range, [xs, xe-1] x [ys, ye] (time_step_ompopt.cpp:141-147), where the
+    serial layer uses [xs, xe] x [ys, ye-1] (time_step.cpp:131-136): column
+    xe of sshn_v keeps its initial value and row ye is written.  So the
+    fields differ from the serial step's; the CPU baseline that times it
+    does the same amount of work on a slightly different computation."""
+    m = T.make_model(40, 33, 1, oracle=oracle)
+    m2 = m.copy()
+    T.run(oracle.oracle_invoke_time_step_ompopt, m, 80)
+    T.run(oracle.oracle_invoke_time_step, m2, 80)
+    assert (m.f["sshn_v"][m.ys:m.ye, m.xe] == 0).all()
+    assert (m2.f["sshn_v"][m.ys:m.ye, m.xe] != 0).any()
+    assert (m.f["sshn_v"][m.ye, m.xs:m.xe] != 0).any()
+    assert (m2.f["sshn_v"][m.ye, :] == 0).all()
+    assert 0 < T.rel_l2(m.f["sshn_t"], m2.f["sshn_t"]) < 1e-3
+
+
 def test_tmask_builder(oracle):
     """model_mod.f90:94-249 for one rank: walls west/north, open south
     (jphgr 1), east (2) or both (3); southern row wins at the corners."""

@@ -14,6 +14,11 @@ import nl2d_testlib as T
 pytestmark = pytest.mark.gpu
 
 CHECKSUM_RTOL = 1e-10  # the tolerance the other checksum tests use
+LIMIT_CELLS = 8192 * 8192  # 16384 partials of 4096 cells
+
+
+def host_sum(a, x0, x1, y0, y1):
+    return float(np.abs(a[y0:y1 + 1, x0:x1 + 1]).sum())
 
 
 def test_noalloc_checksum_matches_library_checksum(gpulib, oracle):
@@ -27,10 +32,12 @@ def test_noalloc_checksum_matches_library_checksum(gpulib, oracle):
     T.gpu_register(gpulib, m)
     out = np.zeros(3)
     P.check(gpulib.nl2d_run_steps(1, 40, 0, T.dptr(out)), "run")
+    T.gpu_read_all(gpulib, m)
 
     d_out = torch.zeros(1, dtype=torch.float64, device="cuda")
     rects = {"sshn_t": (m.xs, m.xe, m.ys, m.ye), "un": (m.xs, m.xe - 1, m.ys, m.ye)}
-    # Two calls in a row, each checked against the allocating entry point.
+    # Two calls in a row, each checked against the allocating entry point
+    # and against a host sum of the same field.
     for name in ("sshn_t", "un"):
         x0, x1, y0, y1 = rects[name]
         want = np.zeros(1)
@@ -46,11 +53,48 @@ def test_noalloc_checksum_matches_library_checksum(gpulib, oracle):
         got = float(d_out.item())
         assert want[0] > 0
         np.testing.assert_allclose(got, want[0], rtol=CHECKSUM_RTOL, atol=0)
+        np.testing.assert_allclose(got, host_sum(m.f[name], x0, x1, y0, y1),
+                                   rtol=CHECKSUM_RTOL, atol=0)
 
-    # Beyond the fixed capacity (more than 8192 x 8192 cells): rejected on
-    # the host before any launch.
+    # Queued on a side stream (the caller's cudaStream_t).
+    side = torch.cuda.Stream()
+    x0, x1, y0, y1 = rects["sshn_t"]
     dptr = gpulib.nl2d_device_ptr(m.f["sshn_t"].ctypes.data)
-    rc = gpulib.nl2d_field_checksum_noalloc(dptr, 10000, 0, 9999, 0, 9999,
+    with torch.cuda.stream(side):
+        d_side = torch.zeros(1, dtype=torch.float64, device="cuda")
+        rc = gpulib.nl2d_field_checksum_noalloc(dptr, m.width, x0, x1, y0, y1,
+                                                d_side.data_ptr(), side.cuda_stream)
+    assert rc == P.NL2D_OK
+    side.synchronize()
+    np.testing.assert_allclose(float(d_side.item()), host_sum(m.f["sshn_t"], x0, x1, y0, y1),
+                               rtol=CHECKSUM_RTOL, atol=0)
+    gpulib.nl2d_finalize()
+
+
+def test_noalloc_checksum_capacity_boundary(gpulib):
+    """Exactly 8192 x 8192 cells fit the fixed array and give the host sum;
+    one column more is rejected on the host before any launch."""
+    import psyclonebench_gb300 as P
+    import torch
+
+    n = 8192
+    g = torch.Generator(device="cuda").manual_seed(5)
+    f = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    d_out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    assert n * n == LIMIT_CELLS
+    rc = gpulib.nl2d_field_checksum_noalloc(f.data_ptr(), n, 0, n - 1, 0, n - 1,
+                                            d_out.data_ptr(), None)
+    assert rc == P.NL2D_OK
+    torch.cuda.synchronize()
+    want = float(np.abs(f.cpu().numpy()).sum())
+    np.testing.assert_allclose(float(d_out.item()), want, rtol=CHECKSUM_RTOL, atol=0)
+    # 8193 x 8192 cells: one partial too many (never launched, so the
+    # rectangle may exceed the allocation).
+    rc = gpulib.nl2d_field_checksum_noalloc(f.data_ptr(), n + 1, 0, n, 0, n - 1,
                                             d_out.data_ptr(), None)
     assert rc == P.NL2D_ERR_TOO_LARGE
-    gpulib.nl2d_finalize()
+    rc = gpulib.nl2d_field_checksum_noalloc(f.data_ptr(), 10000, 0, 9999, 0, 9999,
+                                            d_out.data_ptr(), None)
+    assert rc == P.NL2D_ERR_TOO_LARGE
+    del f
