@@ -355,7 +355,7 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
     specs = ensemble_domains(ndom, seed)
     mine = shard_domains(specs, world)[rank] if world > 1 else list(range(ndom))
     doms = [build_domain(specs[k]) for k in mine]
-    ens = Ensemble(doms, rdt=BATHY_RDT, lib=lib)
+    ens = Ensemble(doms, lib=lib)
     tune = autotune.tune(ens, steps=3)
     ens.run(1, 1)
     ms, _ = ens.run(2, steps)
@@ -370,6 +370,7 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
     # persistent kernel costs.
     seq_ms, seq_cells = 0.0, 0
     import psyclonebench_gb300 as P
+    from psyclonebench_gb300 import workloads as W
     from psyclonebench_gb300.model import Model, register
     sample = doms[:SEQ_SAMPLE]
     for d in sample:
@@ -377,7 +378,7 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
         m = Model.from_extents(w, h, xs, xe, ys, ye).uniform_metrics()
         m.grid["tmask"][:] = np.ascontiguousarray(d["tmask"], np.int32)
         m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = d["ht"], d["hu"], d["hv"]
-        m.rdt, m.cbfr, m.visc = BATHY_RDT, 1.5e-4, 0.1
+        m.rdt, m.cbfr, m.visc = W.ENSEMBLE_RDT, W.ENSEMBLE_CBFR, W.ENSEMBLE_VISC
         register(lib, m)
         t = ctypes.c_double(0.0)
         P.check(lib.nl2d_timed_run(1, 2, ctypes.byref(t)), "seq warm-up")
@@ -385,7 +386,7 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
         seq_ms += t.value
         seq_cells += (xe - xs + 1) * (ye - ys + 1)
     lib.nl2d_finalize()
-    ens_s = Ensemble(sample, rdt=BATHY_RDT, lib=lib)
+    ens_s = Ensemble(sample, lib=lib)
     ens_s.schedule(tune["ctas_per_sm"], tune["policy"], tune["boundary_weight"])
     ens_s.run(1, 1)
     ms_s, _ = ens_s.run(2, steps)
@@ -456,8 +457,12 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
     test = E.Dataset(count=16, nsnap=nsnap, seed=seed + 1000, n=256, lib=lib, scales_from=ds,
                      solver="fp64")
     t_net, t_pers = E.evaluate(test, net, list(range(16)), probe_snaps)
+    # the network on its own over the whole horizon (no judge), then the
+    # judged hybrid
+    free = E.rollout(test, net, range(16), start_snap=0, emu_steps=nsnap - 1, judge_every=50,
+                     threshold=1e-3, judge_share=0.0)
     roll = E.rollout(test, net, range(16), start_snap=0, emu_steps=nsnap - 1, judge_every=50,
-                     threshold=1e-3)
+                     threshold=1e-3, judge_share=0.25)
     return {
         "workload": "nemolite2d_emulator_%d_domains_256x256_%d_pairs_k10_horizon%d" % (
             count, count * len(ds.pair_starts), horizon),
@@ -478,6 +483,10 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
                       "speedup_vs_fp64_solver": emu_value / test.solver_mcells,
                       "mixed_solver_same_size_domains": ds.solver_mcells,
                       "speedup_vs_mixed_solver": emu_value / ds.solver_mcells},
+        "free_running": {k: free[k] for k in ("final_ssh_rms_error_m",
+                                                 "final_ssh_rms_error_worst_domain_m",
+                                                 "final_ssh_rms_m", "final_nonfinite",
+                                                 "emulator_ms", "solver_only_ms")},
         "rollout": roll,
     }
 

@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import NL2D_OK, Nl2dError, load_library
-from .workloads import fourier_depth
+from .workloads import ENSEMBLE_CBFR, ENSEMBLE_RDT, ENSEMBLE_VISC, fourier_depth
 
 PI = 3.1415926535897932
 G = 9.80665
@@ -99,11 +99,12 @@ def gather_results(local, timeout_s=30.0):
 
 class Ensemble:
     """A set of domains resident on the GPU.  `domains` are build_domain()
-    dicts; all share rdt, cbfr and visc, and dx, dy and latitude unless a
+    dicts; all share rdt, cbfr and visc (by default the ensemble
+    configuration's, workloads.ENSEMBLE_*), and dx, dy and latitude unless a
     domain carries its own as "geo": (dx, dy, gphi)."""
 
-    def __init__(self, domains, rdt=5.0, cbfr=1.5e-4, visc=0.1, dx=1000.0, dy=1000.0,
-                 gphi=50.0, lib=None):
+    def __init__(self, domains, rdt=ENSEMBLE_RDT, cbfr=ENSEMBLE_CBFR, visc=ENSEMBLE_VISC,
+                 dx=1000.0, dy=1000.0, gphi=50.0, lib=None):
         self.lib = lib or load_library()
         self.domains = domains
         n = len(domains)

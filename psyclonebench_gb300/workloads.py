@@ -13,6 +13,20 @@ import math
 
 import numpy as np
 
+# Physics of the ensemble and emulator domains (configurations 3 and 4),
+# which state bathymetry, tides and open sides but not viscosity or
+# friction.  These take the reference namelist reader's own defaults,
+# visc = 100 m^2/s and cbfr = 1e-3 (common/gocean2d_io_mod.f90:57-68); the
+# parity namelist's 0.1 and 1.5e-4 (original/namelist.128) describe a
+# flat-bottomed basin with a 0.2 m tide.  With those weak values, tides of
+# up to 0.5 m over 50-500 m Fourier bathymetry drive the open-boundary
+# faces of the scheme's explicit step into growth: about half of the seeded
+# domains overflow within 5000 steps at rdt = 5 s (a quarter at rdt = 1 s,
+# so not a time-step limit), where with the defaults 1 of 64 does.
+ENSEMBLE_RDT = 5.0     # s; 500 m of water carries gravity waves at 70 m/s
+ENSEMBLE_CBFR = 1.0e-3
+ENSEMBLE_VISC = 100.0
+
 
 def fourier_depth(width, height, seed, mean=275.0, nmodes=16, dx=1000.0, dy=1000.0):
     """(ht, hu, hv) as [height][width] FP64 arrays."""

@@ -120,7 +120,7 @@ def gpu_run_graph(lib, m, nsteps, nit000=1, every=0):
     return out[:3 * nsums].reshape(-1, 3)
 
 
-def ensemble_oracle_run(dom, nsteps, rdt=5.0, oracle=None, every=0):
+def ensemble_oracle_run(dom, nsteps, rdt=None, oracle=None, every=0, cbfr=None, visc=None):
     """Runs one ensemble domain (a build_domain() dict, at rest) through the
     oracle with its tide; returns (model, checksums list)."""
     lib = oracle or load_oracle()
@@ -128,7 +128,10 @@ def ensemble_oracle_run(dom, nsteps, rdt=5.0, oracle=None, every=0):
     m = Model.from_extents(*dom["dims"]).uniform_metrics()
     m.grid["tmask"][:] = np.ascontiguousarray(dom["tmask"], np.int32)
     m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = dom["ht"], dom["hu"], dom["hv"]
-    m.rdt, m.cbfr, m.visc = rdt, 1.5e-4, 0.1
+    from psyclonebench_gb300 import workloads as W
+    m.rdt = W.ENSEMBLE_RDT if rdt is None else rdt
+    m.cbfr = W.ENSEMBLE_CBFR if cbfr is None else cbfr
+    m.visc = W.ENSEMBLE_VISC if visc is None else visc
     amp, per = dom["tide"]
     sums = []
     for k in range(nsteps):

@@ -222,19 +222,30 @@ def test_emulator_beats_persistence_on_held_out_domains(gpulib, small_dataset):
 
 
 def test_hybrid_rollout_judges_and_falls_back(gpulib, small_dataset):
-    """A roll-out with the FP64 solver as judge: with an unreachable error
-    threshold every window falls back to the solver, whose result then
-    equals the pure-solver truth up to the FP32 hand-off of the state
-    between windows; with a loose one the emulator keeps every window."""
+    """A roll-out with the FP64 solver re-running each window as judge (every
+    domain judged every window here).  With an unreachable threshold the
+    first window fails for both domains: they take the solver's window-end
+    state and the solver advances them through the second window, so the
+    result equals the pure-solver truth up to the FP32 hand-off of the state
+    between windows.  With a loose threshold the emulator keeps every
+    window and the judge still reports each window's error."""
     from psyclonebench_gb300.emulator import ConvNet, rollout
     ds = small_dataset
     net = ConvNet(4, ds.n, ds.n, seed=2, lib=gpulib)
-    strict = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=0.0)
-    assert strict["windows_solver"] == 2 and strict["windows_emulator"] == 0
+    strict = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=0.0,
+                     judge_share=1.0)
+    assert strict["judged"] == 2 and strict["judge_failed"] == 2
+    assert strict["solver_windows"] == 2
     assert strict["final_ssh_rms_error_m"] < 1e-6
-    loose = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=1e9)
-    assert loose["windows_emulator"] == 2 and loose["windows_solver"] == 0
-    assert len(loose["judge_errors_m"]) == 2
+    loose = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=1e9,
+                    judge_share=1.0)
+    assert loose["judged"] == 4 and loose["judge_failed"] == 0 and loose["solver_windows"] == 0
+    assert len(loose["judge_errors_m"]) == 4
+    assert all(e > 0 for e in loose["judge_errors_m"])
+    # a share of one half judges each domain every other window
+    half = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=1e9,
+                   judge_share=0.5)
+    assert half["judged"] == 2
 
 
 def test_advance_applies_the_solver_boundary_conditions(gpulib, small_dataset):

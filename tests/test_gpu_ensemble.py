@@ -30,7 +30,7 @@ def domains():
 @pytest.mark.parametrize("cps,policy", [(2, 0), (1, 1), (2, 2)])
 def test_ensemble_matches_oracle(gpulib, oracle, domains, cps, policy):
     from psyclonebench_gb300.ensemble import Ensemble
-    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    ens = Ensemble(domains, lib=gpulib)
     ens.schedule(cps, policy, 4.0)
     ms, sums = ens.run(1, 90, checksum_every=30)
     assert sums.shape == (3, len(domains), 3)
@@ -50,7 +50,7 @@ def test_autotuner_picks_a_schedule(gpulib, domains, tmp_path, monkeypatch):
     from psyclonebench_gb300 import autotune
     from psyclonebench_gb300.ensemble import Ensemble
     monkeypatch.setenv("NL2D_TUNE_CACHE", str(tmp_path))
-    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    ens = Ensemble(domains, lib=gpulib)
     choice = autotune.tune(ens, steps=2)
     assert not choice["cached"] and len(choice["timings"]) == len(autotune.CANDIDATES)
     again = autotune.tune(ens, steps=2)
@@ -68,7 +68,7 @@ def test_mixed_ensemble_error_vs_fp64(gpulib, domains):
     """The FP32 form of the ensemble stays within 1e-6 m ssh RMS of the
     FP64 ensemble (itself bit-identical to the reference) after 300 steps."""
     from psyclonebench_gb300.ensemble import Ensemble
-    ens = Ensemble(domains, rdt=5.0, lib=gpulib)
+    ens = Ensemble(domains, lib=gpulib)
     ens.run(1, 300)
     ref = [ens.read(k) for k in range(len(domains))]
     ens.set_precision(1)
@@ -97,7 +97,7 @@ def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
     doms = [dict(d) for d in domains[:4]]
     doms[1]["geo"] = (900.0, 1100.0, 45.0)
     doms[3]["geo"] = (1200.0, 800.0, 30.0)
-    ens = Ensemble(doms, rdt=5.0, lib=gpulib)
+    ens = Ensemble(doms, lib=gpulib)
     ens.run(1, 300)
     ref = [ens.read(k) for k in range(len(doms))]
     ens.set_precision(1)
@@ -113,3 +113,92 @@ def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
     print("tile-form mixed ensemble worst per-domain ssh RMS error:", worst)
     assert worst <= 1e-6
     ens.close()
+
+
+# ---- a sample of the benchmark's own 512-domain draw ----------------------
+
+BENCH_ENSEMBLE_SEED = 7  # bench.py's run_ensemble draw
+
+
+def config3_sample():
+    """24 domains of workloads.ensemble_domains(512, 7): the widest and the
+    tallest, the two largest by cells, and five more per open side; every
+    tide is the domain's own (amplitudes 0.05-0.5 m, periods 10-14 h)."""
+    from psyclonebench_gb300.workloads import ensemble_domains
+    specs = ensemble_domains(512, BENCH_ENSEMBLE_SEED)
+    cells = [s["nx"] * s["ny"] for s in specs]
+    pick = [max(range(512), key=lambda k: specs[k]["nx"]),
+            max(range(512), key=lambda k: specs[k]["ny"])]
+    for k in sorted(range(512), key=lambda k: -cells[k]):
+        if len(pick) == 4:
+            break
+        if k not in pick:
+            pick.append(k)
+    rng = np.random.default_rng(29)
+    for side in "SNEW":
+        cand = [k for k in range(512) if specs[k]["open_side"] == side and k not in pick]
+        pick += [int(k) for k in rng.choice(cand, size=5, replace=False)]
+    return [specs[k] for k in pick]
+
+
+def _oracle_job(args):
+    """Runs in a spawned worker: the oracle's tide-parametrised step of one
+    domain; returns its (sshn_t, un, vn)."""
+    spec, nsteps = args
+    import nl2d_testlib as T
+    from psyclonebench_gb300.ensemble import build_domain
+    m, _ = T.ensemble_oracle_run(build_domain(spec), nsteps)
+    return m.f["sshn_t"], m.f["un"], m.f["vn"]
+
+
+def test_ensemble_bench_sample_matches_oracle(gpulib):
+    """24 domains of the benchmark's 512-domain ensemble (up to 1016 cells
+    wide, all four open sides, their own tides), 60 FP64 steps in one
+    persistent launch per step: every domain bit-identical to the oracle's
+    step with that domain's tide."""
+    import multiprocessing as mp
+
+    from psyclonebench_gb300.ensemble import Ensemble, build_domain
+    specs = config3_sample()
+    assert max(s["nx"] for s in specs) >= 1000 and {s["open_side"] for s in specs} == set("SNEW")
+    assert all((s["tide_amp"], s["tide_period_h"]) != (0.2, 12.42) for s in specs)
+    nsteps = 60
+    with mp.get_context("spawn").Pool(min(8, mp.cpu_count())) as pool:
+        pending = pool.map_async(_oracle_job, [(s, nsteps) for s in specs])
+        doms = [build_domain(s) for s in specs]
+        ens = Ensemble(doms, lib=gpulib)
+        ens.run(1, nsteps)
+        got = [ens.read(k) for k in range(len(doms))]
+        ens.close()
+        want = pending.get(timeout=900)
+    for k, d in enumerate(doms):
+        w, h, xs, xe, ys, ye = d["dims"]
+        for f, name in enumerate(("sshn_t", "un", "vn")):
+            a = got[k][f][ys - 1:ye + 1, xs - 1:xe + 2]
+            b = want[k][f][ys - 1:ye + 1, xs - 1:xe + 2]
+            assert bits_equal(a, b), (k, specs[k], name)
+        assert np.abs(want[k][0]).max() > 0  # the tide has entered
+
+
+def test_mixed_ensemble_bench_sample_2000_steps(gpulib):
+    """The same 24 domains over 2000 steps: the mixed-precision ensemble
+    stays within 1e-6 m ssh RMS of the FP64 ensemble (bit-identical to the
+    reference step, previous test) on every domain."""
+    from psyclonebench_gb300.ensemble import Ensemble, build_domain
+    doms = [build_domain(s) for s in config3_sample()]
+    ens = Ensemble(doms, lib=gpulib)
+    ens.run(1, 2000)
+    ref = [ens.read(k) for k in range(len(doms))]
+    ens.set_precision(1)
+    ens.run(1, 2000)
+    assert ens.uses_march()
+    worst = 0.0
+    for k, d in enumerate(doms):
+        w, h, xs, xe, ys, ye = d["dims"]
+        got = ens.read(k)
+        assert all(np.isfinite(ref[k][f]).all() for f in range(3))
+        diff = got[0][ys:ye + 1, xs:xe + 1] - ref[k][0][ys:ye + 1, xs:xe + 1]
+        worst = max(worst, float(np.sqrt(np.mean(diff * diff))))
+    ens.close()
+    print("bench-sample mixed ensemble worst per-domain ssh RMS error after 2000 steps:", worst)
+    assert worst <= 1e-6
