@@ -361,6 +361,7 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
     ms, _ = ens.run(2, steps)
     cells, ntiles, nctas = ens.info()
     ens.set_precision(1)
+    tune_mixed = autotune.tune(ens, steps=3, precision="mixed", base=tune)
     ens.run(1, 1)
     ms_mix, _ = ens.run(2, steps)
     ens.close()
@@ -387,7 +388,8 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
         seq_cells += (xe - xs + 1) * (ye - ys + 1)
     lib.nl2d_finalize()
     ens_s = Ensemble(sample, lib=lib)
-    ens_s.schedule(tune["ctas_per_sm"], tune["policy"], tune["boundary_weight"])
+    ens_s.schedule(tune["ctas_per_sm"], tune["policy"], tune["boundary_weight"],
+                   tuple(tune["tile"]), tune["march_rows"])
     ens_s.run(1, 1)
     ms_s, _ = ens_s.run(2, steps)
     ens_s.close()
@@ -404,7 +406,13 @@ def run_ensemble(lib, steps=20, ndom=512, seed=7, rank=0, world=1):
                 "persistent_value_same_sample": seq_cells / (ms_s / steps * 1e-3) / 1e6,
                 "speedup_persistent_vs_sequential": seq_ms / ms_s},
             "schedule": {k: tune[k] for k in ("ctas_per_sm", "policy", "boundary_weight",
-                                              "cached")}}
+                                              "tile", "cached")},
+            "schedule_timings_ms": [(t["ctas_per_sm"], t["policy"], t["boundary_weight"],
+                                     t["tile"], round(t["ms_per_step"], 4))
+                                    for t in tune.get("timings", [])],
+            "mixed_march_rows": tune_mixed["march_rows"],
+            "mixed_march_timings_ms": [(t["march_rows"], round(t["ms_per_step"], 4))
+                                       for t in tune_mixed.get("timings", [])]}
 
 
 def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):

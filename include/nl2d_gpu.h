@@ -203,6 +203,14 @@ int nl2d_ens_set_domain(int dom, const int *tmask, const double *ht,
  * hardware block scheduler; the CTA count then does not apply) and the
  * cost weight of a boundary-tile edge cell. */
 int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight);
+/* Tile knobs the autotuner searches (the reference's tiled OpenMP layer,
+ * psykal_omp/time_step_mod.f90:587-1182, fixes its tile size per run): the
+ * FP64 kernel's tile shape tx x ty, one of 32 x 16 (the default), 32 x 8,
+ * 16 x 16, 64 x 8 and 32 x 32, and the mixed form's column-march strip
+ * height, 8, 16 or 32 rows (the default).  Results do not depend on
+ * either.  A new ensemble starts with the defaults.  Returns NL2D_ERR_ARGS
+ * for other values. */
+int nl2d_ens_tile(int tx, int ty, int march_rows);
 /* Advances every domain nsteps steps (istep = istep0 ...); per-domain
  * ssh / u / v checksums after every checksum_every-th step go to
  * checksums_out[(s * ndom + dom) * 3 + f].  *ms_out: device time. */

@@ -58,6 +58,7 @@ EXPORTS = {
     "nl2d_ens_create": (ctypes.c_int, [ctypes.c_int, _IP, _DP, _DP, _DP]),
     "nl2d_ens_set_domain": (ctypes.c_int, [ctypes.c_int, _IP, _DP, _DP, _DP]),
     "nl2d_ens_schedule": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "nl2d_ens_tile": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "nl2d_ens_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     "nl2d_ens_read": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_ens_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),

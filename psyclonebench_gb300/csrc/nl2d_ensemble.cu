@@ -87,7 +87,8 @@ __global__ void k_mixed_statics(const double* __restrict__ ht, const double* __r
 // Ensemble: a persistent grid walks a tile list spanning many independent
 // domains; CTA b takes tiles [first[b], first[b+1]).  `tides` holds this
 // step's bc_ssh value per domain.
-__global__ void __launch_bounds__(NTHREADS, 2)
+template <class T>
+__global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
     k_ensemble_step(const EnsDomain* __restrict__ doms, const int4* __restrict__ tiles,
                     const int* __restrict__ first, int parity,
                     const double* __restrict__ tides) {
@@ -97,7 +98,51 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     const int4 tl = tiles[t];
     const EnsDomain& D = doms[tl.x];
     __syncthreads();  // the previous tile's last readers are done with smem
-    fused_tile(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
+    fused_tile<T>(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
+  }
+}
+
+// The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
+// search space); shape 0 is the single-domain kernel's.
+constexpr int kNumShapes = 5;
+constexpr int kShapes[kNumShapes][2] = {{32, 16}, {32, 8}, {16, 16}, {64, 8}, {32, 32}};
+
+template <class T>
+bool set_ens_attr() {
+  static bool attr = false;
+  if (!attr)
+    attr = cudaFuncSetAttribute(k_ensemble_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)T::kSmemBytes) == cudaSuccess;
+  return attr;
+}
+
+// Opts the chosen shape's kernel into its dynamic shared memory (before any
+// stream capture).
+bool prepare_ens_step(int shape) {
+  switch (shape) {
+    case 1: return set_ens_attr<Tile<32, 8>>();
+    case 2: return set_ens_attr<Tile<16, 16>>();
+    case 3: return set_ens_attr<Tile<64, 8>>();
+    case 4: return set_ens_attr<Tile<32, 32>>();
+    default: return set_ens_attr<DefaultTile>();
+  }
+}
+
+template <class T>
+void launch_ens_step_shape(int nctas, const EnsDomain* doms, const int4* tiles, const int* first,
+                           int parity, const double* tides, cudaStream_t st) {
+  k_ensemble_step<T><<<nctas, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(doms, tiles, first,
+                                                                         parity, tides);
+}
+
+void launch_ens_step(int shape, int nctas, const EnsDomain* doms, const int4* tiles,
+                     const int* first, int parity, const double* tides, cudaStream_t st) {
+  switch (shape) {
+    case 1: launch_ens_step_shape<Tile<32, 8>>(nctas, doms, tiles, first, parity, tides, st); break;
+    case 2: launch_ens_step_shape<Tile<16, 16>>(nctas, doms, tiles, first, parity, tides, st); break;
+    case 3: launch_ens_step_shape<Tile<64, 8>>(nctas, doms, tiles, first, parity, tides, st); break;
+    case 4: launch_ens_step_shape<Tile<32, 32>>(nctas, doms, tiles, first, parity, tides, st); break;
+    default: launch_ens_step_shape<DefaultTile>(nctas, doms, tiles, first, parity, tides, st);
   }
 }
 
@@ -159,8 +204,10 @@ struct Ens {
   int parity = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
-  int graph_key[5] = {-1, -1, -1, -1, -1};
+  int graph_key[7] = {-1, -1, -1, -1, -1, -1, -1};
   bool built = false;
+  int shape = 0;        // index into kShapes: the FP64 kernel's tile
+  int march_rows = 32;  // strip height of the mixed form's column march
   // mixed-precision form
   int precision = 0;
   float2* msn[2] = {};
@@ -234,6 +281,8 @@ void ens_free() {
   e.built = false;
   e.ndom = 0;
   e.dom.clear();
+  e.shape = 0;
+  e.march_rows = mixk::MR;
 }
 
 // Flather chains or reads outside the array exclude a domain (the one-launch
@@ -430,9 +479,10 @@ bool build_march(const std::vector<EnsMixDomain>& desc) {
   for (const EnsMixDomain& x : desc) {
     const int nx = x.d.xe - x.d.xs + 3, ny = x.d.ye - x.d.ys + 2;
     const int dom = (int)(&x - desc.data());
-    for (int gy = 0; gy < (ny + mixk::MR - 1) / mixk::MR; gy++)
+    const int mr = e.march_rows;
+    for (int gy = 0; gy < (ny + mr - 1) / mr; gy++)
       for (int gx = 0; gx < (nx + mixk::MW - 1) / mixk::MW; gx++)
-        units.push_back(make_int4(dom, x.d.xs - 1 + gx * mixk::MW, x.d.ys - 1 + gy * mixk::MR, 0));
+        units.push_back(make_int4(dom, x.d.xs - 1 + gx * mixk::MW, x.d.ys - 1 + gy * mr, 0));
   }
   cudaFree(e.d_units);
   e.d_units = nullptr;
@@ -660,6 +710,19 @@ int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight) {
   return NL2D_OK;
 }
 
+int nl2d_ens_tile(int tx, int ty, int march_rows) {
+  Ens& e = g_ens;
+  int shape = -1;
+  for (int k = 0; k < kNumShapes; k++)
+    if (kShapes[k][0] == tx && kShapes[k][1] == ty) shape = k;
+  if (shape < 0 || (march_rows != 8 && march_rows != 16 && march_rows != 32))
+    return NL2D_ERR_ARGS;
+  e.shape = shape;
+  e.march_rows = march_rows;
+  e.built = false;
+  return NL2D_OK;
+}
+
 int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_out,
                  double* ms_out) {
   nl2d::NvtxRange nvtx_range("nl2d_ens_run");
@@ -672,16 +735,11 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     // a rebuild may move every buffer a captured graph refers to
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_ensemble_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)kSmemBytes);
-      attr = true;
-    }
     if (e.precision == 1) {
       if (!build_mixed() || (!e.march && !build_schedule(mixk::TX, mixk::TY)))
         return NL2D_ERR_CUDA;
-    } else if (!build_descriptors() || !build_schedule(TX, TY)) {
+    } else if (!build_descriptors() ||
+               !build_schedule(kShapes[e.shape][0], kShapes[e.shape][1])) {
       return NL2D_ERR_CUDA;
     }
     e.parity = 0;
@@ -716,11 +774,13 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     if (!ck(cudaMalloc(&e.d_sums, nsum_vals * 8))) return NL2D_ERR_CUDA;
     e.sums_cap = nsum_vals;
   }
-  const int key[5] = {nsteps, checksum_every, e.parity, e.nctas, e.policy * 2 + e.precision};
+  const int key[7] = {nsteps,  checksum_every, e.parity,    e.nctas, e.policy * 2 + e.precision,
+                      e.shape, e.march_rows};
   if (!(e.graph && memcmp(key, e.graph_key, sizeof key) == 0)) {
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
-    cudaGraph_t g;
+    cudaGraph_t g = nullptr;
+    if (e.precision == 0 && !prepare_ens_step(e.shape)) return NL2D_ERR_CUDA;
     if (!ck(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal)))
       return NL2D_ERR_CUDA;
     int par = e.parity;
@@ -731,7 +791,8 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         const MixedFields mf{e.mht, e.mhu, e.mhv, e.mrhu, e.mrhv, e.mreg, nullptr, 0};
         const MixedState ms{e.msn[par], e.mun[par], e.mvn[par],
                             e.msn[1 - par], e.mun[1 - par], e.mvn[1 - par]};
-        launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.stream);
+        launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.march_rows,
+                               e.stream);
         launch_ens_mixed_general(e.d_mdesc, e.mglist, e.mgn, par,
                                  e.d_tides + (size_t)q * e.ndom, e.stream);
         par = 1 - par;
@@ -746,8 +807,8 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
           k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
                                                                             sums);
       } else {
-        k_ensemble_step<<<e.nctas, dim3(TX, ROWS_PER_PASS), kSmemBytes, e.stream>>>(
-            e.d_desc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
+        launch_ens_step(e.shape, e.nctas, e.d_desc, e.d_tiles, e.d_first, par,
+                        e.d_tides + (size_t)q * e.ndom, e.stream);
         par = 1 - par;
         if (want_sums)
           k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,

@@ -32,13 +32,15 @@
 namespace nl2d {
 namespace {
 
-__global__ void __launch_bounds__(NTHREADS, 2)
+using T = DefaultTile;
+
+__global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
     k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
   extern __shared__ double smem[];
   // Tiles cover the copy region [xs-1, xe+1] x [ys-1, ye].
-  fused_tile(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
-             d.xs - 1 + blockIdx.x * TX, d.ys - 1 + blockIdx.y * TY, smem);
+  fused_tile<T>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
+                d.xs - 1 + blockIdx.x * T::TX, d.ys - 1 + blockIdx.y * T::TY, smem);
 }
 
 }  // namespace
@@ -49,14 +51,14 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_fused_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kSmemBytes);
+                         (int)T::kSmemBytes);
     attr_set = true;
   }
   const FastConst k = make_fast_const(s, um);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const dim3 grid((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_fused_step<<<grid, dim3(TX, ROWS_PER_PASS), kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
-                                                       tide_index, tide);
+  const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY);
+  k_fused_step<<<grid, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
+                                                                 tide_index, tide);
 }
 
 // Reciprocals RN(1 / (h + ssha)) of the momentum denominators, or 0 where

@@ -10,10 +10,12 @@ namespace nl2d {
 namespace {
 
 
-// A tile is TX x TY cells; its 256 threads (32 x 8) each update TY / 8 cells
-// of one column in the last phase.
-constexpr int TX = 32, TY = 16, HALO = 2, NTHREADS = 256, ROWS_PER_PASS = NTHREADS / TX;
-constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO;
+// A tile is TX x TY cells, worked on by 256 threads laid out TX x
+// (256 / TX); in the last phase each thread updates TY / (256 / TX) cells
+// of one column.  Tile<TX, TY> holds a shape's constants; the ensemble
+// instantiates several shapes (its autotuner picks one), the single-domain
+// kernel uses DefaultTile.  The arithmetic does not depend on the shape.
+constexpr int HALO = 2, NTHREADS = 256;
 
 // Step-invariant constants of the fast path, evaluated on the host with the
 // operations the reference performs per point (e.g. dx_v[c] + dx_v[e] on a
@@ -49,6 +51,7 @@ __device__ __forceinline__ double dvf(double x, double d, double r) {
   return bits(r) != 0 ? div_rn(x, d, r) : x / d;
 }
 
+template <int SX>
 struct Ctx {
   const double *__restrict__ sn, *__restrict__ un, *__restrict__ vn;
   const double *__restrict__ hu, *__restrict__ hv, *__restrict__ ht;
@@ -92,7 +95,8 @@ __device__ __forceinline__ double hi_only(double w, double p) {
 // range, with the masked (slip-wall) branches; returns false where the
 // kernel returns early (ua keeps its value).  Same operations as the
 // reference, with the exact helpers for halving, upwind picks and division.
-__device__ __forceinline__ bool mom_u(const Ctx& x, int i, int j, double& out) {
+template <int SX>
+__device__ __forceinline__ bool mom_u(const Ctx<SX>& x, int i, int j, double& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             se = s + 1, ne = n + 1;
   const int* m = x.m;
@@ -145,7 +149,8 @@ __device__ __forceinline__ bool mom_u(const Ctx& x, int i, int j, double& out) {
 }
 
 // momentum_v_code (momentum_v_kern.c:125-241) at v face (i,j).
-__device__ __forceinline__ bool mom_v(const Ctx& x, int i, int j, double& out) {
+template <int SX>
+__device__ __forceinline__ bool mom_v(const Ctx<SX>& x, int i, int j, double& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             nw = n - 1, ne = n + 1;
   const int* m = x.m;
@@ -200,7 +205,8 @@ __device__ __forceinline__ bool mom_v(const Ctx& x, int i, int j, double& out) {
 // ua at u face (i,j) after momentum_u and bc_solid_u, before Flather: the
 // value bc_flather_u reads.  On the copy region the previous step's ua is
 // the current un; elsewhere it is the ua array, which no fused step changes.
-__device__ __forceinline__ double ua_pre_flather(const Ctx& x, const double* ua_arr,
+template <int SX>
+__device__ __forceinline__ double ua_pre_flather(const Ctx<SX>& x, const double* ua_arr,
                                                  int i, int j) {
   const int c = j * x.W + i;
   double ua = x.in_copy(i, j) ? x.un[c] : ua_arr[c];
@@ -214,7 +220,8 @@ __device__ __forceinline__ double ua_pre_flather(const Ctx& x, const double* ua_
   return ua;
 }
 
-__device__ __forceinline__ double va_pre_flather(const Ctx& x, const double* va_arr,
+template <int SX>
+__device__ __forceinline__ double va_pre_flather(const Ctx<SX>& x, const double* va_arr,
                                                  int i, int j) {
   const int c = j * x.W + i;
   double va = x.in_copy(i, j) ? x.vn[c] : va_arr[c];
@@ -231,14 +238,27 @@ __device__ __forceinline__ double va_pre_flather(const Ctx& x, const double* va_
 // Shared-memory layout of one tile.  Phase 0 (halo 2) holds the loaded
 // fields and the sshn_u / sshn_v values this step sees; phase 1 (halo 1)
 // holds the terms that two neighbouring updates share.
-constexpr int S0 = SX * SY;            // 36 x 12 positions
-constexpr int P1X = TX + 2, P1Y = TY + 2;
-constexpr int S1 = P1X * P1Y;          // 34 x 10 positions
 enum { A_SN, A_UN, A_VN, A_HU, A_HV, A_SU, A_SV, A_HUS, A_HVS, N_A0 };
 enum { B_FLXU, B_FLXV, B_GX, B_GY, B_FXU, B_FYV, B_VSC, B_FYU, B_QY, B_UWC, B_FXV, B_QX, N_B1 };
-// + the mask, and the list of the tile's general (non-regular) cells
-constexpr size_t kSmemBytes =
-    sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * (S0 + TX * TY + 1);
+
+template <int TX_, int TY_>
+struct Tile {
+  static constexpr int TX = TX_, TY = TY_;
+  static constexpr int RPP = NTHREADS / TX;  // rows per pass of the thread block
+  static constexpr int RPT = TY / RPP;       // cells per thread in the update phase
+  static_assert(NTHREADS % TX == 0 && TY % RPP == 0 && (RPT == 1 || RPT == 2 || RPT == 4),
+                "tile shape");
+  static constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO;
+  static constexpr int S0 = SX * SY;  // phase-0 positions (36 x 20 for 32 x 16)
+  static constexpr int P1X = TX + 2, P1Y = TY + 2;
+  static constexpr int S1 = P1X * P1Y;  // phase-1 positions (34 x 18 for 32 x 16)
+  // + the mask, and the list of the tile's general (non-regular) cells
+  static constexpr size_t kSmemBytes =
+      sizeof(double) * (N_A0 * S0 + N_B1 * S1) + sizeof(int) * (S0 + TX * TY + 1);
+  // two CTAs of 256 threads per SM when their shared memory fits
+  static constexpr int kMinBlocks = 2 * kSmemBytes <= 227 * 1024 ? 2 : 1;
+};
+using DefaultTile = Tile<32, 16>;
 
 // A regular cell's new (sshn_t, un, vn) from the tile's staged fields (a0)
 // and shared terms (b1) at its slots q (phase 0) and r (phase 1): continuity
@@ -249,9 +269,11 @@ constexpr size_t kSmemBytes =
 struct RegOut {
   double ssh, u, v;
 };
+template <class T>
 __device__ __forceinline__ RegOut regular_cell(const double* a0, const double* b1, int q, int r,
                                                double sau, double rhu, double sav, double rhv,
                                                const FastConst& k) {
+  constexpr int S0 = T::S0, S1 = T::S1, SX = T::SX, P1X = T::P1X;
 #define A(qq, t) a0[(qq) * S0 + (t)]
 #define B(qq, t) b1[(qq) * S1 + (t)]
   RegOut o;
@@ -294,15 +316,18 @@ __device__ __forceinline__ RegOut regular_cell(const double* a0, const double* b
 
 // One tile of the fused step: cells [i0, i0+TX) x [j0, j0+TY) of the copy
 // region of one domain.  `tide` is this step's bc_ssh value.
+template <class T>
 __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs, const Dims& d,
                                            const Scalars& p, const UniformMetrics& um,
                                            const FastConst& k, double tide, int i0, int j0,
                                            double* smem) {
+  constexpr int TX = T::TX, SX = T::SX, S0 = T::S0, S1 = T::S1, P1X = T::P1X;
+  constexpr int ROWS_PER_PASS = T::RPP;
   double* a0 = smem;                 // [N_A0][S0]
   double* b1 = smem + N_A0 * S0;     // [N_B1][S1]
   int* mk = (int*)(b1 + N_B1 * S1);  // [S0]
   int* glist = mk + S0;              // [TX * TY] general cells of this tile
-  int* gcount = glist + TX * TY;
+  int* gcount = glist + TX * T::TY;
 #define A(q, t) a0[(q) * S0 + (t)]
 #define B(q, t) b1[(q) * S1 + (t)]
 
@@ -427,14 +452,15 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   // can interleave two independent FP64 chains; the per-face global inputs
   // are loaded first and the results stored last, so no store can alias a
   // later load.
-  static_assert(TY == 2 * ROWS_PER_PASS, "two rows per thread");
-  {
-    const int i = i0 + threadIdx.x;
-    int c[2], q[2], r[2];
-    bool reg[2];
 #pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const int row = threadIdx.y + e * ROWS_PER_PASS, j = j0 + row;
+  for (int pb = 0; pb < T::RPT; pb += 2) {
+    constexpr int NP = T::RPT >= 2 ? 2 : 1;  // rows taken together
+    const int i = i0 + threadIdx.x;
+    int c[NP], q[NP], r[NP];
+    bool reg[NP];
+#pragma unroll
+    for (int e = 0; e < NP; e++) {
+      const int row = threadIdx.y + (pb + e) * ROWS_PER_PASS, j = j0 + row;
       c[e] = j * W + i;
       q[e] = (row + HALO) * SX + (threadIdx.x + HALO);
       r[e] = (row + 1) * P1X + (threadIdx.x + 1);
@@ -449,26 +475,28 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
       reg[e] = regular;
       if (live && !regular) glist[atomicAdd(gcount, 1)] = row * TX + threadIdx.x;
     }
-    double sau[2], rhu[2], sav[2], rhv[2];
+    double sau[NP], rhu[NP], sav[NP], rhv[NP];
 #pragma unroll
-    for (int e = 0; e < 2; e++)
+    for (int e = 0; e < NP; e++)
       if (reg[e]) {
         sau[e] = f.ssha_u[c[e]];
         rhu[e] = f.r_hu[c[e]];
         sav[e] = f.ssha_v[c[e]];
         rhv[e] = f.r_hv[c[e]];
       }
-    RegOut o[2];
-    if (reg[0] && reg[1]) {
-      o[0] = regular_cell(a0, b1, q[0], r[0], sau[0], rhu[0], sav[0], rhv[0], k);
-      o[1] = regular_cell(a0, b1, q[1], r[1], sau[1], rhu[1], sav[1], rhv[1], k);
+    RegOut o[NP];
+    if (NP == 2 && reg[0] && reg[NP - 1]) {
+      o[0] = regular_cell<T>(a0, b1, q[0], r[0], sau[0], rhu[0], sav[0], rhv[0], k);
+      o[NP - 1] = regular_cell<T>(a0, b1, q[NP - 1], r[NP - 1], sau[NP - 1], rhu[NP - 1],
+                                  sav[NP - 1], rhv[NP - 1], k);
     } else {
 #pragma unroll
-      for (int e = 0; e < 2; e++)
-        if (reg[e]) o[e] = regular_cell(a0, b1, q[e], r[e], sau[e], rhu[e], sav[e], rhv[e], k);
+      for (int e = 0; e < NP; e++)
+        if (reg[e])
+          o[e] = regular_cell<T>(a0, b1, q[e], r[e], sau[e], rhu[e], sav[e], rhv[e], k);
     }
 #pragma unroll
-    for (int e = 0; e < 2; e++)
+    for (int e = 0; e < NP; e++)
       if (reg[e]) {
         fs.sshn_out[c[e]] = o[e].ssh;
         fs.un_out[c[e]] = o[e].u;
@@ -486,7 +514,7 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   const int q = (row + HALO) * SX + (col + HALO);
   double* su_tile = &A(A_SU, 0);
   double* sv_tile = &A(A_SV, 0);
-  Ctx x;
+  Ctx<SX> x;
   x.sn = sn;
   x.un = un;
   x.vn = vn;

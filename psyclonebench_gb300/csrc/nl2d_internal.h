@@ -125,7 +125,7 @@ int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, in
 // the step constants all domains share (mixk::MixConst).
 void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
                             const MixedFields& mf, const MixedState& ms, const void* k,
-                            cudaStream_t st);
+                            int march_rows, cudaStream_t st);
 void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,
                               const double* tides, cudaStream_t st);
 void launch_ens_mixed_flags(const void* doms, int dom, unsigned char* reg, int2* glist,

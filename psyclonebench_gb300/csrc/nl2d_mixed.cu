@@ -68,12 +68,12 @@ __global__ void __launch_bounds__(128)
 // with the packed arrays' base pointers in mf / ms.
 __global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
     k_ensemble_mixed_march(const EnsDom* __restrict__ doms, const int4* __restrict__ units,
-                           int nunits, MixedFields mf, MixedState ms, MarchConst k) {
+                           int nunits, MixedFields mf, MixedState ms, MarchConst k, int mr) {
   const int w = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
   const Dims d = doms[u.x].d;
-  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, MR);
+  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, mr);
 }
 
 // The other cells of every domain's copy region: glist[t] = (domain, cell).
@@ -180,11 +180,11 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
 
 void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
                             const MixedFields& mf, const MixedState& ms, const void* k,
-                            cudaStream_t st) {
+                            int march_rows, cudaStream_t st) {
   MixConst kc;
   memcpy(&kc, k, sizeof kc);
   k_ensemble_mixed_march<<<(nunits + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-      (const EnsDom*)doms, units, nunits, mf, ms, make_march_const(kc));
+      (const EnsDom*)doms, units, nunits, mf, ms, make_march_const(kc), march_rows);
 }
 
 void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,

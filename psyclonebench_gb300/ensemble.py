@@ -130,9 +130,15 @@ class Ensemble:
         domains share the step's constants) rather than the tile form."""
         return bool(self.lib.nl2d_ens_uses_march())
 
-    def schedule(self, ctas_per_sm=2, policy=0, boundary_weight=4.0):
+    def schedule(self, ctas_per_sm=2, policy=0, boundary_weight=4.0, tile=(32, 16),
+                 march_rows=32):
+        """Schedule and tile knobs (nl2d_ens_schedule, nl2d_ens_tile): CTAs
+        per SM, tile assignment policy, boundary-edge cost weight, the FP64
+        tile shape and the mixed form's march strip height."""
         self._check(self.lib.nl2d_ens_schedule(ctas_per_sm, policy, boundary_weight),
                     "nl2d_ens_schedule")
+        self._check(self.lib.nl2d_ens_tile(int(tile[0]), int(tile[1]), march_rows),
+                    "nl2d_ens_tile")
 
     def run(self, istep0, nsteps, checksum_every=0):
         """Returns (device ms, checksums [samples, domains, 3])."""

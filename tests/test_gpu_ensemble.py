@@ -27,11 +27,15 @@ def domains():
     return [build_domain(s) for s in small_specs()]
 
 
-@pytest.mark.parametrize("cps,policy", [(2, 0), (1, 1), (2, 2)])
-def test_ensemble_matches_oracle(gpulib, oracle, domains, cps, policy):
+@pytest.mark.parametrize("cps,policy,tile", [(2, 0, (32, 16)), (1, 1, (32, 16)),
+                                             (2, 2, (32, 16)), (2, 0, (32, 8)),
+                                             (2, 1, (16, 16)), (1, 0, (64, 8)),
+                                             (2, 2, (32, 32))])
+def test_ensemble_matches_oracle(gpulib, oracle, domains, cps, policy, tile):
+    """Bit-identical under every schedule and every tile shape."""
     from psyclonebench_gb300.ensemble import Ensemble
     ens = Ensemble(domains, lib=gpulib)
-    ens.schedule(cps, policy, 4.0)
+    ens.schedule(cps, policy, 4.0, tile)
     ms, sums = ens.run(1, 90, checksum_every=30)
     assert sums.shape == (3, len(domains), 3)
     for k, d in enumerate(domains):
@@ -52,15 +56,38 @@ def test_autotuner_picks_a_schedule(gpulib, domains, tmp_path, monkeypatch):
     monkeypatch.setenv("NL2D_TUNE_CACHE", str(tmp_path))
     ens = Ensemble(domains, lib=gpulib)
     choice = autotune.tune(ens, steps=2)
-    assert not choice["cached"] and len(choice["timings"]) == len(autotune.CANDIDATES)
+    n = len(autotune.SCHEDULES) + 2 * (len(autotune.SHAPES) - 1)
+    assert not choice["cached"] and len(choice["timings"]) == n
+    assert choice["ms_per_step"] == min(t["ms_per_step"] for t in choice["timings"])
+    print("autotuner timings (cps, policy, weight, tile: ms/step):",
+          [(t["ctas_per_sm"], t["policy"], t["boundary_weight"], t["tile"],
+            round(t["ms_per_step"], 4)) for t in choice["timings"]])
     again = autotune.tune(ens, steps=2)
     assert again["cached"] and again["policy"] == choice["policy"]
     # the tuned schedule gives the same bits as any other
     a_ms, a = ens.run(1, 20, checksum_every=20)
     ens.reset()
-    ens.schedule(1, 0, 0.0)
+    ens.schedule(1, 0, 0.0, (64, 8))
     b_ms, b = ens.run(1, 20, checksum_every=20)
     assert bits_equal(a, b)
+    ens.close()
+
+
+def test_mixed_march_strip_heights_agree(gpulib, domains):
+    """The mixed form's column march gives the same result for every strip
+    height the autotuner searches (each cell's arithmetic is the same)."""
+    from psyclonebench_gb300.ensemble import Ensemble
+    ens = Ensemble(domains, lib=gpulib)
+    ens.set_precision(1)
+    got = []
+    for mr in (8, 16, 32):
+        ens.schedule(2, 0, 4.0, (32, 16), mr)
+        ens.reset()
+        ens.run(1, 50)
+        assert ens.uses_march()
+        got.append([ens.read(k)[0] for k in range(len(domains))])
+    for k in range(len(domains)):
+        assert bits_equal(got[0][k], got[1][k]) and bits_equal(got[0][k], got[2][k]), k
     ens.close()
 
 
