@@ -645,20 +645,26 @@ def run_ours(args, rank, world, local):
         m2 = make_problem(n, written=True)
         if active:
             make_active(m2)
-        nbytes_in = sum(a.nbytes for a in m2.f.values()) + sum(a.nbytes for a in m2.grid.values())
-        nbytes_out = 3 * m2.f["sshn_t"].nbytes
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        first_path = None
         for k in range(args.steps):
             lib.c_invoke_time_step(*m2.step_args(1 + k))
+            if first_path is None:
+                first_path = lib.nl2d_last_path()
         for k in ("sshn_t", "un", "vn"):
             a = m2.f[k]
             lib.c_read_from_device(a.ctypes.data, a.ctypes.data, 1, 1, m2.width, m2.height, True)
         P.check(None, "e2e")
         secs = time.perf_counter() - t0
+        # the bytes the library copied (the 25 arrays at registration, the
+        # three fields read back)
+        moved = (ctypes.c_longlong * 2)()
+        P.check(lib.nl2d_transfer_bytes(moved), "transfer bytes")
         e2e = {"value": cells * args.steps * world / secs / 1e6, "unit": "Mcell-steps/s",
-               "h2d_bytes_per_step": nbytes_in / args.steps,
-               "d2h_bytes_per_step": nbytes_out / args.steps,
+               "h2d_bytes_per_step": moved[0] / args.steps,
+               "d2h_bytes_per_step": moved[1] / args.steps,
+               "first_step_path": {1: "reference-structured", 2: "fused"}.get(first_path),
                "seconds": secs}
         lib.nl2d_finalize()
 

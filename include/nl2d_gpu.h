@@ -53,6 +53,15 @@ extern "C" {
  * `width`.  Internal bounds are 0-based (time_step_mod.f90:82-85).  As in
  * the reference, the caller may pass dx_v / dx_t in the dy_v / dy_t slots
  * (time_step_mod.f90:76-77); the arrays are used as given.
+ *
+ * Residency: the first call with a set of arrays uploads all 25 of them;
+ * as with the reference's GPU layers (time_step_mod.f90:96-123) the device
+ * copy is authoritative after that call, and host arrays change the device
+ * state only through c_write_to_device.  When the uploaded state is what a
+ * step leaves (ua == un, va == vn, ssha_t == sshn_t on the copy region,
+ * sshn_u / sshn_v as next_sshu / next_sshv make them of sshn_t, as at the
+ * reference's rest start), the first step already takes the fused path;
+ * otherwise it is reference-structured.
  */
 void c_invoke_time_step(
     double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
@@ -351,6 +360,10 @@ int nl2d_checkpoint_read(const char *path, int *istep);
 
 /* Waits for all work queued by the library. */
 int nl2d_sync(void);
+
+/* Bytes copied host -> device (out[0]) and device -> host (out[1]) since the
+ * current problem was registered. */
+int nl2d_transfer_bytes(long long out[2]);
 
 /* ---- host side of the reference executable (no GPU needed) ---- */
 

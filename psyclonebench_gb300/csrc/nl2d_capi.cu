@@ -62,6 +62,9 @@ struct State {
   bool mixed_ahead = false;    // ... and it is newer than the FP64 arrays
   int status = NL2D_OK;
   char msg[512] = {0};
+  unsigned scan_flags = 0;     // last registration scan (kScan* bits)
+  double grid_refs[11] = {};   // the metric arrays' and latitudes' reference values
+  long long h2d_bytes = 0, d2h_bytes = 0;  // copied since registration
 };
 
 State g_state;
@@ -177,35 +180,74 @@ void host_sines(const double* gphi, size_t n, double d2r, double* out) {
   });
 }
 
-// What registration needs to know about the uploaded grid, from the device
-// copies at HBM speed: bit q (0..8) set if metric array q (area_t, area_u,
-// area_v, dx_u, dx_v, dx_t, dy_u, dy_v, dy_t) is not bitwise uniform over
-// [xs-1, xe+1] x [ys-1, ye+1] (every point a step reads it at); bits 9, 10
-// if gphiu / gphiv are not uniform over the whole array; bit 11 / 12 if a
-// Flather face in u / v reads another Flather face; bit 13 if one would read
-// outside the array (time_step.cpp's Flather loops are serial in those
-// cases).  The reference values (the region's first point, gphi's first
-// element) are compared as bit patterns.
+double* cur_sshn();
+double* cur_un();
+double* cur_vn();
+
+// What registration needs to know about the problem it uploads, as bits:
+// 0..8 metric array q (area_t, area_u, area_v, dx_u, dx_v, dx_t, dy_u, dy_v,
+// dy_t) not bitwise uniform over [xs-1, xe+1] x [ys-1, ye+1] (every point a
+// step reads it at); 9, 10 gphiu / gphiv not uniform over the whole array;
+// 11 / 12 a Flather face in u / v reads another Flather face; 13 one would
+// read outside the array (time_step.cpp's Flather loops are serial in those
+// cases); 14 ssha_t differs from sshn_t on the copy region; 15 ua from un or
+// va from vn there; 16 sshn_u or sshn_v is not what next_sshu / next_sshv
+// make of sshn_t.  Bits 14-16 clear mean the state is what a step leaves
+// (time_step.cpp:114-136 end every step with those copies and updates), so
+// the first step may take the fused path.  Reference values are the
+// region's first point of each metric array and gphi's first element,
+// compared as bit patterns.
+enum : unsigned {
+  kScanMetrics = 0x1ffu,
+  kScanGphiU = 1u << 9,
+  kScanGphiV = 1u << 10,
+  kScanChainU = 1u << 11,
+  kScanChainV = 1u << 12,
+  kScanOutside = 1u << 13,
+  kScanSshaT = 1u << 14,
+  kScanCopies = 1u << 15,
+  kScanNextSsh = 1u << 16,
+};
+
 struct ScanIn {
   const double* metric[9];
   const double* gphi[2];
   const int* m;
+  const double *sn, *un, *vn, *ua, *va, *sa, *snu, *snv;
   int xs, xe, ys, ye, W, H;
 };
-enum : unsigned { kScanChainU = 1u << 11, kScanChainV = 1u << 12, kScanOutside = 1u << 13 };
+
+// next_sshu_code / next_sshv_code (time_update_kern.c:90-155) of one face
+// with uniform areas: returns false where the kernel leaves the face alone.
+__device__ __forceinline__ bool next_ssh_value(const int* m, const double* sn, int c, int step,
+                                               double at, double af, double& v) {
+  const int n = c + step;
+  if (m[c] + m[n] <= 0) return false;
+  if (m[c] * m[n] > 0) {
+    const double rtmp1 = at * sn[c] + at * sn[n];
+    v = 0.5 * rtmp1 / af;
+  } else if (m[c] <= 0) {
+    v = sn[n];
+  } else {
+    v = sn[c];
+  }
+  return true;
+}
 
 __global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
   const int W = in.W;
-  const size_t o = (size_t)(in.ys - 1) * W + (in.xs - 1);
-  unsigned long long ref[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) ref[q] = __double_as_longlong(in.metric[q][o]);
-  const unsigned long long g0 = __double_as_longlong(in.gphi[0][0]);
-  const unsigned long long g1 = __double_as_longlong(in.gphi[1][0]);
   const int* m = in.m;
   auto writes = [m](int c, int step) {
     return m[c] + m[c + step] > -1 && (m[c] < 0 || m[c + step] < 0);
   };
+  auto bits = [](double x) { return (unsigned long long)__double_as_longlong(x); };
+  const size_t o = (size_t)(in.ys - 1) * W + (in.xs - 1);
+  unsigned long long ref[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) ref[q] = bits(in.metric[q][o]);
+  const unsigned long long g0 = bits(in.gphi[0][0]), g1 = bits(in.gphi[1][0]);
+  // areas for the next_ssh check (meaningful only when uniform)
+  const double at = in.metric[0][o], au = in.metric[1][o], av = in.metric[2][o];
   unsigned f = 0;
   const int nx = in.xe - in.xs + 3, ny = in.ye - in.ys + 3;
   const long long nr = (long long)nx * ny;
@@ -215,7 +257,7 @@ __global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
     const int c = j * W + i;
 #pragma unroll
     for (int q = 0; q < 9; q++)
-      if ((unsigned long long)__double_as_longlong(in.metric[q][c]) != ref[q]) f |= 1u << q;
+      if (bits(in.metric[q][c]) != ref[q]) f |= 1u << q;
     if (i <= in.xe && writes(c, 1)) {  // Flather u over [xs-1, xe] x [ys-1, ye+1]
       const int nb = m[c] < 0 ? i + 1 : i - 1;
       if (nb < 0)
@@ -230,11 +272,25 @@ __global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
       else if (nb >= in.ys - 1 && nb <= in.ye && writes(nb * W + i, W))
         f |= kScanChainV;
     }
+    // the copy region [xs-1, xe+1] x [ys-1, ye]
+    if (j <= in.ye) {
+      if (bits(in.sa[c]) != bits(in.sn[c])) f |= kScanSshaT;
+      if (bits(in.ua[c]) != bits(in.un[c]) || bits(in.va[c]) != bits(in.vn[c])) f |= kScanCopies;
+    }
+    if (j >= in.ys && j <= in.ye && i >= in.xs && i <= in.xe) {
+      double v;
+      if (i <= in.xe - 1 && next_ssh_value(m, in.sn, c, 1, at, au, v) &&
+          bits(v) != bits(in.snu[c]))
+        f |= kScanNextSsh;
+      if (j <= in.ye - 1 && next_ssh_value(m, in.sn, c, W, at, av, v) &&
+          bits(v) != bits(in.snv[c]))
+        f |= kScanNextSsh;
+    }
   }
   const long long n = (long long)W * in.H;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += stride) {
-    if ((unsigned long long)__double_as_longlong(in.gphi[0][t]) != g0) f |= 1u << 9;
-    if ((unsigned long long)__double_as_longlong(in.gphi[1][t]) != g1) f |= 1u << 10;
+    if (bits(in.gphi[0][t]) != g0) f |= kScanGphiU;
+    if (bits(in.gphi[1][t]) != g1) f |= kScanGphiV;
   }
   if (f) atomicOr(flags, f);
 }
@@ -245,54 +301,24 @@ __global__ void k_fill(double* __restrict__ a, double v, size_t n) {
     a[t] = v;
 }
 
-// The Coriolis sines sin(gphi * d2r) on the device and the fused path's
-// preconditions (uniform metrics, no chained Flather faces), from the
-// device copies of the grid.  A latitude uniform over the array takes one
-// host sin per direction (the host libm, as the reference evaluates it);
-// otherwise every point is evaluated on the host.
-bool scan_grid(double d2r) {
+// The Coriolis sines sin(gphi * d2r) on the device (the reference-
+// structured path reads them per point) and their uniform values for the
+// fused path.  A latitude uniform over the array takes one host sin per
+// direction (the host libm, as the reference evaluates it); otherwise every
+// point is evaluated on the host and the fused path applies only if the
+// sines are uniform over the region the step reads.
+bool update_sines(double d2r) {
   State& s = g_state;
   const Registration& r = s.reg;
   const size_t n = (size_t)r.width * r.height;
-  if (!s.scan && !CK(cudaMalloc(&s.scan, 4 * sizeof(double)))) return false;
-  ScanIn in{};
-  const double* g[11] = {s.dev.area_t, s.dev.area_u, s.dev.area_v, s.dev.dx_u,  s.dev.dx_v,
-                         s.dev.dx_t,   s.dev.dy_u,   s.dev.dy_v,   s.dev.dy_t,  s.dev.gphiu,
-                         s.dev.gphiv};
-  for (int q = 0; q < 9; q++) in.metric[q] = g[q];
-  in.gphi[0] = g[9];
-  in.gphi[1] = g[10];
-  in.m = s.dev.tmask;
-  in.xs = r.xs, in.xe = r.xe, in.ys = r.ys, in.ye = r.ye, in.W = r.width, in.H = r.height;
-  unsigned* d_flags = reinterpret_cast<unsigned*>(s.scan);
-  if (!CK(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s.stream))) return false;
-  k_register_scan<<<152 * 8, 256, 0, s.stream>>>(in, d_flags);
-  if (!CK(cudaGetLastError())) return false;
-  // the reference values: the region's first point of each metric array,
-  // the first element of each latitude array
-  const size_t o = (size_t)(r.ys - 1) * r.width + (r.xs - 1);
-  double refs[11];
-  unsigned flags = 0;
-  for (int q = 0; q < 11; q++)
-    if (!CK(cudaMemcpyAsync(&refs[q], g[q] + (q < 9 ? o : 0), 8, cudaMemcpyDeviceToHost,
-                            s.stream)))
-      return false;
-  if (!CK(cudaMemcpyAsync(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s.stream)) ||
-      !CK(cudaStreamSynchronize(s.stream)))
-    return false;
-  double* um[9] = {&s.um.area_t, &s.um.area_u, &s.um.area_v, &s.um.dx_u, &s.um.dx_v,
-                   &s.um.dx_t,   &s.um.dy_u,   &s.um.dy_v,   &s.um.dy_t};
-  for (int q = 0; q < 9; q++) *um[q] = refs[q];
-  bool uniform = (flags & 0x1ffu) == 0;
-  if ((flags & (3u << 9)) == 0) {
-    s.um.sin_u = std::sin(refs[9] * d2r);
-    s.um.sin_v = std::sin(refs[10] * d2r);
+  bool uniform = true;
+  if ((s.scan_flags & (kScanGphiU | kScanGphiV)) == 0) {
+    s.um.sin_u = std::sin(s.grid_refs[9] * d2r);
+    s.um.sin_v = std::sin(s.grid_refs[10] * d2r);
     k_fill<<<152 * 8, 256, 0, s.stream>>>(s.dev.sin_u, s.um.sin_u, n);
     k_fill<<<152 * 8, 256, 0, s.stream>>>(s.dev.sin_v, s.um.sin_v, n);
     if (!CK(cudaGetLastError())) return false;
   } else {
-    // per-point latitudes: the host libm on every point, the fused path
-    // only if the sines are uniform over the region the step reads
     std::unique_ptr<double[]> su(new double[n]), sv(new double[n]);
     host_sines((const double*)r.host[kNumFields + 10], n, d2r, su.get());
     host_sines((const double*)r.host[kNumFields + 11], n, d2r, sv.get());
@@ -300,6 +326,7 @@ bool scan_grid(double d2r) {
         !CK(cudaMemcpy(s.dev.sin_v, sv.get(), n * 8, cudaMemcpyHostToDevice)))
       return false;
     const int W = r.width;
+    const size_t o = (size_t)(r.ys - 1) * W + (r.xs - 1);
     auto uniform_over = [&](const double* a, double& v) {
       v = a[o];
       uint64_t ref;
@@ -322,10 +349,52 @@ bool scan_grid(double d2r) {
     uniform &= uniform_over(sv.get(), s.um.sin_v);
   }
   s.sin_d2r = d2r;
-  s.chain_u = (flags & kScanChainU) != 0;
-  s.chain_v = (flags & kScanChainV) != 0;
-  s.fused_ok = uniform && (flags & kScanOutside) == 0 && !s.chain_u && !s.chain_v;
+  const unsigned f = s.scan_flags;
+  s.chain_u = (f & kScanChainU) != 0;
+  s.chain_v = (f & kScanChainV) != 0;
+  s.fused_ok = uniform && (f & (kScanMetrics | kScanOutside)) == 0 && !s.chain_u && !s.chain_v;
   return true;
+}
+
+// The registration scan (k_register_scan) over the uploaded arrays, then
+// the sines and the fused path's preconditions.  The state bits (14-16)
+// matter only right after an upload.  Returns false on a CUDA error.
+bool scan_grid(double d2r) {
+  State& s = g_state;
+  const Registration& r = s.reg;
+  if (!s.scan && !CK(cudaMalloc(&s.scan, 4 * sizeof(double)))) return false;
+  const double* g[11] = {s.dev.area_t, s.dev.area_u, s.dev.area_v, s.dev.dx_u,  s.dev.dx_v,
+                         s.dev.dx_t,   s.dev.dy_u,   s.dev.dy_v,   s.dev.dy_t,  s.dev.gphiu,
+                         s.dev.gphiv};
+  ScanIn in{};
+  for (int q = 0; q < 9; q++) in.metric[q] = g[q];
+  in.gphi[0] = g[9];
+  in.gphi[1] = g[10];
+  in.m = s.dev.tmask;
+  in.sn = cur_sshn(), in.un = cur_un(), in.vn = cur_vn();
+  in.ua = s.dev.ua, in.va = s.dev.va, in.sa = s.dev.ssha_t;
+  in.snu = s.dev.sshn_u, in.snv = s.dev.sshn_v;
+  in.xs = r.xs, in.xe = r.xe, in.ys = r.ys, in.ye = r.ye, in.W = r.width, in.H = r.height;
+  unsigned* d_flags = reinterpret_cast<unsigned*>(s.scan);
+  if (!CK(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s.stream))) return false;
+  k_register_scan<<<152 * 8, 256, 0, s.stream>>>(in, d_flags);
+  if (!CK(cudaGetLastError())) return false;
+  // the reference values: the region's first point of each metric array,
+  // the first element of each latitude array
+  const size_t o = (size_t)(r.ys - 1) * r.width + (r.xs - 1);
+  unsigned flags = 0;
+  for (int q = 0; q < 11; q++)
+    if (!CK(cudaMemcpyAsync(&s.grid_refs[q], g[q] + (q < 9 ? o : 0), 8, cudaMemcpyDeviceToHost,
+                            s.stream)))
+      return false;
+  if (!CK(cudaMemcpyAsync(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s.stream)) ||
+      !CK(cudaStreamSynchronize(s.stream)))
+    return false;
+  s.scan_flags = flags;
+  double* um[9] = {&s.um.area_t, &s.um.area_u, &s.um.area_v, &s.um.dx_u, &s.um.dx_v,
+                   &s.um.dx_t,   &s.um.dy_u,   &s.um.dy_v,   &s.um.dy_t};
+  for (int q = 0; q < 9; q++) *um[q] = s.grid_refs[q];
+  return update_sines(d2r);
 }
 
 bool same_registration(void* const* ptrs, int xs, int xe, int ys, int ye, int width,
@@ -364,37 +433,39 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   r.xs = xs, r.xe = xe, r.ys = ys, r.ye = ye, r.width = width, r.height = height;
   const size_t n = (size_t)width * height;
   s.registered = true;  // so free_device releases partial allocations
-  for (int k = 0; k < kNumFields; k++) {
+  s.h2d_bytes = s.d2h_bytes = 0;
+  for (int k = 0; k < kNumFields; k++)
     if (!CK(cudaMalloc(field_slot(s.dev, k), n * 8))) return false;
-    if (!CK(cudaMemcpyAsync(*field_slot(s.dev, k), ptrs[k], n * 8, cudaMemcpyHostToDevice,
-                            s.stream)))
-      return false;
-  }
   if (!CK(cudaMalloc(&s.dev.tmask, n * 4))) return false;
-  if (!CK(cudaMemcpyAsync(s.dev.tmask, ptrs[kNumFields], n * 4, cudaMemcpyHostToDevice,
-                          s.stream)))
-    return false;
-  for (int k = 1; k < kNumGrid; k++) {
+  for (int k = 1; k < kNumGrid; k++)
     if (!CK(cudaMalloc(grid_slot(s.dev, k), n * 8))) return false;
-    if (!CK(cudaMemcpyAsync(*grid_slot(s.dev, k), ptrs[kNumFields + k], n * 8,
-                            cudaMemcpyHostToDevice, s.stream)))
-      return false;
-  }
   if (!CK(cudaMalloc(&s.dev.sin_u, n * 8)) || !CK(cudaMalloc(&s.dev.sin_v, n * 8)))
     return false;
   if (!CK(cudaMalloc(&s.dev.r_hu, n * 8)) || !CK(cudaMalloc(&s.dev.r_hv, n * 8))) return false;
-  launch_depth_reciprocals(s.dev, dims(), s.stream);
-  if (!CK(cudaGetLastError())) return false;
   for (double*& p : s.shadow)
     if (!CK(cudaMalloc(&p, n * 8))) return false;
   if (!s.partials &&
       !CK(cudaMalloc(&s.partials, sizeof(double) * checksum_partials_needed())))
     return false;
-  if (!CK(cudaStreamSynchronize(s.stream))) return false;
+  // every array of the argument list: pageable copies, each returning once
+  // its source is staged
+  for (int k = 0; k < kNumFields + kNumGrid; k++) {
+    const size_t esz = k == kNumFields ? 4 : 8;
+    void* dst = k < kNumFields ? (void*)*field_slot(s.dev, k)
+                               : (k == kNumFields ? (void*)s.dev.tmask
+                                                  : (void*)*grid_slot(s.dev, k - kNumFields));
+    if (!CK(cudaMemcpyAsync(dst, ptrs[k], n * esz, cudaMemcpyHostToDevice, s.stream)))
+      return false;
+    s.h2d_bytes += (long long)(n * esz);
+  }
+  launch_depth_reciprocals(s.dev, dims(), s.stream);
+  if (!CK(cudaGetLastError())) return false;
   s.sc = sc;
-  if (!scan_grid(sc.d2r)) return false;
   s.cur = 0;
-  s.consistent = false;
+  if (!scan_grid(sc.d2r)) return false;
+  // A state that is already what a step leaves needs no reference-
+  // structured first step.
+  s.consistent = s.fused_ok && (s.scan_flags & (kScanSshaT | kScanCopies | kScanNextSsh)) == 0;
   s.shadows_synced = false;
   s.materialized = true;
   s.last_path = 0;
@@ -744,7 +815,7 @@ void c_invoke_time_step(double* ssha_t, double* sshn_t, double* sshn_u, double* 
       return;
   } else {
     s.sc = sc;
-    if (!(d2r == s.sin_d2r) && !scan_grid(d2r)) return;
+    if (!(d2r == s.sin_d2r) && !update_sines(d2r)) return;
   }
   one_step(istep);
 }
@@ -783,13 +854,23 @@ void c_read_from_device(void* from, void* to, int startx, int starty, int nx, in
               r.height);
     return;
   }
-  if (!materialize()) return;
+  // sshn_t, un and vn are read from the buffers that hold the current state
+  // (the fused path's ping-pong partner agrees with the primary outside the
+  // copy region); every other array is made what the reference holds first.
+  const void* src = nullptr;
+  if ((k == 1 || k == 6 || k == 7) && !(s.mixed_valid && s.mixed_ahead))
+    src = k == 1 ? cur_sshn() : (k == 6 ? cur_un() : cur_vn());
+  else if (!materialize())
+    return;
+  else
+    src = device_of(k);
   const size_t esz = k == kNumFields ? 4 : 8, pitch = (size_t)r.width * esz;
   const size_t off = ((size_t)(starty - 1) * r.width + (startx - 1)) * esz;
   if (nx == 0 || ny == 0) return;
-  if (!CK(cudaMemcpy2DAsync((char*)to + off, pitch, (const char*)device_of(k) + off, pitch,
-                            nx * esz, ny, cudaMemcpyDeviceToHost, s.stream)))
+  if (!CK(cudaMemcpy2DAsync((char*)to + off, pitch, (const char*)src + off, pitch, nx * esz, ny,
+                            cudaMemcpyDeviceToHost, s.stream)))
     return;
+  s.d2h_bytes += (long long)nx * ny * (long long)esz;
   if (blocking) CK(cudaStreamSynchronize(s.stream));
 }
 
@@ -821,6 +902,7 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
       !CK(cudaMemcpy2DAsync((char*)device_of(k) + off, pitch, (const char*)from + off, pitch,
                             nx * esz, ny, cudaMemcpyHostToDevice, s.stream)))
     return;
+  s.h2d_bytes += (long long)nx * ny * (long long)esz;
   // Any written array may break the fused path's preconditions: re-derive
   // them from the host copies where they can change, and take the next step
   // on the reference-structured path.
@@ -1132,6 +1214,14 @@ int nl2d_sync(void) {
   CallScope scope;
   if (s.stream) CK(cudaStreamSynchronize(s.stream));
   return scope.rc();
+}
+
+int nl2d_transfer_bytes(long long out[2]) {
+  const State& s = g_state;
+  if (!out) return NL2D_ERR_ARGS;
+  out[0] = s.h2d_bytes;
+  out[1] = s.d2h_bytes;
+  return NL2D_OK;
 }
 
 void* nl2d_device_ptr(const void* field) {

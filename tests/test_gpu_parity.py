@@ -39,7 +39,8 @@ def test_cfg0_2000_steps_bitwise(gpulib, oracle, mode):
     T.run(oracle.oracle_invoke_time_step, want, 2000)
     paths = T.gpu_run_calls(gpulib, m, 2000, mode=mode)
     if mode == 0:
-        assert paths[0] == 1 and set(paths[1:]) == {2}, "fused path not taken"
+        # the rest start is what a step leaves: every step fused, the first too
+        assert set(paths) == {2}, "fused path not taken"
     else:
         assert set(paths) == {1}
     assert_fields_equal(m, want, "mode %d" % mode)
@@ -110,8 +111,8 @@ def test_benchmark_size_bitwise(gpulib, oracle):
     """The benchmark's 4096 x 4096 interior (4098 namelist, width padded to
     4104 as the bench lays it out) with random depths and a random initial
     state, 12 steps through c_invoke_time_step (the first on the reference
-    path, the rest fused): all 13 fields bit-identical to the oracle's
-    OpenMP build."""
+    path, since a random state is not what a step leaves; the rest fused):
+    all 13 fields bit-identical to the oracle's OpenMP build."""
     rng = np.random.default_rng(5)
     m = T.make_model(4098, 4098, 1, width=4104, oracle=oracle)
     for k in ("ht", "hu", "hv"):
@@ -233,6 +234,58 @@ def test_write_to_device_then_step(gpulib, oracle):
     paths = T.gpu_run_calls(gpulib, m, 30, nit000=21, mode=0)
     assert paths[0] == 1 and paths[-1] == 2
     assert_fields_equal(m, want, "after write")
+
+
+@pytest.mark.parametrize("breach", ["ssha_t", "ua", "va", "sshn_u", "sshn_v"])
+def test_first_step_after_upload_checks_step_consistency(gpulib, oracle, breach):
+    """The rest start satisfies what a step leaves (ua == un, va == vn,
+    ssha_t == sshn_t on the copy region; sshn_u / sshn_v as next_ssh makes
+    them), so its first step is fused.  One cell breaking it sends the first
+    step down the reference-structured path; either way 10 steps are bit-
+    identical to the oracle."""
+    m = T.make_model(37, 29, 3, width=40, oracle=oracle)
+    rng = np.random.default_rng(13)
+    for k in ("ht", "hu", "hv"):
+        m.f[k][:] = rng.uniform(50.0, 500.0, size=m.f[k].shape)
+    # a ring cell of the copy region (column xs-1) or an interior face
+    j = m.ys + 3
+    cell = {"ssha_t": (j, m.xs - 1), "ua": (j, m.xs - 1), "va": (m.ys - 1, m.xs + 4),
+            "sshn_u": (j, m.xs + 2), "sshn_v": (j, m.xs + 2)}[breach]
+    m.f[breach][cell] = 1e-3
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 10)
+    paths = T.gpu_run_calls(gpulib, m, 10, mode=0)
+    assert paths[0] == 1 and set(paths[1:]) == {2}, (breach, paths)
+    assert_fields_equal(m, want, breach)
+    gpulib.nl2d_finalize()
+    clean = T.make_model(37, 29, 3, width=40, oracle=oracle)
+    paths = T.gpu_run_calls(gpulib, clean, 3, mode=0)
+    assert set(paths) == {2}
+
+
+def test_transfer_bytes_and_direct_state_read(gpulib, oracle):
+    """Registration copies the 25 arrays once; reading sshn_t, un and vn back
+    after fused steps copies exactly those fields and needs no other work;
+    every field read back equals the oracle."""
+    import ctypes
+    m = T.make_model(50, 41, 1, oracle=oracle)
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 8)
+    n = m.width * m.height
+    for k in range(8):
+        gpulib.c_invoke_time_step(*m.step_args(1 + k))
+        assert gpulib.nl2d_last_path() == 2
+    nb = (ctypes.c_longlong * 2)()
+    assert gpulib.nl2d_transfer_bytes(nb) == 0
+    assert nb[0] == 24 * n * 8 + n * 4 and nb[1] == 0
+    for k in ("sshn_t", "un", "vn"):
+        a = m.f[k]
+        gpulib.c_read_from_device(a.ctypes.data, a.ctypes.data, 1, 1, m.width, m.height, True)
+        assert bits_equal(a, want.f[k]), k
+    assert gpulib.nl2d_transfer_bytes(nb) == 0
+    assert nb[0] == 24 * n * 8 + n * 4 and nb[1] == 3 * n * 8
+    T.gpu_read_all(gpulib, m)
+    assert_fields_equal(m, want, "all fields")
 
 
 def test_partial_read(gpulib, oracle):
