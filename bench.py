@@ -438,7 +438,8 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
     hold = list(range(count - nhold, count))
     net = E.ConvNet(16, 256, 256, lib=lib)
     t0 = time.perf_counter()
-    hist = E.train(ds, net, iters=iters, holdout=nhold, pushforward=0.5, max_unroll=2)
+    hist = E.train(ds, net, iters=iters, holdout=nhold, pushforward=0.5, max_unroll=2,
+                   noise_frac=E.TRAIN_NOISE)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     probe_snaps = sorted(set([1, 5] + [int(v) for v in np.linspace(10, nsnap - 2, 8)]))
@@ -468,9 +469,9 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
     # the network on its own over the whole horizon (no judge), then the
     # judged hybrid
     free = E.rollout(test, net, range(16), start_snap=0, emu_steps=nsnap - 1, judge_every=50,
-                     threshold=1e-3, judge_share=0.0)
+                     threshold=1e-3, judge_share=0.0, track_truth=True)
     roll = E.rollout(test, net, range(16), start_snap=0, emu_steps=nsnap - 1, judge_every=50,
-                     threshold=1e-3, judge_share=0.25)
+                     threshold=1e-3, judge_share=0.5)
     return {
         "workload": "nemolite2d_emulator_%d_domains_256x256_%d_pairs_k10_horizon%d" % (
             count, count * len(ds.pair_starts), horizon),
@@ -494,7 +495,9 @@ def run_emulator(lib, count=200, horizon=5000, iters=8000, seed=11):
         "free_running": {k: free[k] for k in ("final_ssh_rms_error_m",
                                                  "final_ssh_rms_error_worst_domain_m",
                                                  "final_ssh_rms_m", "final_nonfinite",
-                                                 "emulator_ms", "solver_only_ms")},
+                                                 "emulator_ms", "solver_only_ms",
+                                                 "window_errors_m", "window_mean_offsets_m")},
+        "train_input_noise": E.TRAIN_NOISE,
         "rollout": roll,
     }
 

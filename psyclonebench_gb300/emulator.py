@@ -36,6 +36,12 @@ CPAD_OUT = 16  # 3 output channels padded (N multiple of 16)
 WIDTH = 48
 LAYERS = [(CPAD_IN, WIDTH, 1)] + [(WIDTH, WIDTH, 1)] * 4 + [(WIDTH, CPAD_OUT, 0)]
 K_STEPS = 10
+# Input noise of training, as a multiple of each channel's increment scale:
+# trained on perturbed states the network damps its own errors in a free
+# roll-out (measured over 5000 steps on 16 test domains: 1x and below
+# overflows, 2x-4x stays within 2.5-4.2 mm of the solver, 6x overflows
+# again), at the cost of some one-step accuracy (2.8e-5 -> 4.3e-5 m at 3x).
+TRAIN_NOISE = 3.0
 STATE_SCALE = (0.5, 1.0, 1.0)  # m, m/s, m/s
 
 
@@ -433,7 +439,7 @@ def evaluate(ds, net, domains, snaps):
 
 
 def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, threshold=1e-3,
-            judge_share=0.25, track_truth=False):
+            judge_share=0.5, track_truth=False):
     """Hybrid roll-out from snapshot start_snap over emu_steps emulator
     steps (K_STEPS solver steps each), in windows of judge_every steps.
 
@@ -443,20 +449,24 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     the domains that the emulator advanced (domain q is judged in window w
     when q = w mod M, M = round(1 / judge_share)); its error is the ssh RMS
     difference between the emulator's and the solver's window-end states.
-    At or below `threshold` (m) the domain keeps the emulator's state; above
-    it, or if anything is non-finite, the domain falls back: it takes the
-    solver's window-end state and the solver also advances it through the
-    next window, after which the emulator takes over again.
+    A judged domain continues from the solver's window-end state.  Above
+    `threshold` (m), or if anything is non-finite, the domain also falls
+    back: the solver advances it through the next window as well, after
+    which the emulator takes over again.
 
-    What the judge bounds: the difference after one window between the
-    emulator and the FP64 solver started from the same state.  With the
-    ensemble configuration's bottom friction (cbfr = 1e-3 /s, an e-folding
-    time of 200 steps at rdt = 5 s) an error present at a window's start
-    has decayed to exp(-judge_every K_STEPS cbfr rdt) (8 % for 500 steps) by
-    its end, so the judged difference is, to within that share, the error
-    the domain has accumulated against the solver's trajectory through its
-    own state.  Domains outside the window's judged share are not checked
-    in that window; each is checked every M windows.
+    What the judge bounds: the error the emulator adds over one window
+    against the FP64 solver started from the same state.  Every judged
+    domain is re-anchored to an FP64 trajectory, so a domain's error against
+    the truth is at most what the emulator added since its last judged
+    window (at most M windows) plus what remains of the error carried into
+    that window; the report's final error measures the sum against a pure
+    FP64 run.  (Friction damps velocity errors within a few hundred steps,
+    but an offset of the mean level, and other slowly relaxing large-scale
+    errors, outlive a window: measured over 5000 steps a freely running
+    network kept adding error at a steady rate while each window's own
+    error stayed near 3e-4 m, which is why judged domains restart from the
+    solver's state.)  Domains outside a window's judged share are not
+    checked in that window; each is checked every M windows.
 
     A pure FP64 solver run from the same start over the whole horizon gives
     the truth for the final error; its wall time, set-up included, is
@@ -539,6 +549,7 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
     tr_state = initial(domains) if track_truth else None
     if track_truth:
         report["window_errors_m"] = []
+        report["window_mean_offsets_m"] = []
     while k < emu_steps:
         window = min(judge_every, emu_steps - k)
         start = state.clone()
@@ -566,14 +577,18 @@ def rollout(ds, net, domains, start_snap, emu_steps=500, judge_every=50, thresho
                 err = float((state[q, :, 0] - ref[j, :, 0]).pow(2).mean().sqrt())
                 report["judge_errors_m"].append(err)
                 report["judged"] += 1
+                # the re-run is the FP64 trajectory from the same state: the
+                # domain continues from it
+                state[q] = ref[j]
                 if not err <= threshold:  # a non-finite error fails the judge too
                     report["judge_failed"] += 1
-                    state[q] = ref[j]
                     fallback.add(q)
         if track_truth:
             tr_state, _ = solve(list(range(nd)), tr_state, istep, window * K_STEPS)
-            report["window_errors_m"].append(
-                float((state[:, :, 0] - tr_state[:, :, 0]).pow(2).mean().sqrt()))
+            dd = state[:, :, 0] - tr_state[:, :, 0]
+            report["window_errors_m"].append(float(dd.pow(2).mean().sqrt()))
+            # the part of it that is a uniform offset of each domain's level
+            report["window_mean_offsets_m"].append(float(dd.mean(dim=1).pow(2).mean().sqrt()))
         report["windows"] += 1
         istep += window * K_STEPS
         k += window

@@ -242,6 +242,8 @@ def test_hybrid_rollout_judges_and_falls_back(gpulib, small_dataset):
     assert loose["judged"] == 4 and loose["judge_failed"] == 0 and loose["solver_windows"] == 0
     assert len(loose["judge_errors_m"]) == 4
     assert all(e > 0 for e in loose["judge_errors_m"])
+    # every domain judged in the last window continues from the solver's state
+    assert loose["final_ssh_rms_error_m"] < 1e-6
     # a share of one half judges each domain every other window
     half = rollout(ds, net, [6, 7], start_snap=2, emu_steps=6, judge_every=3, threshold=1e9,
                    judge_share=0.5)
