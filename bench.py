@@ -74,7 +74,7 @@ def parse():
     ap.add_argument("--emu-horizon", type=int, default=5000,
                     help="solver steps of the emulator's trajectories and roll-out")
     ap.add_argument("--case", default=None,
-                    choices=["fused", "fused_active", "mixed", "tra_adv", "emu"],
+                    choices=["fused", "fused_active", "mixed", "tra_adv", "emu", "rates"],
                     help="run one small case of one kernel family and print its device time "
                          "(for profiler captures; prints no bench line)")
     ap.add_argument("--batch", type=int, default=24, help="--case emu: images of 256^2")
@@ -685,10 +685,17 @@ def run_ours(args, rank, world, local):
         # start state (the count depends on it: zero dividends skip the
         # division's FP64 work)
         gops = fig["fp64_ops_per_cell"] * cells / (ms_step * 1e-3) / 1e9
-        peak = prof.get("fp64_peak_gops")
+        # the FP64 pipe's rate measured on this GPU now (best of FMA,
+        # multiply and add streams)
+        rates = (ctypes.c_double * 4)()
+        P.check(lib.nl2d_measure_pipe_rates(rates), "pipe rates")
+        peak = max(rates[0], rates[1], rates[2])
         roof["fp64"] = {
             "achieved_gops": gops, "ops_per_cell": fig["fp64_ops_per_cell"],
-            "peak_gops": peak, "frac": gops / peak if peak else None,
+            "peak_gops": peak, "peak_kind": "measured in this run (nl2d_measure_pipe_rates)",
+            "frac": gops / peak if peak else None,
+            "pipe_rates_gops": {"dfma": rates[0], "dmul": rates[1], "dadd": rates[2],
+                                "ffma": rates[3]},
             "profile": fig.get("source"),
         }
 
@@ -784,6 +791,10 @@ def run_case(args):
         if rc or lib.tra_adv_last_error(buf, 256):
             raise RuntimeError("tra_adv: %s" % buf.value.decode())
         lib.tra_adv_finalize()
+    elif args.case == "rates":
+        rates = (ctypes.c_double * 4)()
+        P.check(lib.nl2d_measure_pipe_rates(rates), "pipe rates")
+        out["gops"] = {"dfma": rates[0], "dmul": rates[1], "dadd": rates[2], "ffma": rates[3]}
     elif args.case == "emu":
         import torch
         from psyclonebench_gb300 import emulator as E

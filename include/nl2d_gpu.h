@@ -365,6 +365,14 @@ int nl2d_sync(void);
  * current problem was registered. */
 int nl2d_transfer_bytes(long long out[2]);
 
+/* Issue rates of this GPU's arithmetic pipes in Gop/s (no counterpart in
+ * the reference): out = {FP64 FMA, FP64 multiply, FP64 add, FP32 FMA}, each
+ * over eight independent chains per thread on every SM (best of two timed
+ * launches).  The FP64 step is bound by the FP64 pipe; its roofline divides
+ * by the fastest FP64 rate measured here.  Allocates a scratch buffer of
+ * SMs x 8 x 256 doubles for the duration of the call. */
+int nl2d_measure_pipe_rates(double out[4]);
+
 /* ---- host side of the reference executable (no GPU needed) ---- */
 
 /* Reads the &namctl group of a Fortran namelist file

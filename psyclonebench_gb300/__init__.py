@@ -104,6 +104,7 @@ EXPORTS = {
     "tra_adv_finalize": (None, []),
     "nl2d_sync": (ctypes.c_int, []),
     "nl2d_transfer_bytes": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong)]),
+    "nl2d_measure_pipe_rates": (ctypes.c_int, [_DP]),
     "nl2d_device_ptr": (ctypes.c_void_p, [_VP]),
 }
 
