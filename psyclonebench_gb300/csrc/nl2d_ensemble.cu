@@ -447,16 +447,13 @@ bool build_descriptors() {
 }
 
 // The column march needs one set of step constants for all domains (they
-// are kernel parameters) and even row widths; otherwise the tile kernel runs.  Builds the march
+// are kernel parameters); otherwise the tile kernel runs.  Builds the march
 // flags, the general-cell list and the march units.
 bool build_march(const std::vector<EnsMixDomain>& desc) {
   Ens& e = g_ens;
   e.march = false;
   for (const EnsMixDomain& x : desc)
     if (memcmp(&x.k, &desc[0].k, sizeof x.k) != 0) return true;
-  // the two-column march reads column pairs: every row width must be even
-  for (const EnsMixDomain& x : desc)
-    if (x.d.width % 2 != 0) return true;
   if (!e.mreg && (!ck(cudaMalloc(&e.mreg, e.total)) || !ck(cudaMalloc(&e.mcount, sizeof(int)))))
     return false;
   // two passes: count the general cells, then list them
@@ -484,8 +481,8 @@ bool build_march(const std::vector<EnsMixDomain>& desc) {
     const int dom = (int)(&x - desc.data());
     const int mr = e.march_rows;
     for (int gy = 0; gy < (ny + mr - 1) / mr; gy++)
-      for (int gx = 0; gx < (nx + mixk::MW2 - 1) / mixk::MW2; gx++)
-        units.push_back(make_int4(dom, x.d.xs - 1 + gx * mixk::MW2, x.d.ys - 1 + gy * mr, 0));
+      for (int gx = 0; gx < (nx + mixk::MW - 1) / mixk::MW; gx++)
+        units.push_back(make_int4(dom, x.d.xs - 1 + gx * mixk::MW, x.d.ys - 1 + gy * mr, 0));
   }
   cudaFree(e.d_units);
   e.d_units = nullptr;

@@ -39,17 +39,6 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
   mixed_march(mf, ms, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * mr, 0, mr);
 }
 
-// The same with two columns per lane (MW2 columns per warp), for an even
-// row width: 186 registers, two blocks of four warps per SM.
-__global__ void __launch_bounds__(32 * MARCH_WARPS, 2)
-    k_mixed_march2(MixedFields mf, MixedState ms, Dims d, MarchConst k, int ncol, int nwarps,
-                   int mr) {
-  const int warp = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
-  if (warp >= nwarps) return;  // the whole warp leaves together
-  const int gy = warp / ncol, gx = warp - gy * ncol;
-  mixed_march2(mf, ms, d, k, d.xs - 1 + gx * MW2, d.ys - 1 + gy * mr, 0, mr);
-}
-
 // The copy region's other cells, one thread per listed cell.
 __global__ void __launch_bounds__(128)
     k_mixed_general(MixedFields mf, MixedState ms, Fields f, Dims d, MixConst k,
@@ -77,16 +66,14 @@ __global__ void __launch_bounds__(128)
 // ---- ensemble: the march over every domain when all share the step's
 // constants (kernel parameters); warp w takes units[w] = (domain, i0, j0)
 // with the packed arrays' base pointers in mf / ms.
-__global__ void __launch_bounds__(32 * MARCH_WARPS, 2)
+__global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
     k_ensemble_mixed_march(const EnsDom* __restrict__ doms, const int4* __restrict__ units,
                            int nunits, MixedFields mf, MixedState ms, MarchConst k, int mr) {
   const int w = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
   const Dims d = doms[u.x].d;
-  // every domain's row width is even (checked when the march is built) and
-  // its offset in the packed arrays a multiple of 32 elements
-  mixed_march2(mf, ms, d, k, u.y, u.z, doms[u.x].off, mr);
+  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, mr);
 }
 
 // The other cells of every domain's copy region: glist[t] = (domain, cell).
@@ -180,21 +167,12 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   // Strips of MR rows, halved (down to 8) until the grid holds about two
   // waves of warps: a smaller domain trades halo rows for parallelism.
-  // two columns per lane where pairs of columns are aligned (even width)
-  const bool pairs = d.width % 2 == 0;
-  const int mw = pairs ? MW2 : MW, blocks_per_sm = pairs ? 2 : 5;
-  const int ncol = (nx + mw - 1) / mw;
+  const int ncol = (nx + MW - 1) / MW;
   int mr = MR;
-  while (mr > 8 &&
-         (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * blocks_per_sm * MARCH_WARPS)
-    mr /= 2;
+  while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 5 * MARCH_WARPS) mr /= 2;
   const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
-  if (pairs)
-    k_mixed_march2<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-        mf, ms, d, make_march_const(k), ncol, nwarps, mr);
-  else
-    k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-        mf, ms, d, make_march_const(k), ncol, nwarps, mr);
+  k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
+      mf, ms, d, make_march_const(k), ncol, nwarps, mr);
   if (mf.gcount > 0)
     k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
                                                              tide_index, tide);

@@ -270,216 +270,6 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
   }
 }
 
-// ---- the two-column march ------------------------------------------------
-//
-// The same march with two adjacent columns per lane: lane L holds columns
-// i = i0 - 2 + 2L and i + 1 (i even), so one warp covers 64 columns and
-// outputs MW2 = 60 of them (lanes 1..30; lanes 0 and 31 hold the halo).
-// Every quantity is a float2 over (column i, column i + 1), so the whole
-// update runs on the packed FP32 pair instructions without assembling pairs
-// of unrelated operands; a west neighbour pair is (lane - 1's second
-// column, own first column) and an east one (own second column, lane + 1's
-// first column), one shuffle per pair.  Loads are float2 (float4 for the ssh
-// pair) from an even column of a row padded to an even width, so a pair
-// never straddles the array's edge and is either wholly inside or outside.
-// Per cell the arithmetic is the one-column march's (row_terms and the
-// update above), in the same order.
-constexpr int MW2 = 60;
-
-__device__ __forceinline__ float2 west_of(float2 a) { return make_float2(shu(a.y), a.x); }
-__device__ __forceinline__ float2 east_of(float2 a) { return make_float2(a.y, shd(a.x)); }
-__device__ __forceinline__ float2 lt0_sel(float2 w, float2 a, float2 b) {
-  return make_float2(w.x < 0.f ? a.x : b.x, w.y < 0.f ? a.y : b.y);
-}
-__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
-
-// One loaded row of a column pair (raw, issued ahead of its use).
-struct MRaw2 {
-  float4 s;  // ssh (hi, lo) of the two columns
-  float2 u, v, hu, hv, ht;
-};
-
-// A finished row: the east faces' sshn_u, and sshn_v once the next row is in.
-struct MRow2 {
-  float2 u, v, hu, hv, su, sv, sn, lo, D;  // D: ht + sn
-};
-
-// The shared terms of one row (row_terms of the one-column march).
-struct MTerm2 {
-  float2 Hu, Hv;        // total depths at the u and v faces
-  float2 fu, fv;        // continuity fluxes (hu + su) u, (hv + sv) v
-  float2 gu, gv;        // x gradient of u, y gradient of v, times the depth
-  float2 fxu, fxv;      // advective fluxes of u and v through the west face
-  float2 fyu, fyv;      // advective fluxes of u and v through the south face
-  float2 qu, qv;        // y gradient of u, x gradient of v
-  float2 vws, uws;      // the v sum of u's Coriolis term, the u sum of v's
-};
-
-struct MOut2 {
-  float2 rhu, rhv;
-  uchar2 reg;
-};
-
-__device__ __forceinline__ MRaw2 load_raw2(const MixedFields& mf, const MixedState& ms, int i,
-                                           int j, int W, int H, size_t base) {
-  MRaw2 r;
-  const bool ok = i >= 0 && i + 1 < W && j >= 0 && j < H;
-  if (ok) {
-    const size_t c = base + (size_t)j * W + i;
-    r.s = __ldg(reinterpret_cast<const float4*>(ms.sn_in + c));
-    r.u = __ldg(reinterpret_cast<const float2*>(ms.un_in + c));
-    r.v = __ldg(reinterpret_cast<const float2*>(ms.vn_in + c));
-    r.hu = __ldg(reinterpret_cast<const float2*>(mf.hu + c));
-    r.hv = __ldg(reinterpret_cast<const float2*>(mf.hv + c));
-    r.ht = __ldg(reinterpret_cast<const float2*>(mf.ht + c));
-  } else {
-    r.s = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.u = r.v = r.hu = r.hv = r.ht = make_float2(0.f, 0.f);
-  }
-  return r;
-}
-
-__device__ __forceinline__ MRow2 finish_row2(const MRaw2& a, const MarchConst& c) {
-  MRow2 r;
-  r.sn = make_float2(a.s.x, a.s.z);
-  r.lo = make_float2(a.s.y, a.s.w);
-  r.u = a.u;
-  r.v = a.v;
-  r.hu = a.hu;
-  r.hv = a.hv;
-  r.D = add2(a.ht, r.sn);
-  r.su = mul2(add2(r.sn, east_of(r.sn)), bc2(c.face_u));
-  r.sv = make_float2(0.f, 0.f);
-  return r;
-}
-
-__device__ __forceinline__ MOut2 load_out2(const MixedFields& mf, bool col, int i, int j, int W,
-                                           int jend, size_t base) {
-  MOut2 o{make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_uchar2(0, 0)};
-  if (col && j < jend) {
-    const size_t c = base + (size_t)j * W + i;
-    o.reg = __ldg(reinterpret_cast<const uchar2*>(mf.reg + c));
-    o.rhu = __ldg(reinterpret_cast<const float2*>(mf.rhu + c));
-    o.rhv = __ldg(reinterpret_cast<const float2*>(mf.rhv + c));
-  }
-  return o;
-}
-
-// Terms of row C (P below it, N above it): row_terms per column.
-__device__ __forceinline__ MTerm2 row_terms2(const MRow2& P, const MRow2& C, const MRow2& N,
-                                             const MarchConst& c) {
-  MTerm2 t;
-  t.Hu = add2(C.hu, C.su);
-  t.Hv = add2(C.hv, C.sv);
-  t.fu = mul2(t.Hu, C.u);
-  t.fv = mul2(t.Hv, C.v);
-  const float2 uW = west_of(C.u), vW = west_of(C.v), HuW = west_of(t.Hu);
-  const float2 vE_P = east_of(P.v), hvE_P = east_of(P.hv), svE_P = east_of(P.sv);
-  const float2 uW_N = west_of(N.u), huW_N = west_of(N.hu), suW_N = west_of(N.su);
-  t.gu = mul2(mul2(sub2(C.u, uW), bc2(c.r_dxy.x)), C.D);
-  t.gv = mul2(mul2(sub2(C.v, P.v), bc2(c.r_dxy.y)), C.D);
-  const float2 sAx = add2(C.u, uW), sAy = add2(uW, uW_N);
-  const float2 sBx = add2(P.v, vE_P), sBy = add2(C.v, P.v);
-  t.vws = sBx;
-  t.uws = sAy;
-  const float2 UUx = mul2(sAx, bc2(c.uu.x)), UUy = mul2(sAy, bc2(c.uu.y));
-  const float2 VVx = mul2(sBx, bc2(c.vv.x)), VVy = mul2(sBy, bc2(c.vv.y));
-  const float2 depx = add2(add2(HuW, huW_N), suW_N);
-  const float2 depy = add2(add2(add2(P.hv, P.sv), hvE_P), svE_P);
-  t.fxu = mul2(mul2(lt0_sel(UUx, C.u, uW), UUx), C.D);
-  t.fxv = mul2(mul2(lt0_sel(UUy, C.v, vW), UUy), depx);
-  t.fyu = mul2(mul2(lt0_sel(VVx, C.u, P.u), VVx), depy);
-  t.fyv = mul2(mul2(lt0_sel(VVy, C.v, P.v), VVy), C.D);
-  t.qu = mul2(sub2(C.u, P.u), bc2(c.r_q.x));
-  t.qv = mul2(sub2(C.v, vW), bc2(c.r_q.y));
-  return t;
-}
-
-// One warp: lane L holds columns i0-2+2L and i0-1+2L; output rows j0 ..
-// j0+mr-1 of the copy region, regular cells only (the reg flags).
-__device__ __forceinline__ void mixed_march2(const MixedFields& mf, const MixedState& ms,
-                                             const Dims& d, const MarchConst& k, int i0, int j0,
-                                             size_t base, int mr) {
-  const int lane = threadIdx.x & 31;
-  const int W = d.width, H = d.height;
-  const int i = i0 - 2 + 2 * lane;
-  const int jend = min(j0 + mr, d.ye + 1);
-  const bool out_col = lane >= 1 && lane <= MW2 / 2 && i <= d.xe + 1;
-  MRow2 P = finish_row2(load_raw2(mf, ms, i, j0 - 1, W, H, base), k);
-  MRow2 C = finish_row2(load_raw2(mf, ms, i, j0, W, H, base), k);
-  MRow2 N = finish_row2(load_raw2(mf, ms, i, j0 + 1, W, H, base), k);
-  MRaw2 R1 = load_raw2(mf, ms, i, j0 + 2, W, H, base);
-  MRaw2 R2 = load_raw2(mf, ms, i, j0 + 3, W, H, base);
-  MOut2 O = load_out2(mf, out_col, i, j0, W, jend, base);
-  const float2 face_v = bc2(k.face_v);
-  P.sv = mul2(add2(P.sn, C.sn), face_v);
-  C.sv = mul2(add2(C.sn, N.sn), face_v);
-  // row j0-1: what the updates of row j0 read from it
-  float2 fv0 = mul2(add2(P.hv, P.sv), P.v), hu0 = P.hu, su0 = P.su;
-  MTerm2 T1 = row_terms2(P, C, N, k);  // row j0
-  for (int j = j0; j < jend; j++) {
-    P = C;  // row j
-    C = N;  // row j+1
-    N = finish_row2(R1, k);  // row j+2, loaded two iterations ago
-    R1 = R2;
-    R2 = load_raw2(mf, ms, i, j + 4, W, H, base);  // in flight for two iterations
-    const MOut2 Oc = O;
-    O = load_out2(mf, out_col, i, j + 1, W, jend, base);
-    C.sv = mul2(add2(C.sn, N.sn), face_v);
-    const MTerm2 T2 = row_terms2(P, C, N, k);  // row j+1
-    // x neighbours of row j's terms (every lane takes part)
-    const float2 fuW = west_of(T1.fu), snE = east_of(P.sn);
-    const float2 fxuE = east_of(T1.fxu), fxvE = east_of(T1.fxv);
-    const float2 guE = east_of(T1.gu), qvE = east_of(T1.qv), uwsE = east_of(T1.uws);
-    const float2 hvW = west_of(P.hv), svW = west_of(P.sv);
-    const float2 hvE = east_of(P.hv), svE = east_of(P.sv);
-    if (out_col && (Oc.reg.x | Oc.reg.y)) {
-      const size_t c = base + (size_t)j * W + i;
-      const float2 div = sub2(add2(sub2(fuW, T1.fu), fv0), T1.fv);
-      const float2 dssh = mul2(div, bc2(k.rrat));
-      const float2 advu = sub2(add2(sub2(T1.fxu, fxuE), T1.fyu), T2.fyu);
-      const float2 advv = sub2(add2(sub2(T1.fxv, fxvE), T1.fyv), T2.fyv);
-      const float2 dSu = mul2(T1.qu, add2(add2(T1.Hu, hu0), su0));
-      const float2 dSv = mul2(T1.qv, add2(add2(T1.Hv, hvW), svW));
-      const float2 dNu = mul2(T2.qu, add2(add2(T1.Hu, C.hu), C.su));
-      const float2 dNv = mul2(qvE, add2(add2(T1.Hv, hvE), svE));
-      const float2 visu =
-          fma2(sub2(dNu, dSu), bc2(k.vis2.x), mul2(sub2(guE, T1.gu), bc2(k.vis1.x)));
-      const float2 visv =
-          fma2(sub2(dNv, dSv), bc2(k.vis2.y), mul2(sub2(T2.gv, T1.gv), bc2(k.vis1.y)));
-      const float2 coru = mul2(mul2(add2(T1.vws, T2.vws), bc2(k.cor.x)), T1.Hu);
-      const float2 corv = mul2(mul2(add2(uwsE, T1.uws), bc2(k.cor.y)), T1.Hv);
-      const float2 hpgu = mul2(mul2(T1.Hu, bc2(k.hpg.x)), sub2(snE, P.sn));
-      const float2 hpgv = mul2(mul2(T1.Hv, bc2(k.hpg.y)), sub2(C.sn, P.sn));
-      const float2 tu = add2(add2(add2(advu, visu), coru), hpgu);
-      const float2 tv = add2(add2(add2(advv, visv), corv), hpgv);
-      const float2 ou =
-          mul2(mul2(fma2(tu, bc2(k.rra.x), mul2(P.u, T1.Hu)), Oc.rhu), bc2(k.r_fric));
-      const float2 ov =
-          mul2(mul2(fma2(tv, bc2(k.rra.y), mul2(P.v, T1.Hv)), Oc.rhv), bc2(k.r_fric));
-      if (Oc.reg.x && Oc.reg.y) {
-        const float2 s0 = dd_add(make_float2(P.sn.x, P.lo.x), dssh.x);
-        const float2 s1 = dd_add(make_float2(P.sn.y, P.lo.y), dssh.y);
-        *reinterpret_cast<float4*>(ms.sn_out + c) = make_float4(s0.x, s0.y, s1.x, s1.y);
-        *reinterpret_cast<float2*>(ms.un_out + c) = ou;
-        *reinterpret_cast<float2*>(ms.vn_out + c) = ov;
-      } else if (Oc.reg.x) {
-        ms.sn_out[c] = dd_add(make_float2(P.sn.x, P.lo.x), dssh.x);
-        ms.un_out[c] = ou.x;
-        ms.vn_out[c] = ov.x;
-      } else {
-        ms.sn_out[c + 1] = dd_add(make_float2(P.sn.y, P.lo.y), dssh.y);
-        ms.un_out[c + 1] = ou.y;
-        ms.vn_out[c + 1] = ov.y;
-      }
-    }
-    fv0 = T1.fv;
-    hu0 = P.hu;
-    su0 = P.su;
-    T1 = T2;
-  }
-}
-
 // ---- the other cells of the copy region, on global memory ----------------
 
 // One domain of a mixed-precision ensemble (device descriptor).

@@ -91,12 +91,11 @@ def test_mixed_random_land_vs_fp64(gpulib, oracle):
     assert report["vn"][0] <= 1e-4 * report["vn"][2]
 
 
-@pytest.mark.parametrize("jphgr,nx,ny", [(2, 97, 61), (3, 75, 130), (2, 90, 50)])
+@pytest.mark.parametrize("jphgr,nx,ny", [(2, 97, 61), (3, 75, 130)])
 def test_mixed_other_masks_vs_fp64(gpulib, oracle, jphgr, nx, ny):
     """The T masks of jphgr_msh 2 and 3 (model_mod.f90:94-249) on odd-sized
     grids with a padded width: the column march and its general pass against
-    FP64 after 300 steps, same bar.  Widths nx + 9 are even for the first two
-    (two columns per lane) and odd for the third (one column per lane)."""
+    FP64 after 300 steps, same bar."""
     from psyclonebench_gb300.workloads import fourier_depth
     m = T.make_model(nx + 2, ny + 2, jphgr, width=nx + 9, oracle=oracle)
     ht, hu, hv = fourier_depth(m.width, m.height, 5)
@@ -115,26 +114,3 @@ def test_mixed_other_masks_vs_fp64(gpulib, oracle, jphgr, nx, ny):
             assert rms <= 1e-6, (k, rms)
         else:
             assert rms <= 1e-4 * max(float(np.abs(b).max()), 1e-12), (k, rms)
-
-
-def test_two_column_and_one_column_marches_agree(gpulib, oracle):
-    """The same domain laid out with an even row width (the two-column march)
-    and an odd one (the one-column march): the same arithmetic per cell, so
-    after 200 mixed steps the fields agree far inside the form's error bar
-    against FP64."""
-    from psyclonebench_gb300.workloads import fourier_depth
-    out = []
-    for width in (132, 133):
-        m = T.make_model(130, 98, 1, width=width, oracle=oracle)
-        ht, hu, hv = fourier_depth(132, m.height, 8)
-        for k, a in (("ht", ht), ("hu", hu), ("hv", hv)):
-            m.f[k][:, :132] = a
-            m.f[k][:, 132:] = a[:, -1:]
-        m.rdt = 5.0
-        out.append(run_form(gpulib, m, 200, 1))
-    a, b = out
-    for k, (x0, x1, y0, y1) in (("sshn_t", T.regions(a)["t"]), ("un", T.regions(a)["u"]),
-                                ("vn", T.regions(a)["v"])):
-        d = a.f[k][y0:y1 + 1, x0:x1 + 1] - b.f[k][y0:y1 + 1, x0:x1 + 1]
-        scale = float(np.abs(a.f[k][y0:y1 + 1, x0:x1 + 1]).max())
-        assert np.abs(d).max() <= 1e-5 * scale, (k, float(np.abs(d).max()), scale)
