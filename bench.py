@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the mixed-precision, ensemble and emulator measurements")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator (config 4)")
-    ap.add_argument("--forms", default="mixed,active,sweep,ensemble,tra_adv,emulator",
+    ap.add_argument("--forms", default="mixed,active,df,sweep,ensemble,tra_adv,emulator",
                     help="comma-separated forms to measure after the headline number")
     ap.add_argument("--form-steps", type=int, default=1000,
                     help="timed steps of the mixed-precision form and its FP64 twin")
@@ -314,6 +314,53 @@ def run_active(lib, n, rest_value, steps=200, warmup=5):
             "value": value, "unit": "Mcell-steps/s", "ms_per_step": ms.value / steps,
             "steps": steps, "warmup": warmup, "ratio_to_rest_start": value / rest_value,
             "checksums": {"ssh": sums[0], "u": sums[1], "v": sums[2]}, "dtype": "f64"}
+
+
+def run_df_form(lib, n, steps=200, warmup=5):
+    """The FP64-equivalent form (double-float interior, exact FP64 elsewhere)
+    at the headline workload (n x n from rest) and with every cell in motion
+    (make_active): device-resident rate, and each field's relative L2
+    difference to the bitwise FP64 path after the same warmup + steps
+    steps (the benchmark spec's bar for the FP64 path: 1e-10)."""
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import read_fields, register
+    cells = n * n
+    hbm, _ = peaks()
+    out = {}
+    for state in ("rest", "active"):
+        res = {}
+        for precision in (0, 2):
+            m = make_problem(n)
+            if state == "active":
+                make_active(m)
+            register(lib, m)
+            lib.nl2d_set_precision(precision)
+            ms = ctypes.c_double(0.0)
+            P.check(lib.nl2d_timed_run(1, warmup, ctypes.byref(ms)), "df warm-up")
+            P.check(lib.nl2d_timed_run(1 + warmup, steps, ctypes.byref(ms)), "df run")
+            lib.nl2d_set_precision(0)
+            read_fields(lib, m, ("sshn_t", "un", "vn"))
+            lib.nl2d_finalize()
+            res[precision] = (ms.value / steps, {k: m.f[k].copy() for k in ("sshn_t", "un", "vn")})
+            del m
+        ms64, f64 = res[0]
+        msdf, fdf = res[2]
+        rel = {}
+        for k in ("sshn_t", "un", "vn"):
+            a, b = fdf[k], f64[k]
+            den = float(np.sqrt(np.sum(b * b)))
+            rel[k] = float(np.sqrt(np.sum((a - b) ** 2))) / den if den > 0 else 0.0
+        ach = ALG_BYTES_PER_CELL * cells / (msdf * 1e-3) / 1e9
+        out[state] = {
+            "value": cells / (msdf * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+            "ms_per_step": msdf, "fp64_value_same_inputs": cells / (ms64 * 1e-3) / 1e6,
+            "speedup_vs_fp64": ms64 / msdf, "steps": steps + warmup,
+            "rel_l2_vs_fp64": rel,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                         "frac": ach / hbm, "alg_bytes_per_cell": ALG_BYTES_PER_CELL}}
+    return {"workload": "nemolite2d_fp64_equivalent_%dx%d" % (n, n),
+            "dtype": "double-float (FP32 pairs) interior, FP64 boundary cells and storage",
+            "bar": "relative L2 <= 1e-10 per field against the FP64 path", **out}
 
 
 def run_sweep(lib, sizes=(256, 512, 1024, 2048, 4096, 8192)):
@@ -709,6 +756,8 @@ def run_ours(args, rank, world, local):
             forms.update(run_forms(lib, n, steps=args.form_steps))
         if "active" in want:
             forms["fp64_active"] = run_active(lib, n, value)
+        if "df" in want:
+            forms["fp64_equivalent"] = run_df_form(lib, n)
         if "sweep" in want:
             forms["size_sweep"] = run_sweep(lib)
         if "ensemble" in want:

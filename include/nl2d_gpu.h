@@ -122,7 +122,14 @@ int nl2d_last_path(void);
  * The mixed form applies to problems the fused path accepts; it is not
  * bit-identical to the reference.  Reading a field (c_read_from_device)
  * returns the FP64 image of the mixed state; switching back to 0 continues
- * from that image.  Returns the previous precision. */
+ * from that image.  2 = FP64-equivalent: the fused path with its interior
+ * cells (3x3 wet, one cell inside next_ssh's ranges) computed in
+ * double-float arithmetic (FP32 pairs, about 48 significant bits) and every
+ * other cell in exact FP64, the state kept in FP64; not bit-identical, held
+ * to relative L2 <= 1e-10 per field and checksums to 10 significant digits
+ * after 2000 steps of the parity namelist.  Steps that cannot fuse take the
+ * reference-structured path as for 0, and nl2d_last_path reports 2 for it.
+ * Returns the previous precision. */
 int nl2d_set_precision(int precision);
 
 /* Registers and uploads a problem without stepping (same arguments as

@@ -30,6 +30,7 @@ SOURCES = [
     "nl2d_io.cpp",
     "tra_adv.cu",
     "nl2d_rates.cu",
+    "nl2d_df.cu",
 ]
 # The mixed-precision form has no bit-exactness contract: FMA contraction on.
 PER_FILE_FLAGS = {"nl2d_mixed.cu": ["-fmad=true"]}

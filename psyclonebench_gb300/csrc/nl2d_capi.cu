@@ -51,7 +51,7 @@ struct State {
   cudaGraphExec_t graph = nullptr;
   int graph_key[5] = {-1, -1, -1, -1, -1};
   // mixed-precision form
-  int precision = 0;           // 0 FP64, 1 mixed
+  int precision = 0;           // 0 FP64, 1 mixed, 2 FP64-equivalent (double-float)
   MixedFields mix{};
   int* mix_count = nullptr;    // device int for launch_mixed_flags
   float2* msn[2] = {};
@@ -62,6 +62,9 @@ struct State {
   bool mixed_ahead = false;    // ... and it is newer than the FP64 arrays
   int status = NL2D_OK;
   char msg[512] = {0};
+  // FP64-equivalent form: split statics, march flags, boundary tiles
+  DfFields dfs{};
+  bool df_valid = false;
   unsigned scan_flags = 0;     // last registration scan (kScan* bits)
   double grid_refs[11] = {};   // the metric arrays' and latitudes' reference values
   long long h2d_bytes = 0, d2h_bytes = 0;  // copied since registration
@@ -128,6 +131,11 @@ void free_device() {
     cudaFree(s.mix.glist);
     cudaFree(s.mix_count);
     s.mix_count = nullptr;
+    for (float2* a : {s.dfs.ht, s.dfs.hu, s.dfs.hv, s.dfs.rhu, s.dfs.rhv}) cudaFree(a);
+    cudaFree(s.dfs.reg);
+    cudaFree(s.dfs.tiles);
+    s.dfs = DfFields{};
+    s.df_valid = false;
     s.mix = MixedFields{};
     s.mixed_valid = s.mixed_ahead = false;
   }
@@ -478,6 +486,7 @@ double* cur_un() { return g_state.cur ? g_state.shadow[1] : g_state.dev.un; }
 double* cur_vn() { return g_state.cur ? g_state.shadow[2] : g_state.dev.vn; }
 
 bool sync_from_mixed();
+bool ensure_df();
 
 // Brings the primary device arrays to exactly what the reference would hold
 // after the steps taken so far (for the mixed form: the FP64 image of its
@@ -561,8 +570,43 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
   fs.sshn_out = nxt ? s.shadow[0] : s.dev.sshn_t;
   fs.un_out = nxt ? s.shadow[1] : s.dev.un;
   fs.vn_out = nxt ? s.shadow[2] : s.dev.vn;
-  launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
+  if (s.precision == 2) {
+    // interior cells in double-float, the others in exact FP64; both read
+    // the same buffers and write disjoint cells
+    launch_df_march(fs, s.dfs, dims(), make_df_const(s.sc, s.um), s.stream);
+    launch_fused_boundary(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index,
+                          s.dfs.tiles, s.stream);
+  } else {
+    launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
+  }
   s.cur = nxt;
+}
+
+// The FP64-equivalent form's static arrays (split depths and reciprocal
+// denominators, march flags, boundary tiles), made from the current FP64
+// arrays unless they already are.
+bool ensure_df() {
+  State& s = g_state;
+  if (s.df_valid) return true;
+  const Registration& r = s.reg;
+  const size_t n = (size_t)r.width * r.height;
+  const int nx = r.xe - r.xs + 3, ny = r.ye - r.ys + 2;
+  const size_t ntiles = (size_t)((nx + 31) / 32) * ((ny + 15) / 16);
+  if (!s.dfs.ht) {
+    float2** arrs[5] = {&s.dfs.ht, &s.dfs.hu, &s.dfs.hv, &s.dfs.rhu, &s.dfs.rhv};
+    for (float2** a : arrs)
+      if (!CK(cudaMalloc(a, n * sizeof(float2)))) return false;
+    if (!CK(cudaMalloc(&s.dfs.reg, n)) || !CK(cudaMalloc(&s.dfs.tiles, ntiles * sizeof(int))))
+      return false;
+  }
+  launch_df_setup(s.dev, dims(), s.dfs, s.stream);
+  // the boundary kernel's shared-memory opt-in, outside any capture
+  launch_fused_boundary(s.dev, FusedState{}, dims(), s.sc, s.um, 0.0, nullptr, 0, nullptr,
+                        s.stream);
+  if (!CK(cudaGetLastError())) return false;
+  invalidate_graph();
+  s.df_valid = true;
+  return true;
 }
 
 // Converts the current FP64 state into the mixed buffers (both ping-pong
@@ -638,7 +682,7 @@ bool fused_step(int istep) {
   State& s = g_state;
   if (s.precision == 1) {
     if (!ensure_mixed()) return false;
-  } else if (!sync_shadows()) {
+  } else if (!sync_shadows() || (s.precision == 2 && !ensure_df())) {
     return false;
   }
   fused_launch(nullptr, 0, tide_value(istep, s.sc.rdt));
@@ -730,6 +774,7 @@ void invalidate_graph() {
 bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
   State& s = g_state;
   if (s.precision == 1 ? !ensure_mixed() : !sync_shadows()) return false;
+  if (s.precision == 2 && !ensure_df()) return false;
   if (s.tide_cap < rest) {
     invalidate_graph();  // it holds the old table address
     if (s.tide_table) cudaFree(s.tide_table);
@@ -908,6 +953,7 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
   // on the reference-structured path.
   s.consistent = false;
   s.shadows_synced = false;
+  s.df_valid = false;  // its split statics and flags may be stale
   if (k == 4 || k == 5 || k == 10 || k == 12) {  // hu, hv, ssha_u, ssha_v
     launch_depth_reciprocals(s.dev, dims(), s.stream);
     if (!CK(cudaGetLastError())) return;
@@ -1020,6 +1066,7 @@ int nl2d_checkpoint_read(const char* path, int* istep) {
   // as after c_write_to_device: the next step is reference-structured
   s.consistent = false;
   s.shadows_synced = false;
+  s.df_valid = false;  // its split statics and flags may be stale
   s.mixed_valid = s.mixed_ahead = false;
   launch_depth_reciprocals(s.dev, dims(), s.stream);
   if (!CK(cudaGetLastError()) || !CK(cudaStreamSynchronize(s.stream))) return scope.rc();
@@ -1070,7 +1117,7 @@ int nl2d_last_path(void) { return g_state.last_path; }
 int nl2d_set_precision(int precision) {
   State& s = g_state;
   const int old = s.precision;
-  if (precision != 0 && precision != 1) {
+  if (precision < 0 || precision > 2) {
     set_error(NL2D_ERR_ARGS, "nl2d_set_precision: unknown precision %d", precision);
     return old;
   }

@@ -1,0 +1,299 @@
+// The step's interior cells in double-float arithmetic (nl2d_df.cuh): the
+// FP64-equivalent form.  Not bit-identical to the reference; held to the
+// contract the reference's own comparisons use, relative L2 <= 1e-10 per
+// field and checksums to 10 significant digits after 2000 steps.
+//
+// The state stays FP64 in HBM, in the fused path's ping-pong buffers.  One
+// warp marches down a strip of rows over MW = 30 columns (one per lane,
+// plus a halo lane on each side), exactly as the mixed-precision column
+// march does (nl2d_mixed_march.cuh): rows j-1, j, j+1 of its column in
+// registers, x neighbours by shuffles, every term two neighbouring updates
+// share formed once; but every value is a double-float pair.  It writes the
+// same cells the mixed march writes: interior cells whose 3x3 mask
+// neighbourhood is wet and that lie one cell inside next_ssh's ranges, so
+// every face they read takes next_ssh's two-sided formula and no momentum
+// mask, bc_ssh, solid-wall or Flather rule applies.  Every other cell of the
+// copy region is computed in exact FP64 by the fused tile kernel, launched
+// on the tiles that hold such cells (nl2d_fused.cu).
+//
+// Loads split each FP64 state value into a pair (the depths and the
+// reciprocal momentum denominators are split once at set-up); stores add
+// the pair in FP64.
+#include "nl2d_df.cuh"
+#include "nl2d_internal.h"
+
+namespace nl2d {
+using namespace dfk;
+namespace {
+
+constexpr int MW = 30;
+constexpr int MR = 32;
+constexpr int WARPS = 4;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ df shd(df x) {
+  return df{__shfl_down_sync(FULL, x.hi, 1), __shfl_down_sync(FULL, x.lo, 1)};
+}
+__device__ __forceinline__ df shu(df x) {
+  return df{__shfl_up_sync(FULL, x.hi, 1), __shfl_up_sync(FULL, x.lo, 1)};
+}
+__device__ __forceinline__ df sel_lt0(df w, df a, df b) { return dneg_sign(w) ? a : b; }
+
+struct MRow {
+  df u, v, hu, hv, su, sv, sn, D;  // D = ht + sn
+};
+struct MRaw {
+  double sn, u, v;
+  float2 ht, hu, hv;
+};
+struct MTerm {
+  df Hu, Hv, fu, fv, gu, gv, fxu, fxv, fyu, fyv, qu, qv, vws, uws;
+};
+struct MOut {
+  df rhu, rhv;
+  unsigned char reg;
+};
+
+__device__ __forceinline__ df pair(float2 a) { return df{a.x, a.y}; }
+
+__device__ __forceinline__ MRaw load_raw(const FusedState& fs, const DfFields& ff, int i, int j,
+                                         int W, int H) {
+  MRaw r;
+  const bool ok = i >= 0 && i < W && j >= 0 && j < H;
+  const size_t c = ok ? (size_t)j * W + i : 0;
+  r.sn = ok ? __ldg(fs.sshn_in + c) : 0.0;
+  r.u = ok ? __ldg(fs.un_in + c) : 0.0;
+  r.v = ok ? __ldg(fs.vn_in + c) : 0.0;
+  const float2 z = make_float2(0.f, 0.f);
+  r.ht = ok ? __ldg(ff.ht + c) : z;
+  r.hu = ok ? __ldg(ff.hu + c) : z;
+  r.hv = ok ? __ldg(ff.hv + c) : z;
+  return r;
+}
+
+__device__ __forceinline__ MRow finish_row(const MRaw& a, const DfConst& k) {
+  MRow r;
+  r.sn = from_double(a.sn);
+  r.u = from_double(a.u);
+  r.v = from_double(a.v);
+  r.hu = pair(a.hu);
+  r.hv = pair(a.hv);
+  r.D = dadd(pair(a.ht), r.sn);
+  r.su = dmul(dadd(r.sn, shd(r.sn)), k.face_u);
+  r.sv = df{0.f, 0.f};
+  return r;
+}
+
+__device__ __forceinline__ MOut load_out(const DfFields& ff, bool col, int i, int j, int W,
+                                         int jend) {
+  MOut o{df{0.f, 0.f}, df{0.f, 0.f}, 0};
+  if (col && j < jend) {
+    const size_t c = (size_t)j * W + i;
+    o.reg = __ldg(ff.reg + c);
+    o.rhu = pair(__ldg(ff.rhu + c));
+    o.rhv = pair(__ldg(ff.rhv + c));
+  }
+  return o;
+}
+
+// The shared terms of row C (P below, N above), as in the mixed march's
+// row_terms.
+__device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const MRow& N,
+                                           const DfConst& k) {
+  MTerm t;
+  t.Hu = dadd(C.hu, C.su);
+  t.Hv = dadd(C.hv, C.sv);
+  t.fu = dmul(t.Hu, C.u);
+  t.fv = dmul(t.Hv, C.v);
+  const df uW = shu(C.u), vW = shu(C.v), HuW = shu(t.Hu);
+  const df vE_P = shd(P.v), hvE_P = shd(P.hv), svE_P = shd(P.sv);
+  const df uW_N = shu(N.u), huW_N = shu(N.hu), suW_N = shu(N.su);
+  t.gu = dmul(dmul(dsub(C.u, uW), k.r_dx), C.D);
+  t.gv = dmul(dmul(dsub(C.v, P.v), k.r_dy), C.D);
+  const df sAx = dadd(C.u, uW), sAy = dadd(uW, uW_N);
+  const df sBx = dadd(P.v, vE_P), sBy = dadd(C.v, P.v);
+  t.vws = sBx;
+  t.uws = sAy;
+  const df UUx = dmul(sAx, k.uu_x), UUy = dmul(sAy, k.uu_y);
+  const df VVx = dmul(sBx, k.vv_x), VVy = dmul(sBy, k.vv_y);
+  const df depx = dadd(dadd(HuW, huW_N), suW_N);
+  const df depy = dadd(dadd(dadd(P.hv, P.sv), hvE_P), svE_P);
+  t.fxu = dmul(dmul(sel_lt0(UUx, C.u, uW), UUx), C.D);
+  t.fxv = dmul(dmul(sel_lt0(UUy, C.v, vW), UUy), depx);
+  t.fyu = dmul(dmul(sel_lt0(VVx, C.u, P.u), VVx), depy);
+  t.fyv = dmul(dmul(sel_lt0(VVy, C.v, P.v), VVy), C.D);
+  t.qu = dmul(dsub(C.u, P.u), k.r_qu);
+  t.qv = dmul(dsub(C.v, vW), k.r_qv);
+  return t;
+}
+
+__global__ void __launch_bounds__(32 * WARPS, 2)
+    k_df_march(FusedState fs, DfFields ff, Dims d, DfConst k, int ncol, int nwarps, int mr) {
+  const int warp = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
+  if (warp >= nwarps) return;  // the whole warp leaves together
+  const int gy = warp / ncol, gx = warp - gy * ncol;
+  const int i0 = d.xs - 1 + gx * MW, j0 = d.ys - 1 + gy * mr;
+  const int lane = threadIdx.x & 31;
+  const int W = d.width, H = d.height;
+  const int i = i0 - 1 + lane;
+  const int jend = min(j0 + mr, d.ye + 1);
+  const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
+  MRow P = finish_row(load_raw(fs, ff, i, j0 - 1, W, H), k);
+  MRow C = finish_row(load_raw(fs, ff, i, j0, W, H), k);
+  MRow N = finish_row(load_raw(fs, ff, i, j0 + 1, W, H), k);
+  MRaw R1 = load_raw(fs, ff, i, j0 + 2, W, H);
+  MOut O = load_out(ff, out_col, i, j0, W, jend);
+  P.sv = dmul(dadd(P.sn, C.sn), k.face_v);
+  C.sv = dmul(dadd(C.sn, N.sn), k.face_v);
+  // row j0-1: what the updates of row j0 read from it
+  df fv0 = dmul(dadd(P.hv, P.sv), P.v), hu0 = P.hu, su0 = P.su;
+  MTerm T1 = row_terms(P, C, N, k);  // row j0
+  for (int j = j0; j < jend; j++) {
+    P = C;                  // row j
+    C = N;                  // row j+1
+    N = finish_row(R1, k);  // row j+2, loaded an iteration ago
+    R1 = load_raw(fs, ff, i, j + 3, W, H);
+    const MOut Oc = O;
+    O = load_out(ff, out_col, i, j + 1, W, jend);
+    C.sv = dmul(dadd(C.sn, N.sn), k.face_v);
+    const MTerm T2 = row_terms(P, C, N, k);  // row j+1
+    // x neighbours of row j's terms (every lane takes part)
+    const df fuW = shu(T1.fu), snE = shd(P.sn);
+    const df fxuE = shd(T1.fxu), fxvE = shd(T1.fxv), guE = shd(T1.gu), qvE = shd(T1.qv),
+             uwsE = shd(T1.uws);
+    const df hvW = shu(P.hv), svW = shu(P.sv), hvE = shd(P.hv), svE = shd(P.sv);
+    if (out_col && Oc.reg) {
+      const size_t c = (size_t)j * W + i;
+      const df div = dsub(dadd(dsub(fuW, T1.fu), fv0), T1.fv);
+      const df ssh = dadd(P.sn, dmul(div, k.rrat));
+      const df advu = dsub(dadd(dsub(T1.fxu, fxuE), T1.fyu), T2.fyu);
+      const df advv = dsub(dadd(dsub(T1.fxv, fxvE), T1.fyv), T2.fyv);
+      const df dSu = dmul(T1.qu, dadd(dadd(T1.Hu, hu0), su0));
+      const df dSv = dmul(T1.qv, dadd(dadd(T1.Hv, hvW), svW));
+      const df dNu = dmul(T2.qu, dadd(dadd(T1.Hu, C.hu), C.su));
+      const df dNv = dmul(qvE, dadd(dadd(T1.Hv, hvE), svE));
+      const df visu = dadd(dmul(dsub(dNu, dSu), k.vis2_u), dmul(dsub(guE, T1.gu), k.vis1_u));
+      const df visv = dadd(dmul(dsub(dNv, dSv), k.vis2_v), dmul(dsub(T2.gv, T1.gv), k.vis1_v));
+      const df coru = dmul(dmul(dadd(T1.vws, T2.vws), k.cor_u), T1.Hu);
+      const df corv = dmul(dmul(dadd(uwsE, T1.uws), k.cor_v), T1.Hv);
+      const df hpgu = dmul(dmul(T1.Hu, k.hpg_u), dsub(snE, P.sn));
+      const df hpgv = dmul(dmul(T1.Hv, k.hpg_v), dsub(C.sn, P.sn));
+      const df tu = dadd(dadd(dadd(advu, visu), coru), hpgu);
+      const df tv = dadd(dadd(dadd(advv, visv), corv), hpgv);
+      const df ou = dmul(dmul(dadd(dmul(tu, k.rra_u), dmul(P.u, T1.Hu)), Oc.rhu), k.r_fric);
+      const df ov = dmul(dmul(dadd(dmul(tv, k.rra_v), dmul(P.v, T1.Hv)), Oc.rhv), k.r_fric);
+      fs.sshn_out[c] = to_double(ssh);
+      fs.un_out[c] = to_double(ou);
+      fs.vn_out[c] = to_double(ov);
+    }
+    fv0 = T1.fv;
+    hu0 = P.hu;
+    su0 = P.su;
+    T1 = T2;
+  }
+}
+
+// FP64 arrays split into pairs once per set-up.
+__global__ void k_split(const double* __restrict__ a, float2* __restrict__ out, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const df p = from_double(a[t]);
+    out[t] = make_float2(p.hi, p.lo);
+  }
+}
+
+// Whether the march writes cell (i, j): the mixed march's rule.
+__device__ __forceinline__ bool df_regular(const int* m, const Dims& d, int i, int j) {
+  if (i < d.xs + 1 || i > d.xe - 1 || j < d.ys + 1 || j > d.ye - 1) return false;
+  const int W = d.width;
+#pragma unroll
+  for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+    for (int di = -1; di <= 1; di++)
+      if (m[(j + dj) * W + (i + di)] <= 0) return false;
+  return true;
+}
+
+__global__ void k_df_flags(const int* __restrict__ m, Dims d, unsigned char* __restrict__ reg) {
+  const long long n = (long long)d.width * d.height;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(t / d.width), i = (int)(t - (long long)j * d.width);
+    reg[t] = df_regular(m, d, i, j) ? 1 : 0;
+  }
+}
+
+// tiles[b] = 1 when tile b (tx x ty cells of the copy region, row-major
+// over the tile grid) holds a copy-region cell the march does not write.
+__global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
+                           int ntx, int* __restrict__ tiles) {
+  const int b = blockIdx.x;
+  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
+  int any = 0;
+  for (int t = threadIdx.x; t < tx * ty; t += blockDim.x) {
+    const int i = i0 + t % tx, j = j0 + t / tx;
+    if (i <= d.xe + 1 && j <= d.ye && !reg[(size_t)j * d.width + i]) any = 1;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) tiles[b] = any;
+}
+
+}  // namespace
+
+DfConst make_df_const(const Scalars& s, const UniformMetrics& um) {
+  const double dxv2 = um.dx_v + um.dx_v, dyu2 = um.dy_u + um.dy_u;
+  const double cor_u = 2. * s.omega * um.sin_u, cor_v = 2. * s.omega * um.sin_v;
+  DfConst k;
+  k.r_dx = from_double(1.0 / um.dx_t);
+  k.r_dy = from_double(1.0 / um.dy_t);
+  k.uu_x = from_double(0.5 * um.dy_t);
+  k.uu_y = from_double(0.125 * dyu2);
+  k.vv_x = from_double(0.125 * dxv2);
+  k.vv_y = from_double(0.5 * um.dx_t);
+  k.r_qu = from_double(1.0 / dyu2);
+  k.r_qv = from_double(1.0 / dxv2);
+  k.vis1_u = from_double(s.visc * um.dy_u);
+  k.vis1_v = from_double(s.visc * um.dx_v);
+  k.vis2_u = from_double(0.5 * s.visc * um.dx_u);
+  k.vis2_v = from_double(0.5 * s.visc * um.dy_v);
+  k.cor_u = from_double(0.25 * cor_u * um.area_u);
+  k.cor_v = from_double(-0.25 * cor_v * um.area_v);
+  k.hpg_u = from_double(-s.g * um.dy_u);
+  k.hpg_v = from_double(-s.g * um.dx_v);
+  k.rra_u = from_double(s.rdt / um.area_u);
+  k.rra_v = from_double(s.rdt / um.area_v);
+  k.face_u = from_double(0.5 * um.area_t / um.area_u);
+  k.face_v = from_double(0.5 * um.area_t / um.area_v);
+  k.rrat = from_double(s.rdt / um.area_t);
+  k.r_fric = from_double(1.0 / (1.0 + s.cbfr * s.rdt));
+  return k;
+}
+
+void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st) {
+  const int tx = 32, ty = 16;  // the fused tile kernel's DefaultTile
+  const long long n = (long long)d.width * d.height;
+  k_split<<<152 * 8, 256, 0, st>>>(f.ht, ff.ht, n);
+  k_split<<<152 * 8, 256, 0, st>>>(f.hu, ff.hu, n);
+  k_split<<<152 * 8, 256, 0, st>>>(f.hv, ff.hv, n);
+  k_split<<<152 * 8, 256, 0, st>>>(f.r_hu, ff.rhu, n);
+  k_split<<<152 * 8, 256, 0, st>>>(f.r_hv, ff.rhv, n);
+  k_df_flags<<<152 * 8, 256, 0, st>>>(f.tmask, d, ff.reg);
+  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
+  const int ntx = (nx + tx - 1) / tx, nty = (ny + ty - 1) / ty;
+  k_df_tiles<<<ntx * nty, 256, 0, st>>>(ff.reg, d, tx, ty, ntx, ff.tiles);
+}
+
+void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
+                     cudaStream_t st) {
+  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
+  const int ncol = (nx + MW - 1) / MW;
+  // strips of MR rows, halved (down to 8) until the grid holds about two
+  // waves of warps
+  int mr = MR;
+  while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 2 * WARPS) mr /= 2;
+  const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
+  k_df_march<<<(nwarps + WARPS - 1) / WARPS, 32 * WARPS, 0, st>>>(fs, ff, d, k, ncol, nwarps,
+                                                                  mr);
+}
+
+}  // namespace nl2d

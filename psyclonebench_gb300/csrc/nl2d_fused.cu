@@ -43,7 +43,38 @@ __global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
                 d.xs - 1 + blockIdx.x * T::TX, d.ys - 1 + blockIdx.y * T::TY, smem);
 }
 
+// The FP64-equivalent form's exact part: the fused tile on the tiles that
+// hold cells its double-float march does not write (tiles[b] != 0), those
+// cells only.
+__global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
+    k_fused_boundary(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um,
+                     FastConst k, const double* __restrict__ tide_table, int tide_index,
+                     double tide, const int* __restrict__ tiles) {
+  if (!tiles[blockIdx.y * gridDim.x + blockIdx.x]) return;  // the whole block leaves
+  extern __shared__ double smem[];
+  fused_tile<T, true>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
+                      d.xs - 1 + blockIdx.x * T::TX, d.ys - 1 + blockIdx.y * T::TY, smem);
+}
+
 }  // namespace
+
+void launch_fused_boundary(const Fields& f, const FusedState& fs, const Dims& d,
+                           const Scalars& s, const UniformMetrics& um, double tide,
+                           const double* tide_table, int tide_index, const int* tiles,
+                           cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_fused_boundary, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)T::kSmemBytes);
+    attr_set = true;
+  }
+  if (!tiles) return;  // set-up call: the attribute only
+  const FastConst k = make_fast_const(s, um);
+  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
+  const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY);
+  k_fused_boundary<<<grid, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(
+      f, fs, d, s, um, k, tide_table, tide_index, tide, tiles);
+}
 
 void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,

@@ -9,6 +9,8 @@
 #include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 
+#include "nl2d_df.cuh"
+
 namespace nl2d {
 
 // An NVTX range for the lifetime of the object: each public entry point
@@ -83,6 +85,32 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,
                        const double* tide_table, int tide_index,
                        cudaStream_t st);
+
+// ---- FP64-equivalent (double-float) form, nl2d_df.cu ----
+// The fused path's FP64 state and buffers; the interior cells by a column
+// march in double-float arithmetic, every other cell of the copy region by
+// the fused tile kernel in exact FP64 on the tiles that hold such cells.
+struct DfFields {
+  float2 *ht, *hu, *hv, *rhu, *rhv;  // (hi, lo) splits of the FP64 arrays
+  unsigned char* reg;                // 1 where the march writes the cell
+  int* tiles;                        // 1 where the FP64 tile kernel has work
+};
+struct DfConst {
+  dfk::df r_dx, r_dy, uu_x, uu_y, vv_x, vv_y, r_qu, r_qv, vis1_u, vis1_v, vis2_u, vis2_v;
+  dfk::df cor_u, cor_v, hpg_u, hpg_v, rra_u, rra_v, face_u, face_v, rrat, r_fric;
+};
+DfConst make_df_const(const Scalars& s, const UniformMetrics& um);
+// Splits the depths and reciprocal denominators, marks the march's cells and
+// the fused tile kernel's tiles (DefaultTile's shape).
+void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
+void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
+                     cudaStream_t st);
+// The fused FP64 tile kernel on the tiles with tiles[b] != 0, leaving the
+// march's cells alone.
+void launch_fused_boundary(const Fields& f, const FusedState& fs, const Dims& d,
+                           const Scalars& s, const UniformMetrics& um, double tide,
+                           const double* tide_table, int tide_index, const int* tiles,
+                           cudaStream_t st);
 
 // Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.
 void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
