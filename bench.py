@@ -74,7 +74,7 @@ def parse():
     ap.add_argument("--emu-horizon", type=int, default=5000,
                     help="solver steps of the emulator's trajectories and roll-out")
     ap.add_argument("--case", default=None,
-                    choices=["fused", "fused_active", "mixed", "tra_adv", "emu", "rates"],
+                    choices=["fused", "fused_active", "mixed", "df", "tra_adv", "emu", "rates"],
                     help="run one small case of one kernel family and print its device time "
                          "(for profiler captures; prints no bench line)")
     ap.add_argument("--batch", type=int, default=24, help="--case emu: images of 256^2")
@@ -812,7 +812,7 @@ def run_case(args):
     lib = P.load_library()
     n, out = args.size, {"case": args.case, "size": args.size, "steps": args.steps}
     ms = ctypes.c_double(0.0)
-    if args.case in ("fused", "fused_active", "mixed"):
+    if args.case in ("fused", "fused_active", "mixed", "df"):
         m = make_problem(n)
         if args.case == "fused_active":
             make_active(m)
@@ -821,7 +821,7 @@ def run_case(args):
             m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = fourier_depth(m.width, m.height, 2)
             m.rdt = BATHY_RDT
         register(lib, m)
-        lib.nl2d_set_precision(1 if args.case == "mixed" else 0)
+        lib.nl2d_set_precision({"mixed": 1, "df": 2}.get(args.case, 0))
         P.check(lib.nl2d_timed_run(1, 1 + args.warmup, ctypes.byref(ms)), "case warm-up")
         P.check(lib.nl2d_timed_run(2 + args.warmup, args.steps, ctypes.byref(ms)), "case run")
         lib.nl2d_set_precision(0)
