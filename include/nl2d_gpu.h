@@ -24,6 +24,7 @@
 #define NL2D_GPU_H
 
 #include <stdbool.h>
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -345,6 +346,13 @@ int nl2d_selftest_exact(long long n, unsigned long long seed, double d,
  * out[2] = the two counts.  Returns 0, or 1 on a CUDA error. */
 int nl2d_selftest_intfp(long long n, unsigned long long seed, long long *out);
 
+/* Test hook (no reference counterpart): the double-float march's
+ * conversions (nl2d_df.cuh) on n host values x (1 .. 2^26): hi / lo =
+ * split_bits(x), joined = join_bits of that pair, widened = widen_bits of x
+ * rounded to FP32.  Returns 0, 1 on a CUDA error, 2 for bad arguments. */
+int nl2d_selftest_df(const double *x, long long n, float *hi, float *lo,
+                     double *joined, double *widened);
+
 /* Test hook (no reference counterpart): one thread waits, through the
  * convolution kernels' bounded mbarrier wait, on a barrier that nothing
  * arrives on; after max_cycles (1 .. 2^32 clocks) the wait gives up and
@@ -371,6 +379,18 @@ int nl2d_sync(void);
 /* Bytes copied host -> device (out[0]) and device -> host (out[1]) since the
  * current problem was registered. */
 int nl2d_transfer_bytes(long long out[2]);
+
+/* Page-locks (pins) a caller's host array of `bytes` bytes, or releases it
+ * (no counterpart in the reference, whose OpenCL/OpenACC drivers copy from
+ * pageable arrays).  A driver that registers its 25 arrays once, before its
+ * first c_invoke_time_step, has the registration's upload and every
+ * c_read_from_device / c_write_to_device copy run from pinned memory at the
+ * host link's rate instead of through a staging buffer.  Pinning is slow
+ * (the operating system locks every page), so it belongs to set-up.  Errors:
+ * a null pointer or zero size: NL2D_ERR_ARGS; the CUDA call's failure
+ * (e.g. the range is already pinned): NL2D_ERR_CUDA. */
+int nl2d_host_register(void *p, size_t bytes);
+int nl2d_host_unregister(void *p);
 
 /* Issue rates of this GPU's arithmetic pipes in Gop/s (no counterpart in
  * the reference): out = {FP64 FMA, FP64 multiply, FP64 add, FP32 FMA}, each

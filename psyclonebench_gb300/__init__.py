@@ -59,6 +59,8 @@ EXPORTS = {
     "nl2d_ens_set_domain": (ctypes.c_int, [ctypes.c_int, _IP, _DP, _DP, _DP]),
     "nl2d_ens_schedule": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double]),
     "nl2d_ens_tile": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "nl2d_host_register": (ctypes.c_int, [_VP, ctypes.c_size_t]),
+    "nl2d_host_unregister": (ctypes.c_int, [_VP]),
     "nl2d_ens_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     "nl2d_ens_read": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_ens_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),
@@ -82,6 +84,7 @@ EXPORTS = {
     "nl2d_ens_export_interior": (ctypes.c_int, [_VP]),
     "nl2d_ens_uses_march": (ctypes.c_int, []),
     "nl2d_selftest_wait": (ctypes.c_int, [ctypes.c_longlong, _IP]),
+    "nl2d_selftest_df": (ctypes.c_int, [_DP, ctypes.c_longlong, _VP, _VP, _DP, _DP]),
     "nl2d_checkpoint_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "nl2d_checkpoint_read": (ctypes.c_int, [ctypes.c_char_p, _IP]),
     "nl2d_ens_import_interior": (ctypes.c_int, [_VP]),

@@ -227,11 +227,18 @@ struct ScanIn {
 
 // next_sshu_code / next_sshv_code (time_update_kern.c:90-155) of one face
 // with uniform areas: returns false where the kernel leaves the face alone.
+// zero_pos: at and af are positive and finite, so two +0 heights give
+// 0.5 * (at * +0 + at * +0) / af = +0 exactly, without the FP64 work (a
+// state at rest is almost all +0).
 __device__ __forceinline__ bool next_ssh_value(const int* m, const double* sn, int c, int step,
-                                               double at, double af, double& v) {
+                                               double at, double af, bool zero_pos, double& v) {
   const int n = c + step;
   if (m[c] + m[n] <= 0) return false;
   if (m[c] * m[n] > 0) {
+    if (zero_pos && (__double_as_longlong(sn[c]) | __double_as_longlong(sn[n])) == 0) {
+      v = 0.0;
+      return true;
+    }
     const double rtmp1 = at * sn[c] + at * sn[n];
     v = 0.5 * rtmp1 / af;
   } else if (m[c] <= 0) {
@@ -256,12 +263,13 @@ __global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
   const unsigned long long g0 = bits(in.gphi[0][0]), g1 = bits(in.gphi[1][0]);
   // areas for the next_ssh check (meaningful only when uniform)
   const double at = in.metric[0][o], au = in.metric[1][o], av = in.metric[2][o];
+  auto pos_finite = [](double x) { return x > 0.0 && x <= 1.7976931348623157e308; };
+  const bool zu = pos_finite(at) && pos_finite(au), zv = pos_finite(at) && pos_finite(av);
   unsigned f = 0;
-  const int nx = in.xe - in.xs + 3, ny = in.ye - in.ys + 3;
-  const long long nr = (long long)nx * ny;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nr; t += stride) {
-    const int j = in.ys - 1 + (int)(t / nx), i = in.xs - 1 + (int)(t % nx);
+  // one row of the scanned region per block and pass: rows over blocks,
+  // points of a row over threads (no index division)
+  for (int j = in.ys - 1 + blockIdx.x; j <= in.ye + 1; j += gridDim.x)
+  for (int i = in.xs - 1 + threadIdx.x; i <= in.xe + 1; i += blockDim.x) {
     const int c = j * W + i;
 #pragma unroll
     for (int q = 0; q < 9; q++)
@@ -287,15 +295,16 @@ __global__ void k_register_scan(ScanIn in, unsigned* __restrict__ flags) {
     }
     if (j >= in.ys && j <= in.ye && i >= in.xs && i <= in.xe) {
       double v;
-      if (i <= in.xe - 1 && next_ssh_value(m, in.sn, c, 1, at, au, v) &&
+      if (i <= in.xe - 1 && next_ssh_value(m, in.sn, c, 1, at, au, zu, v) &&
           bits(v) != bits(in.snu[c]))
         f |= kScanNextSsh;
-      if (j <= in.ye - 1 && next_ssh_value(m, in.sn, c, W, at, av, v) &&
+      if (j <= in.ye - 1 && next_ssh_value(m, in.sn, c, W, at, av, zv, v) &&
           bits(v) != bits(in.snv[c]))
         f |= kScanNextSsh;
     }
   }
   const long long n = (long long)W * in.H;
+  const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += stride) {
     if (bits(in.gphi[0][t]) != g0) f |= kScanGphiU;
     if (bits(in.gphi[1][t]) != g1) f |= kScanGphiV;
@@ -1269,6 +1278,26 @@ int nl2d_transfer_bytes(long long out[2]) {
   out[0] = s.h2d_bytes;
   out[1] = s.d2h_bytes;
   return NL2D_OK;
+}
+
+int nl2d_host_register(void* p, size_t bytes) {
+  CallScope scope;
+  if (!p || bytes == 0) {
+    set_error(NL2D_ERR_ARGS, "nl2d_host_register: null pointer or zero size");
+    return scope.rc();
+  }
+  CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+  return scope.rc();
+}
+
+int nl2d_host_unregister(void* p) {
+  CallScope scope;
+  if (!p) {
+    set_error(NL2D_ERR_ARGS, "nl2d_host_unregister: null pointer");
+    return scope.rc();
+  }
+  CK(cudaHostUnregister(p));
+  return scope.rc();
 }
 
 void* nl2d_device_ptr(const void* field) {

@@ -16,9 +16,11 @@
 // copy region is computed in exact FP64 by the fused tile kernel, launched
 // on the tiles that hold such cells (nl2d_fused.cu).
 //
-// Loads split each FP64 state value into a pair (the depths and the
-// reciprocal momentum denominators are split once at set-up); stores add
-// the pair in FP64.
+// Loads split each FP64 state value into a pair from its bit pattern
+// (split_bits; the depths and the reciprocal momentum denominators are split
+// once at set-up); stores widen both halves from their bit patterns and add
+// them in FP64 (join_bits): one FP64 instruction per stored value, none per
+// loaded one.
 #include "nl2d_df.cuh"
 #include "nl2d_internal.h"
 
@@ -73,9 +75,9 @@ __device__ __forceinline__ MRaw load_raw(const FusedState& fs, const DfFields& f
 
 __device__ __forceinline__ MRow finish_row(const MRaw& a, const DfConst& k) {
   MRow r;
-  r.sn = from_double(a.sn);
-  r.u = from_double(a.u);
-  r.v = from_double(a.v);
+  r.sn = split_bits(a.sn);
+  r.u = split_bits(a.u);
+  r.v = split_bits(a.v);
   r.hu = pair(a.hu);
   r.hv = pair(a.hv);
   r.D = dadd(pair(a.ht), r.sn);
@@ -182,9 +184,9 @@ __global__ void __launch_bounds__(32 * WARPS, 2)
       const df tv = dadd(dadd(dadd(advv, visv), corv), hpgv);
       const df ou = dmul(dmul(dadd(dmul(tu, k.rra_u), dmul(P.u, T1.Hu)), Oc.rhu), k.r_fric);
       const df ov = dmul(dmul(dadd(dmul(tv, k.rra_v), dmul(P.v, T1.Hv)), Oc.rhv), k.r_fric);
-      fs.sshn_out[c] = to_double(ssh);
-      fs.un_out[c] = to_double(ou);
-      fs.vn_out[c] = to_double(ov);
+      fs.sshn_out[c] = join_bits(ssh);
+      fs.un_out[c] = join_bits(ou);
+      fs.vn_out[c] = join_bits(ov);
     }
     fv0 = T1.fv;
     hu0 = P.hu;
@@ -236,6 +238,19 @@ __global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx
   }
   any = __syncthreads_or(any);
   if (threadIdx.x == 0) tiles[b] = any;
+}
+
+__global__ void k_selftest_df(const double* __restrict__ x, long long n, float* __restrict__ hi,
+                              float* __restrict__ lo, double* __restrict__ joined,
+                              double* __restrict__ widened) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const df p = split_bits(x[t]);
+    hi[t] = p.hi;
+    lo[t] = p.lo;
+    joined[t] = join_bits(p);
+    widened[t] = widen_bits(__double2float_rn(x[t]));
+  }
 }
 
 }  // namespace
@@ -297,3 +312,29 @@ void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, co
 }
 
 }  // namespace nl2d
+
+extern "C" int nl2d_selftest_df(const double* x, long long n, float* hi, float* lo,
+                                double* joined, double* widened) {
+  if (!x || !hi || !lo || !joined || !widened || n <= 0 || n > (1LL << 26)) return 2;
+  double *dx = nullptr, *dj = nullptr, *dw = nullptr;
+  float *dh = nullptr, *dl = nullptr;
+  const size_t b8 = (size_t)n * 8, b4 = (size_t)n * 4;
+  bool ok = cudaMalloc(&dx, b8) == cudaSuccess && cudaMalloc(&dj, b8) == cudaSuccess &&
+            cudaMalloc(&dw, b8) == cudaSuccess && cudaMalloc(&dh, b4) == cudaSuccess &&
+            cudaMalloc(&dl, b4) == cudaSuccess;
+  ok = ok && cudaMemcpy(dx, x, b8, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    nl2d::k_selftest_df<<<152 * 4, 256>>>(dx, n, dh, dl, dj, dw);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  ok = ok && cudaMemcpy(hi, dh, b4, cudaMemcpyDeviceToHost) == cudaSuccess &&
+       cudaMemcpy(lo, dl, b4, cudaMemcpyDeviceToHost) == cudaSuccess &&
+       cudaMemcpy(joined, dj, b8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+       cudaMemcpy(widened, dw, b8, cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(dx);
+  cudaFree(dj);
+  cudaFree(dw);
+  cudaFree(dh);
+  cudaFree(dl);
+  return ok ? 0 : 1;
+}

@@ -69,6 +69,63 @@ __host__ __device__ inline df from_double(double x) {
 
 __device__ __forceinline__ double to_double(df a) { return (double)a.hi + (double)a.lo; }
 
+// The same two conversions without the FP64 pipe, for kernels that convert
+// every value they load and store: on GB300 the FP64 pipe issues about 1.7
+// operations per clock per SM, the integer and FP32 pipes over 60 each, and
+// the hardware conversions between FP64 and FP32 run on the FP64 pipe.
+//
+// split_bits(x): hi is x truncated to 24 significant bits, built from the
+// bit pattern (exponent rebiased from 1023 to 127, the top 23 mantissa bits
+// kept); lo is the next 29 bits rounded to 23 and made a float exactly (the
+// 2^23 exponent trick: the float with bits 0x4B000000 + m is 2^23 + m for
+// m <= 2^23) and scaled by a power of two; Fast2Sum normalises the pair.
+// 47 of the 53 significant bits are kept (relative error below 2^-46).  Out
+// of range, without branches: |x| < 2^-80 keeps hi only (lo would leave the
+// FP32 normal range), |x| < 2^-126 gives a signed zero, |x| >= 2^127 an
+// infinity (so that hi + lo cannot round past the largest float) and a NaN
+// a NaN.
+__device__ __forceinline__ df split_bits(double x) {
+  unsigned lw, hw;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lw), "=r"(hw) : "d"(x));
+  const unsigned sign = hw & 0x80000000u;
+  const unsigned e = (hw >> 20) & 0x7ffu;
+  // bits 31..23 of the funnel shift are e mod 512; subtracting 384 << 23
+  // leaves e - 896 there for 897 <= e <= 1149
+  const unsigned hb_n = (__funnelshift_l(lw, hw, 3) - 0xC0000000u) | sign;
+  const bool nan = e == 0x7ffu && ((hw & 0xfffffu) | lw) != 0u;
+  const unsigned hb = e - 897u <= 1149u - 897u ? hb_n
+                      : e > 1149u ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u))
+                                  : sign;
+  const unsigned r23 = ((lw & 0x1fffffffu) + 32u) >> 6;  // 0 .. 2^23
+  const float m = __fsub_rn(__uint_as_float(0x4B000000u + r23), 8388608.0f);
+  const float scale = __uint_as_float((e - 942u) << 23);  // 2^(e - 1069)
+  const float lo_n = __uint_as_float(__float_as_uint(__fmul_rn(m, scale)) | sign);
+  const float lo = e - 943u <= 1149u - 943u ? lo_n : __uint_as_float(sign);
+  return fast_two_sum(__uint_as_float(hb), lo);
+}
+
+// f widened exactly to FP64 from its bit pattern (exponent rebiased from
+// 127 to 1023, mantissa moved up 29 bits); zeros and subnormals give a
+// signed zero, infinities and NaN the same in FP64.
+__device__ __forceinline__ double widen_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned sign = b & 0x80000000u;
+  const unsigned ef = (b >> 23) & 0xffu;
+  const unsigned hw_n = sign | (((b >> 3) & 0x0fffffffu) + (896u << 20));
+  const unsigned hw = ef - 1u <= 253u ? hw_n
+                      : ef == 0u ? sign
+                                 : (sign | 0x7ff00000u | ((b & 0x7fffffu) ? 0x80000u : 0u));
+  const unsigned lw = ef - 1u <= 253u ? b << 29 : 0u;
+  double x;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lw), "r"(hw));
+  return x;
+}
+
+// hi + lo rounded to FP64: one FP64 add.
+__device__ __forceinline__ double join_bits(df a) {
+  return __dadd_rn(widen_bits(a.hi), widen_bits(a.lo));
+}
+
 // The sign test of an upwind switch: the sign of the value, which is the
 // sign of hi for a normalised pair.
 __device__ __forceinline__ bool dneg_sign(df a) { return a.hi < 0.f; }

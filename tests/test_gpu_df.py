@@ -110,3 +110,55 @@ def test_df_graph_run_matches_calls(gpulib, oracle):
     gpulib.nl2d_set_precision(0)
     for k in T.FIELDS:
         assert np.array_equal(a.f[k].view(np.int64), b.f[k].view(np.int64)), k
+
+
+def test_df_bit_conversions(gpulib):
+    """split_bits / join_bits / widen_bits (the march's conversions done on
+    the integer and FP32 pipes) on values across every range boundary and
+    on random values: 47 significant bits kept in range, normalised pairs,
+    the stated flushes, infinities and NaN carried through; the join equals
+    the FP64 sum of the exactly widened halves, the widening equals the
+    exact FP32 -> FP64 conversion (subnormal floats flushed)."""
+    rng = np.random.default_rng(5)
+    edges = [0.0, -0.0, 1.0, -1.0, np.pi, 2.0 ** -80, -(2.0 ** -80),
+             np.nextafter(2.0 ** -80, 0), 2.0 ** -126, np.nextafter(2.0 ** -126, 0),
+             2.0 ** -127, 5e-324, -1e-310, np.nextafter(2.0 ** 128, 0), 2.0 ** 128, np.nextafter(2.0 ** 127, 0),
+             2.0 ** 127, -1e300,
+             np.inf, -np.inf, np.nan, 0.1, -0.2, 3.4e38, 1.0 + 2.0 ** -30, 1.0 - 2.0 ** -40]
+    rand = rng.standard_normal(200000) * np.exp(rng.uniform(-60, 60, 200000))
+    x = np.concatenate([np.array(edges), rand, rng.uniform(-0.5, 0.5, 50000)])
+    n = x.size
+    hi, lo = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    joined, widened = np.zeros(n), np.zeros(n)
+    assert gpulib.nl2d_selftest_df(T.dptr(x), n, hi.ctypes.data, lo.ctypes.data,
+                                   T.dptr(joined), T.dptr(widened)) == 0
+    ax = np.abs(x)
+    fin = np.isfinite(x)
+    full = fin & (ax >= 2.0 ** -80) & (ax < 2.0 ** 127)
+    pair = hi[full].astype(np.float64) + lo[full].astype(np.float64)
+    assert np.all(np.abs(pair - x[full]) <= 2.0 ** -46 * ax[full])
+    # normalised: hi is the FP32 rounding of hi + lo
+    assert np.array_equal((hi[full] + lo[full]).view(np.int32), hi[full].view(np.int32))
+    mid = fin & (ax >= 2.0 ** -126) & (ax < 2.0 ** -80)
+    assert np.all(np.abs(hi[mid] - x[mid]) <= 2.0 ** -23 * ax[mid]) and np.all(lo[mid] == 0)
+    tiny = fin & (ax < 2.0 ** -126)
+    assert np.all(hi[tiny] == 0) and np.all(lo[tiny] == 0)
+    assert np.array_equal(np.signbit(hi[tiny]), np.signbit(x[tiny]))
+    big = ~np.isnan(x) & (ax >= 2.0 ** 127)
+    assert np.array_equal(hi[big], np.where(x[big] > 0, np.inf, -np.inf).astype(np.float32))
+    assert np.all(np.isnan(hi[np.isnan(x)]))
+    # join: the FP64 sum of the halves, exactly widened
+    want = hi[full].astype(np.float64) + lo[full].astype(np.float64)
+    assert np.array_equal(joined[full].view(np.int64), want.view(np.int64))
+    # widen: exact FP32 -> FP64 for normal floats, signed zero for subnormals
+    with np.errstate(over="ignore"):
+        f = x.astype(np.float32)
+    normal = np.isfinite(f) & (np.abs(f) >= np.float32(2.0 ** -126))
+    assert np.array_equal(widened[normal].view(np.int64),
+                          f[normal].astype(np.float64).view(np.int64))
+    sub = np.isfinite(f) & (np.abs(f) < np.float32(2.0 ** -126))
+    assert np.all(widened[sub] == 0)
+    assert np.array_equal(np.signbit(widened[sub]), np.signbit(f[sub]))
+    inf = np.isinf(f)
+    assert np.array_equal(widened[inf], f[inf].astype(np.float64))
+    assert np.all(np.isnan(widened[np.isnan(f)]))
