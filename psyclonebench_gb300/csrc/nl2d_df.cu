@@ -81,7 +81,7 @@ __device__ __forceinline__ MRow finish_row(const MRaw& a, const DfConst& k) {
   r.hu = pair(a.hu);
   r.hv = pair(a.hv);
   r.D = dadd(pair(a.ht), r.sn);
-  r.su = dmul(dadd(r.sn, shd(r.sn)), k.face_u);
+  r.su = dmul_u(dadd(r.sn, shd(r.sn)), k.face_u);
   r.sv = df{0.f, 0.f};
   return r;
 }
@@ -105,31 +105,31 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
   MTerm t;
   t.Hu = dadd(C.hu, C.su);
   t.Hv = dadd(C.hv, C.sv);
-  t.fu = dmul(t.Hu, C.u);
-  t.fv = dmul(t.Hv, C.v);
+  t.fu = dmul_u(t.Hu, C.u);
+  t.fv = dmul_u(t.Hv, C.v);
   const df uW = shu(C.u), vW = shu(C.v), HuW = shu(t.Hu);
   const df vE_P = shd(P.v), hvE_P = shd(P.hv), svE_P = shd(P.sv);
   const df uW_N = shu(N.u), huW_N = shu(N.hu), suW_N = shu(N.su);
-  t.gu = dmul(dmul(dsub(C.u, uW), k.r_dx), C.D);
-  t.gv = dmul(dmul(dsub(C.v, P.v), k.r_dy), C.D);
+  t.gu = dmul_u(dmul_u(dsub(C.u, uW), k.r_dx), C.D);
+  t.gv = dmul_u(dmul_u(dsub(C.v, P.v), k.r_dy), C.D);
   const df sAx = dadd(C.u, uW), sAy = dadd(uW, uW_N);
   const df sBx = dadd(P.v, vE_P), sBy = dadd(C.v, P.v);
   t.vws = sBx;
   t.uws = sAy;
-  const df UUx = dmul(sAx, k.uu_x), UUy = dmul(sAy, k.uu_y);
-  const df VVx = dmul(sBx, k.vv_x), VVy = dmul(sBy, k.vv_y);
-  const df depx = dadd(dadd(HuW, huW_N), suW_N);
-  const df depy = dadd(dadd(dadd(P.hv, P.sv), hvE_P), svE_P);
-  t.fxu = dmul(dmul(sel_lt0(UUx, C.u, uW), UUx), C.D);
-  t.fxv = dmul(dmul(sel_lt0(UUy, C.v, vW), UUy), depx);
-  t.fyu = dmul(dmul(sel_lt0(VVx, C.u, P.u), VVx), depy);
-  t.fyv = dmul(dmul(sel_lt0(VVy, C.v, P.v), VVy), C.D);
-  t.qu = dmul(dsub(C.u, P.u), k.r_qu);
-  t.qv = dmul(dsub(C.v, vW), k.r_qv);
+  const df UUx = dmul_u(sAx, k.uu_x), UUy = dmul_u(sAy, k.uu_y);
+  const df VVx = dmul_u(sBx, k.vv_x), VVy = dmul_u(sBy, k.vv_y);
+  const df depx = dsum3(HuW, huW_N, suW_N);
+  const df depy = dsum4(P.hv, P.sv, hvE_P, svE_P);
+  t.fxu = dmul_u(dmul_u(sel_lt0(UUx, C.u, uW), UUx), C.D);
+  t.fxv = dmul_u(dmul_u(sel_lt0(UUy, C.v, vW), UUy), depx);
+  t.fyu = dmul_u(dmul_u(sel_lt0(VVx, C.u, P.u), VVx), depy);
+  t.fyv = dmul_u(dmul_u(sel_lt0(VVy, C.v, P.v), VVy), C.D);
+  t.qu = dmul_u(dsub(C.u, P.u), k.r_qu);
+  t.qv = dmul_u(dsub(C.v, vW), k.r_qv);
   return t;
 }
 
-__global__ void __launch_bounds__(32 * WARPS, 2)
+__global__ void __launch_bounds__(32 * WARPS, 3)
     k_df_march(FusedState fs, DfFields ff, Dims d, DfConst k, int ncol, int nwarps, int mr) {
   const int warp = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
   if (warp >= nwarps) return;  // the whole warp leaves together
@@ -145,10 +145,10 @@ __global__ void __launch_bounds__(32 * WARPS, 2)
   MRow N = finish_row(load_raw(fs, ff, i, j0 + 1, W, H), k);
   MRaw R1 = load_raw(fs, ff, i, j0 + 2, W, H);
   MOut O = load_out(ff, out_col, i, j0, W, jend);
-  P.sv = dmul(dadd(P.sn, C.sn), k.face_v);
-  C.sv = dmul(dadd(C.sn, N.sn), k.face_v);
+  P.sv = dmul_u(dadd(P.sn, C.sn), k.face_v);
+  C.sv = dmul_u(dadd(C.sn, N.sn), k.face_v);
   // row j0-1: what the updates of row j0 read from it
-  df fv0 = dmul(dadd(P.hv, P.sv), P.v), hu0 = P.hu, su0 = P.su;
+  df fv0 = dmul_u(dadd(P.hv, P.sv), P.v), hu0 = P.hu, su0 = P.su;
   MTerm T1 = row_terms(P, C, N, k);  // row j0
   for (int j = j0; j < jend; j++) {
     P = C;                  // row j
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(32 * WARPS, 2)
     R1 = load_raw(fs, ff, i, j + 3, W, H);
     const MOut Oc = O;
     O = load_out(ff, out_col, i, j + 1, W, jend);
-    C.sv = dmul(dadd(C.sn, N.sn), k.face_v);
+    C.sv = dmul_u(dadd(C.sn, N.sn), k.face_v);
     const MTerm T2 = row_terms(P, C, N, k);  // row j+1
     // x neighbours of row j's terms (every lane takes part)
     const df fuW = shu(T1.fu), snE = shd(P.sn);
@@ -166,24 +166,24 @@ __global__ void __launch_bounds__(32 * WARPS, 2)
     const df hvW = shu(P.hv), svW = shu(P.sv), hvE = shd(P.hv), svE = shd(P.sv);
     if (out_col && Oc.reg) {
       const size_t c = (size_t)j * W + i;
-      const df div = dsub(dadd(dsub(fuW, T1.fu), fv0), T1.fv);
-      const df ssh = dadd(P.sn, dmul(div, k.rrat));
-      const df advu = dsub(dadd(dsub(T1.fxu, fxuE), T1.fyu), T2.fyu);
-      const df advv = dsub(dadd(dsub(T1.fxv, fxvE), T1.fyv), T2.fyv);
-      const df dSu = dmul(T1.qu, dadd(dadd(T1.Hu, hu0), su0));
-      const df dSv = dmul(T1.qv, dadd(dadd(T1.Hv, hvW), svW));
-      const df dNu = dmul(T2.qu, dadd(dadd(T1.Hu, C.hu), C.su));
-      const df dNv = dmul(qvE, dadd(dadd(T1.Hv, hvE), svE));
-      const df visu = dadd(dmul(dsub(dNu, dSu), k.vis2_u), dmul(dsub(guE, T1.gu), k.vis1_u));
-      const df visv = dadd(dmul(dsub(dNv, dSv), k.vis2_v), dmul(dsub(T2.gv, T1.gv), k.vis1_v));
-      const df coru = dmul(dmul(dadd(T1.vws, T2.vws), k.cor_u), T1.Hu);
-      const df corv = dmul(dmul(dadd(uwsE, T1.uws), k.cor_v), T1.Hv);
-      const df hpgu = dmul(dmul(T1.Hu, k.hpg_u), dsub(snE, P.sn));
-      const df hpgv = dmul(dmul(T1.Hv, k.hpg_v), dsub(C.sn, P.sn));
-      const df tu = dadd(dadd(dadd(advu, visu), coru), hpgu);
-      const df tv = dadd(dadd(dadd(advv, visv), corv), hpgv);
-      const df ou = dmul(dmul(dadd(dmul(tu, k.rra_u), dmul(P.u, T1.Hu)), Oc.rhu), k.r_fric);
-      const df ov = dmul(dmul(dadd(dmul(tv, k.rra_v), dmul(P.v, T1.Hv)), Oc.rhv), k.r_fric);
+      const df div = dsum4(fuW, dneg(T1.fu), fv0, dneg(T1.fv));
+      const df ssh = dadd(P.sn, dmul_u(div, k.rrat));
+      const df advu = dsum4(T1.fxu, dneg(fxuE), T1.fyu, dneg(T2.fyu));
+      const df advv = dsum4(T1.fxv, dneg(fxvE), T1.fyv, dneg(T2.fyv));
+      const df dSu = dmul_u(T1.qu, dsum3(T1.Hu, hu0, su0));
+      const df dSv = dmul_u(T1.qv, dsum3(T1.Hv, hvW, svW));
+      const df dNu = dmul_u(T2.qu, dsum3(T1.Hu, C.hu, C.su));
+      const df dNv = dmul_u(qvE, dsum3(T1.Hv, hvE, svE));
+      const df visu = dadd(dmul_u(dsub(dNu, dSu), k.vis2_u), dmul_u(dsub(guE, T1.gu), k.vis1_u));
+      const df visv = dadd(dmul_u(dsub(dNv, dSv), k.vis2_v), dmul_u(dsub(T2.gv, T1.gv), k.vis1_v));
+      const df coru = dmul_u(dmul_u(dadd(T1.vws, T2.vws), k.cor_u), T1.Hu);
+      const df corv = dmul_u(dmul_u(dadd(uwsE, T1.uws), k.cor_v), T1.Hv);
+      const df hpgu = dmul_u(dmul_u(T1.Hu, k.hpg_u), dsub(snE, P.sn));
+      const df hpgv = dmul_u(dmul_u(T1.Hv, k.hpg_v), dsub(C.sn, P.sn));
+      const df tu = dsum4(advu, visu, coru, hpgu);
+      const df tv = dsum4(advv, visv, corv, hpgv);
+      const df ou = dmul_u(dmul_u(dadd(dmul_u(tu, k.rra_u), dmul_u(P.u, T1.Hu)), Oc.rhu), k.r_fric);
+      const df ov = dmul_u(dmul_u(dadd(dmul_u(tv, k.rra_v), dmul_u(P.v, T1.Hv)), Oc.rhv), k.r_fric);
       fs.sshn_out[c] = join_bits(ssh);
       fs.un_out[c] = join_bits(ou);
       fs.vn_out[c] = join_bits(ov);
