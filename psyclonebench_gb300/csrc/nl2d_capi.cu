@@ -133,7 +133,9 @@ void free_device() {
     s.mix_count = nullptr;
     for (float2* a : {s.dfs.ht, s.dfs.hu, s.dfs.hv, s.dfs.rhu, s.dfs.rhv}) cudaFree(a);
     cudaFree(s.dfs.reg);
-    cudaFree(s.dfs.tiles);
+    cudaFree(s.dfs.tiles_rows);
+    cudaFree(s.dfs.tiles_cols);
+    cudaFree(s.dfs.count);
     s.dfs = DfFields{};
     s.df_valid = false;
     s.mix = MixedFields{};
@@ -583,8 +585,8 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
     // interior cells in double-float, the others in exact FP64; both read
     // the same buffers and write disjoint cells
     launch_df_march(fs, s.dfs, dims(), make_df_const(s.sc, s.um), s.stream);
-    launch_fused_boundary(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index,
-                          s.dfs.tiles, s.stream);
+    launch_fused_boundary(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, &s.dfs,
+                          s.stream);
   } else {
     launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
   }
@@ -600,19 +602,32 @@ bool ensure_df() {
   const Registration& r = s.reg;
   const size_t n = (size_t)r.width * r.height;
   const int nx = r.xe - r.xs + 3, ny = r.ye - r.ys + 2;
-  const size_t ntiles = (size_t)((nx + 31) / 32) * ((ny + 15) / 16);
+  const size_t nrows = (size_t)((nx + kDfRowsTX - 1) / kDfRowsTX) *
+                       ((ny + kDfRowsTY - 1) / kDfRowsTY);
+  const size_t ncols = (size_t)((nx + kDfColsTX - 1) / kDfColsTX) *
+                       ((ny + kDfColsTY - 1) / kDfColsTY);
   if (!s.dfs.ht) {
     float2** arrs[5] = {&s.dfs.ht, &s.dfs.hu, &s.dfs.hv, &s.dfs.rhu, &s.dfs.rhv};
     for (float2** a : arrs)
       if (!CK(cudaMalloc(a, n * sizeof(float2)))) return false;
-    if (!CK(cudaMalloc(&s.dfs.reg, n)) || !CK(cudaMalloc(&s.dfs.tiles, ntiles * sizeof(int))))
+    if (!CK(cudaMalloc(&s.dfs.reg, n)) ||
+        !CK(cudaMalloc(&s.dfs.tiles_rows, nrows * sizeof(int))) ||
+        !CK(cudaMalloc(&s.dfs.tiles_cols, ncols * sizeof(int))) ||
+        !CK(cudaMalloc(&s.dfs.count, 2 * sizeof(int))))
       return false;
   }
   launch_df_setup(s.dev, dims(), s.dfs, s.stream);
-  // the boundary kernel's shared-memory opt-in, outside any capture
+  // the boundary kernels' shared-memory opt-in, outside any capture
   launch_fused_boundary(s.dev, FusedState{}, dims(), s.sc, s.um, 0.0, nullptr, 0, nullptr,
                         s.stream);
-  if (!CK(cudaGetLastError())) return false;
+  int counts[2] = {0, 0};
+  if (!CK(cudaGetLastError()) ||
+      !CK(cudaMemcpyAsync(counts, s.dfs.count, sizeof counts, cudaMemcpyDeviceToHost,
+                          s.stream)) ||
+      !CK(cudaStreamSynchronize(s.stream)))
+    return false;
+  s.dfs.n_rows = counts[0];
+  s.dfs.n_cols = counts[1];
   invalidate_graph();
   s.df_valid = true;
   return true;

@@ -225,19 +225,25 @@ __global__ void k_df_flags(const int* __restrict__ m, Dims d, unsigned char* __r
   }
 }
 
-// tiles[b] = 1 when tile b (tx x ty cells of the copy region, row-major
-// over the tile grid) holds a copy-region cell the march does not write.
+// Appends to `list` every tile of a tx x ty grid over the copy region
+// (row-major, ntx tiles per row) that holds a cell of its kind the march
+// does not write: side 1 the side strips (columns xs-1, xs, xe, xe+1 of
+// rows ys+1 .. ye-1), side 0 every other such cell.  The two kinds cover
+// every copy-region cell the march leaves; the order of the list does not
+// matter (each tile writes its own cells).
 __global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
-                           int ntx, int* __restrict__ tiles) {
+                           int ntx, int side, int* __restrict__ list, int* __restrict__ count) {
   const int b = blockIdx.x;
   const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
   int any = 0;
   for (int t = threadIdx.x; t < tx * ty; t += blockDim.x) {
     const int i = i0 + t % tx, j = j0 + t / tx;
-    if (i <= d.xe + 1 && j <= d.ye && !reg[(size_t)j * d.width + i]) any = 1;
+    if (i > d.xe + 1 || j > d.ye || reg[(size_t)j * d.width + i]) continue;
+    const bool strip = (i <= d.xs || i >= d.xe) && j >= d.ys + 1 && j <= d.ye - 1;
+    if (strip == (side == 1)) any = 1;
   }
   any = __syncthreads_or(any);
-  if (threadIdx.x == 0) tiles[b] = any;
+  if (threadIdx.x == 0 && any) list[atomicAdd(count + side, 1)] = b;
 }
 
 __global__ void k_selftest_df(const double* __restrict__ x, long long n, float* __restrict__ hi,
@@ -285,7 +291,6 @@ DfConst make_df_const(const Scalars& s, const UniformMetrics& um) {
 }
 
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st) {
-  const int tx = 32, ty = 16;  // the fused tile kernel's DefaultTile
   const long long n = (long long)d.width * d.height;
   k_split<<<152 * 8, 256, 0, st>>>(f.ht, ff.ht, n);
   k_split<<<152 * 8, 256, 0, st>>>(f.hu, ff.hu, n);
@@ -293,9 +298,14 @@ void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStr
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hu, ff.rhu, n);
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hv, ff.rhv, n);
   k_df_flags<<<152 * 8, 256, 0, st>>>(f.tmask, d, ff.reg);
+  cudaMemsetAsync(ff.count, 0, 2 * sizeof(int), st);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const int ntx = (nx + tx - 1) / tx, nty = (ny + ty - 1) / ty;
-  k_df_tiles<<<ntx * nty, 256, 0, st>>>(ff.reg, d, tx, ty, ntx, ff.tiles);
+  const int rx = (nx + kDfRowsTX - 1) / kDfRowsTX, ry = (ny + kDfRowsTY - 1) / kDfRowsTY;
+  const int cx = (nx + kDfColsTX - 1) / kDfColsTX, cy = (ny + kDfColsTY - 1) / kDfColsTY;
+  k_df_tiles<<<rx * ry, 256, 0, st>>>(ff.reg, d, kDfRowsTX, kDfRowsTY, rx, 0, ff.tiles_rows,
+                                      ff.count);
+  k_df_tiles<<<cx * cy, 256, 0, st>>>(ff.reg, d, kDfColsTX, kDfColsTY, cx, 1, ff.tiles_cols,
+                                      ff.count);
 }
 
 void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,

@@ -90,26 +90,35 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
 // The fused path's FP64 state and buffers; the interior cells by a column
 // march in double-float arithmetic, every other cell of the copy region by
 // the fused tile kernel in exact FP64 on the tiles that hold such cells.
+// The exact part runs on thin tiles: DfEdgeRows (128 x 2) over the rows
+// ys-1, ys and ye and every other cell off the side strips, DfEdgeCols
+// (4 x 128) over the side strips (columns xs-1, xs, xe, xe+1 of rows ys+1 ..
+// ye-1); 32 x 16 tiles spent 8x (rows) and 16x (columns) the work there.
 struct DfFields {
   float2 *ht, *hu, *hv, *rhu, *rhv;  // (hi, lo) splits of the FP64 arrays
   unsigned char* reg;                // 1 where the march writes the cell
-  int* tiles;                        // 1 where the FP64 tile kernel has work
+  int* tiles_rows;                   // DfEdgeRows tiles with work (indices)
+  int* tiles_cols;                   // DfEdgeCols tiles with work (indices)
+  int* count;                        // device: the two list lengths
+  int n_rows, n_cols;                // host copies of the list lengths
 };
 struct DfConst {
   dfk::df r_dx, r_dy, uu_x, uu_y, vv_x, vv_y, r_qu, r_qv, vis1_u, vis1_v, vis2_u, vis2_v;
   dfk::df cor_u, cor_v, hpg_u, hpg_v, rra_u, rra_v, face_u, face_v, rrat, r_fric;
 };
 DfConst make_df_const(const Scalars& s, const UniformMetrics& um);
+constexpr int kDfRowsTX = 128, kDfRowsTY = 2, kDfColsTX = 4, kDfColsTY = 128;
 // Splits the depths and reciprocal denominators, marks the march's cells and
-// the fused tile kernel's tiles (DefaultTile's shape).
+// lists the exact part's tiles (ff.count receives the list lengths).
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
 void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
                      cudaStream_t st);
-// The fused FP64 tile kernel on the tiles with tiles[b] != 0, leaving the
-// march's cells alone.
+// The fused FP64 tile kernel on the listed tiles of both shapes, leaving
+// the march's cells alone.  ff == nullptr: only sets the kernels' shared-
+// memory attributes (call outside any capture).
 void launch_fused_boundary(const Fields& f, const FusedState& fs, const Dims& d,
                            const Scalars& s, const UniformMetrics& um, double tide,
-                           const double* tide_table, int tide_index, const int* tiles,
+                           const double* tide_table, int tide_index, const DfFields* ff,
                            cudaStream_t st);
 
 // Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.

@@ -162,3 +162,55 @@ def test_df_bit_conversions(gpulib):
     inf = np.isinf(f)
     assert np.array_equal(widened[inf], f[inf].astype(np.float64))
     assert np.all(np.isnan(widened[np.isnan(f)]))
+
+
+@pytest.mark.parametrize("case", ["cfg0", "random_land", "open_east_south"])
+def test_df_exact_cells_equal_fp64_step(gpulib, oracle, case):
+    """One step of the form from a state both paths share: every copy-region
+    cell the double-float march does not write (the exact part's thin tiles:
+    the edge rows, the side strips, the cells next to land) is bit-identical
+    to the FP64 step's, so no such cell is left unwritten; the march's cells
+    agree to 1e-12 relative to the field's size."""
+    rng = np.random.default_rng({"cfg0": 7, "random_land": 8, "open_east_south": 9}[case])
+    if case == "open_east_south":
+        m = T.make_model(97, 75, 3, width=104, oracle=oracle)
+    else:
+        m = T.make_model(262, 140, 1, width=264, oracle=oracle)
+    from psyclonebench_gb300.workloads import fourier_depth
+    if case != "cfg0":
+        ht, hu, hv = fourier_depth(m.width, m.height, 4)
+        m.f["ht"][:], m.f["hu"][:], m.f["hv"][:] = ht, hu, hv
+        m.rdt = 5.0
+        for k, a in (("sshn_t", 0.05), ("un", 0.02), ("vn", 0.02)):
+            m.f[k][:] = rng.uniform(-a, a, size=m.f[k].shape)
+    if case == "random_land":
+        inner = m.grid["tmask"][m.ys + 1:m.ye, m.xs + 1:m.xe]
+        inner[rng.random(inner.shape) < 0.05] = 0
+    # two steps of the FP64 path: the state is then what a step leaves
+    T.gpu_run_calls(gpulib, m, 2)
+    gpulib.nl2d_finalize()
+    a, b = m.copy(), m.copy()
+    T.gpu_run_calls(gpulib, a, 1, nit000=3)
+    gpulib.nl2d_finalize()
+    T.gpu_register(gpulib, b)
+    paths, _ = run_df(gpulib, b, 1, nit000=3)
+    gpulib.nl2d_finalize()
+    assert paths == [2]
+    # the march's cells: interior one inside next_ssh's ranges, 3x3 wet
+    tm = m.grid["tmask"]
+    H, W = tm.shape
+    march = np.zeros((H, W), bool)
+    wet = np.ones((m.ye - m.ys - 1, m.xe - m.xs - 1), bool)
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            wet &= tm[m.ys + 1 + dj:m.ye + dj, m.xs + 1 + di:m.xe + di] > 0
+    march[m.ys + 1:m.ye, m.xs + 1:m.xe] = wet
+    copy = np.zeros((H, W), bool)
+    copy[m.ys - 1:m.ye + 1, m.xs - 1:m.xe + 2] = True
+    exact = copy & ~march
+    assert exact.sum() > 0 and march.sum() > 0
+    for k in ("sshn_t", "un", "vn"):
+        ga, gb = a.f[k], b.f[k]
+        assert np.array_equal(ga[exact].view(np.int64), gb[exact].view(np.int64)), k
+        scale = max(np.abs(ga[copy]).max(), 1e-30)
+        assert np.abs(ga[march] - gb[march]).max() <= 1e-12 * scale, k
