@@ -121,11 +121,24 @@ struct MTerm {
   float sn, lo;
 };
 
-// The values of one row of one column, as loaded.
+// The loaded values of row j of column i (zeros outside the array),
+// issued ahead of their use.
 struct MRaw {
   float2 s, uv, hh;
   float ht;
 };
+
+__device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int i,
+                                         int j, int W, int H, size_t base) {
+  MRaw r;
+  const bool ok = i >= 0 && i < W && j >= 0 && j < H;
+  const size_t c = base + (ok ? (size_t)j * W + i : 0);
+  r.s = ok ? __ldg(ms.sn_in + c) : make_float2(0.f, 0.f);
+  r.uv = make_float2(ok ? __ldg(ms.un_in + c) : 0.f, ok ? __ldg(ms.vn_in + c) : 0.f);
+  r.hh = make_float2(ok ? __ldg(mf.hu + c) : 0.f, ok ? __ldg(mf.hv + c) : 0.f);
+  r.ht = ok ? __ldg(mf.ht + c) : 0.f;
+  return r;
+}
 
 // A loaded row and its east face's sshn_u; the east neighbour's ssh comes
 // from lane + 1 (lane 31's su is not used).
@@ -147,69 +160,15 @@ struct MOut {
   unsigned char reg;
 };
 
-__device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int c) {
+__device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int i, int j, int W,
+                                         int jend, size_t base) {
   MOut o{make_float2(0.f, 0.f), 0};
-  if (col) {
+  if (col && j < jend) {
+    const size_t c = base + (size_t)j * W + i;
     o.reg = __ldg(mf.reg + c);
     o.rh = make_float2(__ldg(mf.rhu + c), __ldg(mf.rhv + c));
   }
   return o;
-}
-
-// Rows reach the march through a ring of shared-memory slots filled by
-// cp.async (each lane copies and later reads its own column only, so no
-// other lane's progress matters and no barrier is needed): RING rows in
-// flight per warp against two in registers before, which left the kernel
-// waiting on memory (5.2 long-scoreboard stalls per issued instruction at
-// 20 warps per SM).  A slot is refilled one row after it was read: the
-// values read from it have been used by then, so the copy cannot overtake
-// the read.
-constexpr int RING = 6;
-constexpr int SLOTS = RING + 1;
-
-struct MRing {  // one warp's slots
-  float2 s[SLOTS][32];
-  float u[SLOTS][32], v[SLOTS][32], hu[SLOTS][32], hv[SLOTS][32], ht[SLOTS][32];
-};
-
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(dst)),
-               "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(dst)),
-               "l"(src)
-               : "memory");
-}
-
-// Starts the copies of one row (element offset c) into a slot and commits
-// them as one group; a row past the strip commits an empty group, so that
-// every taken row finds exactly RING groups in flight.
-__device__ __forceinline__ void ring_issue(MRing& r, int slot, int lane, bool live,
-                                           const MixedFields& mf, const MixedState& ms, int c) {
-  if (live) {
-    cp_async8(&r.s[slot][lane], ms.sn_in + c);
-    cp_async4(&r.u[slot][lane], ms.un_in + c);
-    cp_async4(&r.v[slot][lane], ms.vn_in + c);
-    cp_async4(&r.hu[slot][lane], mf.hu + c);
-    cp_async4(&r.hv[slot][lane], mf.hv + c);
-    cp_async4(&r.ht[slot][lane], mf.ht + c);
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-// The oldest row in flight, once this lane's copies of it have landed.
-__device__ __forceinline__ MRaw ring_take(const MRing& r, int slot, int lane) {
-  asm volatile("cp.async.wait_group %0;" ::"n"(RING - 1) : "memory");
-  MRaw x;
-  x.s = r.s[slot][lane];
-  x.uv = make_float2(r.u[slot][lane], r.v[slot][lane]);
-  x.hh = make_float2(r.hu[slot][lane], r.hv[slot][lane]);
-  x.ht = r.ht[slot][lane];
-  return x;
 }
 
 // The shared terms at (i, r) from rows r-1 (P), r (C), r+1 (N): the tile
@@ -251,39 +210,17 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
 // the arrays (an ensemble packs its domains back to back; 0 otherwise).
 __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedState& ms,
                                             const Dims& d, const MarchConst& k, int i0, int j0,
-                                            size_t base, int mr, MRing& ring) {
+                                            size_t base, int mr) {
   const int lane = threadIdx.x & 31;
   const int W = d.width, H = d.height;
   const int i = i0 - 1 + lane;
   const int jend = min(j0 + mr, d.ye + 1);
-  const int jlast = jend + 1;  // the last row an update of the strip reads
   const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
-  // Element offsets are 32-bit: every array the march reads holds fewer
-  // than 2^31 elements (a single domain of 2^31 cells would need 25 FP64
-  // arrays of 16 GB; an ensemble packs fewer cells still).  Rows and columns
-  // outside the array are clamped onto it: a clamped value only reaches
-  // terms of cells the march does not write (it writes regular cells, whose
-  // stencil rows j-1 .. j+2 and columns i-1 .. i+1 lie inside the array), so
-  // the copies need no bounds test.
-  const int cb = (int)base + min(max(i, 0), W - 1);  // this lane's column
-  auto at = [cb, W, H](int j) { return cb + min(max(j, 0), H - 1) * W; };
-  for (int q = 0; q < RING; q++)
-    ring_issue(ring, q, lane, j0 - 1 + q <= jlast, mf, ms, at(j0 - 1 + q));
-  int rs = 0;  // slot of the next row to take
-  // takes row `row` (the oldest in flight) and starts row + RING in the
-  // slot read one row earlier
-  auto take = [&](int row) {
-    const MRaw x = ring_take(ring, rs, lane);
-    ring_issue(ring, rs == 0 ? RING : rs - 1, lane, row + RING <= jlast, mf, ms,
-               at(row + RING));
-    rs = rs == RING ? 0 : rs + 1;
-    return x;
-  };
-  MRow P = finish_row(take(j0 - 1), k);
-  MRow C = finish_row(take(j0), k);
-  MRow N = finish_row(take(j0 + 1), k);
-  // rows j0 .. jend lie inside the array (jend <= ye + 1 <= H - 1)
-  MOut O = load_out(mf, out_col, cb + j0 * W);
+  MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H, base), k);
+  MRow C = finish_row(load_raw(mf, ms, i, j0, W, H, base), k);
+  MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H, base), k);
+  MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H, base), R2 = load_raw(mf, ms, i, j0 + 3, W, H, base);
+  MOut O = load_out(mf, out_col, i, j0, W, jend, base);
   P.ss.y = (P.sn + C.sn) * k.face_v;
   C.ss.y = (C.sn + N.sn) * k.face_v;
   // row j0-1: what the updates of row j0 read from it
@@ -292,9 +229,11 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
   for (int j = j0; j < jend; j++) {
     P = C;  // row j
     C = N;  // row j+1
-    N = finish_row(take(j + 2), k);  // row j+2
+    N = finish_row(R1, k);  // row j+2, loaded two iterations ago
+    R1 = R2;
+    R2 = load_raw(mf, ms, i, j + 4, W, H, base);  // in flight for two iterations
     const MOut Oc = O;
-    O = load_out(mf, out_col, cb + (j + 1) * W);
+    O = load_out(mf, out_col, i, j + 1, W, jend, base);
     C.ss.y = (C.sn + N.sn) * k.face_v;
     const MTerm T2 = row_terms(P, C, N, k);  // row j+1
     // x neighbours of row j's terms (every lane takes part)
@@ -303,7 +242,7 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     const float gxE = shd(T1.g.x), qxE = shd(T1.q.y), uwcE = shd(T1.vw.y);
     const float hvW = shu(T1.hh.y), svW = shu(T1.ss.y), hvE = shd(T1.hh.y), svE = shd(T1.ss.y);
     if (out_col && Oc.reg) {
-      const int c = cb + j * W;
+      const size_t c = base + (size_t)j * W + i;
       const float div = ((flxuW - T1.flx.x) + flxv0) - T1.flx.y;
       ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rrat);
       const float2 Hf = T1.H;
