@@ -121,22 +121,18 @@ struct MTerm {
   float sn, lo;
 };
 
-// The loaded values of row j of column i (zeros outside the array),
-// issued ahead of their use.
+// The values of one row of one column, as loaded.
 struct MRaw {
   float2 s, uv, hh;
   float ht;
 };
 
-__device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int i,
-                                         int j, int W, int H, size_t base) {
+__device__ __forceinline__ MRaw load_raw(const MixedFields& mf, const MixedState& ms, int c) {
   MRaw r;
-  const bool ok = i >= 0 && i < W && j >= 0 && j < H;
-  const size_t c = base + (ok ? (size_t)j * W + i : 0);
-  r.s = ok ? __ldg(ms.sn_in + c) : make_float2(0.f, 0.f);
-  r.uv = make_float2(ok ? __ldg(ms.un_in + c) : 0.f, ok ? __ldg(ms.vn_in + c) : 0.f);
-  r.hh = make_float2(ok ? __ldg(mf.hu + c) : 0.f, ok ? __ldg(mf.hv + c) : 0.f);
-  r.ht = ok ? __ldg(mf.ht + c) : 0.f;
+  r.s = __ldg(ms.sn_in + c);
+  r.uv = make_float2(__ldg(ms.un_in + c), __ldg(ms.vn_in + c));
+  r.hh = make_float2(__ldg(mf.hu + c), __ldg(mf.hv + c));
+  r.ht = __ldg(mf.ht + c);
   return r;
 }
 
@@ -160,11 +156,9 @@ struct MOut {
   unsigned char reg;
 };
 
-__device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int i, int j, int W,
-                                         int jend, size_t base) {
+__device__ __forceinline__ MOut load_out(const MixedFields& mf, bool col, int c) {
   MOut o{make_float2(0.f, 0.f), 0};
-  if (col && j < jend) {
-    const size_t c = base + (size_t)j * W + i;
+  if (col) {
     o.reg = __ldg(mf.reg + c);
     o.rh = make_float2(__ldg(mf.rhu + c), __ldg(mf.rhv + c));
   }
@@ -216,11 +210,21 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
   const int i = i0 - 1 + lane;
   const int jend = min(j0 + mr, d.ye + 1);
   const bool out_col = lane >= 1 && lane <= MW && i <= d.xe + 1;
-  MRow P = finish_row(load_raw(mf, ms, i, j0 - 1, W, H, base), k);
-  MRow C = finish_row(load_raw(mf, ms, i, j0, W, H, base), k);
-  MRow N = finish_row(load_raw(mf, ms, i, j0 + 1, W, H, base), k);
-  MRaw R1 = load_raw(mf, ms, i, j0 + 2, W, H, base), R2 = load_raw(mf, ms, i, j0 + 3, W, H, base);
-  MOut O = load_out(mf, out_col, i, j0, W, jend, base);
+  // Element offsets are 32-bit: every array the march reads holds fewer
+  // than 2^31 elements (a single domain of 2^31 cells would need 25 FP64
+  // arrays of 16 GB; an ensemble packs fewer cells still).  Rows and columns
+  // outside the array are clamped onto it: a clamped value only reaches
+  // terms of cells the march does not write (it writes regular cells, whose
+  // stencil rows j-1 .. j+2 and columns i-1 .. i+1 lie inside the array), so
+  // the loads need no bounds test and no select.
+  const int cb = (int)base + min(max(i, 0), W - 1);  // this lane's column
+  auto at = [cb, W, H](int j) { return cb + min(max(j, 0), H - 1) * W; };
+  MRow P = finish_row(load_raw(mf, ms, at(j0 - 1)), k);
+  MRow C = finish_row(load_raw(mf, ms, at(j0)), k);
+  MRow N = finish_row(load_raw(mf, ms, at(j0 + 1)), k);
+  MRaw R1 = load_raw(mf, ms, at(j0 + 2)), R2 = load_raw(mf, ms, at(j0 + 3));
+  // rows j0 .. jend lie inside the array (jend <= ye + 1 <= H - 1)
+  MOut O = load_out(mf, out_col, cb + j0 * W);
   P.ss.y = (P.sn + C.sn) * k.face_v;
   C.ss.y = (C.sn + N.sn) * k.face_v;
   // row j0-1: what the updates of row j0 read from it
@@ -231,9 +235,9 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     C = N;  // row j+1
     N = finish_row(R1, k);  // row j+2, loaded two iterations ago
     R1 = R2;
-    R2 = load_raw(mf, ms, i, j + 4, W, H, base);  // in flight for two iterations
+    R2 = load_raw(mf, ms, at(j + 4));  // in flight for two iterations
     const MOut Oc = O;
-    O = load_out(mf, out_col, i, j + 1, W, jend, base);
+    O = load_out(mf, out_col, cb + (j + 1) * W);
     C.ss.y = (C.sn + N.sn) * k.face_v;
     const MTerm T2 = row_terms(P, C, N, k);  // row j+1
     // x neighbours of row j's terms (every lane takes part)
@@ -242,7 +246,7 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     const float gxE = shd(T1.g.x), qxE = shd(T1.q.y), uwcE = shd(T1.vw.y);
     const float hvW = shu(T1.hh.y), svW = shu(T1.ss.y), hvE = shd(T1.hh.y), svE = shd(T1.ss.y);
     if (out_col && Oc.reg) {
-      const size_t c = base + (size_t)j * W + i;
+      const int c = cb + j * W;
       const float div = ((flxuW - T1.flx.x) + flxv0) - T1.flx.y;
       ms.sn_out[c] = dd_add(make_float2(T1.sn, T1.lo), div * k.rrat);
       const float2 Hf = T1.H;
