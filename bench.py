@@ -17,9 +17,11 @@ ours:
          needed.
   e2e    the same K steps through the reference-facing C-ABI from HOST
          buffers (initialised by writing them, as the reference's driver
-         does): c_invoke_time_step per step (the first call uploads all 25
+         does, and pinned with nl2d_host_register during set-up):
+         c_invoke_time_step per step (the first call uploads all 25
          arrays), then c_read_from_device of sshn_t, un and vn; host wall
-         clock around all of it.
+         clock around all of it.  `e2e.pageable`: the same from pageable
+         arrays.
   roofline  HBM: 76 algorithmic bytes per interior cell-step (read sshn_t,
          un, vn, ht, hu, hv as FP64 + tmask as int32; write sshn_t, un, vn)
          divided by the fused kernel's event time, against the measured HBM
@@ -357,7 +359,11 @@ def run_df_form(lib, n, steps=200, warmup=5):
             "speedup_vs_fp64": ms64 / msdf, "steps": steps + warmup,
             "rel_l2_vs_fp64": rel,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                         "frac": ach / hbm, "alg_bytes_per_cell": ALG_BYTES_PER_CELL}}
+                         "frac": ach / hbm, "alg_bytes_per_cell": ALG_BYTES_PER_CELL,
+                         # what the march moves per cell it writes: the FP64
+                         # state in and out plus five double-float statics
+                         # and a flag byte (89.0 B measured by ncu at 2048^2)
+                         "march_bytes_per_cell": 89}}
     return {"workload": "nemolite2d_fp64_equivalent_%dx%d" % (n, n),
             "dtype": "double-float (FP32 pairs) interior, FP64 boundary cells and storage",
             "bar": "relative L2 <= 1e-10 per field against the FP64 path", **out}
@@ -618,6 +624,9 @@ def run_tra_adv(lib, jpi=512, jpj=512, jpk=75, iters=500, cpu_iters=10):
                          "sample": "%d iterations of the same domain (oracle OpenMP port)" %
                                    cpu_iters},
         "dtype": "f64",
+        # bitwise against the oracle's restatement of tra_adv.F90, which no
+        # reference build checks here (no Fortran compiler)
+        "parity": "unpinned",
     }
 
 

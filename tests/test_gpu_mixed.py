@@ -48,6 +48,44 @@ def test_mixed_error_vs_fp64(gpulib, oracle):
     assert report["vn"][0] <= 1e-4 * report["vn"][2]
 
 
+def test_mixed_error_vs_fp64_4096(gpulib, oracle):
+    """The benchmark's own size (4096^2 interior, config 2's bathymetry):
+    after 500 steps the mixed state's ssh RMS error against the FP64 path
+    stays within 1e-6 m and u, v within 1e-4 of their largest value."""
+    base = bathy_model(4096, 2, oracle)
+    ref = run_form(gpulib, base.copy(), 500, 0)
+    mix = run_form(gpulib, base, 500, 1)
+    report = {}
+    for k, (x0, x1, y0, y1) in (("sshn_t", T.regions(ref)["t"]), ("un", T.regions(ref)["u"]),
+                                ("vn", T.regions(ref)["v"])):
+        a = mix.f[k][y0:y1 + 1, x0:x1 + 1]
+        b = ref.f[k][y0:y1 + 1, x0:x1 + 1]
+        assert np.isfinite(a).all(), k
+        report[k] = (float(np.sqrt(np.mean((a - b) ** 2))), float(np.abs(b).max()))
+    print("mixed vs fp64 at 4096^2 after 500 steps (rms, field max):", report)
+    assert report["sshn_t"][0] <= 1e-6
+    assert report["un"][0] <= 1e-4 * report["un"][1]
+    assert report["vn"][0] <= 1e-4 * report["vn"][1]
+
+
+def test_mixed_nonzero_ssha_uv_vs_fp64(gpulib, oracle):
+    """With ssha_u and ssha_v nonzero (1 m and 0.5 m on 50-500 m depths) the
+    march must read the stored reciprocals 1 / (hu + ssha_u), 1 / (hv +
+    ssha_v) rather than form them from the depths alone (an error of about
+    1 % in u and v): the same bars against the FP64 path hold."""
+    base = bathy_model(192, 5, oracle)
+    base.f["ssha_u"][:] = 1.0
+    base.f["ssha_v"][:] = 0.5
+    ref = run_form(gpulib, base.copy(), 300, 0)
+    mix = run_form(gpulib, base, 300, 1)
+    for k, reg, bar in (("sshn_t", "t", None), ("un", "u", 1e-4), ("vn", "v", 1e-4)):
+        x0, x1, y0, y1 = T.regions(ref)[reg]
+        a = mix.f[k][y0:y1 + 1, x0:x1 + 1]
+        b = ref.f[k][y0:y1 + 1, x0:x1 + 1]
+        rms = float(np.sqrt(np.mean((a - b) ** 2)))
+        assert rms <= (1e-6 if bar is None else bar * float(np.abs(b).max())), (k, rms)
+
+
 def test_mixed_checksums_and_roundtrip(gpulib, oracle):
     """In-graph checksums of the mixed state agree with the FP64 image that
     c_read_from_device returns, and switching back to FP64 continues."""
