@@ -87,7 +87,8 @@ constexpr int kRowPix = 136;
 // every role's loop, and the MMA thread waits for its last commit before the
 // tensor memory is freed.
 constexpr int kStripRows = 8;
-constexpr int kSlots = 4;
+constexpr int kSlots = 4;      // the weight gradient's X ring
+constexpr int kConvSlots = 5;  // the convolution's input ring: 3 rows read, 2 in flight
 constexpr int kPipeThreads = 256;
 constexpr int kEpiWarps = 4;
 constexpr int kStageThreads = 96;  // warps 5-7
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(kPipeThreads)
                    float* __restrict__ y32, int batch, int H, int W, int cin, int cout,
                    int relu, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full_bar[kSlots], empty_bar[kSlots];
+  __shared__ __align__(8) uint64_t full_bar[kConvSlots], empty_bar[kConvSlots];
   __shared__ __align__(8) uint64_t done_bar[2], drained_bar[2], last_bar;
   __shared__ uint32_t taddr_slot;
   __shared__ int abort_flag;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(kPipeThreads)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int q = 0; q < kSlots; q++) {
+    for (int q = 0; q < kConvSlots; q++) {
       mbar_init(&full_bar[q], kStageThreads);
       mbar_init(&empty_bar[q], 1);
     }
@@ -219,43 +220,50 @@ __global__ void __launch_bounds__(kPipeThreads)
   const long long units = (long long)batch * ((H + kStripRows - 1) / kStripRows) * segs;
 
   if (warp >= 5) {
-    // ---- stagers: input rows y0-1 .. y0+rows of every strip, in order ----
+    // ---- stagers: input rows y0-1 .. y0+rows of every strip, in order.
+    // cp.async copies each 16-byte group of 8 channels straight into its
+    // ring slot (zero-filled outside the image), so a stager does not hold
+    // a row in registers: it starts row q, then waits for its own copies of
+    // row q-1, makes them visible to the tensor core's (async) proxy and
+    // marks that slot full.  Two rows are in flight per CTA (the ring's
+    // other three slots hold the rows the MMAs read), where register
+    // staging kept one.
     const int st = tid - 5 * 32;
-    long long q = 0;  // input rows staged so far (ring sequence)
+    long long q = 0;      // input rows started so far (ring sequence)
+    bool pending = false;  // row q-1 started, its slot not yet marked full
     for (long long u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
       const StripWalk sw(u, H, segs);
       for (int a = 0; a < sw.rows + 2 && !*abort_v; a++, q++) {
-        const int slot = (int)(q % kSlots);
+        const int slot = (int)(q % kConvSlots);
         const int yy = sw.y0 - 1 + a;
-        // the whole row's loads in flight before waiting for the slot
-        uint4 v[kStageBatch];
-#pragma unroll
-        for (int b = 0; b < kStageBatch; b++) {
-          const int t = st + b * kStageThreads;
-          v[b] = make_uint4(0, 0, 0, 0);
-          if (t < kc * kRowPix) {
-            const int p = t % kRowPix, ch = t / kRowPix;
-            const int xx = sw.x0 - 1 + p;
-            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-              v[b] = *reinterpret_cast<const uint4*>(
-                  x + (((size_t)sw.img * H + yy) * W + xx) * cin + ch * 8);
-          }
-        }
-        if (q >= kSlots &&
-            !mbar_wait(&empty_bar[slot], (uint32_t)((q / kSlots - 1) & 1), abort_v, err))
+        if (q >= kConvSlots &&
+            !mbar_wait(&empty_bar[slot], (uint32_t)((q / kConvSlots - 1) & 1), abort_v, err))
           break;
-        unsigned char* dst = ring + slot * row_bytes;
-#pragma unroll
-        for (int b = 0; b < kStageBatch; b++) {
-          const int t = st + b * kStageThreads;
-          if (t < kc * kRowPix) {
-            const int p = t % kRowPix, ch = t / kRowPix;
-            *reinterpret_cast<uint4*>(dst + ch * lbo_a + p * 16) = v[b];
-          }
+        const uint32_t dst = smem_u32(ring + slot * row_bytes);
+        for (int t = st; t < kc * kRowPix; t += kStageThreads) {
+          const int p = t % kRowPix, ch = t / kRowPix;
+          const int xx = sw.x0 - 1 + p;
+          const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
+          const __nv_bfloat16* src =
+              in ? x + (((size_t)sw.img * H + yy) * W + xx) * cin + ch * 8 : x;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                           dst + (uint32_t)(ch * lbo_a + p * 16)),
+                       "l"(src), "r"(in ? 16 : 0)
+                       : "memory");
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(&full_bar[slot]);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (pending) {  // row q-1 has landed once at most one group is open
+          asm volatile("cp.async.wait_group 1;" ::: "memory");
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          mbar_arrive(&full_bar[(q - 1) % kConvSlots]);
+        }
+        pending = true;
       }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (pending && !*abort_v) {  // the last row started
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&full_bar[(q - 1) % kConvSlots]);
     }
   } else if (warp == 4) {
     // ---- MMA issuer ----
@@ -270,14 +278,15 @@ __global__ void __launch_bounds__(kPipeThreads)
         const StripWalk sw(u, H, segs);
         const long long qb = q;  // sequence number of this strip's first input row
         // its first two input rows
-        bool ok = mbar_wait(&full_bar[qb % kSlots], (uint32_t)((qb / kSlots) & 1), abort_v,
-                            err) &&
-                  mbar_wait(&full_bar[(qb + 1) % kSlots], (uint32_t)(((qb + 1) / kSlots) & 1),
-                            abort_v, err);
+        bool ok = mbar_wait(&full_bar[qb % kConvSlots], (uint32_t)((qb / kConvSlots) & 1),
+                            abort_v, err) &&
+                  mbar_wait(&full_bar[(qb + 1) % kConvSlots],
+                            (uint32_t)(((qb + 1) / kConvSlots) & 1), abort_v, err);
         for (int o = 0; o < sw.rows && ok; o++, p++) {
           const long long qn = qb + o + 2;  // the new input row this output needs
           const int buf = (int)(p & 1);
-          ok = mbar_wait(&full_bar[qn % kSlots], (uint32_t)((qn / kSlots) & 1), abort_v, err);
+          ok = mbar_wait(&full_bar[qn % kConvSlots], (uint32_t)((qn / kConvSlots) & 1), abort_v,
+                         err);
           if (ok && p >= 2)
             ok = mbar_wait(&drained_bar[buf], (uint32_t)((p / 2 - 1) & 1), abort_v, err);
           if (!ok) break;
@@ -291,7 +300,7 @@ __global__ void __launch_bounds__(kPipeThreads)
           uint64_t arow[3];
 #pragma unroll
           for (int dy = 0; dy < 3; dy++)
-            arow[dy] = smem_desc(smem_u32(ring + (int)((qb + o + dy) % kSlots) * row_bytes),
+            arow[dy] = smem_desc(smem_u32(ring + (int)((qb + o + dy) % kConvSlots) * row_bytes),
                                  lbo_a, 128);
           uint64_t btap = b_desc0;
           uint32_t acc = 0u;
@@ -309,12 +318,12 @@ __global__ void __launch_bounds__(kPipeThreads)
           issued = true;
           tc_commit(&done_bar[buf]);
           // input row o is not read by later outputs of this strip
-          tc_commit(&empty_bar[(qb + o) % kSlots]);
+          tc_commit(&empty_bar[(qb + o) % kConvSlots]);
         }
         q = qb + sw.rows + 2;
         if (ok) {  // the strip's last two input rows are free too
-          tc_commit(&empty_bar[(q - 2) % kSlots]);
-          tc_commit(&empty_bar[(q - 1) % kSlots]);
+          tc_commit(&empty_bar[(q - 2) % kConvSlots]);
+          tc_commit(&empty_bar[(q - 1) % kConvSlots]);
         } else {
           break;
         }
@@ -891,7 +900,7 @@ int nl2d_emu_conv3x3(const void* x, const void* w, const float* bias, void* y, f
       batch < 1 || !x || !w || !err || (!y && !y32))
     return NL2D_ERR_ARGS;
   const size_t wbytes = ((9 * (size_t)cout * cin * 2) + 1023) & ~(size_t)1023;
-  const size_t smem = wbytes + kSlots * (size_t)(cin / 8) * kRowPix * 16;
+  const size_t smem = wbytes + kConvSlots * (size_t)(cin / 8) * kRowPix * 16;
   constexpr int kMaxSmem = 200 * 1024;
   static bool attr = false;
   if (!attr) {
