@@ -62,7 +62,14 @@ extern "C" {
  * step leaves (ua == un, va == vn, ssha_t == sshn_t on the copy region,
  * sshn_u / sshn_v as next_sshu / next_sshv make them of sshn_t, as at the
  * reference's rest start), the first step already takes the fused path;
- * otherwise it is reference-structured.
+ * otherwise it is reference-structured.  With the arrays pinned
+ * (nl2d_host_register) the first call uploads only the arrays a fused step
+ * reads and starts that step; the other arrays (ssha_t, the metrics, the
+ * latitudes) and the registration checks follow on a second stream.  If
+ * the checks refuse the fused path or find a state that is not what a step
+ * leaves, the steps taken meanwhile are undone and taken again by the
+ * reference's rules, so the results are the same bits either way.  Every
+ * other entry point waits for the checks first.
  */
 void c_invoke_time_step(
     double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
@@ -390,6 +397,12 @@ int nl2d_transfer_bytes(long long out[2]);
  * a null pointer or zero size: NL2D_ERR_ARGS; the CUDA call's failure
  * (e.g. the range is already pinned): NL2D_ERR_CUDA. */
 int nl2d_host_register(void *p, size_t bytes);
+
+/* Verdicts on speculative registrations since the library was loaded
+ * (no counterpart in the reference): out[0] kept (the fused steps taken
+ * before the checks answered stood), out[1] redone (they were undone and
+ * taken again by the reference's rules). */
+int nl2d_speculation_counts(int out[2]);
 int nl2d_host_unregister(void *p);
 
 /* Issue rates of this GPU's arithmetic pipes in Gop/s (no counterpart in

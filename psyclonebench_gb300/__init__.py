@@ -61,6 +61,7 @@ EXPORTS = {
     "nl2d_ens_tile": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "nl2d_host_register": (ctypes.c_int, [_VP, ctypes.c_size_t]),
     "nl2d_host_unregister": (ctypes.c_int, [_VP]),
+    "nl2d_speculation_counts": (ctypes.c_int, [_IP]),
     "nl2d_ens_run": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     "nl2d_ens_read": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP]),
     "nl2d_ens_info": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),

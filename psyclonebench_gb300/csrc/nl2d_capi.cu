@@ -68,6 +68,20 @@ struct State {
   unsigned scan_flags = 0;     // last registration scan (kScan* bits)
   double grid_refs[11] = {};   // the metric arrays' and latitudes' reference values
   long long h2d_bytes = 0, d2h_bytes = 0;  // copied since registration
+  // Speculative registration (c_invoke_time_step over pinned arrays): the
+  // arrays a fused step reads go first and steps start on `stream`; the
+  // other arrays and the registration scan follow on `side`, and a later
+  // call keeps the steps or takes them again by the scan's verdict.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ess_done = nullptr, spec_ready = nullptr;
+  bool spec_pending = false;
+  double* spec_backup[3] = {};  // sshn_t, un, vn as uploaded
+  struct SpecOut {              // pinned host copy of the scan's results
+    unsigned flags;
+    double refs[11];
+  }* spec_out = nullptr;
+  std::vector<int> spec_steps;  // isteps taken before the verdict
+  int spec_kept = 0, spec_redone = 0;  // verdicts since the library loaded
 };
 
 State g_state;
@@ -103,9 +117,21 @@ double** grid_slot(Fields& f, int k) {  // k = 1..11 (0 is tmask)
 
 void invalidate_graph();
 
+void drop_spec() {
+  State& s = g_state;
+  if (s.spec_pending && s.side) cudaStreamSynchronize(s.side);
+  s.spec_pending = false;
+  s.spec_steps.clear();
+  for (double*& p : s.spec_backup) {
+    cudaFree(p);
+    p = nullptr;
+  }
+}
+
 void free_device() {
   State& s = g_state;
   invalidate_graph();
+  drop_spec();
   if (s.registered) {
     for (int k = 0; k < kNumFields; k++) cudaFree(*field_slot(s.dev, k));
     cudaFree(s.dev.tmask);
@@ -375,10 +401,14 @@ bool update_sines(double d2r) {
   return true;
 }
 
-// The registration scan (k_register_scan) over the uploaded arrays, then
-// the sines and the fused path's preconditions.  The state bits (14-16)
-// matter only right after an upload.  Returns false on a CUDA error.
-bool scan_grid(double d2r) {
+// Launches the registration scan (k_register_scan) over the uploaded
+// arrays on stream st; its flags word and the 11 reference values (the
+// region's first point of each metric array, gphi's first elements) land
+// in *flags_out / refs_out once st reaches them (host memory: pinned for a
+// scan that the caller does not wait for).
+// state: the sshn_t, un, vn to check (null: the current buffers).
+bool launch_scan(cudaStream_t st, unsigned* flags_out, double* refs_out,
+                 double* const* state = nullptr) {
   State& s = g_state;
   const Registration& r = s.reg;
   if (!s.scan && !CK(cudaMalloc(&s.scan, 4 * sizeof(double)))) return false;
@@ -390,30 +420,45 @@ bool scan_grid(double d2r) {
   in.gphi[0] = g[9];
   in.gphi[1] = g[10];
   in.m = s.dev.tmask;
-  in.sn = cur_sshn(), in.un = cur_un(), in.vn = cur_vn();
+  in.sn = state ? state[0] : cur_sshn();
+  in.un = state ? state[1] : cur_un();
+  in.vn = state ? state[2] : cur_vn();
   in.ua = s.dev.ua, in.va = s.dev.va, in.sa = s.dev.ssha_t;
   in.snu = s.dev.sshn_u, in.snv = s.dev.sshn_v;
   in.xs = r.xs, in.xe = r.xe, in.ys = r.ys, in.ye = r.ye, in.W = r.width, in.H = r.height;
   unsigned* d_flags = reinterpret_cast<unsigned*>(s.scan);
-  if (!CK(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s.stream))) return false;
-  k_register_scan<<<152 * 8, 256, 0, s.stream>>>(in, d_flags);
+  if (!CK(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st))) return false;
+  k_register_scan<<<152 * 8, 256, 0, st>>>(in, d_flags);
   if (!CK(cudaGetLastError())) return false;
-  // the reference values: the region's first point of each metric array,
-  // the first element of each latitude array
   const size_t o = (size_t)(r.ys - 1) * r.width + (r.xs - 1);
-  unsigned flags = 0;
   for (int q = 0; q < 11; q++)
-    if (!CK(cudaMemcpyAsync(&s.grid_refs[q], g[q] + (q < 9 ? o : 0), 8, cudaMemcpyDeviceToHost,
-                            s.stream)))
+    if (!CK(cudaMemcpyAsync(&refs_out[q], g[q] + (q < 9 ? o : 0), 8, cudaMemcpyDeviceToHost,
+                            st)))
       return false;
-  if (!CK(cudaMemcpyAsync(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s.stream)) ||
-      !CK(cudaStreamSynchronize(s.stream)))
-    return false;
+  return CK(cudaMemcpyAsync(flags_out, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+}
+
+// The scan's results into the state: the uniform metric values, the sines
+// and the fused path's preconditions.
+bool apply_scan(unsigned flags, const double* refs, double d2r) {
+  State& s = g_state;
   s.scan_flags = flags;
+  for (int q = 0; q < 11; q++) s.grid_refs[q] = refs[q];
   double* um[9] = {&s.um.area_t, &s.um.area_u, &s.um.area_v, &s.um.dx_u, &s.um.dx_v,
                    &s.um.dx_t,   &s.um.dy_u,   &s.um.dy_v,   &s.um.dy_t};
   for (int q = 0; q < 9; q++) *um[q] = s.grid_refs[q];
   return update_sines(d2r);
+}
+
+// The scan, waited for, then applied.  The state bits (14-16) matter only
+// right after an upload.  Returns false on a CUDA error.
+bool scan_grid(double d2r) {
+  State& s = g_state;
+  unsigned flags = 0;
+  double refs[11];
+  if (!launch_scan(s.stream, &flags, refs) || !CK(cudaStreamSynchronize(s.stream)))
+    return false;
+  return apply_scan(flags, refs, d2r);
 }
 
 bool same_registration(void* const* ptrs, int xs, int xe, int ys, int ye, int width,
@@ -429,8 +474,40 @@ bool same_registration(void* const* ptrs, int xs, int xe, int ys, int ye, int wi
   return true;
 }
 
+bool host_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // not a CUDA-known pointer: pageable
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// Argument positions (c_invoke_time_step's order) of the arrays a fused
+// step reads: every field but ssha_t, and the T mask.  The others (ssha_t,
+// the metric and latitude arrays) only the registration scan and the
+// reference-structured path read.
+constexpr int kStepArrays[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, kNumFields};
+constexpr int kLateArrays[] = {0,  kNumFields + 1, kNumFields + 2, kNumFields + 3,
+                               kNumFields + 4,  kNumFields + 5,  kNumFields + 6,
+                               kNumFields + 7,  kNumFields + 8,  kNumFields + 9,
+                               kNumFields + 10, kNumFields + 11};
+
+bool upload(void* const* ptrs, int k, cudaStream_t st) {
+  State& s = g_state;
+  const size_t n = (size_t)s.reg.width * s.reg.height, esz = k == kNumFields ? 4 : 8;
+  void* dst = k < kNumFields ? (void*)*field_slot(s.dev, k)
+                             : (k == kNumFields ? (void*)s.dev.tmask
+                                                : (void*)*grid_slot(s.dev, k - kNumFields));
+  if (!CK(cudaMemcpyAsync(dst, ptrs[k], n * esz, cudaMemcpyHostToDevice, st))) return false;
+  s.h2d_bytes += (long long)(n * esz);
+  return true;
+}
+
+// speculate: the caller is c_invoke_time_step, which can take fused steps
+// before the scan has answered (see State::spec_pending).
 bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, int height,
-                 const Scalars& sc) {
+                 const Scalars& sc, bool speculate = false) {
   State& s = g_state;
   if (xs < 1 || ys < 1 || xe < xs || ye < ys || xe > width - 2 || ye > height - 2) {
     set_error(NL2D_ERR_ARGS,
@@ -466,30 +543,138 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   if (!s.partials &&
       !CK(cudaMalloc(&s.partials, sizeof(double) * checksum_partials_needed())))
     return false;
-  // every array of the argument list: pageable copies, each returning once
-  // its source is staged
-  for (int k = 0; k < kNumFields + kNumGrid; k++) {
-    const size_t esz = k == kNumFields ? 4 : 8;
-    void* dst = k < kNumFields ? (void*)*field_slot(s.dev, k)
-                               : (k == kNumFields ? (void*)s.dev.tmask
-                                                  : (void*)*grid_slot(s.dev, k - kNumFields));
-    if (!CK(cudaMemcpyAsync(dst, ptrs[k], n * esz, cudaMemcpyHostToDevice, s.stream)))
-      return false;
-    s.h2d_bytes += (long long)(n * esz);
-  }
+  // The arrays a fused step reads first (a pageable copy returns once its
+  // source is staged, a pinned one at once).
+  for (int k : kStepArrays)
+    if (!upload(ptrs, k, s.stream)) return false;
   launch_depth_reciprocals(s.dev, dims(), s.stream);
   if (!CK(cudaGetLastError())) return false;
   s.sc = sc;
   s.cur = 0;
-  if (!scan_grid(sc.d2r)) return false;
-  // A state that is already what a step leaves needs no reference-
-  // structured first step.
-  s.consistent = s.fused_ok && (s.scan_flags & (kScanSshaT | kScanCopies | kScanNextSsh)) == 0;
   s.shadows_synced = false;
   s.materialized = true;
   s.last_path = 0;
+  // Speculation pays only when the other arrays' copies do not hold the
+  // host: pinned sources, the FP64 fused path.
+  bool spec = speculate && s.precision == 0 && s.mode == NL2D_MODE_AUTO;
+  for (int k : kLateArrays) spec = spec && host_pinned(ptrs[k]);
+  if (!spec) {
+    for (int k : kLateArrays)
+      if (!upload(ptrs, k, s.stream)) return false;
+    if (!scan_grid(sc.d2r)) return false;
+    // A state that is already what a step leaves needs no reference-
+    // structured first step.
+    s.consistent =
+        s.fused_ok && (s.scan_flags & (kScanSshaT | kScanCopies | kScanNextSsh)) == 0;
+    return true;
+  }
+  if (!s.side && !CK(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking))) return false;
+  if (!s.ess_done && (!CK(cudaEventCreateWithFlags(&s.ess_done, cudaEventDisableTiming)) ||
+                      !CK(cudaEventCreateWithFlags(&s.spec_ready, cudaEventDisableTiming))))
+    return false;
+  if (!s.spec_out && !CK(cudaMallocHost(&s.spec_out, sizeof(State::SpecOut)))) return false;
+  double* prim[3] = {s.dev.sshn_t, s.dev.un, s.dev.vn};
+  for (int q = 0; q < 3; q++)
+    if (!CK(cudaMalloc(&s.spec_backup[q], n * 8)) ||
+        !CK(cudaMemcpyAsync(s.spec_backup[q], prim[q], n * 8, cudaMemcpyDeviceToDevice,
+                            s.stream)))
+      return false;
+  // the other arrays and the scan behind the first steps, on the side
+  // stream (nothing on the library's stream reads those arrays before the
+  // verdict: resolve_spec makes it wait for them)
+  if (!CK(cudaEventRecord(s.ess_done, s.stream)) ||
+      !CK(cudaStreamWaitEvent(s.side, s.ess_done, 0)))
+    return false;
+  for (int k : kLateArrays)
+    if (!upload(ptrs, k, s.side)) return false;
+  // the scan checks the uploaded state in its backup: the steps taken
+  // meanwhile overwrite the primary buffers
+  if (!launch_scan(s.side, &s.spec_out->flags, s.spec_out->refs, s.spec_backup) ||
+      !CK(cudaEventRecord(s.spec_ready, s.side)))
+    return false;
+  // Until then the fused path runs on the values the scan will compare
+  // against: the region's first point of each metric array and the first
+  // latitudes, read from the caller's arrays (the device copies are the same
+  // bytes), and assumes the state is what a step leaves.
+  const size_t o = (size_t)(ys - 1) * width + (xs - 1);
+  double refs[11];
+  for (int q = 0; q < 11; q++)
+    refs[q] = static_cast<const double*>(ptrs[kNumFields + 1 + q])[q < 9 ? o : 0];
+  for (int q = 0; q < 11; q++) s.grid_refs[q] = refs[q];
+  double* um[9] = {&s.um.area_t, &s.um.area_u, &s.um.area_v, &s.um.dx_u, &s.um.dx_v,
+                   &s.um.dx_t,   &s.um.dy_u,   &s.um.dy_v,   &s.um.dy_t};
+  for (int q = 0; q < 9; q++) *um[q] = refs[q];
+  s.um.sin_u = std::sin(refs[9] * sc.d2r);
+  s.um.sin_v = std::sin(refs[10] * sc.d2r);
+  s.sin_d2r = sc.d2r;
+  s.scan_flags = 0;
+  s.fused_ok = true;
+  s.chain_u = s.chain_v = false;
+  s.consistent = true;
+  s.spec_pending = true;
+  s.spec_steps.clear();
   return true;
 }
+
+bool one_step(int istep);
+
+// Ends a speculative registration.  With wait false it returns at once
+// unless the scan has answered.  The verdict either keeps the steps taken
+// (the fused path's preconditions hold, the state was what a step leaves,
+// the values assumed are the device's) or restores the uploaded sshn_t,
+// un, vn and takes the same steps again by the path rules the scan decides,
+// which gives the bits an unspeculative run gives.  Returns false on a CUDA
+// error.
+bool resolve_spec(bool wait) {
+  State& s = g_state;
+  if (!s.spec_pending) return true;
+  if (!wait) {
+    const cudaError_t q = cudaEventQuery(s.spec_ready);
+    if (q == cudaErrorNotReady) return true;
+    if (!CK(q)) return false;
+  } else if (!CK(cudaEventSynchronize(s.spec_ready))) {
+    return false;
+  }
+  s.spec_pending = false;
+  std::vector<int> steps;
+  steps.swap(s.spec_steps);
+  double assumed[11];
+  for (int q = 0; q < 11; q++) assumed[q] = s.grid_refs[q];
+  if (!CK(cudaStreamWaitEvent(s.stream, s.spec_ready, 0)) ||
+      !apply_scan(s.spec_out->flags, s.spec_out->refs, s.sc.d2r))
+    return false;
+  const bool same = memcmp(assumed, s.grid_refs, sizeof assumed) == 0;
+  const bool consistent =
+      s.fused_ok && (s.scan_flags & (kScanSshaT | kScanCopies | kScanNextSsh)) == 0;
+  bool ok = true;
+  if (s.fused_ok && consistent && same) {
+    s.spec_kept++;
+  } else {
+    s.spec_redone++;
+    double* prim[3] = {s.dev.sshn_t, s.dev.un, s.dev.vn};
+    const size_t n = (size_t)s.reg.width * s.reg.height;
+    for (int q = 0; q < 3 && ok; q++)
+      ok = CK(cudaMemcpyAsync(prim[q], s.spec_backup[q], n * 8, cudaMemcpyDeviceToDevice,
+                              s.stream));
+    s.cur = 0;
+    s.shadows_synced = false;
+    s.materialized = true;
+    s.consistent = consistent;
+    s.last_path = 0;
+    invalidate_graph();
+    for (size_t t = 0; t < steps.size() && ok; t++) ok = one_step(steps[t]);
+    // the restoring copies read the backups: let them finish first
+    ok = ok && CK(cudaStreamSynchronize(s.stream));
+  }
+  // (without a rollback nothing reads them: their copies finished before
+  // the side stream started)
+  for (double*& p : s.spec_backup) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  return ok;
+}
+
 
 // Current device buffers of sshn_t / un / vn.
 double* cur_sshn() { return g_state.cur ? g_state.shadow[0] : g_state.dev.sshn_t; }
@@ -880,13 +1065,18 @@ void c_invoke_time_step(double* ssha_t, double* sshn_t, double* sshn_u, double* 
   if (!same_registration(ptrs, internal_xstart, internal_xstop, internal_ystart,
                          internal_ystop, width, height)) {
     if (!do_register(ptrs, internal_xstart, internal_xstop, internal_ystart, internal_ystop,
-                     width, height, sc))
+                     width, height, sc, true))
       return;
   } else {
+    // steps taken before the scan's verdict are replayed with the
+    // registration's scalars: new ones wait for the verdict
+    if (s.spec_pending && memcmp(&sc, &s.sc, sizeof sc) != 0 && !resolve_spec(true)) return;
     s.sc = sc;
     if (!(d2r == s.sin_d2r) && !update_sines(d2r)) return;
   }
-  one_step(istep);
+  if (s.spec_pending && !resolve_spec(false)) return;
+  if (!one_step(istep)) return;
+  if (s.spec_pending) s.spec_steps.push_back(istep);
 }
 
 int nl2d_register(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v, double* hu,
@@ -909,6 +1099,7 @@ int nl2d_register(double* ssha_t, double* sshn_t, double* sshn_u, double* sshn_v
 void c_read_from_device(void* from, void* to, int startx, int starty, int nx, int ny,
                         bool blocking) {
   nl2d::NvtxRange nvtx_range("c_read_from_device");
+  if (!resolve_spec(true)) return;
   State& s = g_state;
   const int k = find_field(from);
   if (k < 0) {
@@ -946,6 +1137,7 @@ void c_read_from_device(void* from, void* to, int startx, int starty, int nx, in
 void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int ny,
                        bool blocking) {
   nl2d::NvtxRange nvtx_range("c_write_to_device");
+  if (!resolve_spec(true)) return;
   State& s = g_state;
   const int k = find_field(to);
   if (k < 0) {
@@ -1002,6 +1194,7 @@ int nl2d_checkpoint_write(const char* path, int istep) {
   nl2d::NvtxRange nvtx_range("nl2d_checkpoint_write");
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_checkpoint_write: no problem registered");
     return scope.rc();
@@ -1040,6 +1233,7 @@ int nl2d_checkpoint_read(const char* path, int* istep) {
   nl2d::NvtxRange nvtx_range("nl2d_checkpoint_read");
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_checkpoint_read: no problem registered");
     return scope.rc();
@@ -1122,10 +1316,18 @@ void nl2d_finalize(void) {
   s.sums_cap = s.tide_cap = 0;
   if (s.stream) cudaStreamDestroy(s.stream);
   s.stream = nullptr;
+  if (s.side) cudaStreamDestroy(s.side);
+  s.side = nullptr;
+  if (s.ess_done) cudaEventDestroy(s.ess_done);
+  if (s.spec_ready) cudaEventDestroy(s.spec_ready);
+  s.ess_done = s.spec_ready = nullptr;
+  if (s.spec_out) cudaFreeHost(s.spec_out);
+  s.spec_out = nullptr;
   noalloc_forget();
 }
 
 int nl2d_set_mode(int mode) {
+  resolve_spec(true);  // steps taken before the verdict keep their path rules
   State& s = g_state;
   const int old = s.mode;
   if (mode != NL2D_MODE_AUTO && mode != NL2D_MODE_REFERENCE) {
@@ -1139,6 +1341,7 @@ int nl2d_set_mode(int mode) {
 int nl2d_last_path(void) { return g_state.last_path; }
 
 int nl2d_set_precision(int precision) {
+  resolve_spec(true);  // steps taken before the verdict keep their path rules
   State& s = g_state;
   const int old = s.precision;
   if (precision < 0 || precision > 2) {
@@ -1157,6 +1360,7 @@ int nl2d_run_steps(int istep0, int nsteps, int checksum_every, double* checksums
   nl2d::NvtxRange nvtx_range("nl2d_run_steps");
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_run_steps: no problem registered");
     return scope.rc();
@@ -1199,6 +1403,7 @@ int nl2d_timed_run(int istep0, int nsteps, double* ms_out) {
   nl2d::NvtxRange nvtx_range("nl2d_timed_run");
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   if (ms_out) *ms_out = 0.0;
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_timed_run: no problem registered");
@@ -1237,6 +1442,7 @@ int nl2d_checksums(double out[3]) {
   nl2d::NvtxRange nvtx_range("nl2d_checksums");
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   auto take_status = [&]() { return scope.rc(); };
   if (!s.registered) {
     set_error(NL2D_ERR_STATE, "nl2d_checksums: no problem registered");
@@ -1259,6 +1465,7 @@ int nl2d_checksums(double out[3]) {
 int nl2d_field_checksum(const void* field, int x0, int x1, int y0, int y1, double* out) {
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   auto take_status = [&]() { return scope.rc(); };
   const int k = find_field(field);
   if (k < 0 || k >= kNumFields) {
@@ -1283,6 +1490,7 @@ int nl2d_field_checksum(const void* field, int x0, int x1, int y0, int y1, doubl
 int nl2d_sync(void) {
   State& s = g_state;
   CallScope scope;
+  if (!resolve_spec(true)) return scope.rc();
   if (s.stream) CK(cudaStreamSynchronize(s.stream));
   return scope.rc();
 }
@@ -1292,6 +1500,13 @@ int nl2d_transfer_bytes(long long out[2]) {
   if (!out) return NL2D_ERR_ARGS;
   out[0] = s.h2d_bytes;
   out[1] = s.d2h_bytes;
+  return NL2D_OK;
+}
+
+int nl2d_speculation_counts(int out[2]) {
+  if (!out) return NL2D_ERR_ARGS;
+  out[0] = g_state.spec_kept;
+  out[1] = g_state.spec_redone;
   return NL2D_OK;
 }
 
@@ -1316,6 +1531,7 @@ int nl2d_host_unregister(void* p) {
 }
 
 void* nl2d_device_ptr(const void* field) {
+  if (!resolve_spec(true)) return nullptr;
   const int k = find_field(field);
   if (k < 0) return nullptr;
   if (!materialize()) return nullptr;

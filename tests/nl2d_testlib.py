@@ -139,3 +139,26 @@ def ensemble_oracle_run(dom, nsteps, rdt=None, oracle=None, every=0, cbfr=None, 
         if every and (k + 1) % every == 0:
             sums.append(model_checksums(m, lib))
     return m, sums
+
+
+def pin_model(lib, m, page=4096):
+    """Moves every array of m into page-aligned buffers of its own and pins
+    them (nl2d_host_register); returns what unpin_model releases."""
+    import psyclonebench_gb300 as P
+    held = []
+    for d in (m.f, m.grid):
+        for k, a in list(d.items()):
+            nb = -(-a.nbytes // page) * page
+            raw = np.empty(nb + page, np.uint8)
+            off = (-raw.ctypes.data) % page
+            b = raw[off:off + a.nbytes].view(a.dtype).reshape(a.shape)
+            b[...] = a
+            d[k] = b
+            P.check(lib.nl2d_host_register(b.ctypes.data, b.nbytes), "host register")
+            held.append(b)
+    return held
+
+
+def unpin_model(lib, held):
+    for b in held:
+        lib.nl2d_host_unregister(b.ctypes.data)
