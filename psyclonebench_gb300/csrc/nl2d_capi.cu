@@ -68,6 +68,7 @@ struct State {
   unsigned scan_flags = 0;     // last registration scan (kScan* bits)
   double grid_refs[11] = {};   // the metric arrays' and latitudes' reference values
   long long h2d_bytes = 0, d2h_bytes = 0;  // copied since registration
+  void* slab = nullptr;        // the allocation the registration's arrays live in
   // Speculative registration (c_invoke_time_step over pinned arrays): the
   // arrays a fused step reads go first and steps start on `stream`; the
   // other arrays and the registration scan follow on `side`, and a later
@@ -133,14 +134,8 @@ void free_device() {
   invalidate_graph();
   drop_spec();
   if (s.registered) {
-    for (int k = 0; k < kNumFields; k++) cudaFree(*field_slot(s.dev, k));
-    cudaFree(s.dev.tmask);
-    for (int k = 1; k < kNumGrid; k++) cudaFree(*grid_slot(s.dev, k));
-    cudaFree(s.dev.sin_u);
-    cudaFree(s.dev.sin_v);
-    cudaFree(s.dev.r_hu);
-    cudaFree(s.dev.r_hv);
-    for (double* p : s.shadow) cudaFree(p);
+    cudaFree(s.slab);  // every array of the registration
+    s.slab = nullptr;
     for (int b = 0; b < 2; b++) {
       cudaFree(s.msn[b]);
       cudaFree(s.mun[b]);
@@ -530,16 +525,27 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   const size_t n = (size_t)width * height;
   s.registered = true;  // so free_device releases partial allocations
   s.h2d_bytes = s.d2h_bytes = 0;
-  for (int k = 0; k < kNumFields; k++)
-    if (!CK(cudaMalloc(field_slot(s.dev, k), n * 8))) return false;
-  if (!CK(cudaMalloc(&s.dev.tmask, n * 4))) return false;
-  for (int k = 1; k < kNumGrid; k++)
-    if (!CK(cudaMalloc(grid_slot(s.dev, k), n * 8))) return false;
-  if (!CK(cudaMalloc(&s.dev.sin_u, n * 8)) || !CK(cudaMalloc(&s.dev.sin_v, n * 8)))
+  // One allocation carved into the registration's 32 arrays (256-byte
+  // aligned): 34 separate cudaMalloc calls took 1.7-2.9 ms on the GB300
+  // box, one of the same total 0.18 ms, and the first call waits for them
+  // before its first copy.
+  const size_t a8 = (n * 8 + 255) & ~(size_t)255, a4 = (n * 4 + 255) & ~(size_t)255;
+  if (!CK(cudaMalloc(&s.slab, (size_t)(kNumFields + kNumGrid - 1 + 4 + 3) * a8 + a4)))
     return false;
-  if (!CK(cudaMalloc(&s.dev.r_hu, n * 8)) || !CK(cudaMalloc(&s.dev.r_hv, n * 8))) return false;
-  for (double*& p : s.shadow)
-    if (!CK(cudaMalloc(&p, n * 8))) return false;
+  char* cut = static_cast<char*>(s.slab);
+  auto take = [&cut](size_t bytes) {
+    char* p = cut;
+    cut += bytes;
+    return p;
+  };
+  for (int k = 0; k < kNumFields; k++) *field_slot(s.dev, k) = (double*)take(a8);
+  s.dev.tmask = (int*)take(a4);
+  for (int k = 1; k < kNumGrid; k++) *grid_slot(s.dev, k) = (double*)take(a8);
+  s.dev.sin_u = (double*)take(a8);
+  s.dev.sin_v = (double*)take(a8);
+  s.dev.r_hu = (double*)take(a8);
+  s.dev.r_hv = (double*)take(a8);
+  for (double*& p : s.shadow) p = (double*)take(a8);
   if (!s.partials &&
       !CK(cudaMalloc(&s.partials, sizeof(double) * checksum_partials_needed())))
     return false;
