@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the mixed-precision, ensemble and emulator measurements")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator (config 4)")
-    ap.add_argument("--forms", default="mixed,active,df,sweep,ensemble,tra_adv,emulator",
+    ap.add_argument("--forms", default="cfg0,mixed,active,df,sweep,ensemble,tra_adv,emulator",
                     help="comma-separated forms to measure after the headline number")
     ap.add_argument("--form-steps", type=int, default=1000,
                     help="timed steps of the mixed-precision form and its FP64 twin")
@@ -367,6 +367,59 @@ def run_df_form(lib, n, steps=200, warmup=5):
     return {"workload": "nemolite2d_fp64_equivalent_%dx%d" % (n, n),
             "dtype": "double-float (FP32 pairs) interior, FP64 boundary cells and storage",
             "bar": "relative L2 <= 1e-10 per field against the FP64 path", **out}
+
+
+def run_cfg0(lib, nsteps=2000, every=100):
+    """Config 0, the parity namelist (128^2 interior, rest start, 2000
+    steps): on the GPU as one captured graph of fused steps (CUDA events,
+    nl2d_timed_run), then again through nl2d_run_steps with the ssh / u / v
+    checksums every 100 steps in the graph; on one host core through the
+    serial step (the reference's own serial build where oracle/_ref holds
+    it, else the oracle's restatement) from the same start, its checksums at
+    the same steps beside the GPU's."""
+    import psyclonebench_gb300 as P
+    from psyclonebench_gb300.model import dptr, register
+    from oracle import cpu as O
+    n = 128
+    out = {"workload": "nemolite2d_cfg0_128x128_%d_steps" % nsteps, "unit": "Mcell-steps/s"}
+    m = make_problem(n)
+    register(lib, m)
+    ms = ctypes.c_double(0.0)
+    P.check(lib.nl2d_timed_run(1, nsteps, ctypes.byref(ms)), "cfg0 warm-up")
+    lib.nl2d_finalize()
+    m = make_problem(n)
+    register(lib, m)
+    P.check(lib.nl2d_timed_run(1, nsteps, ctypes.byref(ms)), "cfg0 run")
+    out["gpu"] = {"value": n * n * nsteps / (ms.value * 1e-3) / 1e6, "ms": ms.value}
+    lib.nl2d_finalize()
+    m = make_problem(n)
+    register(lib, m)
+    sums = np.zeros(3 * (nsteps // every))
+    P.check(lib.nl2d_run_steps(1, nsteps, every, dptr(sums)), "cfg0 checksums")
+    lib.nl2d_finalize()
+    ref = O.load_ref("serial")
+    fn, kind = ((ref.c_invoke_time_step, "reference") if ref is not None else
+                (O.load_oracle().oracle_invoke_time_step, "port"))
+    o = O.load_oracle()
+    c = make_problem_oracle(n)
+    cpu_sums, t0 = [], time.perf_counter()
+    for k in range(nsteps):
+        O.call_step(fn, c.step_args(1 + k))
+        if (k + 1) % every == 0:
+            r = c.regions()
+            cpu_sums.append([o.oracle_field_checksum(dptr(c.f[f]), c.width, *r[kk])
+                             for f, kk in (("sshn_t", "t"), ("un", "u"), ("vn", "v"))])
+    secs = time.perf_counter() - t0
+    out["cpu_serial"] = {"value": n * n * nsteps / secs / 1e6, "seconds": secs, "cores": 1,
+                         "kind": kind,
+                         "sample": "the full %d steps, checksums every %d included" %
+                                   (nsteps, every)}
+    got = sums.reshape(-1, 3)
+    want = np.array(cpu_sums)
+    out["checksums_max_rel_diff"] = float(np.max(np.abs(got - want) /
+                                                 np.maximum(np.abs(want), 1e-300)))
+    out["speedup_gpu_vs_cpu_serial"] = out["gpu"]["value"] / out["cpu_serial"]["value"]
+    return out
 
 
 def run_sweep(lib, sizes=(256, 512, 1024, 2048, 4096, 8192)):
@@ -814,6 +867,8 @@ def run_ours(args, rank, world, local):
         want.discard("emulator")
     if rank == 0 and not args.no_forms:
         forms = {}
+        if "cfg0" in want:
+            forms["cfg0"] = run_cfg0(lib)
         if "mixed" in want:
             forms.update(run_forms(lib, n, steps=args.form_steps))
         if "active" in want:
