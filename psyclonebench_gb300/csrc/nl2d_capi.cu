@@ -73,8 +73,9 @@ struct State {
   // arrays a fused step reads go first and steps start on `stream`; the
   // other arrays and the registration scan follow on `side`, and a later
   // call keeps the steps or takes them again by the scan's verdict.
-  cudaStream_t side = nullptr;
+  cudaStream_t side = nullptr;  // also the FP64-equivalent form's exact tiles
   cudaEvent_t ess_done = nullptr, spec_ready = nullptr;
+  cudaEvent_t df_fork = nullptr, df_join = nullptr;
   bool spec_pending = false;
   double* spec_backup[3] = {};  // sshn_t, un, vn as uploaded
   struct SpecOut {              // pinned host copy of the scan's results
@@ -469,6 +470,16 @@ bool same_registration(void* const* ptrs, int xs, int xe, int ys, int ye, int wi
   return true;
 }
 
+// The second stream, at the device's highest priority: work queued there
+// is scheduled ahead of the library stream's.
+bool ensure_side() {
+  State& s = g_state;
+  if (s.side) return true;
+  int least = 0, greatest = 0;
+  if (!CK(cudaDeviceGetStreamPriorityRange(&least, &greatest))) return false;
+  return CK(cudaStreamCreateWithPriority(&s.side, cudaStreamNonBlocking, greatest));
+}
+
 bool host_pinned(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -574,7 +585,7 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
         s.fused_ok && (s.scan_flags & (kScanSshaT | kScanCopies | kScanNextSsh)) == 0;
     return true;
   }
-  if (!s.side && !CK(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking))) return false;
+  if (!ensure_side()) return false;
   if (!s.ess_done && (!CK(cudaEventCreateWithFlags(&s.ess_done, cudaEventDisableTiming)) ||
                       !CK(cudaEventCreateWithFlags(&s.spec_ready, cudaEventDisableTiming))))
     return false;
@@ -773,11 +784,18 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
   fs.un_out = nxt ? s.shadow[1] : s.dev.un;
   fs.vn_out = nxt ? s.shadow[2] : s.dev.vn;
   if (s.precision == 2) {
-    // interior cells in double-float, the others in exact FP64; both read
-    // the same buffers and write disjoint cells
-    launch_df_march(fs, s.dfs, dims(), make_df_const(s.sc, s.um), s.stream);
+    // Interior cells in double-float, the others in exact FP64; both read
+    // the same buffers and write disjoint cells.  The exact tiles (a few
+    // hundred CTAs, each a long FP64 chain on one SM) start first on the
+    // high-priority side stream and run beside the march's waves instead of
+    // after them.
+    CK(cudaEventRecord(s.df_fork, s.stream));
+    CK(cudaStreamWaitEvent(s.side, s.df_fork, 0));
     launch_fused_boundary(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, &s.dfs,
-                          s.stream);
+                          s.side);
+    launch_df_march(fs, s.dfs, dims(), make_df_const(s.sc, s.um), s.stream);
+    CK(cudaEventRecord(s.df_join, s.side));
+    CK(cudaStreamWaitEvent(s.stream, s.df_join, 0));
   } else {
     launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
   }
@@ -807,6 +825,10 @@ bool ensure_df() {
         !CK(cudaMalloc(&s.dfs.count, 2 * sizeof(int))))
       return false;
   }
+  if (!ensure_side() ||
+      (!s.df_fork && (!CK(cudaEventCreateWithFlags(&s.df_fork, cudaEventDisableTiming)) ||
+                      !CK(cudaEventCreateWithFlags(&s.df_join, cudaEventDisableTiming)))))
+    return false;
   launch_df_setup(s.dev, dims(), s.dfs, s.stream);
   // the boundary kernels' shared-memory opt-in, outside any capture
   launch_fused_boundary(s.dev, FusedState{}, dims(), s.sc, s.um, 0.0, nullptr, 0, nullptr,
@@ -1327,6 +1349,9 @@ void nl2d_finalize(void) {
   if (s.ess_done) cudaEventDestroy(s.ess_done);
   if (s.spec_ready) cudaEventDestroy(s.spec_ready);
   s.ess_done = s.spec_ready = nullptr;
+  if (s.df_fork) cudaEventDestroy(s.df_fork);
+  if (s.df_join) cudaEventDestroy(s.df_join);
+  s.df_fork = s.df_join = nullptr;
   if (s.spec_out) cudaFreeHost(s.spec_out);
   s.spec_out = nullptr;
   noalloc_forget();
