@@ -33,14 +33,19 @@ namespace nl2d {
 namespace {
 
 using T = DefaultTile;
+// Domains too small to give every SM a few 32 x 16 tiles take 16 x 16 ones:
+// one cell per thread instead of two, twice the tiles, the same bits (the
+// arithmetic does not depend on the shape).
+using SmallTile = Tile<16, 16>;
 
-__global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
+template <class TT>
+__global__ void __launch_bounds__(NTHREADS, TT::kMinBlocks)
     k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
                  const double* __restrict__ tide_table, int tide_index, double tide) {
   extern __shared__ double smem[];
   // Tiles cover the copy region [xs-1, xe+1] x [ys-1, ye].
-  fused_tile<T>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
-                d.xs - 1 + blockIdx.x * T::TX, d.ys - 1 + blockIdx.y * T::TY, smem);
+  fused_tile<TT>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
+                 d.xs - 1 + blockIdx.x * TT::TX, d.ys - 1 + blockIdx.y * TT::TY, smem);
 }
 
 // The FP64-equivalent form's exact part: the fused tile on listed tiles of
@@ -97,15 +102,25 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const double* tide_table, int tide_index, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_fused_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_fused_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)T::kSmemBytes);
+    cudaFuncSetAttribute(k_fused_step<SmallTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)SmallTile::kSmemBytes);
     attr_set = true;
   }
   const FastConst k = make_fast_const(s, um);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY);
-  k_fused_step<<<grid, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(f, fs, d, s, um, k, tide_table,
-                                                                 tide_index, tide);
+  // fewer than four 32 x 16 tiles per SM: 16 x 16 tiles
+  if ((long long)grid.x * grid.y < 4LL * 152) {
+    using S = SmallTile;
+    const dim3 gs((nx + S::TX - 1) / S::TX, (ny + S::TY - 1) / S::TY);
+    k_fused_step<S><<<gs, dim3(S::TX, S::RPP), S::kSmemBytes, st>>>(f, fs, d, s, um, k,
+                                                                    tide_table, tide_index, tide);
+    return;
+  }
+  k_fused_step<T><<<grid, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(f, fs, d, s, um, k,
+                                                                    tide_table, tide_index, tide);
 }
 
 // Reciprocals RN(1 / (h + ssha)) of the momentum denominators, or 0 where
