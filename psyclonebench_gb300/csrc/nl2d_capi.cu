@@ -770,7 +770,7 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
     ms.un_out = s.mun[1 - s.mcur];
     ms.vn_out = s.mvn[1 - s.mcur];
     launch_mixed_step(s.mix, ms, s.dev, dims(), s.sc, s.um, tide, tide_table, tide_index,
-                      s.stream);
+                      s.stream, s.side, s.df_fork, s.df_join);
     s.mcur = 1 - s.mcur;
     return;
   }
@@ -867,6 +867,11 @@ bool ensure_mixed() {
     s.mixed_valid = false;
   }
   if (s.mixed_valid) return true;
+  // the second stream and its events for the general cells' pass
+  if (!ensure_side() ||
+      (!s.df_fork && (!CK(cudaEventCreateWithFlags(&s.df_fork, cudaEventDisableTiming)) ||
+                      !CK(cudaEventCreateWithFlags(&s.df_join, cudaEventDisableTiming)))))
+    return false;
   if (!materialize()) return false;
   const Dims d = dims();
   for (int b = 0; b < 2; b++) {

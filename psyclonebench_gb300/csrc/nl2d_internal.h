@@ -141,10 +141,13 @@ struct MixedState {  // ssh as (hi, lo) float pairs; velocities FP32
   float2* sn_out;
   float *un_out, *vn_out;
 };
+// side, fork, join (all or none): the general cells' pass starts first on
+// stream `side` and runs beside the march (fork / join by the two events).
 void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields& f,
                        const Dims& d, const Scalars& s, const UniformMetrics& um,
                        double tide, const double* tide_table, int tide_index,
-                       cudaStream_t st);
+                       cudaStream_t st, cudaStream_t side = nullptr,
+                       cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // FP64 (sshn, un, vn) -> ms.{sn,un,vn}_out; with `statics`, also the FP32
 // depths mf.{ht,hu,hv} from f.
 void launch_to_mixed(const double* sn, const double* un, const double* vn,

@@ -162,7 +162,8 @@ __global__ void k_from_mixed(const float2* __restrict__ sn2, const float* __rest
 
 void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields& f,
                        const Dims& d, const Scalars& s, const UniformMetrics& um, double tide,
-                       const double* tide_table, int tide_index, cudaStream_t st) {
+                       const double* tide_table, int tide_index, cudaStream_t st,
+                       cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   const MixConst k = make_mix_const(s, um);
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   // Strips of MR rows, halved (down to 8) until the grid holds about two
@@ -171,11 +172,26 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
   int mr = MR;
   while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 5 * MARCH_WARPS) mr /= 2;
   const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
+  // The general cells (a list of a few thousand, each a long chain of
+  // global loads) and the march read the same buffers and write disjoint
+  // cells: with a side stream the general pass starts first there and runs
+  // beside the march's waves instead of after them.
+  const bool beside = side && fork && join && mf.gcount > 0;
+  if (beside) {
+    cudaEventRecord(fork, st);
+    cudaStreamWaitEvent(side, fork, 0);
+    k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, side>>>(mf, ms, f, d, k, tide_table,
+                                                               tide_index, tide);
+  }
   k_mixed_march<<<(nwarps + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
       mf, ms, d, make_march_const(k), ncol, nwarps, mr);
-  if (mf.gcount > 0)
+  if (beside) {
+    cudaEventRecord(join, side);
+    cudaStreamWaitEvent(st, join, 0);
+  } else if (mf.gcount > 0) {
     k_mixed_general<<<(mf.gcount + 127) / 128, 128, 0, st>>>(mf, ms, f, d, k, tide_table,
                                                              tide_index, tide);
+  }
 }
 
 void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
