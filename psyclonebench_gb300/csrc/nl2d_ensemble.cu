@@ -203,6 +203,10 @@ struct Ens {
   size_t sums_cap = 0;
   int parity = 0;
   cudaStream_t stream = nullptr;
+  // the mixed form's general cells run on `side` (highest priority) beside
+  // the march: fork / join by the two events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_key[7] = {-1, -1, -1, -1, -1, -1, -1};
   bool built = false;
@@ -277,6 +281,11 @@ void ens_free() {
   e.d_first = nullptr;
   if (e.stream) cudaStreamDestroy(e.stream);
   e.stream = nullptr;
+  if (e.side) cudaStreamDestroy(e.side);
+  if (e.fork) cudaEventDestroy(e.fork);
+  if (e.join) cudaEventDestroy(e.join);
+  e.side = nullptr;
+  e.fork = e.join = nullptr;
   e.tides_cap = e.sums_cap = 0;
   e.built = false;
   e.ndom = 0;
@@ -663,6 +672,12 @@ int nl2d_ens_create(int ndom, const int* dims6, const double* geo3, const double
   e.total = off;
   const size_t bytes = off * sizeof(double);
   if (!ck(cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking))) return NL2D_ERR_CUDA;
+  int least = 0, greatest = 0;
+  if (!ck(cudaDeviceGetStreamPriorityRange(&least, &greatest)) ||
+      !ck(cudaStreamCreateWithPriority(&e.side, cudaStreamNonBlocking, greatest)) ||
+      !ck(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming)) ||
+      !ck(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming)))
+    return NL2D_ERR_CUDA;
   for (int b = 0; b < 2; b++)
     if (!ck(cudaMalloc(&e.sn[b], bytes)) || !ck(cudaMalloc(&e.un[b], bytes)) ||
         !ck(cudaMalloc(&e.vn[b], bytes)))
@@ -791,10 +806,17 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         const MixedFields mf{e.mht, e.mhu, e.mhv, e.mrhu, e.mrhv, e.mreg, nullptr, 0};
         const MixedState ms{e.msn[par], e.mun[par], e.mvn[par],
                             e.msn[1 - par], e.mun[1 - par], e.mvn[1 - par]};
+        // the general cells (each a long chain of global loads) start first
+        // on the side stream and run beside the march: both read the same
+        // buffers and write disjoint cells
+        cudaEventRecord(e.fork, e.stream);
+        cudaStreamWaitEvent(e.side, e.fork, 0);
+        launch_ens_mixed_general(e.d_mdesc, e.mglist, e.mgn, par,
+                                 e.d_tides + (size_t)q * e.ndom, e.side);
         launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.march_rows,
                                e.stream);
-        launch_ens_mixed_general(e.d_mdesc, e.mglist, e.mgn, par,
-                                 e.d_tides + (size_t)q * e.ndom, e.stream);
+        cudaEventRecord(e.join, e.side);
+        cudaStreamWaitEvent(e.stream, e.join, 0);
         par = 1 - par;
         if (want_sums)
           k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
