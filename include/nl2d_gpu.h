@@ -69,7 +69,10 @@ extern "C" {
  * the checks refuse the fused path or find a state that is not what a step
  * leaves, the steps taken meanwhile are undone and taken again by the
  * reference's rules, so the results are the same bits either way.  Every
- * other entry point waits for the checks first.
+ * other entry point waits for the checks first.  As with any asynchronous
+ * copy from pinned memory, the caller must not write those 12 arrays
+ * directly until a later library call has returned (c_write_to_device, the
+ * way to change a registered array, waits for them itself).
  */
 void c_invoke_time_step(
     double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
