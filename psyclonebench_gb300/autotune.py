@@ -12,8 +12,9 @@ nl2d_ens_tile):
   size as a run parameter; here it is searched.  The search has two stages:
   every schedule at the default shape, then every shape under the best
   schedule and under one-tile-per-CTA.
-* Mixed form, when it runs the column march: the march's strip height (8,
-  16 or 32 rows), under the FP64 knobs already applied.
+* Mixed form, when it runs the column march, and the FP64-equivalent form
+  ("df"): the march's strip height (8, 16 or 32 rows), under the FP64 knobs
+  already applied.
 
 Each candidate is timed on a few steps of the actual ensemble (after one
 untimed step), the domains are put back at rest, and the fastest candidate
@@ -99,9 +100,9 @@ def _fp64_candidates(best_schedule=None):
 
 def tune(ens, steps=4, precision="fp64", use_cache=True, base=None):
     """Picks and applies the fastest knobs for `ens` in its current form
-    (precision "fp64" or "mixed"); returns a dict with the choice and the
-    timings.  For "mixed", `base` holds the FP64 knobs to keep (default:
-    the defaults).  Leaves the ensemble at rest."""
+    (precision "fp64", "mixed" or "df"); returns a dict with the choice and
+    the timings.  For "mixed" and "df", `base` holds the FP64 knobs to keep
+    (default: the defaults).  Leaves the ensemble at rest."""
     sig = signature(ens.domains, precision)
     db = _load() if use_cache else {}
     if sig in db:
@@ -109,7 +110,7 @@ def tune(ens, steps=4, precision="fp64", use_cache=True, base=None):
         _apply(ens, c)
         return dict(c, cached=True)
     timings = []
-    if precision == "mixed":
+    if precision in ("mixed", "df"):
         b = dict(base or {"ctas_per_sm": 2, "policy": 0, "boundary_weight": 4.0,
                           "tile": list(DEFAULT_SHAPE)})
         for mr in MARCH_ROWS:

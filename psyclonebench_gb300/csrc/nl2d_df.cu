@@ -28,7 +28,7 @@ namespace nl2d {
 using namespace dfk;
 namespace {
 
-constexpr int MW = 30;
+constexpr int MW = kDfMarchCols;
 constexpr int MR = 32;
 constexpr int WARPS = 4;
 constexpr unsigned FULL = 0xffffffffu;
@@ -129,12 +129,10 @@ __device__ __forceinline__ MTerm row_terms(const MRow& P, const MRow& C, const M
   return t;
 }
 
-__global__ void __launch_bounds__(32 * WARPS, 3)
-    k_df_march(FusedState fs, DfFields ff, Dims d, DfConst k, int ncol, int nwarps, int mr) {
-  const int warp = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
-  if (warp >= nwarps) return;  // the whole warp leaves together
-  const int gy = warp / ncol, gx = warp - gy * ncol;
-  const int i0 = d.xs - 1 + gx * MW, j0 = d.ys - 1 + gy * mr;
+// One warp's strip: columns i0 .. i0 + MW - 1, rows j0 .. j0 + mr - 1 of the
+// copy region of the domain whose arrays fs and ff point into.
+__device__ __forceinline__ void df_march(const FusedState& fs, const DfFields& ff, const Dims& d,
+                                         const DfConst& k, int i0, int j0, int mr) {
   const int lane = threadIdx.x & 31;
   const int W = d.width, H = d.height;
   const int i = i0 - 1 + lane;
@@ -195,6 +193,26 @@ __global__ void __launch_bounds__(32 * WARPS, 3)
   }
 }
 
+__global__ void __launch_bounds__(32 * WARPS, 3)
+    k_df_march(FusedState fs, DfFields ff, Dims d, DfConst k, int ncol, int nwarps, int mr) {
+  const int warp = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
+  if (warp >= nwarps) return;  // the whole warp leaves together
+  const int gy = warp / ncol, gx = warp - gy * ncol;
+  df_march(fs, ff, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * mr, mr);
+}
+
+// The ensemble form: warp w takes units[w] = (domain, i0, j0) with the
+// domain's buffers in doms[domain] (every domain shares the constants k).
+__global__ void __launch_bounds__(32 * WARPS, 3)
+    k_ensemble_df_march(const EnsDfDomain* __restrict__ doms, const int4* __restrict__ units,
+                        int nunits, int parity, DfConst k, int mr) {
+  const int w = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
+  if (w >= nunits) return;  // the whole warp leaves together
+  const int4 u = units[w];
+  const EnsDfDomain& D = doms[u.x];
+  df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
+}
+
 // FP64 arrays split into pairs once per set-up.
 __global__ void k_split(const double* __restrict__ a, float2* __restrict__ out, long long n) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
@@ -231,10 +249,9 @@ __global__ void k_df_flags(const int* __restrict__ m, Dims d, unsigned char* __r
 // rows ys+1 .. ye-1), side 0 every other such cell.  The two kinds cover
 // every copy-region cell the march leaves; the order of the list does not
 // matter (each tile writes its own cells).
-__global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
-                           int ntx, int side, int* __restrict__ list, int* __restrict__ count) {
-  const int b = blockIdx.x;
-  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
+__device__ __forceinline__ bool tile_has_work(const unsigned char* __restrict__ reg,
+                                              const Dims& d, int tx, int ty, int i0, int j0,
+                                              int side) {
   int any = 0;
   for (int t = threadIdx.x; t < tx * ty; t += blockDim.x) {
     const int i = i0 + t % tx, j = j0 + t / tx;
@@ -242,8 +259,26 @@ __global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx
     const bool strip = (i <= d.xs || i >= d.xe) && j >= d.ys + 1 && j <= d.ye - 1;
     if (strip == (side == 1)) any = 1;
   }
-  any = __syncthreads_or(any);
-  if (threadIdx.x == 0 && any) list[atomicAdd(count + side, 1)] = b;
+  return __syncthreads_or(any) != 0;
+}
+
+__global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
+                           int ntx, int side, int* __restrict__ list, int* __restrict__ count) {
+  const int b = blockIdx.x;
+  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
+  if (tile_has_work(reg, d, tx, ty, i0, j0, side) && threadIdx.x == 0)
+    list[atomicAdd(count + side, 1)] = b;
+}
+
+// The same for one domain of an ensemble: the tiles go to `list` as
+// (domain, i0, j0).
+__global__ void k_ens_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
+                               int ntx, int side, int dom, int4* __restrict__ list,
+                               int* __restrict__ count) {
+  const int b = blockIdx.x;
+  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
+  if (tile_has_work(reg, d, tx, ty, i0, j0, side) && threadIdx.x == 0)
+    list[atomicAdd(count + side, 1)] = make_int4(dom, i0, j0, 0);
 }
 
 __global__ void k_selftest_df(const double* __restrict__ x, long long n, float* __restrict__ hi,
@@ -348,3 +383,30 @@ extern "C" int nl2d_selftest_df(const double* x, long long n, float* hi, float* 
   cudaFree(dl);
   return ok ? 0 : 1;
 }
+
+namespace nl2d {
+
+void launch_ens_df_march(const EnsDfDomain* doms, const int4* units, int nunits, int parity,
+                         const DfConst& k, int march_rows, cudaStream_t st) {
+  k_ensemble_df_march<<<(nunits + WARPS - 1) / WARPS, 32 * WARPS, 0, st>>>(doms, units, nunits,
+                                                                           parity, k, march_rows);
+}
+
+void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st) {
+  k_split<<<152 * 8, 256, 0, st>>>(a, out, n);
+}
+
+void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st) {
+  k_df_flags<<<152 * 8, 256, 0, st>>>(tmask, d, reg);
+}
+
+int launch_ens_df_tiles(const unsigned char* reg, const Dims& d, int dom, int side, int4* list,
+                        int* count, cudaStream_t st) {
+  const int tx = side ? kDfColsTX : kDfRowsTX, ty = side ? kDfColsTY : kDfRowsTY;
+  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
+  const int ntx = (nx + tx - 1) / tx, nty = (ny + ty - 1) / ty;
+  if (list) k_ens_df_tiles<<<ntx * nty, 256, 0, st>>>(reg, d, tx, ty, ntx, side, dom, list, count);
+  return ntx * nty;
+}
+
+}  // namespace nl2d

@@ -13,6 +13,12 @@
 //
 // Domains start from rest (ssh = u = v = 0), where the state is already
 // step-consistent, so every step takes the fused path.
+//
+// Three forms share the domain layout: FP64 (the tiles above), mixed
+// precision (its own FP32 / compensated state), and FP64-equivalent, which
+// keeps the FP64 state and runs the double-float column march (nl2d_df.cu)
+// over every domain's interior while the fused tile, in exact FP64, takes
+// the thin edge tiles that hold every other cell, on a second stream.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -100,6 +106,45 @@ __global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
     __syncthreads();  // the previous tile's last readers are done with smem
     fused_tile<T>(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
   }
+}
+
+// The FP64-equivalent form's exact part: the fused tile on the listed thin
+// tiles, tile b being (domain, i0, j0) = tiles[b], with that domain's
+// arrays, constants and tide; the cells the double-float march writes are
+// left alone.  A cell that tiles of both shapes hold is written twice with
+// the same bits.
+using DfEdgeRows = Tile<kDfRowsTX, kDfRowsTY>;
+using DfEdgeCols = Tile<kDfColsTX, kDfColsTY>;
+
+template <class TE>
+__global__ void __launch_bounds__(NTHREADS, TE::kMinBlocks)
+    k_ensemble_df_exact(const EnsDomain* __restrict__ doms, const int4* __restrict__ tiles,
+                        int parity, const double* __restrict__ tides) {
+  const int4 tl = tiles[blockIdx.x];
+  const EnsDomain& D = doms[tl.x];
+  extern __shared__ double smem[];
+  fused_tile<TE, true>(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
+}
+
+// side 0 the edge-row tiles, 1 the side-strip tiles; doms == nullptr: only
+// sets the kernels' shared-memory attributes (call outside any capture).
+void launch_ens_df_exact(int side, int ntiles, const EnsDomain* doms, const int4* tiles,
+                         int parity, const double* tides, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_ensemble_df_exact<DfEdgeRows>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DfEdgeRows::kSmemBytes);
+    cudaFuncSetAttribute(k_ensemble_df_exact<DfEdgeCols>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DfEdgeCols::kSmemBytes);
+    attr_set = true;
+  }
+  if (!doms || ntiles < 1) return;
+  if (side == 0)
+    k_ensemble_df_exact<DfEdgeRows><<<ntiles, dim3(DfEdgeRows::TX, DfEdgeRows::RPP),
+                                      DfEdgeRows::kSmemBytes, st>>>(doms, tiles, parity, tides);
+  else
+    k_ensemble_df_exact<DfEdgeCols><<<ntiles, dim3(DfEdgeCols::TX, DfEdgeCols::RPP),
+                                      DfEdgeCols::kSmemBytes, st>>>(doms, tiles, parity, tides);
 }
 
 // The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
@@ -208,7 +253,7 @@ struct Ens {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraphExec_t graph = nullptr;
-  int graph_key[7] = {-1, -1, -1, -1, -1, -1, -1};
+  int graph_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   bool built = false;
   int shape = 0;        // index into kShapes: the FP64 kernel's tile
   int march_rows = 32;  // strip height of the mixed form's column march
@@ -227,6 +272,18 @@ struct Ens {
   int mgn = 0;
   int4* d_units = nullptr;
   int nunits = 0;
+  // FP64-equivalent form: (hi, lo) pairs of ht, hu, hv, r_hu, r_hv (one
+  // allocation, `total` pairs each), the march flags, the domains'
+  // descriptors and march units, and the exact tiles of both shapes
+  float2* dfs = nullptr;
+  unsigned char* dfreg = nullptr;
+  EnsDfDomain* d_dfdesc = nullptr;
+  DfConst dk{};
+  int4* d_dfunits = nullptr;
+  int ndfunits = 0;
+  int4* dfx[2] = {};
+  int dfxn[2] = {0, 0};
+  int* dfcount = nullptr;
 };
 
 Ens g_ens;
@@ -270,6 +327,20 @@ void ens_free() {
   e.d_units = nullptr;
   e.mgn = e.nunits = 0;
   e.march = false;
+  cudaFree(e.dfs);
+  cudaFree(e.dfreg);
+  cudaFree(e.d_dfdesc);
+  cudaFree(e.d_dfunits);
+  cudaFree(e.dfx[0]);
+  cudaFree(e.dfx[1]);
+  cudaFree(e.dfcount);
+  e.dfs = nullptr;
+  e.dfreg = nullptr;
+  e.d_dfdesc = nullptr;
+  e.d_dfunits = nullptr;
+  e.dfx[0] = e.dfx[1] = nullptr;
+  e.dfcount = nullptr;
+  e.ndfunits = e.dfxn[0] = e.dfxn[1] = 0;
   e.precision = 0;
   cudaFree(e.tmask);
   cudaFree(e.d_desc);
@@ -558,6 +629,112 @@ bool build_mixed() {
   return build_march(desc);
 }
 
+UniformMetrics domain_metrics(const DomainHost& D, const Scalars& sc) {
+  UniformMetrics um{};
+  um.area_t = um.area_u = um.area_v = D.dx * D.dy;
+  um.dx_u = um.dx_v = um.dx_t = D.dx;
+  um.dy_u = um.dy_v = um.dy_t = D.dy;
+  um.sin_u = um.sin_v = std::sin(D.gphi * sc.d2r);
+  return um;
+}
+
+// Whether every domain has the same grid spacing and latitude, so that one
+// set of step constants (kernel parameters) serves the whole ensemble.
+bool shared_constants() {
+  const Ens& e = g_ens;
+  for (const DomainHost& D : e.dom)
+    if (D.dx != e.dom[0].dx || D.dy != e.dom[0].dy || D.gphi != e.dom[0].gphi) return false;
+  return true;
+}
+
+// The FP64-equivalent form's set-up, after build_descriptors(): the
+// double-float statics, the march flags, units and descriptors, and the
+// exact tiles (rebuilt whenever the ensemble is).
+bool build_df() {
+  Ens& e = g_ens;
+  const size_t n = e.total;
+  cudaStream_t st = e.stream;
+  if (!e.dfs && (!ck(cudaMalloc(&e.dfs, 5 * n * sizeof(float2))) ||
+                 !ck(cudaMalloc(&e.dfreg, n)) || !ck(cudaMalloc(&e.dfcount, 2 * sizeof(int)))))
+    return false;
+  float2* pr[5] = {e.dfs, e.dfs + n, e.dfs + 2 * n, e.dfs + 3 * n, e.dfs + 4 * n};
+  const double* src[5] = {e.ht, e.hu, e.hv, e.r_hu, e.r_hv};
+  for (int a = 0; a < 5; a++) launch_df_split(src[a], pr[a], (long long)n, st);
+  if (!ck(cudaMemsetAsync(e.dfreg, 0, n, st))) return false;
+  int cap[2] = {0, 0};
+  std::vector<EnsDfDomain> desc(e.ndom);
+  std::vector<int4> units;
+  for (int k = 0; k < e.ndom; k++) {
+    const DomainHost& D = e.dom[k];
+    const size_t o = D.off;
+    const Dims d{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
+    launch_df_flags(e.tmask + o, d, e.dfreg + o, st);
+    for (int side = 0; side < 2; side++)
+      cap[side] += launch_ens_df_tiles(nullptr, d, k, side, nullptr, nullptr, st);
+    EnsDfDomain& x = desc[k];
+    memset(&x, 0, sizeof x);
+    for (int p = 0; p < 2; p++)
+      x.fs[p] = FusedState{e.sn[p] + o,     e.un[p] + o,     e.vn[p] + o,
+                           e.sn[1 - p] + o, e.un[1 - p] + o, e.vn[1 - p] + o};
+    x.ff.ht = pr[0] + o;
+    x.ff.hu = pr[1] + o;
+    x.ff.hv = pr[2] + o;
+    x.ff.rhu = pr[3] + o;
+    x.ff.rhv = pr[4] + o;
+    x.ff.reg = e.dfreg + o;
+    x.d = d;
+    const int nx = D.xe - D.xs + 3, ny = D.ye - D.ys + 2, mr = e.march_rows;
+    for (int gy = 0; gy < (ny + mr - 1) / mr; gy++)
+      for (int gx = 0; gx < (nx + kDfMarchCols - 1) / kDfMarchCols; gx++)
+        units.push_back(make_int4(k, D.xs - 1 + gx * kDfMarchCols, D.ys - 1 + gy * mr, 0));
+  }
+  for (int side = 0; side < 2; side++) {
+    cudaFree(e.dfx[side]);
+    e.dfx[side] = nullptr;
+    if (!ck(cudaMalloc(&e.dfx[side], sizeof(int4) * std::max(1, cap[side])))) return false;
+  }
+  if (!ck(cudaMemsetAsync(e.dfcount, 0, 2 * sizeof(int), st))) return false;
+  for (int k = 0; k < e.ndom; k++) {
+    const DomainHost& D = e.dom[k];
+    const Dims d{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
+    for (int side = 0; side < 2; side++)
+      launch_ens_df_tiles(e.dfreg + D.off, d, k, side, e.dfx[side], e.dfcount, st);
+  }
+  int cnt[2] = {0, 0};
+  if (!ck(cudaGetLastError()) ||
+      !ck(cudaMemcpyAsync(cnt, e.dfcount, sizeof cnt, cudaMemcpyDeviceToHost, st)) ||
+      !ck(cudaStreamSynchronize(st)))
+    return false;
+  e.dfxn[0] = cnt[0];
+  e.dfxn[1] = cnt[1];
+  cudaFree(e.d_dfdesc);
+  cudaFree(e.d_dfunits);
+  e.d_dfdesc = nullptr;
+  e.d_dfunits = nullptr;
+  if (!ck(cudaMalloc(&e.d_dfdesc, sizeof(EnsDfDomain) * e.ndom)) ||
+      !ck(cudaMalloc(&e.d_dfunits, sizeof(int4) * units.size())) ||
+      !ck(cudaMemcpy(e.d_dfdesc, desc.data(), sizeof(EnsDfDomain) * e.ndom,
+                     cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.d_dfunits, units.data(), sizeof(int4) * units.size(),
+                     cudaMemcpyHostToDevice)))
+    return false;
+  e.ndfunits = (int)units.size();
+  e.dk = make_df_const(e.sc, domain_metrics(e.dom[0], e.sc));
+  launch_ens_df_exact(0, 0, nullptr, nullptr, 0, nullptr, st);  // kernel attributes
+  return ck(cudaGetLastError());
+}
+
+// FP64 state of every domain back to rest.
+bool zero_fp64_state() {
+  Ens& e = g_ens;
+  const size_t bytes = e.total * sizeof(double);
+  cudaStreamSynchronize(e.stream);
+  for (double* p : {e.sn[0], e.sn[1], e.un[0], e.un[1], e.vn[0], e.vn[1]})
+    if (!ck(cudaMemset(p, 0, bytes))) return false;
+  e.parity = 0;
+  return true;
+}
+
 // Interior (ssh, u, v) of every domain, all of size nx x ny, as FP32
 // [dom][ny][nx][3] (the emulator's snapshot layout).
 __global__ void k_export_interior(const EnsDomain* __restrict__ doms, int parity, int ndom,
@@ -753,11 +930,12 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     if (e.precision == 1) {
       if (!build_mixed() || (!e.march && !build_schedule(mixk::TX, mixk::TY)))
         return NL2D_ERR_CUDA;
+      e.parity = 0;  // the mixed state was set to rest
     } else if (!build_descriptors() ||
-               !build_schedule(kShapes[e.shape][0], kShapes[e.shape][1])) {
+               !build_schedule(kShapes[e.shape][0], kShapes[e.shape][1]) ||
+               (e.precision == 2 && !build_df())) {
       return NL2D_ERR_CUDA;
     }
-    e.parity = 0;
     e.built = true;
   }
   if (nsteps == 0) return NL2D_OK;
@@ -789,8 +967,8 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     if (!ck(cudaMalloc(&e.d_sums, nsum_vals * 8))) return NL2D_ERR_CUDA;
     e.sums_cap = nsum_vals;
   }
-  const int key[7] = {nsteps,  checksum_every, e.parity,    e.nctas, e.policy * 2 + e.precision,
-                      e.shape, e.march_rows};
+  const int key[8] = {nsteps,   checksum_every, e.parity, e.nctas,
+                      e.policy, e.precision,    e.shape,  e.march_rows};
   if (!(e.graph && memcmp(key, e.graph_key, sizeof key) == 0)) {
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
@@ -821,6 +999,22 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         if (want_sums)
           k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
                                                                             sums);
+      } else if (e.precision == 2) {
+        // exact tiles on the side stream beside the march: both read the
+        // same state buffers and write disjoint cells
+        const double* tq = e.d_tides + (size_t)q * e.ndom;
+        cudaEventRecord(e.fork, e.stream);
+        cudaStreamWaitEvent(e.side, e.fork, 0);
+        launch_ens_df_exact(0, e.dfxn[0], e.d_desc, e.dfx[0], par, tq, e.side);
+        launch_ens_df_exact(1, e.dfxn[1], e.d_desc, e.dfx[1], par, tq, e.side);
+        launch_ens_df_march(e.d_dfdesc, e.d_dfunits, e.ndfunits, par, e.dk, e.march_rows,
+                            e.stream);
+        cudaEventRecord(e.join, e.side);
+        cudaStreamWaitEvent(e.stream, e.join, 0);
+        par = 1 - par;
+        if (want_sums)
+          k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,
+                                                                      sums);
       } else if (e.precision == 1) {
         k_ensemble_mixed_step<<<e.nctas, dim3(mixk::TX, mixk::TY), 0, e.stream>>>(
             e.d_mdesc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
@@ -907,13 +1101,17 @@ int nl2d_ens_info(long long* cells, int* ntiles, int* nctas) {
 
 int nl2d_ens_set_precision(int precision) {
   Ens& e = g_ens;
-  if (precision != 0 && precision != 1) return NL2D_ERR_ARGS;
+  if (precision < 0 || precision > 2) return NL2D_ERR_ARGS;
   if (e.ndom < 1) return NL2D_ERR_STATE;
+  // the FP64-equivalent march takes one set of step constants
+  if (precision == 2 && !shared_constants()) return NL2D_ERR_ARGS;
   if (precision != e.precision) {
     e.precision = precision;
     e.built = false;  // the next run starts this form from rest
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
+    // the mixed form's rebuild sets its own state to rest
+    if (precision != 1 && !zero_fp64_state()) return NL2D_ERR_CUDA;
   }
   return NL2D_OK;
 }
@@ -935,7 +1133,7 @@ int nl2d_ens_export_interior(float* d_out) {
 
 int nl2d_ens_import_interior(const float* d_in) {
   Ens& e = g_ens;
-  if (e.ndom < 1 || !d_in || e.precision != 0 || !e.built) return NL2D_ERR_STATE;
+  if (e.ndom < 1 || !d_in || e.precision == 1 || !e.built) return NL2D_ERR_STATE;
   const int nx = e.dom[0].xe - e.dom[0].xs + 1, ny = e.dom[0].ye - e.dom[0].ys + 1;
   for (const DomainHost& D : e.dom)
     if (D.xe - D.xs + 1 != nx || D.ye - D.ys + 1 != ny) return NL2D_ERR_ARGS;
@@ -951,12 +1149,7 @@ int nl2d_ens_reset(void) {
     e.built = false;  // mixed state is re-zeroed when rebuilt
     return NL2D_OK;
   }
-  const size_t bytes = e.total * sizeof(double);
-  cudaStreamSynchronize(e.stream);
-  for (double* p : {e.sn[0], e.sn[1], e.un[0], e.un[1], e.vn[0], e.vn[1]})
-    if (!ck(cudaMemset(p, 0, bytes))) return NL2D_ERR_CUDA;
-  e.parity = 0;
-  return NL2D_OK;
+  return zero_fp64_state() ? NL2D_OK : NL2D_ERR_CUDA;
 }
 
 int nl2d_ens_uses_march(void) { return g_ens.march ? 1 : 0; }

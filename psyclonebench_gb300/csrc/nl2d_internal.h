@@ -102,17 +102,39 @@ struct DfFields {
   int* count;                        // device: the two list lengths
   int n_rows, n_cols;                // host copies of the list lengths
 };
+// One domain of an FP64-equivalent ensemble (device descriptor): its state
+// buffers per parity and its double-float statics, pointers into the
+// ensemble's packed arrays.
+struct EnsDfDomain {
+  FusedState fs[2];
+  DfFields ff;
+  Dims d;
+};
 struct DfConst {
   dfk::df r_dx, r_dy, uu_x, uu_y, vv_x, vv_y, r_qu, r_qv, vis1_u, vis1_v, vis2_u, vis2_v;
   dfk::df cor_u, cor_v, hpg_u, hpg_v, rra_u, rra_v, face_u, face_v, rrat, r_fric;
 };
 DfConst make_df_const(const Scalars& s, const UniformMetrics& um);
 constexpr int kDfRowsTX = 128, kDfRowsTY = 2, kDfColsTX = 4, kDfColsTY = 128;
+constexpr int kDfMarchCols = 30;  // columns one warp of the march updates
 // Splits the depths and reciprocal denominators, marks the march's cells and
 // lists the exact part's tiles (ff.count receives the list lengths).
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
 void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
                      cudaStream_t st);
+// The ensemble's march over (domain, i0, j0) units of march_rows rows.
+void launch_ens_df_march(const EnsDfDomain* doms, const int4* units, int nunits, int parity,
+                         const DfConst& k, int march_rows, cudaStream_t st);
+// Split of one packed FP64 array into (hi, lo) pairs; the march flags of one
+// domain (tmask and reg point at the domain's first element).
+void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st);
+void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st);
+// Appends to `list` the exact tiles of one ensemble domain (side 0 the
+// kDfRowsTX x kDfRowsTY tiles, side 1 the side-strip kDfColsTX x kDfColsTY
+// tiles, as (dom, i0, j0)), counting them in count[side]; returns how many
+// tiles of that shape the domain has (list == nullptr: only that).
+int launch_ens_df_tiles(const unsigned char* reg, const Dims& d, int dom, int side, int4* list,
+                        int* count, cudaStream_t st);
 // The fused FP64 tile kernel on the listed tiles of both shapes, leaving
 // the march's cells alone.  ff == nullptr: only sets the kernels' shared-
 // memory attributes (call outside any capture).
