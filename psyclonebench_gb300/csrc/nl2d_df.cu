@@ -270,17 +270,6 @@ __global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx
     list[atomicAdd(count + side, 1)] = b;
 }
 
-// The same for one domain of an ensemble: the tiles go to `list` as
-// (domain, i0, j0).
-__global__ void k_ens_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
-                               int ntx, int side, int dom, int4* __restrict__ list,
-                               int* __restrict__ count) {
-  const int b = blockIdx.x;
-  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
-  if (tile_has_work(reg, d, tx, ty, i0, j0, side) && threadIdx.x == 0)
-    list[atomicAdd(count + side, 1)] = make_int4(dom, i0, j0, 0);
-}
-
 __global__ void k_selftest_df(const double* __restrict__ x, long long n, float* __restrict__ hi,
                               float* __restrict__ lo, double* __restrict__ joined,
                               double* __restrict__ widened) {
@@ -398,15 +387,6 @@ void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st)
 
 void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st) {
   k_df_flags<<<152 * 8, 256, 0, st>>>(tmask, d, reg);
-}
-
-int launch_ens_df_tiles(const unsigned char* reg, const Dims& d, int dom, int side, int4* list,
-                        int* count, cudaStream_t st) {
-  const int tx = side ? kDfColsTX : kDfRowsTX, ty = side ? kDfColsTY : kDfRowsTY;
-  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const int ntx = (nx + tx - 1) / tx, nty = (ny + ty - 1) / ty;
-  if (list) k_ens_df_tiles<<<ntx * nty, 256, 0, st>>>(reg, d, tx, ty, ntx, side, dom, list, count);
-  return ntx * nty;
 }
 
 }  // namespace nl2d

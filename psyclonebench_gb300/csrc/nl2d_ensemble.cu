@@ -17,8 +17,8 @@
 // Three forms share the domain layout: FP64 (the tiles above), mixed
 // precision (its own FP32 / compensated state), and FP64-equivalent, which
 // keeps the FP64 state and runs the double-float column march (nl2d_df.cu)
-// over every domain's interior while the fused tile, in exact FP64, takes
-// the thin edge tiles that hold every other cell, on a second stream.
+// over every domain's interior while the fused step's general per-cell code,
+// in exact FP64, takes every other cell, on a second stream.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -108,43 +108,25 @@ __global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
   }
 }
 
-// The FP64-equivalent form's exact part: the fused tile on the listed thin
-// tiles, tile b being (domain, i0, j0) = tiles[b], with that domain's
-// arrays, constants and tide; the cells the double-float march writes are
-// left alone.  A cell that tiles of both shapes hold is written twice with
-// the same bits.
-using DfEdgeRows = Tile<kDfRowsTX, kDfRowsTY>;
-using DfEdgeCols = Tile<kDfColsTX, kDfColsTY>;
-
-template <class TE>
-__global__ void __launch_bounds__(NTHREADS, TE::kMinBlocks)
-    k_ensemble_df_exact(const EnsDomain* __restrict__ doms, const int4* __restrict__ tiles,
-                        int parity, const double* __restrict__ tides) {
-  const int4 tl = tiles[blockIdx.x];
-  const EnsDomain& D = doms[tl.x];
-  extern __shared__ double smem[];
-  fused_tile<TE, true>(D.f, D.fs[parity], D.d, D.p, D.um, D.k, tides[tl.x], tl.y, tl.z, smem);
-}
-
-// side 0 the edge-row tiles, 1 the side-strip tiles; doms == nullptr: only
-// sets the kernels' shared-memory attributes (call outside any capture).
-void launch_ens_df_exact(int side, int ntiles, const EnsDomain* doms, const int4* tiles,
-                         int parity, const double* tides, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_ensemble_df_exact<DfEdgeRows>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DfEdgeRows::kSmemBytes);
-    cudaFuncSetAttribute(k_ensemble_df_exact<DfEdgeCols>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DfEdgeCols::kSmemBytes);
-    attr_set = true;
-  }
-  if (!doms || ntiles < 1) return;
-  if (side == 0)
-    k_ensemble_df_exact<DfEdgeRows><<<ntiles, dim3(DfEdgeRows::TX, DfEdgeRows::RPP),
-                                      DfEdgeRows::kSmemBytes, st>>>(doms, tiles, parity, tides);
-  else
-    k_ensemble_df_exact<DfEdgeCols><<<ntiles, dim3(DfEdgeCols::TX, DfEdgeCols::RPP),
-                                      DfEdgeCols::kSmemBytes, st>>>(doms, tiles, parity, tides);
+// The FP64-equivalent form's exact part: every copy-region cell the
+// double-float march does not write (the ring of boundary rows and columns,
+// and cells beside land), one thread each, by the fused step's general
+// per-cell code reading the domain's arrays in global memory.  Entry g of
+// `cells` is (domain, cell index); the result is the FP64 step's, bit for
+// bit, with that domain's tide.
+__global__ void __launch_bounds__(128)
+    k_ensemble_df_ring(const EnsDomain* __restrict__ doms, const int2* __restrict__ cells,
+                       int ncells, int parity, const double* __restrict__ tides) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ncells) return;
+  const int2 e = cells[g];
+  const EnsDomain& D = doms[e.x];
+  const FusedState& st = D.fs[parity];
+  const GlobalCtx x{st.sshn_in, st.un_in,    st.vn_in,  D.f.hu,     D.f.hv,     D.f.ht,
+                    D.f.ssha_u, D.f.ssha_v,  D.f.r_hu,  D.f.r_hv,   D.f.tmask,  D.f.sshn_u,
+                    D.f.sshn_v, D.d.width,   D.d,       D.k};
+  const int j = e.y / D.d.width, i = e.y - j * D.d.width;
+  general_cell(x, D.f, st, D.p, tides[e.x], i, j);
 }
 
 // The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
@@ -226,7 +208,37 @@ struct DomainHost {
   double dx, dy, gphi, amp, period_h;
   size_t off;  // element offset of this domain in every packed array
   bool ready = false;
+  // copy-region cells the FP64-equivalent form's march does not write
+  // (row-major cell indices), from the mask
+  std::vector<int> ring;
 };
+
+// The double-float march writes cell (i, j) when it lies one inside the
+// interior's edge and its 3x3 mask neighbourhood is wet (df_regular in
+// nl2d_df.cu); every other copy-region cell is listed here.
+std::vector<int> ring_cells(const DomainHost& D, const int* m) {
+  const int W = D.W;
+  std::vector<int> out;
+  // r[i] = wet(i-1) & wet(i) & wet(i+1) along row j
+  auto row3 = [&](int j, std::vector<unsigned char>& r) {
+    for (int i = 1; i < W - 1; i++)
+      r[i] = m[j * W + i - 1] > 0 && m[j * W + i] > 0 && m[j * W + i + 1] > 0;
+  };
+  std::vector<unsigned char> a(W, 0), b(W, 0), c(W, 0);
+  for (int j = D.ys - 1; j <= D.ye; j++) {
+    const bool inner_row = j >= D.ys + 1 && j <= D.ye - 1;
+    if (inner_row) {
+      row3(j - 1, a);
+      row3(j, b);
+      row3(j + 1, c);
+    }
+    for (int i = D.xs - 1; i <= D.xe + 1; i++) {
+      const bool march = inner_row && i >= D.xs + 1 && i <= D.xe - 1 && a[i] && b[i] && c[i];
+      if (!march) out.push_back(j * W + i);
+    }
+  }
+  return out;
+}
 
 struct Ens {
   int ndom = 0;
@@ -281,9 +293,8 @@ struct Ens {
   DfConst dk{};
   int4* d_dfunits = nullptr;
   int ndfunits = 0;
-  int4* dfx[2] = {};
-  int dfxn[2] = {0, 0};
-  int* dfcount = nullptr;
+  int2* dfring = nullptr;  // the exact cells, (domain, cell index)
+  int ndfring = 0;
 };
 
 Ens g_ens;
@@ -331,16 +342,13 @@ void ens_free() {
   cudaFree(e.dfreg);
   cudaFree(e.d_dfdesc);
   cudaFree(e.d_dfunits);
-  cudaFree(e.dfx[0]);
-  cudaFree(e.dfx[1]);
-  cudaFree(e.dfcount);
+  cudaFree(e.dfring);
   e.dfs = nullptr;
   e.dfreg = nullptr;
   e.d_dfdesc = nullptr;
   e.d_dfunits = nullptr;
-  e.dfx[0] = e.dfx[1] = nullptr;
-  e.dfcount = nullptr;
-  e.ndfunits = e.dfxn[0] = e.dfxn[1] = 0;
+  e.dfring = nullptr;
+  e.ndfunits = e.ndfring = 0;
   e.precision = 0;
   cudaFree(e.tmask);
   cudaFree(e.d_desc);
@@ -649,28 +657,26 @@ bool shared_constants() {
 
 // The FP64-equivalent form's set-up, after build_descriptors(): the
 // double-float statics, the march flags, units and descriptors, and the
-// exact tiles (rebuilt whenever the ensemble is).
+// list of exact cells (rebuilt whenever the ensemble is).
 bool build_df() {
   Ens& e = g_ens;
   const size_t n = e.total;
   cudaStream_t st = e.stream;
-  if (!e.dfs && (!ck(cudaMalloc(&e.dfs, 5 * n * sizeof(float2))) ||
-                 !ck(cudaMalloc(&e.dfreg, n)) || !ck(cudaMalloc(&e.dfcount, 2 * sizeof(int)))))
+  if (!e.dfs && (!ck(cudaMalloc(&e.dfs, 5 * n * sizeof(float2))) || !ck(cudaMalloc(&e.dfreg, n))))
     return false;
   float2* pr[5] = {e.dfs, e.dfs + n, e.dfs + 2 * n, e.dfs + 3 * n, e.dfs + 4 * n};
   const double* src[5] = {e.ht, e.hu, e.hv, e.r_hu, e.r_hv};
   for (int a = 0; a < 5; a++) launch_df_split(src[a], pr[a], (long long)n, st);
   if (!ck(cudaMemsetAsync(e.dfreg, 0, n, st))) return false;
-  int cap[2] = {0, 0};
   std::vector<EnsDfDomain> desc(e.ndom);
   std::vector<int4> units;
+  std::vector<int2> ring;
   for (int k = 0; k < e.ndom; k++) {
     const DomainHost& D = e.dom[k];
     const size_t o = D.off;
     const Dims d{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
     launch_df_flags(e.tmask + o, d, e.dfreg + o, st);
-    for (int side = 0; side < 2; side++)
-      cap[side] += launch_ens_df_tiles(nullptr, d, k, side, nullptr, nullptr, st);
+    for (int c : D.ring) ring.push_back(make_int2(k, c));
     EnsDfDomain& x = desc[k];
     memset(&x, 0, sizeof x);
     for (int p = 0; p < 2; p++)
@@ -688,40 +694,27 @@ bool build_df() {
       for (int gx = 0; gx < (nx + kDfMarchCols - 1) / kDfMarchCols; gx++)
         units.push_back(make_int4(k, D.xs - 1 + gx * kDfMarchCols, D.ys - 1 + gy * mr, 0));
   }
-  for (int side = 0; side < 2; side++) {
-    cudaFree(e.dfx[side]);
-    e.dfx[side] = nullptr;
-    if (!ck(cudaMalloc(&e.dfx[side], sizeof(int4) * std::max(1, cap[side])))) return false;
-  }
-  if (!ck(cudaMemsetAsync(e.dfcount, 0, 2 * sizeof(int), st))) return false;
-  for (int k = 0; k < e.ndom; k++) {
-    const DomainHost& D = e.dom[k];
-    const Dims d{D.xs, D.xe, D.ys, D.ye, D.W, D.H};
-    for (int side = 0; side < 2; side++)
-      launch_ens_df_tiles(e.dfreg + D.off, d, k, side, e.dfx[side], e.dfcount, st);
-  }
-  int cnt[2] = {0, 0};
-  if (!ck(cudaGetLastError()) ||
-      !ck(cudaMemcpyAsync(cnt, e.dfcount, sizeof cnt, cudaMemcpyDeviceToHost, st)) ||
-      !ck(cudaStreamSynchronize(st)))
-    return false;
-  e.dfxn[0] = cnt[0];
-  e.dfxn[1] = cnt[1];
+  if (!ck(cudaGetLastError()) || !ck(cudaStreamSynchronize(st))) return false;
   cudaFree(e.d_dfdesc);
   cudaFree(e.d_dfunits);
+  cudaFree(e.dfring);
   e.d_dfdesc = nullptr;
   e.d_dfunits = nullptr;
+  e.dfring = nullptr;
   if (!ck(cudaMalloc(&e.d_dfdesc, sizeof(EnsDfDomain) * e.ndom)) ||
       !ck(cudaMalloc(&e.d_dfunits, sizeof(int4) * units.size())) ||
+      !ck(cudaMalloc(&e.dfring, sizeof(int2) * std::max<size_t>(1, ring.size()))) ||
       !ck(cudaMemcpy(e.d_dfdesc, desc.data(), sizeof(EnsDfDomain) * e.ndom,
                      cudaMemcpyHostToDevice)) ||
       !ck(cudaMemcpy(e.d_dfunits, units.data(), sizeof(int4) * units.size(),
+                     cudaMemcpyHostToDevice)) ||
+      !ck(cudaMemcpy(e.dfring, ring.data(), sizeof(int2) * ring.size(),
                      cudaMemcpyHostToDevice)))
     return false;
   e.ndfunits = (int)units.size();
+  e.ndfring = (int)ring.size();
   e.dk = make_df_const(e.sc, domain_metrics(e.dom[0], e.sc));
-  launch_ens_df_exact(0, 0, nullptr, nullptr, 0, nullptr, st);  // kernel attributes
-  return ck(cudaGetLastError());
+  return true;
 }
 
 // FP64 state of every domain back to rest.
@@ -875,6 +868,7 @@ int nl2d_ens_set_domain(int dom, const int* tmask, const double* ht, const doubl
   if (dom < 0 || dom >= e.ndom || !tmask || !ht || !hu || !hv) return NL2D_ERR_ARGS;
   DomainHost& D = e.dom[dom];
   if (!mask_ok(D, tmask)) return NL2D_ERR_ARGS;
+  D.ring = ring_cells(D, tmask);
   const size_t n = (size_t)D.W * D.H;
   for (size_t t = 0; t < n; t++)
     if (!(hu[t] > 0.0) || !(hv[t] > 0.0)) return NL2D_ERR_ARGS;
@@ -1000,13 +994,14 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
           k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
                                                                             sums);
       } else if (e.precision == 2) {
-        // exact tiles on the side stream beside the march: both read the
-        // same state buffers and write disjoint cells
+        // the exact cells on the side stream beside the march: both read
+        // the same state buffers and write disjoint cells
         const double* tq = e.d_tides + (size_t)q * e.ndom;
         cudaEventRecord(e.fork, e.stream);
         cudaStreamWaitEvent(e.side, e.fork, 0);
-        launch_ens_df_exact(0, e.dfxn[0], e.d_desc, e.dfx[0], par, tq, e.side);
-        launch_ens_df_exact(1, e.dfxn[1], e.d_desc, e.dfx[1], par, tq, e.side);
+        if (e.ndfring > 0)
+          k_ensemble_df_ring<<<(e.ndfring + 127) / 128, 128, 0, e.side>>>(e.d_desc, e.dfring,
+                                                                          e.ndfring, par, tq);
         launch_ens_df_march(e.d_dfdesc, e.d_dfunits, e.ndfunits, par, e.dk, e.march_rows,
                             e.stream);
         cudaEventRecord(e.join, e.side);

@@ -72,6 +72,82 @@ struct Ctx {
   __device__ __forceinline__ bool in_copy(int i, int j) const {
     return i >= d.xs - 1 && i <= d.xe + 1 && j >= d.ys - 1 && j <= d.ye;
   }
+  // sshn_u / sshn_v this step sees at face (i,j)
+  __device__ __forceinline__ double su(int i, int j) const { return su_tile[slot(i, j)]; }
+  __device__ __forceinline__ double sv(int i, int j) const { return sv_tile[slot(i, j)]; }
+};
+
+// next_sshu_code / next_sshv_code (time_update_kern.c:90-155) at face
+// (i,j) over their loop ranges; faces outside them keep the stored value.
+// The tile stages these in shared memory (phase 0 of fused_tile); the
+// general pass without a tile computes them where it reads them.
+__device__ __forceinline__ bool next_sshu_at(const int* __restrict__ m,
+                                             const double* __restrict__ sn, const Dims& d,
+                                             const FastConst& k, int i, int j, double& su) {
+  if (!(j >= d.ys && j <= d.ye && i >= d.xs && i <= d.xe - 1)) return false;
+  const int c = j * d.width + i, n = c + 1, mm = m[c], mn = m[n];
+  if (mm + mn <= 0) return false;
+  if (mm * mn > 0) {
+    double rtmp1 = k.area_t * sn[c] + k.area_t * sn[n];
+    su = dvc(half(rtmp1), k.area_u, k.r_area_u, k.fast_div);
+  } else if (mm <= 0) {
+    su = sn[n];
+  } else {
+    su = sn[c];
+  }
+  return true;
+}
+__device__ __forceinline__ bool next_sshv_at(const int* __restrict__ m,
+                                             const double* __restrict__ sn, const Dims& d,
+                                             const FastConst& k, int i, int j, double& sv) {
+  if (!(j >= d.ys && j <= d.ye - 1 && i >= d.xs && i <= d.xe)) return false;
+  const int c = j * d.width + i, n = c + d.width, mm = m[c], mn = m[n];
+  if (mm + mn <= 0) return false;
+  if (mm * mn > 0) {
+    double rtmp1 = k.area_t * sn[c] + k.area_t * sn[n];
+    sv = dvc(half(rtmp1), k.area_v, k.r_area_v, k.fast_div);
+  } else if (mm <= 0) {
+    sv = sn[n];
+  } else {
+    sv = sn[c];
+  }
+  return true;
+}
+
+// The general pass's context without a tile: every input read from the
+// domain's arrays in global memory (the members refer to the domain's
+// descriptor, so no thread holds a copy of it), sshn_u / sshn_v computed
+// where they are read.  Valid for the faces a copy-region cell's general
+// update reads, all of which lie inside the array.
+struct GlobalCtx {
+  const double* const& sn;  // the state buffers read this step
+  const double* const& un;
+  const double* const& vn;
+  double* const& hu;  // the domain's Fields
+  double* const& hv;
+  double* const& ht;
+  double* const& ssha_u;
+  double* const& ssha_v;
+  double* const& r_hu;
+  double* const& r_hv;
+  int* const& m;
+  double* const& sshn_u;
+  double* const& sshn_v;
+  const int& W;
+  const Dims& d;
+  const FastConst& k;
+
+  __device__ __forceinline__ bool in_copy(int i, int j) const {
+    return i >= d.xs - 1 && i <= d.xe + 1 && j >= d.ys - 1 && j <= d.ye;
+  }
+  __device__ __forceinline__ double su(int i, int j) const {
+    double v;
+    return next_sshu_at(m, sn, d, k, i, j, v) ? v : sshn_u[j * W + i];
+  }
+  __device__ __forceinline__ double sv(int i, int j) const {
+    double v;
+    return next_sshv_at(m, sn, d, k, i, j, v) ? v : sshn_v[j * W + i];
+  }
 };
 
 // (0.5 - copysign(0.5, w)) * p and (0.5 + copysign(0.5, w)) * p alone (the
@@ -95,8 +171,8 @@ __device__ __forceinline__ double hi_only(double w, double p) {
 // range, with the masked (slip-wall) branches; returns false where the
 // kernel returns early (ua keeps its value).  Same operations as the
 // reference, with the exact helpers for halving, upwind picks and division.
-template <int SX>
-__device__ __forceinline__ bool mom_u(const Ctx<SX>& x, int i, int j, double& out) {
+template <class X>
+__device__ __forceinline__ bool mom_u(const X& x, int i, int j, double& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             se = s + 1, ne = n + 1;
   const int* m = x.m;
@@ -104,10 +180,9 @@ __device__ __forceinline__ bool mom_u(const Ctx<SX>& x, int i, int j, double& ou
   if (m[c] <= 0 || m[e] <= 0) return false;
   const double *un = x.un, *vn = x.vn, *hu = x.hu, *hv = x.hv, *ht = x.ht, *sn = x.sn;
   const FastConst& k = x.k;
-  const int t = x.slot(i, j);
-  const double su_c = x.su_tile[t], su_s = x.su_tile[t - SX], su_n = x.su_tile[t + SX];
-  const double sv_s = x.sv_tile[t - SX], sv_se = x.sv_tile[t - SX + 1], sv_c = x.sv_tile[t],
-               sv_e = x.sv_tile[t + 1];
+  const double su_c = x.su(i, j), su_s = x.su(i, j - 1), su_n = x.su(i, j + 1);
+  const double sv_s = x.sv(i, j - 1), sv_se = x.sv(i + 1, j - 1), sv_c = x.sv(i, j),
+               sv_e = x.sv(i + 1, j);
 
   double u_e = half(un[c] + un[e]) * k.dy_t;
   double depe = ht[e] + sn[e];
@@ -149,8 +224,8 @@ __device__ __forceinline__ bool mom_u(const Ctx<SX>& x, int i, int j, double& ou
 }
 
 // momentum_v_code (momentum_v_kern.c:125-241) at v face (i,j).
-template <int SX>
-__device__ __forceinline__ bool mom_v(const Ctx<SX>& x, int i, int j, double& out) {
+template <class X>
+__device__ __forceinline__ bool mom_v(const X& x, int i, int j, double& out) {
   const int W = x.W, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             nw = n - 1, ne = n + 1;
   const int* m = x.m;
@@ -158,10 +233,9 @@ __device__ __forceinline__ bool mom_v(const Ctx<SX>& x, int i, int j, double& ou
   if (m[c] <= 0 || m[n] <= 0) return false;
   const double *un = x.un, *vn = x.vn, *hu = x.hu, *hv = x.hv, *ht = x.ht, *sn = x.sn;
   const FastConst& k = x.k;
-  const int t = x.slot(i, j);
-  const double su_w = x.su_tile[t - 1], su_nw = x.su_tile[t + SX - 1], su_c = x.su_tile[t],
-               su_n = x.su_tile[t + SX];
-  const double sv_c = x.sv_tile[t], sv_w = x.sv_tile[t - 1], sv_e = x.sv_tile[t + 1];
+  const double su_w = x.su(i - 1, j), su_nw = x.su(i - 1, j + 1), su_c = x.su(i, j),
+               su_n = x.su(i, j + 1);
+  const double sv_c = x.sv(i, j), sv_w = x.sv(i - 1, j), sv_e = x.sv(i + 1, j);
 
   double v_n = half(vn[c] + vn[n]) * k.dx_t;
   double depn = ht[n] + sn[n];
@@ -205,8 +279,8 @@ __device__ __forceinline__ bool mom_v(const Ctx<SX>& x, int i, int j, double& ou
 // ua at u face (i,j) after momentum_u and bc_solid_u, before Flather: the
 // value bc_flather_u reads.  On the copy region the previous step's ua is
 // the current un; elsewhere it is the ua array, which no fused step changes.
-template <int SX>
-__device__ __forceinline__ double ua_pre_flather(const Ctx<SX>& x, const double* ua_arr,
+template <class X>
+__device__ __forceinline__ double ua_pre_flather(const X& x, const double* ua_arr,
                                                  int i, int j) {
   const int c = j * x.W + i;
   double ua = x.in_copy(i, j) ? x.un[c] : ua_arr[c];
@@ -220,8 +294,8 @@ __device__ __forceinline__ double ua_pre_flather(const Ctx<SX>& x, const double*
   return ua;
 }
 
-template <int SX>
-__device__ __forceinline__ double va_pre_flather(const Ctx<SX>& x, const double* va_arr,
+template <class X>
+__device__ __forceinline__ double va_pre_flather(const X& x, const double* va_arr,
                                                  int i, int j) {
   const int c = j * x.W + i;
   double va = x.in_copy(i, j) ? x.vn[c] : va_arr[c];
@@ -233,6 +307,65 @@ __device__ __forceinline__ double va_pre_flather(const Ctx<SX>& x, const double*
       x.m[c] * x.m[c + x.W] == 0)
     va = 0.0;  // bc_solid_v
   return va;
+}
+
+// A copy-region cell's update by the reference's per-point code, in its
+// order: sea-surface height (continuity_kern.c:90-117, then bc_ssh), u at
+// the east face (momentum_u, bc_solid_u, bc_flather_u), v at the north face
+// (momentum_v, bc_solid_v, bc_flather_v).  x supplies the fields and the
+// sshn_u / sshn_v this step sees (a tile's shared memory, or global memory).
+template <class X>
+__device__ __forceinline__ void general_cell(const X& x, const Fields& f, const FusedState& fs,
+                                             const Scalars& p, double tide, int i, int j) {
+  const int W = x.W;
+  const Dims& d = x.d;
+  const FastConst& k = x.k;
+  const int* __restrict__ m = x.m;
+  const double* __restrict__ sn = x.sn;
+  const double* __restrict__ un = x.un;
+  const double* __restrict__ vn = x.vn;
+  const int c = j * W + i;
+
+  double ssh = sn[c];
+  if (i >= d.xs && i <= d.xe && j >= d.ys && j <= d.ye) {
+    const int w = c - 1, s = c - W;
+    double r1 = (x.su(i, j) + f.hu[c]) * un[c];
+    double r2 = (x.su(i - 1, j) + f.hu[w]) * un[w];
+    double r3 = (x.sv(i, j) + f.hv[c]) * vn[c];
+    double r4 = (x.sv(i, j - 1) + f.hv[s]) * vn[s];
+    ssh = sn[c] + dvc((r2 - r1 + r4 - r3) * k.rdt, k.area_t, k.r_area_t, k.fast_div);
+    if (m[c] > 0 && (m[c - W] < 0 || m[c + W] < 0 || m[c + 1] < 0 || m[c - 1] < 0))
+      ssh = tide;
+  }
+  fs.sshn_out[c] = ssh;
+
+  double ua = un[c];
+  if (i <= d.xe) {  // u whole range [xs-1, xe] x [ys-1, ye+1] (tiling gives the rest)
+    ua = ua_pre_flather(x, f.ua, i, j);
+    if (m[c] + m[c + 1] > -1) {
+      if (m[c] < 0) {
+        ua = ua_pre_flather(x, f.ua, i + 1, j) +
+             sqrt(p.g / f.hu[c]) * (x.su(i, j) - x.su(i + 1, j));
+      } else if (m[c + 1] < 0 && i >= 1) {  // i == 0 would read outside the array
+        ua = ua_pre_flather(x, f.ua, i - 1, j) +
+             sqrt(p.g / f.hu[c]) * (x.su(i, j) - x.su(i - 1, j));
+      }
+    }
+  }
+  fs.un_out[c] = ua;
+
+  // the copy region is exactly the v whole range [xs-1, xe+1] x [ys-1, ye]
+  double va = va_pre_flather(x, f.va, i, j);
+  if (m[c] + m[c + W] > -1) {
+    if (m[c] < 0) {
+      va = va_pre_flather(x, f.va, i, j + 1) +
+           sqrt(p.g / f.hv[c]) * (x.sv(i, j) - x.sv(i, j + 1));
+    } else if (m[c + W] < 0 && j >= 1) {
+      va = va_pre_flather(x, f.va, i, j - 1) +
+           sqrt(p.g / f.hv[c]) * (x.sv(i, j) - x.sv(i, j - 1));
+    }
+  }
+  fs.vn_out[c] = va;
 }
 
 // Shared-memory layout of one tile.  Phase 0 (halo 2) holds the loaded
@@ -511,75 +644,27 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
   // ---- general cells: the reference's per-point code, in its order ----
   const int ngen = *gcount;
   for (int g = tid; g < ngen; g += NTHREADS) {
-  const int row = glist[g] / TX, col = glist[g] - (glist[g] / TX) * TX;
-  const int i = i0 + col, j = j0 + row;
-  const int c = j * W + i;
-  const int q = (row + HALO) * SX + (col + HALO);
-  double* su_tile = &A(A_SU, 0);
-  double* sv_tile = &A(A_SV, 0);
-  Ctx<SX> x;
-  x.sn = sn;
-  x.un = un;
-  x.vn = vn;
-  x.hu = f.hu;
-  x.hv = f.hv;
-  x.ht = f.ht;
-  x.ssha_u = f.ssha_u;
-  x.ssha_v = f.ssha_v;
-  x.r_hu = f.r_hu;
-  x.r_hv = f.r_hv;
-  x.m = m;
-  x.su_tile = su_tile;
-  x.sv_tile = sv_tile;
-  x.W = W;
-  x.i0 = i0;
-  x.j0 = j0;
-  x.d = d;
-  x.k = k;
-
-  // sea-surface height at T (continuity_kern.c:90-117, then bc_ssh)
-  double ssh = sn[c];
-  if (i >= d.xs && i <= d.xe && j >= d.ys && j <= d.ye) {
-    const int w = c - 1, s = c - W;
-    double r1 = (su_tile[q] + f.hu[c]) * un[c];
-    double r2 = (su_tile[q - 1] + f.hu[w]) * un[w];
-    double r3 = (sv_tile[q] + f.hv[c]) * vn[c];
-    double r4 = (sv_tile[q - SX] + f.hv[s]) * vn[s];
-    ssh = sn[c] + dvc((r2 - r1 + r4 - r3) * k.rdt, k.area_t, k.r_area_t, k.fast_div);
-    if (m[c] > 0 && (m[c - W] < 0 || m[c + W] < 0 || m[c + 1] < 0 || m[c - 1] < 0))
-      ssh = tide;
-  }
-  fs.sshn_out[c] = ssh;
-
-  // u at the east face (momentum_u, bc_solid_u, bc_flather_u)
-  double ua = un[c];
-  if (i <= d.xe) {  // u whole range [xs-1, xe] x [ys-1, ye+1] (tiling gives the rest)
-    ua = ua_pre_flather(x, f.ua, i, j);
-    if (m[c] + m[c + 1] > -1) {
-      if (m[c] < 0) {
-        ua = ua_pre_flather(x, f.ua, i + 1, j) +
-             sqrt(p.g / f.hu[c]) * (su_tile[q] - su_tile[q + 1]);
-      } else if (m[c + 1] < 0 && i >= 1) {  // i == 0 would read outside the array
-        ua = ua_pre_flather(x, f.ua, i - 1, j) +
-             sqrt(p.g / f.hu[c]) * (su_tile[q] - su_tile[q - 1]);
-      }
-    }
-  }
-  fs.un_out[c] = ua;
-
-  // v at the north face (momentum_v, bc_solid_v, bc_flather_v); the copy
-  // region is exactly the v whole range [xs-1, xe+1] x [ys-1, ye].
-  double va = va_pre_flather(x, f.va, i, j);
-  if (m[c] + m[c + W] > -1) {
-    if (m[c] < 0) {
-      va = va_pre_flather(x, f.va, i, j + 1) +
-           sqrt(p.g / f.hv[c]) * (sv_tile[q] - sv_tile[q + SX]);
-    } else if (m[c + W] < 0 && j >= 1) {
-      va = va_pre_flather(x, f.va, i, j - 1) +
-           sqrt(p.g / f.hv[c]) * (sv_tile[q] - sv_tile[q - SX]);
-    }
-  }
-  fs.vn_out[c] = va;
+    const int row = glist[g] / TX, col = glist[g] - (glist[g] / TX) * TX;
+    Ctx<SX> x;
+    x.sn = sn;
+    x.un = un;
+    x.vn = vn;
+    x.hu = f.hu;
+    x.hv = f.hv;
+    x.ht = f.ht;
+    x.ssha_u = f.ssha_u;
+    x.ssha_v = f.ssha_v;
+    x.r_hu = f.r_hu;
+    x.r_hv = f.r_hv;
+    x.m = m;
+    x.su_tile = &A(A_SU, 0);
+    x.sv_tile = &A(A_SV, 0);
+    x.W = W;
+    x.i0 = i0;
+    x.j0 = j0;
+    x.d = d;
+    x.k = k;
+    general_cell(x, f, fs, p, tide, i0 + col, j0 + row);
   }  // general cells
 #undef A
 #undef B

@@ -129,12 +129,6 @@ void launch_ens_df_march(const EnsDfDomain* doms, const int4* units, int nunits,
 // domain (tmask and reg point at the domain's first element).
 void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st);
 void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st);
-// Appends to `list` the exact tiles of one ensemble domain (side 0 the
-// kDfRowsTX x kDfRowsTY tiles, side 1 the side-strip kDfColsTX x kDfColsTY
-// tiles, as (dom, i0, j0)), counting them in count[side]; returns how many
-// tiles of that shape the domain has (list == nullptr: only that).
-int launch_ens_df_tiles(const unsigned char* reg, const Dims& d, int dom, int side, int4* list,
-                        int* count, cudaStream_t st);
 // The fused FP64 tile kernel on the listed tiles of both shapes, leaving
 // the march's cells alone.  ff == nullptr: only sets the kernels' shared-
 // memory attributes (call outside any capture).
