@@ -17,8 +17,8 @@
 // Three forms share the domain layout: FP64 (the tiles above), mixed
 // precision (its own FP32 / compensated state), and FP64-equivalent, which
 // keeps the FP64 state and runs the double-float column march (nl2d_df.cu)
-// over every domain's interior while the fused step's general per-cell code,
-// in exact FP64, takes every other cell, on a second stream.
+// over every domain's interior while, in the same launch, the fused step's
+// general per-cell code takes every other cell in exact FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/nl2d_gpu.h"
+#include "nl2d_df_march.cuh"
 #include "nl2d_fused_tile.cuh"
 #include "nl2d_mixed_march.cuh"
 
@@ -108,25 +109,48 @@ __global__ void __launch_bounds__(NTHREADS, T::kMinBlocks)
   }
 }
 
-// The FP64-equivalent form's exact part: every copy-region cell the
+// The FP64-equivalent form's exact part: a copy-region cell the
 // double-float march does not write (the ring of boundary rows and columns,
-// and cells beside land), one thread each, by the fused step's general
-// per-cell code reading the domain's arrays in global memory.  Entry g of
-// `cells` is (domain, cell index); the result is the FP64 step's, bit for
-// bit, with that domain's tide.
-__global__ void __launch_bounds__(128)
-    k_ensemble_df_ring(const EnsDomain* __restrict__ doms, const int2* __restrict__ cells,
-                       int ncells, int parity, const double* __restrict__ tides) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ncells) return;
-  const int2 e = cells[g];
+// and cells beside land), given as (domain, cell index), by the fused step's
+// general per-cell code reading the domain's arrays in global memory.  The
+// result is the FP64 step's, bit for bit, with that domain's tide.
+__device__ __forceinline__ void ring_cell(const EnsDomain* __restrict__ doms, int2 e, int parity,
+                                          const double* __restrict__ tides) {
   const EnsDomain& D = doms[e.x];
   const FusedState& st = D.fs[parity];
-  const GlobalCtx x{st.sshn_in, st.un_in,    st.vn_in,  D.f.hu,     D.f.hv,     D.f.ht,
-                    D.f.ssha_u, D.f.ssha_v,  D.f.r_hu,  D.f.r_hv,   D.f.tmask,  D.f.sshn_u,
-                    D.f.sshn_v, D.d.width,   D.d,       D.k};
+  const GlobalCtx x{st.sshn_in, st.un_in,   st.vn_in, D.f.hu,    D.f.hv,    D.f.ht,
+                    D.f.ssha_u, D.f.ssha_v, D.f.r_hu, D.f.r_hv,  D.f.tmask, D.f.sshn_u,
+                    D.f.sshn_v, D.d.width,  D.d,      D.k};
   const int j = e.y / D.d.width, i = e.y - j * D.d.width;
   general_cell(x, D.f, st, D.p, tides[e.x], i, j);
+}
+
+// One launch per step of the FP64-equivalent form.  A block takes one of two
+// roles: a march block runs four warps' (domain, i0, j0) units of the
+// double-float column march (nl2d_df_march.cuh); a ring block runs 128 exact
+// cells, one per thread.  The nring ring blocks are spread evenly through the
+// grid (block b is one when floor((b+1) nring / grid) > floor(b nring /
+// grid)), so both kinds share every SM: the march issues on the FP32 and
+// integer pipes while the exact cells wait on the FP64 pipe.  Both read the
+// state buffers of this parity and write disjoint cells.
+__global__ void __launch_bounds__(32 * dfm::WARPS, 3)
+    k_ensemble_df_step(const EnsDfDomain* __restrict__ ddoms, const int4* __restrict__ units,
+                       int nunits, const EnsDomain* __restrict__ doms,
+                       const int2* __restrict__ cells, int ncells, int nring, int parity,
+                       DfConst k, int mr, const double* __restrict__ tides) {
+  const long long grid = gridDim.x, b = blockIdx.x;
+  const int q0 = (int)(b * nring / grid), q1 = (int)((b + 1) * nring / grid);
+  if (q1 > q0) {  // ring block q0
+    const int g = q0 * (32 * dfm::WARPS) + (int)threadIdx.x;
+    if (g < ncells) ring_cell(doms, cells[g], parity, tides);
+    return;
+  }
+  // march block b - q0: q0 ring blocks precede it
+  const int w = (int)(b - q0) * dfm::WARPS + (int)(threadIdx.x >> 5);
+  if (w >= nunits) return;  // the whole warp leaves together
+  const int4 u = units[w];
+  const EnsDfDomain& D = ddoms[u.x];
+  dfm::df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
 }
 
 // The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
@@ -994,18 +1018,12 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
           k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
                                                                             sums);
       } else if (e.precision == 2) {
-        // the exact cells on the side stream beside the march: both read
-        // the same state buffers and write disjoint cells
-        const double* tq = e.d_tides + (size_t)q * e.ndom;
-        cudaEventRecord(e.fork, e.stream);
-        cudaStreamWaitEvent(e.side, e.fork, 0);
-        if (e.ndfring > 0)
-          k_ensemble_df_ring<<<(e.ndfring + 127) / 128, 128, 0, e.side>>>(e.d_desc, e.dfring,
-                                                                          e.ndfring, par, tq);
-        launch_ens_df_march(e.d_dfdesc, e.d_dfunits, e.ndfunits, par, e.dk, e.march_rows,
-                            e.stream);
-        cudaEventRecord(e.join, e.side);
-        cudaStreamWaitEvent(e.stream, e.join, 0);
+        constexpr int B = 32 * dfm::WARPS;
+        const int nring = (e.ndfring + B - 1) / B;
+        const int nmarch = (e.ndfunits + dfm::WARPS - 1) / dfm::WARPS;
+        k_ensemble_df_step<<<nring + nmarch, B, 0, e.stream>>>(
+            e.d_dfdesc, e.d_dfunits, e.ndfunits, e.d_desc, e.dfring, e.ndfring, nring, par, e.dk,
+            e.march_rows, e.d_tides + (size_t)q * e.ndom);
         par = 1 - par;
         if (want_sums)
           k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,

@@ -122,9 +122,6 @@ constexpr int kDfMarchCols = 30;  // columns one warp of the march updates
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
 void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
                      cudaStream_t st);
-// The ensemble's march over (domain, i0, j0) units of march_rows rows.
-void launch_ens_df_march(const EnsDfDomain* doms, const int4* units, int nunits, int parity,
-                         const DfConst& k, int march_rows, cudaStream_t st);
 // Split of one packed FP64 array into (hi, lo) pairs; the march flags of one
 // domain (tmask and reg point at the domain's first element).
 void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st);
