@@ -76,10 +76,13 @@ def parse():
     ap.add_argument("--emu-horizon", type=int, default=5000,
                     help="solver steps of the emulator's trajectories and roll-out")
     ap.add_argument("--case", default=None,
-                    choices=["fused", "fused_active", "mixed", "df", "tra_adv", "emu", "rates"],
+                    choices=["fused", "fused_active", "mixed", "df", "tra_adv", "emu", "rates",
+                             "ensemble", "ensemble_mixed", "ensemble_df"],
                     help="run one small case of one kernel family and print its device time "
                          "(for profiler captures; prints no bench line)")
     ap.add_argument("--batch", type=int, default=24, help="--case emu: images of 256^2")
+    ap.add_argument("--domains", type=int, default=512,
+                    help="--case ensemble*: the first N domains of the 512-domain draw")
     return ap.parse_args()
 
 
@@ -975,6 +978,18 @@ def run_case(args):
         if rc or lib.tra_adv_last_error(buf, 256):
             raise RuntimeError("tra_adv: %s" % buf.value.decode())
         lib.tra_adv_finalize()
+    elif args.case in ("ensemble", "ensemble_mixed", "ensemble_df"):
+        # the first --domains domains of run_ensemble's 512-domain draw on
+        # the default schedule, in the case's form
+        from psyclonebench_gb300.ensemble import Ensemble, build_domain
+        from psyclonebench_gb300.workloads import ensemble_domains
+        specs = ensemble_domains(512, 7)[:max(1, min(512, args.domains))]
+        ens = Ensemble([build_domain(sp) for sp in specs], lib=lib)
+        ens.set_precision({"ensemble_mixed": 1, "ensemble_df": 2}.get(args.case, 0))
+        ens.run(1, 1 + args.warmup)
+        ms.value, _ = ens.run(2 + args.warmup, args.steps)
+        out["cells"] = ens.info()[0]
+        ens.close()
     elif args.case == "rates":
         rates = (ctypes.c_double * 4)()
         P.check(lib.nl2d_measure_pipe_rates(rates), "pipe rates")
