@@ -155,8 +155,7 @@ void free_device() {
     s.mix_count = nullptr;
     for (float2* a : {s.dfs.ht, s.dfs.hu, s.dfs.hv, s.dfs.rhu, s.dfs.rhv}) cudaFree(a);
     cudaFree(s.dfs.reg);
-    cudaFree(s.dfs.tiles_rows);
-    cudaFree(s.dfs.tiles_cols);
+    cudaFree(s.dfs.ring);
     cudaFree(s.dfs.count);
     s.dfs = DfFields{};
     s.df_valid = false;
@@ -784,18 +783,8 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
   fs.un_out = nxt ? s.shadow[1] : s.dev.un;
   fs.vn_out = nxt ? s.shadow[2] : s.dev.vn;
   if (s.precision == 2) {
-    // Interior cells in double-float, the others in exact FP64; both read
-    // the same buffers and write disjoint cells.  The exact tiles (a few
-    // hundred CTAs, each a long FP64 chain on one SM) start first on the
-    // high-priority side stream and run beside the march's waves instead of
-    // after them.
-    CK(cudaEventRecord(s.df_fork, s.stream));
-    CK(cudaStreamWaitEvent(s.side, s.df_fork, 0));
-    launch_fused_boundary(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, &s.dfs,
-                          s.side);
-    launch_df_march(fs, s.dfs, dims(), make_df_const(s.sc, s.um), s.stream);
-    CK(cudaEventRecord(s.df_join, s.side));
-    CK(cudaStreamWaitEvent(s.stream, s.df_join, 0));
+    // interior cells in double-float, the others in exact FP64, one launch
+    launch_df_step(s.dev, fs, dims(), s.sc, s.um, s.dfs, tide, tide_table, tide_index, s.stream);
   } else {
     launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
   }
@@ -803,44 +792,36 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
 }
 
 // The FP64-equivalent form's static arrays (split depths and reciprocal
-// denominators, march flags, boundary tiles), made from the current FP64
-// arrays unless they already are.
+// denominators, march flags, the exact cells' list), made from the current
+// FP64 arrays unless they already are.
 bool ensure_df() {
   State& s = g_state;
   if (s.df_valid) return true;
   const Registration& r = s.reg;
   const size_t n = (size_t)r.width * r.height;
-  const int nx = r.xe - r.xs + 3, ny = r.ye - r.ys + 2;
-  const size_t nrows = (size_t)((nx + kDfRowsTX - 1) / kDfRowsTX) *
-                       ((ny + kDfRowsTY - 1) / kDfRowsTY);
-  const size_t ncols = (size_t)((nx + kDfColsTX - 1) / kDfColsTX) *
-                       ((ny + kDfColsTY - 1) / kDfColsTY);
   if (!s.dfs.ht) {
     float2** arrs[5] = {&s.dfs.ht, &s.dfs.hu, &s.dfs.hv, &s.dfs.rhu, &s.dfs.rhv};
     for (float2** a : arrs)
       if (!CK(cudaMalloc(a, n * sizeof(float2)))) return false;
-    if (!CK(cudaMalloc(&s.dfs.reg, n)) ||
-        !CK(cudaMalloc(&s.dfs.tiles_rows, nrows * sizeof(int))) ||
-        !CK(cudaMalloc(&s.dfs.tiles_cols, ncols * sizeof(int))) ||
-        !CK(cudaMalloc(&s.dfs.count, 2 * sizeof(int))))
+    if (!CK(cudaMalloc(&s.dfs.reg, n)) || !CK(cudaMalloc(&s.dfs.count, sizeof(int))))
       return false;
   }
-  if (!ensure_side() ||
-      (!s.df_fork && (!CK(cudaEventCreateWithFlags(&s.df_fork, cudaEventDisableTiming)) ||
-                      !CK(cudaEventCreateWithFlags(&s.df_join, cudaEventDisableTiming)))))
-    return false;
-  launch_df_setup(s.dev, dims(), s.dfs, s.stream);
-  // the boundary kernels' shared-memory opt-in, outside any capture
-  launch_fused_boundary(s.dev, FusedState{}, dims(), s.sc, s.um, 0.0, nullptr, 0, nullptr,
-                        s.stream);
-  int counts[2] = {0, 0};
-  if (!CK(cudaGetLastError()) ||
-      !CK(cudaMemcpyAsync(counts, s.dfs.count, sizeof counts, cudaMemcpyDeviceToHost,
-                          s.stream)) ||
-      !CK(cudaStreamSynchronize(s.stream)))
-    return false;
-  s.dfs.n_rows = counts[0];
-  s.dfs.n_cols = counts[1];
+  // two passes: count the exact cells, then list them
+  cudaFree(s.dfs.ring);
+  s.dfs.ring = nullptr;
+  for (int pass = 0; pass < 2; pass++) {
+    launch_df_setup(s.dev, dims(), s.dfs, s.stream);
+    int count = 0;
+    if (!CK(cudaGetLastError()) ||
+        !CK(cudaMemcpyAsync(&count, s.dfs.count, sizeof count, cudaMemcpyDeviceToHost,
+                            s.stream)) ||
+        !CK(cudaStreamSynchronize(s.stream)))
+      return false;
+    if (pass == 1 && count != s.dfs.n_ring) return false;
+    s.dfs.n_ring = count;
+    if (pass == 0 && !CK(cudaMalloc(&s.dfs.ring, sizeof(int) * std::max(1, count))))
+      return false;
+  }
   invalidate_graph();
   s.df_valid = true;
   return true;

@@ -13,8 +13,10 @@
 // neighbourhood is wet and that lie one cell inside next_ssh's ranges, so
 // every face they read takes next_ssh's two-sided formula and no momentum
 // mask, bc_ssh, solid-wall or Flather rule applies.  Every other cell of the
-// copy region is computed in exact FP64 by the fused tile kernel, launched
-// on the tiles that hold such cells (nl2d_fused.cu).
+// copy region (the exact cells) is computed in exact FP64 by the fused
+// step's general per-cell code reading global memory (general_cell with a
+// GlobalCtx, nl2d_fused_tile.cuh), one thread each, by blocks of the same
+// launch spread evenly among the march's blocks.
 //
 // Loads split each FP64 state value into a pair from its bit pattern
 // (split_bits; the depths and the reciprocal momentum denominators are split
@@ -22,6 +24,7 @@
 // them in FP64 (join_bits): one FP64 instruction per stored value, none per
 // loaded one.
 #include "nl2d_df_march.cuh"
+#include "nl2d_fused_tile.cuh"
 
 namespace nl2d {
 using namespace dfk;
@@ -30,9 +33,36 @@ namespace {
 using namespace dfm;
 constexpr int MR = 32;
 
+// One step.  Of the grid's blocks, nring take the exact cells (128 each,
+// one per thread; block b is one when floor((b+1) nring / grid) >
+// floor(b nring / grid)), so that they spread evenly among the march's
+// blocks and share the SMs with them: the march issues on the FP32 and
+// integer pipes, the exact cells wait on the FP64 pipe.  The others march
+// strips of mr rows over ncol column groups.  Both read the state buffers
+// of fs and write disjoint cells.
 __global__ void __launch_bounds__(32 * WARPS, 3)
-    k_df_march(FusedState fs, DfFields ff, Dims d, DfConst k, int ncol, int nwarps, int mr) {
-  const int warp = blockIdx.x * WARPS + (int)(threadIdx.x >> 5);
+    k_df_step(const __grid_constant__ FusedState fs, const __grid_constant__ DfFields ff,
+              const __grid_constant__ Dims d, const __grid_constant__ DfConst k, int ncol,
+              int nwarps, int mr, const __grid_constant__ Fields f,
+              const __grid_constant__ Scalars p, const __grid_constant__ FastConst fk,
+              const double* __restrict__ tide_table, int tide_index, double tide, int nring) {
+  const long long grid = gridDim.x, b = blockIdx.x;
+  const int q0 = (int)(b * nring / grid), q1 = (int)((b + 1) * nring / grid);
+  if (q1 > q0) {  // exact-cell block q0
+    const int g = q0 * (32 * WARPS) + (int)threadIdx.x;
+    if (g < ff.n_ring) {
+      const int c = ff.ring[g];
+      const int j = c / d.width, i = c - j * d.width;
+      const GlobalCtx x{fs.sshn_in, fs.un_in,    fs.vn_in, f.hu,      f.hv,
+                        f.ht,       f.ssha_u,    f.ssha_v, f.r_hu,    f.r_hv,
+                        f.tmask,    f.sshn_u,    f.sshn_v, d.width,   d,
+                        fk};
+      general_cell(x, f, fs, p, tide_table ? tide_table[tide_index] : tide, i, j);
+    }
+    return;
+  }
+  // march block b - q0: q0 exact-cell blocks precede it
+  const int warp = (int)(b - q0) * WARPS + (int)(threadIdx.x >> 5);
   if (warp >= nwarps) return;  // the whole warp leaves together
   const int gy = warp / ncol, gx = warp - gy * ncol;
   df_march(fs, ff, d, k, d.xs - 1 + gx * MW, d.ys - 1 + gy * mr, mr);
@@ -68,31 +98,22 @@ __global__ void k_df_flags(const int* __restrict__ m, Dims d, unsigned char* __r
   }
 }
 
-// Appends to `list` every tile of a tx x ty grid over the copy region
-// (row-major, ntx tiles per row) that holds a cell of its kind the march
-// does not write: side 1 the side strips (columns xs-1, xs, xe, xe+1 of
-// rows ys+1 .. ye-1), side 0 every other such cell.  The two kinds cover
-// every copy-region cell the march leaves; the order of the list does not
-// matter (each tile writes its own cells).
-__device__ __forceinline__ bool tile_has_work(const unsigned char* __restrict__ reg,
-                                              const Dims& d, int tx, int ty, int i0, int j0,
-                                              int side) {
-  int any = 0;
-  for (int t = threadIdx.x; t < tx * ty; t += blockDim.x) {
-    const int i = i0 + t % tx, j = j0 + t / tx;
-    if (i > d.xe + 1 || j > d.ye || reg[(size_t)j * d.width + i]) continue;
-    const bool strip = (i <= d.xs || i >= d.xe) && j >= d.ys + 1 && j <= d.ye - 1;
-    if (strip == (side == 1)) any = 1;
+// The exact cells: every copy-region cell the march does not write, listed
+// in `ring` (cell indices, in no particular order) and counted in *count;
+// ring == nullptr counts only.
+__global__ void k_df_ring(const unsigned char* __restrict__ reg, Dims d, int* __restrict__ ring,
+                          int* __restrict__ count) {
+  const int nx = d.xe - d.xs + 3;
+  const long long n = (long long)nx * (d.ye - d.ys + 2);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int j = d.ys - 1 + (int)(t / nx), i = d.xs - 1 + (int)(t % nx);
+    const int c = j * d.width + i;
+    if (!reg[c]) {
+      const int k = atomicAdd(count, 1);
+      if (ring) ring[k] = c;
+    }
   }
-  return __syncthreads_or(any) != 0;
-}
-
-__global__ void k_df_tiles(const unsigned char* __restrict__ reg, Dims d, int tx, int ty,
-                           int ntx, int side, int* __restrict__ list, int* __restrict__ count) {
-  const int b = blockIdx.x;
-  const int i0 = d.xs - 1 + (b % ntx) * tx, j0 = d.ys - 1 + (b / ntx) * ty;
-  if (tile_has_work(reg, d, tx, ty, i0, j0, side) && threadIdx.x == 0)
-    list[atomicAdd(count + side, 1)] = b;
 }
 
 __global__ void k_selftest_df(const double* __restrict__ x, long long n, float* __restrict__ hi,
@@ -147,18 +168,13 @@ void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStr
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hu, ff.rhu, n);
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hv, ff.rhv, n);
   k_df_flags<<<152 * 8, 256, 0, st>>>(f.tmask, d, ff.reg);
-  cudaMemsetAsync(ff.count, 0, 2 * sizeof(int), st);
-  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const int rx = (nx + kDfRowsTX - 1) / kDfRowsTX, ry = (ny + kDfRowsTY - 1) / kDfRowsTY;
-  const int cx = (nx + kDfColsTX - 1) / kDfColsTX, cy = (ny + kDfColsTY - 1) / kDfColsTY;
-  k_df_tiles<<<rx * ry, 256, 0, st>>>(ff.reg, d, kDfRowsTX, kDfRowsTY, rx, 0, ff.tiles_rows,
-                                      ff.count);
-  k_df_tiles<<<cx * cy, 256, 0, st>>>(ff.reg, d, kDfColsTX, kDfColsTY, cx, 1, ff.tiles_cols,
-                                      ff.count);
+  cudaMemsetAsync(ff.count, 0, sizeof(int), st);
+  k_df_ring<<<152 * 8, 256, 0, st>>>(ff.reg, d, ff.ring, ff.count);
 }
 
-void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
-                     cudaStream_t st) {
+void launch_df_step(const Fields& f, const FusedState& fs, const Dims& d, const Scalars& s,
+                    const UniformMetrics& um, const DfFields& ff, double tide,
+                    const double* tide_table, int tide_index, cudaStream_t st) {
   const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
   const int ncol = (nx + MW - 1) / MW;
   // strips of MR rows, halved (down to 8) until the grid holds about two
@@ -166,8 +182,10 @@ void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, co
   int mr = MR;
   while (mr > 8 && (long long)ncol * ((ny + mr - 1) / mr) < 2 * 152 * 2 * WARPS) mr /= 2;
   const int nrow = (ny + mr - 1) / mr, nwarps = ncol * nrow;
-  k_df_march<<<(nwarps + WARPS - 1) / WARPS, 32 * WARPS, 0, st>>>(fs, ff, d, k, ncol, nwarps,
-                                                                  mr);
+  const int nring = (ff.n_ring + 32 * WARPS - 1) / (32 * WARPS);
+  k_df_step<<<(nwarps + WARPS - 1) / WARPS + nring, 32 * WARPS, 0, st>>>(
+      fs, ff, d, make_df_const(s, um), ncol, nwarps, mr, f, s, make_fast_const(s, um),
+      tide_table, tide_index, tide, nring);
 }
 
 }  // namespace nl2d

@@ -48,54 +48,7 @@ __global__ void __launch_bounds__(NTHREADS, TT::kMinBlocks)
                  d.xs - 1 + blockIdx.x * TT::TX, d.ys - 1 + blockIdx.y * TT::TY, smem);
 }
 
-// The FP64-equivalent form's exact part: the fused tile on listed tiles of
-// shape TE (tile index b, row-major over that shape's tile grid of the copy
-// region, ntx tiles per row), cells the double-float march does not write
-// only.  A cell that tiles of both shapes hold is written twice with the
-// same bits: both compute the reference's FP64 result from the same inputs.
-template <class TE>
-__global__ void __launch_bounds__(NTHREADS, TE::kMinBlocks)
-    k_fused_boundary(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um,
-                     FastConst k, const double* __restrict__ tide_table, int tide_index,
-                     double tide, const int* __restrict__ list, int ntx) {
-  const int b = list[blockIdx.x];
-  const int by = b / ntx, bx = b - by * ntx;
-  extern __shared__ double smem[];
-  fused_tile<TE, true>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
-                       d.xs - 1 + bx * TE::TX, d.ys - 1 + by * TE::TY, smem);
-}
-
-using EdgeRows = Tile<kDfRowsTX, kDfRowsTY>;
-using EdgeCols = Tile<kDfColsTX, kDfColsTY>;
-
 }  // namespace
-
-void launch_fused_boundary(const Fields& f, const FusedState& fs, const Dims& d,
-                           const Scalars& s, const UniformMetrics& um, double tide,
-                           const double* tide_table, int tide_index, const DfFields* ff,
-                           cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_fused_boundary<EdgeRows>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)EdgeRows::kSmemBytes);
-    cudaFuncSetAttribute(k_fused_boundary<EdgeCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)EdgeCols::kSmemBytes);
-    attr_set = true;
-  }
-  if (!ff) return;  // set-up call: the attributes only
-  const FastConst k = make_fast_const(s, um);
-  const int nx = d.xe - d.xs + 3;
-  if (ff->n_rows > 0)
-    k_fused_boundary<EdgeRows><<<ff->n_rows, dim3(EdgeRows::TX, EdgeRows::RPP),
-                                 EdgeRows::kSmemBytes, st>>>(
-        f, fs, d, s, um, k, tide_table, tide_index, tide, ff->tiles_rows,
-        (nx + EdgeRows::TX - 1) / EdgeRows::TX);
-  if (ff->n_cols > 0)
-    k_fused_boundary<EdgeCols><<<ff->n_cols, dim3(EdgeCols::TX, EdgeCols::RPP),
-                                 EdgeCols::kSmemBytes, st>>>(
-        f, fs, d, s, um, k, tide_table, tide_index, tide, ff->tiles_cols,
-        (nx + EdgeCols::TX - 1) / EdgeCols::TX);
-}
 
 void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,

@@ -448,10 +448,8 @@ __device__ __forceinline__ RegOut regular_cell(const double* a0, const double* b
 }
 
 // One tile of the fused step: cells [i0, i0+TX) x [j0, j0+TY) of the copy
-// region of one domain.  `tide` is this step's bc_ssh value.  With
-// SKIP_MARCH the cells the FP64-equivalent form's column march writes
-// (regular cells one inside next_ssh's ranges, nl2d_df.cu) are left alone.
-template <class T, bool SKIP_MARCH = false>
+// region of one domain.  `tide` is this step's bc_ssh value.
+template <class T>
 __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs, const Dims& d,
                                            const Scalars& p, const UniformMetrics& um,
                                            const FastConst& k, double tide, int i0, int j0,
@@ -607,8 +605,7 @@ __device__ __forceinline__ void fused_tile(const Fields& f, const FusedState& fs
 #pragma unroll
           for (int di = -1; di <= 1; di++) regular &= mk[q[e] + dj * SX + di] > 0;
       }
-      const bool skip = SKIP_MARCH && regular && i >= d.xs + 1 && j >= d.ys + 1;
-      reg[e] = regular && !skip;
+      reg[e] = regular;
       if (live && !regular) glist[atomicAdd(gcount, 1)] = row * TX + threadIdx.x;
     }
     double sau[NP], rhu[NP], sav[NP], rhv[NP];

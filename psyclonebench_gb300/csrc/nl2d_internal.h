@@ -88,19 +88,15 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
 
 // ---- FP64-equivalent (double-float) form, nl2d_df.cu ----
 // The fused path's FP64 state and buffers; the interior cells by a column
-// march in double-float arithmetic, every other cell of the copy region by
-// the fused tile kernel in exact FP64 on the tiles that hold such cells.
-// The exact part runs on thin tiles: DfEdgeRows (128 x 2) over the rows
-// ys-1, ys and ye and every other cell off the side strips, DfEdgeCols
-// (4 x 128) over the side strips (columns xs-1, xs, xe, xe+1 of rows ys+1 ..
-// ye-1); 32 x 16 tiles spent 8x (rows) and 16x (columns) the work there.
+// march in double-float arithmetic, every other cell of the copy region (the
+// exact cells: the boundary rows and columns and the cells beside land) in
+// exact FP64 by the fused step's general per-cell code, in the same launch.
 struct DfFields {
   float2 *ht, *hu, *hv, *rhu, *rhv;  // (hi, lo) splits of the FP64 arrays
   unsigned char* reg;                // 1 where the march writes the cell
-  int* tiles_rows;                   // DfEdgeRows tiles with work (indices)
-  int* tiles_cols;                   // DfEdgeCols tiles with work (indices)
-  int* count;                        // device: the two list lengths
-  int n_rows, n_cols;                // host copies of the list lengths
+  int* ring;                         // the exact cells (cell indices)
+  int* count;                        // device: the exact-cell count
+  int n_ring;                        // host copy of the count
 };
 // One domain of an FP64-equivalent ensemble (device descriptor): its state
 // buffers per parity and its double-float statics, pointers into the
@@ -115,24 +111,20 @@ struct DfConst {
   dfk::df cor_u, cor_v, hpg_u, hpg_v, rra_u, rra_v, face_u, face_v, rrat, r_fric;
 };
 DfConst make_df_const(const Scalars& s, const UniformMetrics& um);
-constexpr int kDfRowsTX = 128, kDfRowsTY = 2, kDfColsTX = 4, kDfColsTY = 128;
 constexpr int kDfMarchCols = 30;  // columns one warp of the march updates
-// Splits the depths and reciprocal denominators, marks the march's cells and
-// lists the exact part's tiles (ff.count receives the list lengths).
+// Splits the depths and reciprocal denominators, marks the march's cells
+// and counts the exact cells into ff.count; with ff.ring set, also lists
+// them there (in no particular order: each is computed on its own).
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
-void launch_df_march(const FusedState& fs, const DfFields& ff, const Dims& d, const DfConst& k,
-                     cudaStream_t st);
+// One step of the form: one launch, the march's blocks and the exact cells'
+// blocks interleaved.  `tide` as for the fused step.
+void launch_df_step(const Fields& f, const FusedState& fs, const Dims& d, const Scalars& s,
+                    const UniformMetrics& um, const DfFields& ff, double tide,
+                    const double* tide_table, int tide_index, cudaStream_t st);
 // Split of one packed FP64 array into (hi, lo) pairs; the march flags of one
 // domain (tmask and reg point at the domain's first element).
 void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st);
 void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st);
-// The fused FP64 tile kernel on the listed tiles of both shapes, leaving
-// the march's cells alone.  ff == nullptr: only sets the kernels' shared-
-// memory attributes (call outside any capture).
-void launch_fused_boundary(const Fields& f, const FusedState& fs, const Dims& d,
-                           const Scalars& s, const UniformMetrics& um, double tide,
-                           const double* tide_table, int tide_index, const DfFields* ff,
-                           cudaStream_t st);
 
 // Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.
 void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
