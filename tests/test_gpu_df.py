@@ -167,8 +167,8 @@ def test_df_bit_conversions(gpulib):
 @pytest.mark.parametrize("case", ["cfg0", "random_land", "open_east_south"])
 def test_df_exact_cells_equal_fp64_step(gpulib, oracle, case):
     """One step of the form from a state both paths share: every copy-region
-    cell the double-float march does not write (the exact part's thin tiles:
-    the edge rows, the side strips, the cells next to land) is bit-identical
+    cell the double-float march does not write (the exact cells: the edge
+    rows, the side columns, the cells next to land) is bit-identical
     to the FP64 step's, so no such cell is left unwritten; the march's cells
     agree to 1e-12 relative to the field's size."""
     rng = np.random.default_rng({"cfg0": 7, "random_land": 8, "open_east_south": 9}[case])

@@ -1,6 +1,6 @@
 """The ensemble's FP64-equivalent form (precision 2): the FP64 state, every
 domain's interior by the double-float column march, every other cell by the
-fused FP64 tile on thin edge tiles.  Held to the FP64-equivalent contract
+fused step's general per-cell code in exact FP64.  Held to the FP64-equivalent contract
 against the FP64 ensemble (itself bit-identical to the reference's step with
 each domain's tide): relative L2 <= 1e-10 per field and checksums to 10
 significant digits; the cells the march does not write are bit-identical
