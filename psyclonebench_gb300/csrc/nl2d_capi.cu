@@ -806,11 +806,12 @@ bool ensure_df() {
     if (!CK(cudaMalloc(&s.dfs.reg, n)) || !CK(cudaMalloc(&s.dfs.count, sizeof(int))))
       return false;
   }
+  launch_df_setup(s.dev, dims(), s.dfs, s.stream);
   // two passes: count the exact cells, then list them
   cudaFree(s.dfs.ring);
   s.dfs.ring = nullptr;
   for (int pass = 0; pass < 2; pass++) {
-    launch_df_setup(s.dev, dims(), s.dfs, s.stream);
+    launch_df_ring(dims(), s.dfs, s.stream);
     int count = 0;
     if (!CK(cudaGetLastError()) ||
         !CK(cudaMemcpyAsync(&count, s.dfs.count, sizeof count, cudaMemcpyDeviceToHost,

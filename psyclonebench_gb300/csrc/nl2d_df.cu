@@ -168,6 +168,9 @@ void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStr
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hu, ff.rhu, n);
   k_split<<<152 * 8, 256, 0, st>>>(f.r_hv, ff.rhv, n);
   k_df_flags<<<152 * 8, 256, 0, st>>>(f.tmask, d, ff.reg);
+}
+
+void launch_df_ring(const Dims& d, const DfFields& ff, cudaStream_t st) {
   cudaMemsetAsync(ff.count, 0, sizeof(int), st);
   k_df_ring<<<152 * 8, 256, 0, st>>>(ff.reg, d, ff.ring, ff.count);
 }

@@ -112,10 +112,11 @@ struct DfConst {
 };
 DfConst make_df_const(const Scalars& s, const UniformMetrics& um);
 constexpr int kDfMarchCols = 30;  // columns one warp of the march updates
-// Splits the depths and reciprocal denominators, marks the march's cells
-// and counts the exact cells into ff.count; with ff.ring set, also lists
-// them there (in no particular order: each is computed on its own).
+// Splits the depths and reciprocal denominators and marks the march's cells.
 void launch_df_setup(const Fields& f, const Dims& d, const DfFields& ff, cudaStream_t st);
+// Counts the exact cells into ff.count and, with ff.ring set, lists them
+// there (in no particular order: each is computed on its own).
+void launch_df_ring(const Dims& d, const DfFields& ff, cudaStream_t st);
 // One step of the form: one launch, the march's blocks and the exact cells'
 // blocks interleaved.  `tide` as for the fused step.
 void launch_df_step(const Fields& f, const FusedState& fs, const Dims& d, const Scalars& s,
