@@ -84,6 +84,19 @@ struct State {
   }* spec_out = nullptr;
   std::vector<int> spec_steps;  // isteps taken before the verdict
   int spec_kept = 0, spec_redone = 0;  // verdicts since the library loaded
+  // A speculative registration over pinned step arrays uploads them in
+  // row bands on `side` (band b's copies complete band_up[b]) and its first
+  // fused step runs band by band behind them, each band's tiles once their
+  // rows and the next band's are on the device.  bands_pending: the bands'
+  // depth reciprocals and shadow copies are still to be made (by the first
+  // step, or by finish_bands for whatever comes first).
+  static constexpr int kMaxBands = 8;
+  cudaEvent_t band_up[kMaxBands] = {};
+  cudaEvent_t backups_done = nullptr;  // spec_backup made (step 2 overwrites its source)
+  int nbands = 0;
+  int band_row[kMaxBands + 1] = {};   // array-row cuts
+  int band_tile[kMaxBands + 1] = {};  // tile-row cuts of the fused step's grid
+  bool bands_pending = false;
 };
 
 State g_state;
@@ -123,6 +136,7 @@ void drop_spec() {
   State& s = g_state;
   if (s.spec_pending && s.side) cudaStreamSynchronize(s.side);
   s.spec_pending = false;
+  s.bands_pending = false;
   s.spec_steps.clear();
   for (double*& p : s.spec_backup) {
     cudaFree(p);
@@ -509,6 +523,22 @@ bool upload(void* const* ptrs, int k, cudaStream_t st) {
   return true;
 }
 
+// Rows [r0, r1) of array k.
+bool upload_rows(void* const* ptrs, int k, int r0, int r1, cudaStream_t st) {
+  State& s = g_state;
+  const size_t w = (size_t)s.reg.width, esz = k == kNumFields ? 4 : 8;
+  char* dst = static_cast<char*>(
+      k < kNumFields ? (void*)*field_slot(s.dev, k)
+                     : (k == kNumFields ? (void*)s.dev.tmask
+                                        : (void*)*grid_slot(s.dev, k - kNumFields)));
+  const size_t off = (size_t)r0 * w * esz, bytes = (size_t)(r1 - r0) * w * esz;
+  if (!CK(cudaMemcpyAsync(dst + off, static_cast<const char*>(ptrs[k]) + off, bytes,
+                          cudaMemcpyHostToDevice, st)))
+    return false;
+  s.h2d_bytes += (long long)bytes;
+  return true;
+}
+
 // speculate: the caller is c_invoke_time_step, which can take fused steps
 // before the scan has answered (see State::spec_pending).
 bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, int height,
@@ -559,21 +589,46 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   if (!s.partials &&
       !CK(cudaMalloc(&s.partials, sizeof(double) * checksum_partials_needed())))
     return false;
-  // The arrays a fused step reads first (a pageable copy returns once its
-  // source is staged, a pinned one at once).
-  for (int k : kStepArrays)
-    if (!upload(ptrs, k, s.stream)) return false;
-  launch_depth_reciprocals(s.dev, dims(), s.stream);
-  if (!CK(cudaGetLastError())) return false;
   s.sc = sc;
   s.cur = 0;
   s.shadows_synced = false;
   s.materialized = true;
   s.last_path = 0;
   // Speculation pays only when the other arrays' copies do not hold the
-  // host: pinned sources, the FP64 fused path.
+  // host: pinned sources, the FP64 fused path.  With the step arrays pinned
+  // too, they go up in row bands that the first step follows.
   bool spec = speculate && s.precision == 0 && s.mode == NL2D_MODE_AUTO;
   for (int k : kLateArrays) spec = spec && host_pinned(ptrs[k]);
+  bool banded = spec;
+  for (int k : kStepArrays) banded = banded && host_pinned(ptrs[k]);
+  if (banded) {
+    if (!ensure_side()) return false;
+    for (int b = 0; b < State::kMaxBands; b++)
+      if (!s.band_up[b] && !CK(cudaEventCreateWithFlags(&s.band_up[b], cudaEventDisableTiming)))
+        return false;
+    if (!s.backups_done &&
+        !CK(cudaEventCreateWithFlags(&s.backups_done, cudaEventDisableTiming)))
+      return false;
+    int th = 0;
+    const int ntr = fused_step_tile_rows(dims(), &th);
+    s.nbands = std::min(State::kMaxBands, ntr);
+    for (int b = 0; b <= s.nbands; b++) {
+      s.band_tile[b] = (int)((long long)ntr * b / s.nbands);
+      s.band_row[b] = b == 0 ? 0 : (b == s.nbands ? height : ys - 1 + s.band_tile[b] * th);
+    }
+    for (int b = 0; b < s.nbands; b++) {
+      for (int k : kStepArrays)
+        if (!upload_rows(ptrs, k, s.band_row[b], s.band_row[b + 1], s.side)) return false;
+      if (!CK(cudaEventRecord(s.band_up[b], s.side))) return false;
+    }
+  } else {
+    // The arrays a fused step reads first (a pageable copy returns once its
+    // source is staged, a pinned one at once).
+    for (int k : kStepArrays)
+      if (!upload(ptrs, k, s.stream)) return false;
+    launch_depth_reciprocals(s.dev, dims(), s.stream);
+    if (!CK(cudaGetLastError())) return false;
+  }
   if (!spec) {
     for (int k : kLateArrays)
       if (!upload(ptrs, k, s.stream)) return false;
@@ -590,16 +645,20 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
     return false;
   if (!s.spec_out && !CK(cudaMallocHost(&s.spec_out, sizeof(State::SpecOut)))) return false;
   double* prim[3] = {s.dev.sshn_t, s.dev.un, s.dev.vn};
+  // the backups of the uploaded state: on the side stream behind the bands
+  // (the second step, which overwrites their source, waits for them), else
+  // on the library's stream before the first step
+  cudaStream_t bst = banded ? s.side : s.stream;
   for (int q = 0; q < 3; q++)
     if (!CK(cudaMalloc(&s.spec_backup[q], n * 8)) ||
-        !CK(cudaMemcpyAsync(s.spec_backup[q], prim[q], n * 8, cudaMemcpyDeviceToDevice,
-                            s.stream)))
+        !CK(cudaMemcpyAsync(s.spec_backup[q], prim[q], n * 8, cudaMemcpyDeviceToDevice, bst)))
       return false;
+  if (banded && !CK(cudaEventRecord(s.backups_done, s.side))) return false;
   // the other arrays and the scan behind the first steps, on the side
   // stream (nothing on the library's stream reads those arrays before the
   // verdict: resolve_spec makes it wait for them)
-  if (!CK(cudaEventRecord(s.ess_done, s.stream)) ||
-      !CK(cudaStreamWaitEvent(s.side, s.ess_done, 0)))
+  if (!banded && (!CK(cudaEventRecord(s.ess_done, s.stream)) ||
+                  !CK(cudaStreamWaitEvent(s.side, s.ess_done, 0))))
     return false;
   for (int k : kLateArrays)
     if (!upload(ptrs, k, s.side)) return false;
@@ -629,10 +688,60 @@ bool do_register(void* const* ptrs, int xs, int xe, int ys, int ye, int width, i
   s.consistent = true;
   s.spec_pending = true;
   s.spec_steps.clear();
+  s.bands_pending = banded;
   return true;
 }
 
 bool one_step(int istep);
+
+// Makes what the banded first step would have made band by band (the depth
+// reciprocals) when something else comes first, and orders the library's
+// stream behind the bands and the backups.
+bool finish_bands() {
+  State& s = g_state;
+  if (!s.bands_pending) return true;
+  s.bands_pending = false;
+  if (!CK(cudaStreamWaitEvent(s.stream, s.band_up[s.nbands - 1], 0)) ||
+      !CK(cudaStreamWaitEvent(s.stream, s.backups_done, 0)))
+    return false;
+  launch_depth_reciprocals(s.dev, dims(), s.stream);
+  return CK(cudaGetLastError());
+}
+
+// The first fused step of a banded registration: band b's tiles run once
+// rows up to the end of band b + 1 are on the device (the tiles read two
+// rows beyond their own, and a Flather face's momentum the reciprocal depth
+// of the next row), after that band's depth reciprocals and shadow rows.
+bool banded_first_step(const FusedState& fs, double tide) {
+  State& s = g_state;
+  s.bands_pending = false;
+  const Dims d = dims();
+  const size_t w = (size_t)s.reg.width;
+  double* prim[3] = {s.dev.sshn_t, s.dev.un, s.dev.vn};
+  for (int b = 0; b < s.nbands; b++) {
+    const int nb = std::min(b + 1, s.nbands - 1);
+    if (b == 0) {
+      if (!CK(cudaStreamWaitEvent(s.stream, s.band_up[0], 0))) return false;
+      launch_depth_reciprocals(s.dev, d, s.stream, s.band_row[0], s.band_row[1]);
+    }
+    if (nb > b) {
+      if (!CK(cudaStreamWaitEvent(s.stream, s.band_up[nb], 0))) return false;
+      launch_depth_reciprocals(s.dev, d, s.stream, s.band_row[nb], s.band_row[nb + 1]);
+    }
+    // the shadows (this step's output buffers) equal the uploaded state
+    // outside the copy region
+    const size_t off = s.band_row[b] * w, cnt = (s.band_row[b + 1] - s.band_row[b]) * w;
+    for (int q = 0; q < 3; q++)
+      if (!CK(cudaMemcpyAsync(s.shadow[q] + off, prim[q] + off, cnt * 8,
+                              cudaMemcpyDeviceToDevice, s.stream)))
+        return false;
+    launch_fused_step_rows(s.dev, fs, d, s.sc, s.um, tide, s.band_tile[b], s.band_tile[b + 1],
+                           s.stream);
+  }
+  s.shadows_synced = true;
+  // the next step writes the primaries, which the backups copy
+  return CK(cudaStreamWaitEvent(s.stream, s.backups_done, 0));
+}
 
 // Ends a speculative registration.  With wait false it returns at once
 // unless the scan has answered.  The verdict either keeps the steps taken
@@ -651,6 +760,7 @@ bool resolve_spec(bool wait) {
   } else if (!CK(cudaEventSynchronize(s.spec_ready))) {
     return false;
   }
+  if (!finish_bands()) return false;
   s.spec_pending = false;
   std::vector<int> steps;
   steps.swap(s.spec_steps);
@@ -748,7 +858,7 @@ bool can_fuse() {
 
 bool reference_step(int istep) {
   State& s = g_state;
-  if (!materialize()) return false;
+  if (!finish_bands() || !materialize()) return false;
   launch_reference_step(s.dev, dims(), s.sc, istep, s.chain_u, s.chain_v, s.stream);
   if (!CK(cudaGetLastError())) return false;
   s.mixed_valid = false;
@@ -785,6 +895,8 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
   if (s.precision == 2) {
     // interior cells in double-float, the others in exact FP64, one launch
     launch_df_step(s.dev, fs, dims(), s.sc, s.um, s.dfs, tide, tide_table, tide_index, s.stream);
+  } else if (s.bands_pending) {  // (never inside a graph: prepare_graph finishes them)
+    banded_first_step(fs, tide);
   } else {
     launch_fused_step(s.dev, fs, dims(), s.sc, s.um, tide, tide_table, tide_index, s.stream);
   }
@@ -904,9 +1016,10 @@ bool sync_from_mixed() {
 
 bool fused_step(int istep) {
   State& s = g_state;
+  if (s.precision != 0 && !finish_bands()) return false;
   if (s.precision == 1) {
     if (!ensure_mixed()) return false;
-  } else if (!sync_shadows() || (s.precision == 2 && !ensure_df())) {
+  } else if (!(s.bands_pending || sync_shadows()) || (s.precision == 2 && !ensure_df())) {
     return false;
   }
   fused_launch(nullptr, 0, tide_value(istep, s.sc.rdt));
@@ -997,6 +1110,7 @@ void invalidate_graph() {
 // the cached one matches.  Nothing is launched; s.cur is left unchanged.
 bool prepare_graph(int istep0, int rest, int checksum_every, int done_before) {
   State& s = g_state;
+  if (!finish_bands()) return false;  // a graph's steps take the whole grid
   if (s.precision == 1 ? !ensure_mixed() : !sync_shadows()) return false;
   if (s.precision == 2 && !ensure_df()) return false;
   if (s.tide_cap < rest) {
@@ -1061,6 +1175,14 @@ using namespace nl2d;
                                        vn,     ua,     ht,     ssha_u, va,   ssha_v, tmask, \
                                        area_t, area_u, area_v, dx_u,   dx_v, dx_t,  dy_u,  \
                                        dy_v,   dy_t,   gphiu,  gphiv}
+
+// ny rows of `width` bytes at the same pitch on both sides: one linear copy
+// when the rows are whole (the usual read of a full field), else a 2-D one.
+static bool copy_rows(char* dst, const char* src, size_t pitch, size_t width, int ny,
+                      cudaMemcpyKind kind, cudaStream_t st) {
+  if (width == pitch) return CK(cudaMemcpyAsync(dst, src, width * ny, kind, st));
+  return CK(cudaMemcpy2DAsync(dst, pitch, src, pitch, width, ny, kind, st));
+}
 
 extern "C" {
 
@@ -1142,8 +1264,8 @@ void c_read_from_device(void* from, void* to, int startx, int starty, int nx, in
   const size_t esz = k == kNumFields ? 4 : 8, pitch = (size_t)r.width * esz;
   const size_t off = ((size_t)(starty - 1) * r.width + (startx - 1)) * esz;
   if (nx == 0 || ny == 0) return;
-  if (!CK(cudaMemcpy2DAsync((char*)to + off, pitch, (const char*)src + off, pitch, nx * esz, ny,
-                            cudaMemcpyDeviceToHost, s.stream)))
+  if (!copy_rows((char*)to + off, (const char*)src + off, pitch, nx * esz, ny,
+                 cudaMemcpyDeviceToHost, s.stream))
     return;
   s.d2h_bytes += (long long)nx * ny * (long long)esz;
   if (blocking) CK(cudaStreamSynchronize(s.stream));
@@ -1175,8 +1297,8 @@ void c_write_to_device(void* from, void* to, int startx, int starty, int nx, int
   const size_t esz = k == kNumFields ? 4 : 8, pitch = (size_t)r.width * esz;
   const size_t off = ((size_t)(starty - 1) * r.width + (startx - 1)) * esz;
   if (nx > 0 && ny > 0 &&
-      !CK(cudaMemcpy2DAsync((char*)device_of(k) + off, pitch, (const char*)from + off, pitch,
-                            nx * esz, ny, cudaMemcpyHostToDevice, s.stream)))
+      !copy_rows((char*)device_of(k) + off, (const char*)from + off, pitch, nx * esz, ny,
+                 cudaMemcpyHostToDevice, s.stream))
     return;
   s.h2d_bytes += (long long)nx * ny * (long long)esz;
   // Any written array may break the fused path's preconditions: re-derive

@@ -41,18 +41,33 @@ using SmallTile = Tile<16, 16>;
 template <class TT>
 __global__ void __launch_bounds__(NTHREADS, TT::kMinBlocks)
     k_fused_step(Fields f, FusedState fs, Dims d, Scalars p, UniformMetrics um, FastConst k,
-                 const double* __restrict__ tide_table, int tide_index, double tide) {
+                 const double* __restrict__ tide_table, int tide_index, double tide, int row0) {
   extern __shared__ double smem[];
-  // Tiles cover the copy region [xs-1, xe+1] x [ys-1, ye].
+  // Tiles cover the copy region [xs-1, xe+1] x [ys-1, ye]; this launch takes
+  // tile rows row0 .. row0 + gridDim.y - 1.
   fused_tile<TT>(f, fs, d, p, um, k, tide_table ? tide_table[tide_index] : tide,
-                 d.xs - 1 + blockIdx.x * TT::TX, d.ys - 1 + blockIdx.y * TT::TY, smem);
+                 d.xs - 1 + blockIdx.x * TT::TX, d.ys - 1 + (row0 + blockIdx.y) * TT::TY,
+                 smem);
 }
 
-}  // namespace
+// Domains too small for four 32 x 16 tiles per SM take 16 x 16 tiles.
+bool small_tiles(const Dims& d) {
+  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
+  return (long long)((nx + T::TX - 1) / T::TX) * ((ny + T::TY - 1) / T::TY) < 4LL * 152;
+}
 
-void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
-                       const Scalars& s, const UniformMetrics& um, double tide,
-                       const double* tide_table, int tide_index, cudaStream_t st) {
+template <class TT>
+void launch_rows(const Fields& f, const FusedState& fs, const Dims& d, const Scalars& s,
+                 const UniformMetrics& um, double tide, const double* tide_table, int tide_index,
+                 int row0, int row1, cudaStream_t st) {
+  const int nx = d.xe - d.xs + 3;
+  if (row1 <= row0) return;
+  const dim3 grid((nx + TT::TX - 1) / TT::TX, row1 - row0);
+  k_fused_step<TT><<<grid, dim3(TT::TX, TT::RPP), TT::kSmemBytes, st>>>(
+      f, fs, d, s, um, make_fast_const(s, um), tide_table, tide_index, tide, row0);
+}
+
+void set_step_attrs() {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_fused_step<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -61,20 +76,38 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                          (int)SmallTile::kSmemBytes);
     attr_set = true;
   }
-  const FastConst k = make_fast_const(s, um);
-  const int nx = d.xe - d.xs + 3, ny = d.ye - d.ys + 2;
-  const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY);
-  // fewer than four 32 x 16 tiles per SM: 16 x 16 tiles
-  if ((long long)grid.x * grid.y < 4LL * 152) {
-    using S = SmallTile;
-    const dim3 gs((nx + S::TX - 1) / S::TX, (ny + S::TY - 1) / S::TY);
-    k_fused_step<S><<<gs, dim3(S::TX, S::RPP), S::kSmemBytes, st>>>(f, fs, d, s, um, k,
-                                                                    tide_table, tide_index, tide);
-    return;
-  }
-  k_fused_step<T><<<grid, dim3(T::TX, T::RPP), T::kSmemBytes, st>>>(f, fs, d, s, um, k,
-                                                                    tide_table, tide_index, tide);
 }
+
+}  // namespace
+
+int fused_step_tile_rows(const Dims& d, int* tile_height) {
+  const int ty = small_tiles(d) ? SmallTile::TY : T::TY;
+  if (tile_height) *tile_height = ty;
+  return (d.ye - d.ys + 2 + ty - 1) / ty;
+}
+
+void launch_fused_step_rows(const Fields& f, const FusedState& fs, const Dims& d,
+                            const Scalars& s, const UniformMetrics& um, double tide, int row0,
+                            int row1, cudaStream_t st) {
+  set_step_attrs();
+  if (small_tiles(d))
+    launch_rows<SmallTile>(f, fs, d, s, um, tide, nullptr, 0, row0, row1, st);
+  else
+    launch_rows<T>(f, fs, d, s, um, tide, nullptr, 0, row0, row1, st);
+}
+
+void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
+                       const Scalars& s, const UniformMetrics& um, double tide,
+                       const double* tide_table, int tide_index, cudaStream_t st) {
+  set_step_attrs();
+  const int rows = fused_step_tile_rows(d, nullptr);
+  if (small_tiles(d))
+    launch_rows<SmallTile>(f, fs, d, s, um, tide, tide_table, tide_index, 0, rows, st);
+  else
+    launch_rows<T>(f, fs, d, s, um, tide, tide_table, tide_index, 0, rows, st);
+}
+
+namespace {
 
 // Reciprocals RN(1 / (h + ssha)) of the momentum denominators, or 0 where
 // the depth lies outside [2^-100, 2^100] (the kernel then divides).
@@ -88,10 +121,16 @@ __global__ void k_depth_reciprocal(const double* __restrict__ h,
   }
 }
 
-void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st) {
-  const long long n = (long long)d.width * d.height;
-  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hu, f.ssha_u, f.r_hu, n);
-  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hv, f.ssha_v, f.r_hv, n);
+}  // namespace
+
+void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st, int row0,
+                              int row1) {
+  if (row1 < 0) row1 = d.height;
+  const size_t o = (size_t)row0 * d.width;
+  const long long n = (long long)(row1 - row0) * d.width;
+  if (n <= 0) return;
+  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hu + o, f.ssha_u + o, f.r_hu + o, n);
+  k_depth_reciprocal<<<152 * 8, 256, 0, st>>>(f.hv + o, f.ssha_v + o, f.r_hv + o, n);
 }
 
 }  // namespace nl2d

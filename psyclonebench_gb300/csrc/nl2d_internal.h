@@ -85,6 +85,13 @@ void launch_fused_step(const Fields& f, const FusedState& fs, const Dims& d,
                        const Scalars& s, const UniformMetrics& um, double tide,
                        const double* tide_table, int tide_index,
                        cudaStream_t st);
+// The rows of tiles the fused step's grid has for this domain, and the
+// tile's height in cells (its tile rows start at row ys - 1).
+int fused_step_tile_rows(const Dims& d, int* tile_height);
+// The fused step on tile rows [row0, row1) of that grid only.
+void launch_fused_step_rows(const Fields& f, const FusedState& fs, const Dims& d,
+                            const Scalars& s, const UniformMetrics& um, double tide, int row0,
+                            int row1, cudaStream_t st);
 
 // ---- FP64-equivalent (double-float) form, nl2d_df.cu ----
 // The fused path's FP64 state and buffers; the interior cells by a column
@@ -127,8 +134,10 @@ void launch_df_step(const Fields& f, const FusedState& fs, const Dims& d, const 
 void launch_df_split(const double* a, float2* out, long long n, cudaStream_t st);
 void launch_df_flags(const int* tmask, const Dims& d, unsigned char* reg, cudaStream_t st);
 
-// Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v.
-void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st);
+// Recomputes Fields::r_hu / r_hv from hu, ssha_u, hv, ssha_v (array rows
+// [row0, row1) only, when given).
+void launch_depth_reciprocals(const Fields& f, const Dims& d, cudaStream_t st, int row0 = 0,
+                              int row1 = -1);
 
 // ---- mixed-precision step (nl2d_mixed.cu) ----
 struct MixedFields {  // static FP32 copies of the depths and the

@@ -26,16 +26,17 @@ def counts(gpulib):
     return out[0], out[1]
 
 
-def run_pinned(gpulib, m, nsteps, read_after=None, verdict=None):
-    """nsteps calls over m's arrays pinned; with read_after = k, sshn_t is
-    read back right after step k (before the next call).  verdict "kept" or
-    "redone": the speculation must have ended that way."""
+def run_pinned(gpulib, m, nsteps, read_after=None, verdict=None, istep0=1):
+    """nsteps calls (isteps istep0 ...) over m's arrays pinned; with
+    read_after = k, sshn_t is read back right after step k (before the next
+    call).  verdict "kept" or "redone": the speculation must have ended that
+    way."""
     before = counts(gpulib)
     held = T.pin_model(gpulib, m)
     try:
         paths = []
         for k in range(nsteps):
-            gpulib.c_invoke_time_step(*m.step_args(1 + k))
+            gpulib.c_invoke_time_step(*m.step_args(istep0 + k))
             paths.append(gpulib.nl2d_last_path())
             if read_after == k + 1:
                 a = m.f["sshn_t"]
@@ -113,3 +114,20 @@ def test_read_during_speculation(gpulib, oracle):
     got1 = [p for p in paths if isinstance(p, tuple)][0][1]
     assert bits_equal(got1, one.f["sshn_t"])
     assert_fields_equal(m, want, "read")
+
+
+@pytest.mark.parametrize("jpiglo,jpjglo", [(32, 14), (64, 52), (302, 132), (1026, 1026)])
+def test_banded_first_step(gpulib, oracle, jpiglo, jpjglo):
+    """The step arrays go up in row bands (1, 4, 8 and 8 bands of the fused
+    step's tile rows here) and the first fused step runs band by band behind
+    them.  From a state the oracle's own steps left (so the speculation is
+    kept and every field is in motion), 20 steps bit-identical to the
+    oracle's next 20."""
+    m = T.make_model(jpiglo, jpjglo, 1, oracle=oracle)
+    T.run(oracle.oracle_invoke_time_step, m, 30)
+    assert np.abs(m.f["un"]).max() > 0
+    want = m.copy()
+    T.run(oracle.oracle_invoke_time_step, want, 20, nit000=31)
+    paths = run_pinned(gpulib, m, 20, verdict="kept", istep0=31)
+    assert set(paths) == {2}, paths
+    assert_fields_equal(m, want, "banded")
