@@ -63,16 +63,18 @@ extern "C" {
  * sshn_u / sshn_v as next_sshu / next_sshv make them of sshn_t, as at the
  * reference's rest start), the first step already takes the fused path;
  * otherwise it is reference-structured.  With the arrays pinned
- * (nl2d_host_register) the first call uploads only the arrays a fused step
- * reads and starts that step; the other arrays (ssha_t, the metrics, the
- * latitudes) and the registration checks follow on a second stream.  If
- * the checks refuse the fused path or find a state that is not what a step
- * leaves, the steps taken meanwhile are undone and taken again by the
- * reference's rules, so the results are the same bits either way.  Every
- * other entry point waits for the checks first.  As with any asynchronous
- * copy from pinned memory, the caller must not write those 12 arrays
- * directly until a later library call has returned (c_write_to_device, the
- * way to change a registered array, waits for them itself).
+ * (nl2d_host_register) the first call uploads the arrays a fused step
+ * reads in row bands and starts that step band by band behind them; the
+ * other arrays (ssha_t, the metrics, the latitudes) and the registration
+ * checks follow on a second stream.  If the checks refuse the fused path or
+ * find a state that is not what a step leaves, the steps taken meanwhile
+ * are undone and taken again by the reference's rules, so the results are
+ * the same bits either way.  Every entry point but c_invoke_time_step waits
+ * for the checks (and so for every copy) first.  As with any asynchronous
+ * copy from pinned memory, the caller must not write the 25 arrays
+ * directly until such a call (nl2d_sync, c_read_from_device, ...) has
+ * returned; c_write_to_device, the way to change a registered array, waits
+ * for them itself.
  */
 void c_invoke_time_step(
     double *ssha_t, double *sshn_t, double *sshn_u, double *sshn_v,
