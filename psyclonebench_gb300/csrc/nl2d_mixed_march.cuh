@@ -30,7 +30,16 @@ namespace {
 constexpr int MW = 30;  // output columns per warp
 constexpr int MR = 32;  // output rows per warp (at most; smaller domains take shorter strips)
 constexpr int MARCH_WARPS = 4;
+constexpr int PF = 2;  // rows between an L2 prefetch and the row's loads
 constexpr unsigned FULL = 0xffffffffu;
+
+// log2 of the element size of the array this lane prefetches in the march
+// (the lane id is read again where it is needed, not held in a register)
+__device__ __forceinline__ int pf_shift() {
+  unsigned l;
+  asm("mov.u32 %0, %%laneid;" : "=r"(l));
+  return l < 3 ? 3 : (l < 17 ? 2 : 0);
+}
 
 __device__ __forceinline__ float shd(float x) { return __shfl_down_sync(FULL, x, 1); }
 __device__ __forceinline__ float shu(float x) { return __shfl_up_sync(FULL, x, 1); }
@@ -219,6 +228,30 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
   // the loads need no bounds test and no select.
   const int cb = (int)base + min(max(i, 0), W - 1);  // this lane's column
   auto at = [cb, W, H](int j) { return cb + min(max(j, 0), H - 1) * W; };
+  // The row PF ahead of the loads goes into L2 first, one line per lane:
+  // lanes 0-2 the first, middle and last of the warp's columns in the
+  // 8-byte ssh pairs, lanes 3-16 the first and last in each of the seven
+  // 4-byte arrays, lanes 17-18 in the flag bytes (pf_shift gives each lane's
+  // element size), so that the loads PF rows later find their lines there.
+  const char* pf = nullptr;
+  {
+    const int c0 = (int)base + min(max(i0 - 1, 0), W - 1);
+    const int c1 = (int)base + min(i0 + MW, W - 1), cm = (int)base + min(i0 + MW / 2, W - 1);
+    switch (lane) {
+      case 0: pf = (const char*)(ms.sn_in + c0); break;
+      case 1: pf = (const char*)(ms.sn_in + cm); break;
+      case 2: pf = (const char*)(ms.sn_in + c1); break;
+      case 3: case 4: pf = (const char*)(ms.un_in + (lane & 1 ? c0 : c1)); break;
+      case 5: case 6: pf = (const char*)(ms.vn_in + (lane & 1 ? c0 : c1)); break;
+      case 7: case 8: pf = (const char*)(mf.hu + (lane & 1 ? c0 : c1)); break;
+      case 9: case 10: pf = (const char*)(mf.hv + (lane & 1 ? c0 : c1)); break;
+      case 11: case 12: pf = (const char*)(mf.ht + (lane & 1 ? c0 : c1)); break;
+      case 13: case 14: pf = (const char*)(mf.rhu + (lane & 1 ? c0 : c1)); break;
+      case 15: case 16: pf = (const char*)(mf.rhv + (lane & 1 ? c0 : c1)); break;
+      case 17: case 18: pf = (const char*)(mf.reg + (lane & 1 ? c0 : c1)); break;
+      default: break;
+    }
+  }
   MRow P = finish_row(load_raw(mf, ms, at(j0 - 1)), k);
   MRow C = finish_row(load_raw(mf, ms, at(j0)), k);
   MRow N = finish_row(load_raw(mf, ms, at(j0 + 1)), k);
@@ -236,6 +269,10 @@ __device__ __forceinline__ void mixed_march(const MixedFields& mf, const MixedSt
     N = finish_row(R1, k);  // row j+2, loaded two iterations ago
     R1 = R2;
     R2 = load_raw(mf, ms, at(j + 4));  // in flight for two iterations
+    if (pf) {
+      const size_t off = (size_t)min(j + 4 + PF, H - 1) * W;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(pf + (off << pf_shift())));
+    }
     const MOut Oc = O;
     O = load_out(mf, out_col, cb + (j + 1) * W);
     C.ss.y = (C.sn + N.sn) * k.face_v;
