@@ -22,6 +22,7 @@
 // kernel records an error flag, skips its epilogue, frees its tensor memory
 // and returns.
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/nl2d_gpu.h"
@@ -410,8 +411,10 @@ __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w,
 // M = co (padded to 128 with zero rows), N = ci, K = pixels.  X is staged as
 // in the convolution, so the tap (dy, dx) operand is again a row block
 // started 16 * dx bytes later.  The nine accumulators (9 x ci FP32 columns)
-// stay in tensor memory for the CTA's lifetime; at the end each CTA adds its
-// partial sums to dw atomically.
+// stay in tensor memory for the CTA's lifetime; at the end each CTA writes
+// its partial sums to its own slot of `part`, and k_sum_parts adds the
+// slots in CTA order, so that the gradient has the same bits on every run
+// (atomic additions would sum in whatever order the CTAs finished).
 constexpr int kWgTmemCols = 512;
 constexpr int kWgGroups = 16;  // 128 M rows = 16 groups of 8 output channels
 constexpr size_t kWgSmem = 120 * 1024;
@@ -435,7 +438,7 @@ constexpr int kWgYBatch = 16;      // 16-byte loads per thread per dY row (cout 
 
 __global__ void __launch_bounds__(kPipeThreads)
     k_conv_wgrad_pipe(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ dy,
-                      float* __restrict__ dw, int batch, int H, int W, int cin, int cout,
+                      float* __restrict__ part, int batch, int H, int W, int cin, int cout,
                       int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t xfull[kSlots], xempty[kSlots];
@@ -631,9 +634,10 @@ __global__ void __launch_bounds__(kPipeThreads)
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (co < cout) {
           const int tap = c0 / cin, ci0 = c0 - tap * cin;
+          float* mine = part + (size_t)blockIdx.x * 9 * cout * cin;
 #pragma unroll
           for (int k = 0; k < 16; k++)
-            atomicAdd(&dw[((size_t)tap * cout + co) * cin + ci0 + k], __uint_as_float(r[k]));
+            mine[((size_t)tap * cout + co) * cin + ci0 + k] = __uint_as_float(r[k]);
         }
       }
     }
@@ -646,13 +650,13 @@ __global__ void __launch_bounds__(kPipeThreads)
                  "r"(kWgTmemCols));
 }
 
-// db[co] += sum over pixels of dy[p][co] (FP32 partial sums per block,
-// atomics per channel).
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, float* __restrict__ db,
-                            long long P, int cout) {
-  __shared__ float part[128];
-  for (int c = threadIdx.x; c < cout; c += blockDim.x) part[c] = 0.f;
-  __syncthreads();
+// Block b's partial bias gradient, part[b][co] = sum over its pixels of
+// dy[p][co], in a fixed order (each thread a channel pair over a fixed set
+// of rows, then the block's rows in order); k_sum_parts adds the blocks.
+__global__ void __launch_bounds__(256)
+    k_bias_grad(const __nv_bfloat16* __restrict__ dy, float* __restrict__ part, long long P,
+                int cout) {
+  __shared__ float sp[256 * 2];
   // thread -> one channel pair, rows strided over the grid
   const int pairs = cout >> 1;
   const int lanes_per_row = pairs;  // <= 64
@@ -666,11 +670,39 @@ __global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, float* __restr
       s0 += __low2float(v);
       s1 += __high2float(v);
     }
-    atomicAdd(&part[2 * c2], s0);
-    atomicAdd(&part[2 * c2 + 1], s1);
+    sp[r0 * cout + 2 * c2] = s0;
+    sp[r0 * cout + 2 * c2 + 1] = s1;
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < cout; c += blockDim.x) atomicAdd(&db[c], part[c]);
+  for (int c = threadIdx.x; c < cout; c += blockDim.x) {
+    float acc = 0.f;
+    for (int r = 0; r < rows_per_block; r++) acc += sp[r * cout + c];
+    part[(size_t)blockIdx.x * cout + c] = acc;
+  }
+}
+
+// out[e] += part[0][e] + part[1][e] + ... in that order.
+__global__ void k_sum_parts(const float* __restrict__ part, int nparts, long long nel,
+                            float* __restrict__ out) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel;
+       e += (long long)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int b = 0; b < nparts; b++) acc += part[(size_t)b * nel + e];
+    out[e] += acc;
+  }
+}
+
+// Scratch for the per-CTA partial gradients (grown on demand, kept).
+float* g_parts = nullptr;
+size_t g_parts_cap = 0;
+bool ensure_parts(size_t n) {
+  if (n <= g_parts_cap) return true;
+  cudaFree(g_parts);
+  g_parts = nullptr;
+  g_parts_cap = 0;
+  if (cudaMalloc(&g_parts, n * sizeof(float)) != cudaSuccess) return false;
+  g_parts_cap = n;
+  return true;
 }
 
 // dx = (y > 0) ? g : 0 for a ReLU output y (BF16), g FP32 -> BF16.
@@ -977,11 +1009,18 @@ int nl2d_emu_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int
   const long long units =
       (long long)batch * ((H + kStripRows - 1) / kStripRows) * (W / kTileM);
   const int grid = (int)(units < sms ? units : sms);  // 512 TMEM columns: one CTA per SM
-  k_conv_wgrad_pipe<<<grid, kPipeThreads, smem, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, dw, batch, H, W, cin, cout, err);
+  constexpr int kBiasBlocks = 152 * 8;
+  const long long nel = 9LL * cout * cin;
+  if (!ensure_parts((size_t)std::max<long long>(grid * nel, (long long)kBiasBlocks * cout)))
+    return NL2D_ERR_CUDA;
+  const cudaStream_t st = (cudaStream_t)stream;
+  k_conv_wgrad_pipe<<<grid, kPipeThreads, smem, st>>>(
+      (const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, g_parts, batch, H, W, cin, cout, err);
+  k_sum_parts<<<(int)((nel + 255) / 256), 256, 0, st>>>(g_parts, grid, nel, dw);
   if (cudaGetLastError() != cudaSuccess) return NL2D_ERR_CUDA;
-  k_bias_grad<<<152 * 8, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)dy, db,
-                                                         (long long)batch * H * W, cout);
+  k_bias_grad<<<kBiasBlocks, 256, 0, st>>>((const __nv_bfloat16*)dy, g_parts,
+                                            (long long)batch * H * W, cout);
+  k_sum_parts<<<1, 128, 0, st>>>(g_parts, kBiasBlocks, cout, db);
   return cudaGetLastError() == cudaSuccess ? NL2D_OK : NL2D_ERR_CUDA;
 }
 

@@ -103,6 +103,14 @@ def test_conv_backward_matches_fp64(gpulib, B, H, W, cin, cout):
     for got, want in ((gx, dx_ref), (gw, dw_ref), (gb, db_ref)):
         g = got.cpu().numpy()
         np.testing.assert_allclose(g, want, rtol=0, atol=1e-4 * np.abs(want).max())
+    # the partial sums are added in a fixed order: the same call gives the
+    # same bits again
+    gw2, gb2 = torch.zeros_like(gw), torch.zeros_like(gb)
+    assert gpulib.nl2d_emu_conv_wgrad(dxd.data_ptr(), dG.data_ptr(), gw2.data_ptr(),
+                                      gb2.data_ptr(), B, H, W, cin, cout, err.data_ptr(),
+                                      None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(gw, gw2) and torch.equal(gb, gb2)
 
 
 def test_training_fits_a_known_convolution(gpulib):
@@ -126,6 +134,28 @@ def test_training_fits_a_known_convolution(gpulib):
     for _ in range(300):
         last = net.train_step(x, t, lr=3e-3)
     assert last < 0.1 * first, (first, last)
+
+
+def test_training_is_reproducible(gpulib):
+    """Two networks from the same seed, trained on the same batches, end
+    with the same weights bit for bit: no reduction of the training step
+    depends on the order in which blocks finish."""
+    import torch
+    from psyclonebench_gb300.emulator import CPAD_IN, ConvNet
+    B, H, W = 2, 16, 128
+    P = B * H * W
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.zeros(P, CPAD_IN, dtype=torch.bfloat16, device="cuda")
+    x[:, :5] = torch.randn(P, 5, device="cuda", generator=g).to(torch.bfloat16)
+    t = torch.randn(P, 3, device="cuda", generator=g)
+    weights = []
+    for _ in range(2):
+        net = ConvNet(B, H, W, seed=1, lib=gpulib)
+        for _ in range(40):
+            net.train_step(x, t, lr=3e-3)
+        torch.cuda.synchronize()
+        weights.append([w.clone() for w in net.w32])
+    assert all(torch.equal(a, b) for a, b in zip(*weights))
 
 
 @pytest.fixture(scope="module")
