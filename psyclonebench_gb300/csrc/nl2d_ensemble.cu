@@ -153,6 +153,10 @@ __global__ void __launch_bounds__(32 * dfm::WARPS, 3)
   dfm::df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
 }
 
+// The column marches' strip height until the autotuner chooses one (8, 16
+// or 32 rows).
+constexpr int kDefaultMarchRows = 32;
+
 // The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
 // search space); shape 0 is the single-domain kernel's.
 constexpr int kNumShapes = 5;
@@ -292,7 +296,7 @@ struct Ens {
   int graph_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   bool built = false;
   int shape = 0;        // index into kShapes: the FP64 kernel's tile
-  int march_rows = 32;  // strip height of the mixed form's column march
+  int march_rows = kDefaultMarchRows;  // strip height of the column marches
   // mixed-precision form
   int precision = 0;
   float2* msn[2] = {};
@@ -394,7 +398,7 @@ void ens_free() {
   e.ndom = 0;
   e.dom.clear();
   e.shape = 0;
-  e.march_rows = mixk::MR;
+  e.march_rows = kDefaultMarchRows;
 }
 
 // Flather chains or reads outside the array exclude a domain (the one-launch

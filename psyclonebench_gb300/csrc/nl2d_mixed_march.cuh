@@ -28,7 +28,7 @@ namespace mixk {
 namespace {
 
 constexpr int MW = 30;  // output columns per warp
-constexpr int MR = 32;  // output rows per warp (at most; smaller domains take shorter strips)
+constexpr int MR = 64;  // output rows per warp (at most; smaller domains take shorter strips)
 constexpr int MARCH_WARPS = 4;
 constexpr int PF = 2;  // rows between an L2 prefetch and the row's loads
 constexpr unsigned FULL = 0xffffffffu;
