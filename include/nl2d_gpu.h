@@ -235,8 +235,9 @@ int nl2d_ens_schedule(int ctas_per_sm, int policy, double boundary_weight);
 /* Tile knobs the autotuner searches (the reference's tiled OpenMP layer,
  * psykal_omp/time_step_mod.f90:587-1182, fixes its tile size per run): the
  * FP64 kernel's tile shape tx x ty, one of 32 x 16 (the default), 32 x 8,
- * 16 x 16, 64 x 8 and 32 x 32, and the mixed form's column-march strip
- * height, 8, 16 or 32 rows (the default).  Results do not depend on
+ * 16 x 16, 64 x 8 and 32 x 32, and the column marches' strip height (the
+ * mixed and FP64-equivalent forms), 8, 16, 32 (the default) or 64 rows.
+ * Results do not depend on
  * either.  A new ensemble starts with the defaults.  Returns NL2D_ERR_ARGS
  * for other values. */
 int nl2d_ens_tile(int tx, int ty, int march_rows);

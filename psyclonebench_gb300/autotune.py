@@ -13,7 +13,7 @@ nl2d_ens_tile):
   every schedule at the default shape, then every shape under the best
   schedule and under one-tile-per-CTA.
 * Mixed form, when it runs the column march, and the FP64-equivalent form
-  ("df"): the march's strip height (8, 16 or 32 rows), under the FP64 knobs
+  ("df"): the march's strip height (8, 16, 32 or 64 rows), under the FP64 knobs
   already applied.
 
 Each candidate is timed on a few steps of the actual ensemble (after one
@@ -32,7 +32,7 @@ SCHEDULES = ([(cps, pol, bw) for cps in (1, 2) for pol in (0, 1) for bw in (0.0,
              [(2, 2, 0.0)])
 SHAPES = ((32, 16), (32, 8), (16, 16), (64, 8), (32, 32))
 DEFAULT_SHAPE = SHAPES[0]
-MARCH_ROWS = (8, 16, 32)
+MARCH_ROWS = (8, 16, 32, 64)
 DEFAULT_MARCH_ROWS = 32
 
 

@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(32 * dfm::WARPS, 3)
   dfm::df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
 }
 
-// The column marches' strip height until the autotuner chooses one (8, 16
-// or 32 rows).
+// The column marches' strip height until the autotuner chooses one (8, 16,
+// 32 or 64 rows).
 constexpr int kDefaultMarchRows = 32;
 
 // The tile shapes the ensemble's FP64 kernel is built for (the autotuner's
@@ -929,7 +929,8 @@ int nl2d_ens_tile(int tx, int ty, int march_rows) {
   int shape = -1;
   for (int k = 0; k < kNumShapes; k++)
     if (kShapes[k][0] == tx && kShapes[k][1] == ty) shape = k;
-  if (shape < 0 || (march_rows != 8 && march_rows != 16 && march_rows != 32))
+  if (shape < 0 ||
+      (march_rows != 8 && march_rows != 16 && march_rows != 32 && march_rows != 64))
     return NL2D_ERR_ARGS;
   e.shape = shape;
   e.march_rows = march_rows;

@@ -71,7 +71,7 @@ def test_a_non_default_tile_shape_can_win(tmp_path, monkeypatch):
 def test_mixed_form_searches_the_march_strip(tmp_path, monkeypatch):
     monkeypatch.setenv("NL2D_TUNE_CACHE", str(tmp_path))
     base = {"ctas_per_sm": 1, "policy": 2, "boundary_weight": 0.0, "tile": [64, 8]}
-    ens = FakeEnsemble([dom(64, 64)], lambda c: {8: 3.0, 16: 1.0, 32: 2.0}[c[4]])
+    ens = FakeEnsemble([dom(64, 64)], lambda c: {8: 3.0, 16: 1.0, 32: 2.0, 64: 2.5}[c[4]])
     r = autotune.tune(ens, precision="mixed", base=base)
     assert r["march_rows"] == 16 and len(r["timings"]) == len(autotune.MARCH_ROWS)
     assert ens.cur == (1, 2, 0.0, (64, 8), 16)  # the FP64 knobs are kept
