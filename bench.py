@@ -326,7 +326,7 @@ def run_df_form(lib, n, steps=200, warmup=5):
     at the headline workload (n x n from rest) and with every cell in motion
     (make_active): device-resident rate, and each field's relative L2
     difference to the bitwise FP64 path after the same warmup + steps
-    steps (the benchmark spec's bar for the FP64 path: 1e-10)."""
+    steps (the FP64-equivalent contract: 1e-10 per field)."""
     import psyclonebench_gb300 as P
     from psyclonebench_gb300.model import read_fields, register
     cells = n * n

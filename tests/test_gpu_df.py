@@ -1,7 +1,7 @@
 """The FP64-equivalent form (nl2d_set_precision(2)): interior cells in
 double-float arithmetic on the FP32 pipe, the other cells in exact FP64.
-Not bit-identical; held to the benchmark spec's contract for the FP64 path
-against the reference: relative L2 <= 1e-10 per field and checksums agreeing
+Not bit-identical; held to the FP64-equivalent contract against the
+reference: relative L2 <= 1e-10 per field and checksums agreeing
 to 10 significant digits (relative 1e-10) after 2000 steps of the parity
 namelist, and the same bar on bathymetry, random starts and land."""
 import os
