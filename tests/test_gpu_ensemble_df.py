@@ -167,3 +167,26 @@ def test_df_ensemble_bench_sample_2000_steps(gpulib):
     print("bench-sample FP64-equivalent ensemble worst relative L2 after 2000 steps:", worst)
     assert worst <= REL_L2
     np.testing.assert_allclose(sdf, s64, rtol=CHECKSUM_RTOL, atol=1e-300)
+
+
+def test_df_ensemble_with_interior_land(gpulib, domains):
+    """Blocks of land inside every domain: the cells beside them join the
+    exact cells (the march takes only cells whose 3x3 neighbourhood is
+    wet).  200 steps within relative L2 1e-10 of the FP64 ensemble."""
+    rng = np.random.default_rng(9)
+    doms = []
+    for d in domains:
+        d = dict(d)
+        m = d["tmask"].copy()
+        w, h, xs, xe, ys, ye = d["dims"]
+        for _ in range(3):
+            i = int(rng.integers(xs + 3, max(xs + 4, xe - 5)))
+            j = int(rng.integers(ys + 3, max(ys + 4, ye - 4)))
+            m[j:j + 2, i:i + 3] = 0
+        d["tmask"] = m
+        doms.append(d)
+    ref, s64, got, sdf = run_pair(gpulib, doms, 200, every=100)
+    worst = worst_rel_l2(doms, ref, got)
+    print("FP64-equivalent ensemble with land, worst relative L2:", worst)
+    assert worst <= REL_L2
+    np.testing.assert_allclose(sdf, s64, rtol=CHECKSUM_RTOL, atol=1e-300)
