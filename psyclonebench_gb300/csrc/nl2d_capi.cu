@@ -62,7 +62,7 @@ struct State {
   bool mixed_ahead = false;    // ... and it is newer than the FP64 arrays
   int status = NL2D_OK;
   char msg[512] = {0};
-  // FP64-equivalent form: split statics, march flags, boundary tiles
+  // FP64-equivalent form: split statics, march flags, the exact cells' list
   DfFields dfs{};
   bool df_valid = false;
   unsigned scan_flags = 0;     // last registration scan (kScan* bits)
@@ -73,9 +73,9 @@ struct State {
   // arrays a fused step reads go first and steps start on `stream`; the
   // other arrays and the registration scan follow on `side`, and a later
   // call keeps the steps or takes them again by the scan's verdict.
-  cudaStream_t side = nullptr;  // also the FP64-equivalent form's exact tiles
+  cudaStream_t side = nullptr;  // also the mixed form's general cells
   cudaEvent_t ess_done = nullptr, spec_ready = nullptr;
-  cudaEvent_t df_fork = nullptr, df_join = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   bool spec_pending = false;
   double* spec_backup[3] = {};  // sshn_t, un, vn as uploaded
   struct SpecOut {              // pinned host copy of the scan's results
@@ -879,7 +879,7 @@ void fused_launch(const double* tide_table, int tide_index, double tide) {
     ms.un_out = s.mun[1 - s.mcur];
     ms.vn_out = s.mvn[1 - s.mcur];
     launch_mixed_step(s.mix, ms, s.dev, dims(), s.sc, s.um, tide, tide_table, tide_index,
-                      s.stream, s.side, s.df_fork, s.df_join);
+                      s.stream, s.side, s.side_fork, s.side_join);
     s.mcur = 1 - s.mcur;
     return;
   }
@@ -963,8 +963,8 @@ bool ensure_mixed() {
   if (s.mixed_valid) return true;
   // the second stream and its events for the general cells' pass
   if (!ensure_side() ||
-      (!s.df_fork && (!CK(cudaEventCreateWithFlags(&s.df_fork, cudaEventDisableTiming)) ||
-                      !CK(cudaEventCreateWithFlags(&s.df_join, cudaEventDisableTiming)))))
+      (!s.side_fork && (!CK(cudaEventCreateWithFlags(&s.side_fork, cudaEventDisableTiming)) ||
+                      !CK(cudaEventCreateWithFlags(&s.side_join, cudaEventDisableTiming)))))
     return false;
   if (!materialize()) return false;
   const Dims d = dims();
@@ -1458,9 +1458,9 @@ void nl2d_finalize(void) {
   if (s.ess_done) cudaEventDestroy(s.ess_done);
   if (s.spec_ready) cudaEventDestroy(s.spec_ready);
   s.ess_done = s.spec_ready = nullptr;
-  if (s.df_fork) cudaEventDestroy(s.df_fork);
-  if (s.df_join) cudaEventDestroy(s.df_join);
-  s.df_fork = s.df_join = nullptr;
+  if (s.side_fork) cudaEventDestroy(s.side_fork);
+  if (s.side_join) cudaEventDestroy(s.side_join);
+  s.side_fork = s.side_join = nullptr;
   if (s.spec_out) cudaFreeHost(s.spec_out);
   s.spec_out = nullptr;
   noalloc_forget();

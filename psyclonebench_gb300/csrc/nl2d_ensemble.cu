@@ -314,7 +314,7 @@ struct Ens {
   int nunits = 0;
   // FP64-equivalent form: (hi, lo) pairs of ht, hu, hv, r_hu, r_hv (one
   // allocation, `total` pairs each), the march flags, the domains'
-  // descriptors and march units, and the exact tiles of both shapes
+  // descriptors and march units, and the list of exact cells
   float2* dfs = nullptr;
   unsigned char* dfreg = nullptr;
   EnsDfDomain* d_dfdesc = nullptr;
