@@ -300,6 +300,28 @@ def test_partial_read(gpulib, oracle):
     assert (dst == 7.0).all()
 
 
+def test_partial_writes(gpulib, oracle):
+    """A write of whole rows (one linear copy) and a write of a rectangle (a
+    2-D copy) change exactly the cells asked for."""
+    m = T.make_model(20, 20, 1, oracle=oracle)
+    T.gpu_run_calls(gpulib, m, 5, mode=0)
+    before = np.zeros_like(m.f["un"])
+    gpulib.c_read_from_device(m.f["un"].ctypes.data, before.ctypes.data, 1, 1, m.width,
+                              m.height, True)
+    src = np.full_like(before, 1.5)
+    src[10:13, 3:9] = -2.5
+    gpulib.c_write_to_device(src.ctypes.data, m.f["un"].ctypes.data, 1, 5, m.width, 4, True)
+    gpulib.c_write_to_device(src.ctypes.data, m.f["un"].ctypes.data, 4, 11, 6, 3, True)
+    got = np.zeros_like(before)
+    gpulib.c_read_from_device(m.f["un"].ctypes.data, got.ctypes.data, 1, 1, m.width, m.height,
+                              True)
+    T.gpu_check(gpulib, "partial writes")
+    want = before.copy()
+    want[4:8, :] = 1.5
+    want[10:13, 3:9] = -2.5
+    assert bits_equal(got, want)
+
+
 def test_errors_are_reported_not_fatal(gpulib, oracle):
     import psyclonebench_gb300 as P
     m = T.make_model(12, 12, 1, oracle=oracle)
