@@ -1,7 +1,7 @@
 """CPU tests of the ensemble autotuner's host logic with a stand-in
 ensemble: it times every candidate (schedules at the default tile shape,
 then every shape under the best schedule; the march's strip heights for the
-mixed form), applies the fastest, leaves the ensemble at rest after each
+mixed and FP64-equivalent forms), applies the fastest, leaves the ensemble at rest after each
 trial, caches the choice per domain-size signature and reuses it without
 timing again."""
 import pytest
@@ -75,6 +75,21 @@ def test_mixed_form_searches_the_march_strip(tmp_path, monkeypatch):
     r = autotune.tune(ens, precision="mixed", base=base)
     assert r["march_rows"] == 16 and len(r["timings"]) == len(autotune.MARCH_ROWS)
     assert ens.cur == (1, 2, 0.0, (64, 8), 16)  # the FP64 knobs are kept
+
+
+def test_df_form_searches_the_march_strip_and_caches_apart(tmp_path, monkeypatch):
+    """The FP64-equivalent form searches the strip height like the mixed
+    form, keeps the FP64 knobs, and is cached under its own signature."""
+    monkeypatch.setenv("NL2D_TUNE_CACHE", str(tmp_path))
+    base = {"ctas_per_sm": 2, "policy": 2, "boundary_weight": 0.0, "tile": [32, 16]}
+    ens = FakeEnsemble([dom(64, 64)], lambda c: {8: 3.0, 16: 2.0, 32: 1.5, 64: 1.0}[c[4]])
+    r = autotune.tune(ens, precision="df", base=base)
+    assert r["march_rows"] == 64 and not r["cached"]
+    assert ens.cur == (2, 2, 0.0, (32, 16), 64)
+    assert autotune.signature(ens.domains, "df") != autotune.signature(ens.domains, "mixed")
+    m = autotune.tune(ens, precision="mixed", base=base)
+    assert not m["cached"]  # a df entry does not answer for the mixed form
+    assert autotune.tune(ens, precision="df", base=base)["cached"]
 
 
 def test_no_cache_times_every_time(tmp_path, monkeypatch):
