@@ -252,9 +252,8 @@ int nl2d_ens_read(int dom, double *sshn_t, double *un, double *vn);
 /* Form of later runs: 0 FP64 (bit-identical to the reference), 1 mixed
  * precision (FP32 momentum, compensated-FP32 ssh), 2 FP64-equivalent (the
  * FP64 state; interior cells in double-float arithmetic, every other cell
- * exactly as form 0; held to relative L2 <= 1e-10 against form 0).  Form 2
- * needs every domain to share dx, dy and gphi (NL2D_ERR_ARGS otherwise).
- * A change of form restarts every domain from rest. */
+ * exactly as form 0; held to relative L2 <= 1e-10 against form 0).  A
+ * change of form restarts every domain from rest. */
 int nl2d_ens_set_precision(int precision);
 /* Puts every domain back at rest (step 0). */
 int nl2d_ens_reset(void);

@@ -133,11 +133,17 @@ __device__ __forceinline__ void ring_cell(const EnsDomain* __restrict__ doms, in
 // grid)), so both kinds share every SM: the march issues on the FP32 and
 // integer pipes while the exact cells wait on the FP64 pipe.  Both read the
 // state buffers of this parity and write disjoint cells.
+//
+// EACH: the domains' step constants differ; each march warp copies its
+// domain's (dks[domain]) into its shared-memory slot and marches with those.
+// Otherwise every domain takes the kernel parameter k.
+template <bool EACH>
 __global__ void __launch_bounds__(32 * dfm::WARPS, 3)
     k_ensemble_df_step(const EnsDfDomain* __restrict__ ddoms, const int4* __restrict__ units,
                        int nunits, const EnsDomain* __restrict__ doms,
                        const int2* __restrict__ cells, int ncells, int nring, int parity,
-                       DfConst k, int mr, const double* __restrict__ tides) {
+                       DfConst k, const DfConst* __restrict__ dks, int mr,
+                       const double* __restrict__ tides) {
   const long long grid = gridDim.x, b = blockIdx.x;
   const int q0 = (int)(b * nring / grid), q1 = (int)((b + 1) * nring / grid);
   if (q1 > q0) {  // ring block q0
@@ -146,11 +152,22 @@ __global__ void __launch_bounds__(32 * dfm::WARPS, 3)
     return;
   }
   // march block b - q0: q0 ring blocks precede it
-  const int w = (int)(b - q0) * dfm::WARPS + (int)(threadIdx.x >> 5);
+  const int wib = (int)(threadIdx.x >> 5);
+  const int w = (int)(b - q0) * dfm::WARPS + wib;
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
   const EnsDfDomain& D = ddoms[u.x];
-  dfm::df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
+  if constexpr (EACH) {
+    __shared__ DfConst sk[dfm::WARPS];
+    constexpr int kWords = sizeof(DfConst) / sizeof(float);
+    const float* src = reinterpret_cast<const float*>(dks + u.x);
+    float* dst = reinterpret_cast<float*>(sk + wib);
+    for (int q = (int)(threadIdx.x & 31); q < kWords; q += 32) dst[q] = src[q];
+    __syncwarp();
+    dfm::df_march(D.fs[parity], D.ff, D.d, sk[wib], u.y, u.z, mr);
+  } else {
+    dfm::df_march(D.fs[parity], D.ff, D.d, k, u.y, u.z, mr);
+  }
 }
 
 // The column marches' strip height until the autotuner chooses one (8, 16,
@@ -323,6 +340,7 @@ struct Ens {
   int ndfunits = 0;
   int2* dfring = nullptr;  // the exact cells, (domain, cell index)
   int ndfring = 0;
+  DfConst* d_dks = nullptr;  // per-domain constants when they differ, else null
 };
 
 Ens g_ens;
@@ -371,6 +389,8 @@ void ens_free() {
   cudaFree(e.d_dfdesc);
   cudaFree(e.d_dfunits);
   cudaFree(e.dfring);
+  cudaFree(e.d_dks);
+  e.d_dks = nullptr;
   e.dfs = nullptr;
   e.dfreg = nullptr;
   e.d_dfdesc = nullptr;
@@ -675,7 +695,7 @@ UniformMetrics domain_metrics(const DomainHost& D, const Scalars& sc) {
 }
 
 // Whether every domain has the same grid spacing and latitude, so that one
-// set of step constants (kernel parameters) serves the whole ensemble.
+// set of step constants (kernel parameters) serves the whole march.
 bool shared_constants() {
   const Ens& e = g_ens;
   for (const DomainHost& D : e.dom)
@@ -742,6 +762,17 @@ bool build_df() {
   e.ndfunits = (int)units.size();
   e.ndfring = (int)ring.size();
   e.dk = make_df_const(e.sc, domain_metrics(e.dom[0], e.sc));
+  // the march's constants: kernel parameters when every domain shares them,
+  // else one set per domain
+  cudaFree(e.d_dks);
+  e.d_dks = nullptr;
+  if (!shared_constants()) {
+    std::vector<DfConst> dks(e.ndom);
+    for (int k = 0; k < e.ndom; k++) dks[k] = make_df_const(e.sc, domain_metrics(e.dom[k], e.sc));
+    if (!ck(cudaMalloc(&e.d_dks, sizeof(DfConst) * e.ndom)) ||
+        !ck(cudaMemcpy(e.d_dks, dks.data(), sizeof(DfConst) * e.ndom, cudaMemcpyHostToDevice)))
+      return false;
+  }
   return true;
 }
 
@@ -1026,9 +1057,15 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         constexpr int B = 32 * dfm::WARPS;
         const int nring = (e.ndfring + B - 1) / B;
         const int nmarch = (e.ndfunits + dfm::WARPS - 1) / dfm::WARPS;
-        k_ensemble_df_step<<<nring + nmarch, B, 0, e.stream>>>(
-            e.d_dfdesc, e.d_dfunits, e.ndfunits, e.d_desc, e.dfring, e.ndfring, nring, par, e.dk,
-            e.march_rows, e.d_tides + (size_t)q * e.ndom);
+        const double* tq = e.d_tides + (size_t)q * e.ndom;
+        if (e.d_dks)
+          k_ensemble_df_step<true><<<nring + nmarch, B, 0, e.stream>>>(
+              e.d_dfdesc, e.d_dfunits, e.ndfunits, e.d_desc, e.dfring, e.ndfring, nring, par,
+              e.dk, e.d_dks, e.march_rows, tq);
+        else
+          k_ensemble_df_step<false><<<nring + nmarch, B, 0, e.stream>>>(
+              e.d_dfdesc, e.d_dfunits, e.ndfunits, e.d_desc, e.dfring, e.ndfring, nring, par,
+              e.dk, nullptr, e.march_rows, tq);
         par = 1 - par;
         if (want_sums)
           k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,
@@ -1121,8 +1158,6 @@ int nl2d_ens_set_precision(int precision) {
   Ens& e = g_ens;
   if (precision < 0 || precision > 2) return NL2D_ERR_ARGS;
   if (e.ndom < 1) return NL2D_ERR_STATE;
-  // the FP64-equivalent march takes one set of step constants
-  if (precision == 2 && !shared_constants()) return NL2D_ERR_ARGS;
   if (precision != e.precision) {
     e.precision = precision;
     e.built = false;  // the next run starts this form from rest

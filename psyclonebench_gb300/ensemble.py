@@ -151,9 +151,8 @@ class Ensemble:
 
     def set_precision(self, precision):
         """0: FP64 (bit-identical to the reference); 1: mixed; 2:
-        FP64-equivalent (double-float interior, exact FP64 elsewhere; all
-        domains must share dx, dy and gphi).  Restarts every domain from
-        rest."""
+        FP64-equivalent (double-float interior, exact FP64 elsewhere).
+        Restarts every domain from rest."""
         self._check(self.lib.nl2d_ens_set_precision(precision), "nl2d_ens_set_precision")
 
     def reset(self):
