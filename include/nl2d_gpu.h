@@ -330,13 +330,13 @@ int nl2d_emu_assemble(const float *snaps, const float *statics, const int *src,
 int nl2d_emu_advance(float *state, const float *inc, const float *inc_scale3,
                      const float *statics, const int *dom, const float *forcing,
                      long long HW, long long P, int cpad, void *stream);
+/* 1 when the mixed-precision ensemble has been built (it runs the column
+ * march: with the step's constants as kernel parameters when every domain
+ * shares them, else each warp with its own domain's), 0 before. */
+int nl2d_ens_uses_march(void);
 /* Interior (ssh, u, v) of every ensemble domain (all the same size) into a
  * device FP32 array [dom][ny][nx][3], from the FP64 or the mixed-precision
  * state (ssh = hi + lo). */
-/* 1 when the built mixed-precision ensemble runs the column march (every
- * domain shares the step's constants), 0 when it runs the shared-memory
- * tile form (or nothing is built). */
-int nl2d_ens_uses_march(void);
 int nl2d_ens_export_interior(float *d_out);
 
 /* Sets the interior (ssh, u, v) of every ensemble domain from a device FP32

@@ -35,19 +35,6 @@ namespace {
 
 using EnsMixDomain = mixk::EnsDom;  // one domain of a mixed-precision ensemble
 
-__global__ void __launch_bounds__(mixk::TX* mixk::TY)
-    k_ensemble_mixed_step(const EnsMixDomain* __restrict__ doms, const int4* __restrict__ tiles,
-                          const int* __restrict__ first, int parity,
-                          const double* __restrict__ tides) {
-  const int t1 = first[blockIdx.x + 1];
-  for (int t = first[blockIdx.x]; t < t1; t++) {
-    const int4 tl = tiles[t];
-    const EnsMixDomain& D = doms[tl.x];
-    __syncthreads();
-    mixk::mixed_tile(D.mf, D.ms[parity], D.f, D.d, D.k, tides[tl.x], tl.y, tl.z);
-  }
-}
-
 __global__ void __launch_bounds__(256)
     k_ensemble_mixed_checksums(const EnsMixDomain* __restrict__ doms, int parity,
                                double* __restrict__ out) {
@@ -320,8 +307,9 @@ struct Ens {
   float *mun[2] = {}, *mvn[2] = {};
   float *mht = nullptr, *mhu = nullptr, *mhv = nullptr, *mrhu = nullptr, *mrhv = nullptr;
   EnsMixDomain* d_mdesc = nullptr;
-  // the column march (all domains share the step's constants)
+  // the column march (built with the mixed form)
   bool march = false;
+  mixk::MarchConst* d_mks = nullptr;  // per-domain march constants, or null when shared
   mixk::MixConst mk{};
   unsigned char* mreg = nullptr;
   int2* mglist = nullptr;
@@ -378,6 +366,8 @@ void ens_free() {
   cudaFree(e.mglist);
   cudaFree(e.mcount);
   cudaFree(e.d_units);
+  cudaFree(e.d_mks);
+  e.d_mks = nullptr;
   e.mreg = nullptr;
   e.mglist = nullptr;
   e.mcount = nullptr;
@@ -582,14 +572,24 @@ bool build_descriptors() {
                        cudaMemcpyHostToDevice));
 }
 
-// The column march needs one set of step constants for all domains (they
-// are kernel parameters); otherwise the tile kernel runs.  Builds the march
-// flags, the general-cell list and the march units.
+// The column march's flags, general-cell list and units; its step constants
+// are kernel parameters when every domain shares them, else one set per
+// domain (e.d_mks).
 bool build_march(const std::vector<EnsMixDomain>& desc) {
   Ens& e = g_ens;
   e.march = false;
-  for (const EnsMixDomain& x : desc)
-    if (memcmp(&x.k, &desc[0].k, sizeof x.k) != 0) return true;
+  bool shared = true;
+  for (const EnsMixDomain& x : desc) shared = shared && memcmp(&x.k, &desc[0].k, sizeof x.k) == 0;
+  cudaFree(e.d_mks);
+  e.d_mks = nullptr;
+  if (!shared) {
+    std::vector<mixk::MarchConst> mks(desc.size());
+    for (size_t q = 0; q < desc.size(); q++) mks[q] = mixk::make_march_const(desc[q].k);
+    if (!ck(cudaMalloc(&e.d_mks, sizeof(mixk::MarchConst) * mks.size())) ||
+        !ck(cudaMemcpy(e.d_mks, mks.data(), sizeof(mixk::MarchConst) * mks.size(),
+                       cudaMemcpyHostToDevice)))
+      return false;
+  }
   if (!e.mreg && (!ck(cudaMalloc(&e.mreg, e.total)) || !ck(cudaMalloc(&e.mcount, sizeof(int)))))
     return false;
   // two passes: count the general cells, then list them
@@ -982,8 +982,7 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     if (e.graph) cudaGraphExecDestroy(e.graph);
     e.graph = nullptr;
     if (e.precision == 1) {
-      if (!build_mixed() || (!e.march && !build_schedule(mixk::TX, mixk::TY)))
-        return NL2D_ERR_CUDA;
+      if (!build_mixed()) return NL2D_ERR_CUDA;
       e.parity = 0;  // the mixed state was set to rest
     } else if (!build_descriptors() ||
                !build_schedule(kShapes[e.shape][0], kShapes[e.shape][1]) ||
@@ -1034,7 +1033,7 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
     for (int q = 0; q < nsteps; q++) {
       double* sums = e.d_sums + (size_t)((q + 1) / std::max(checksum_every, 1) - 1) * e.ndom * 3;
       const bool want_sums = checksum_every > 0 && (q + 1) % checksum_every == 0;
-      if (e.precision == 1 && e.march) {
+      if (e.precision == 1) {
         const MixedFields mf{e.mht, e.mhu, e.mhv, e.mrhu, e.mrhv, e.mreg, nullptr, 0};
         const MixedState ms{e.msn[par], e.mun[par], e.mvn[par],
                             e.msn[1 - par], e.mun[1 - par], e.mvn[1 - par]};
@@ -1045,8 +1044,8 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         cudaStreamWaitEvent(e.side, e.fork, 0);
         launch_ens_mixed_general(e.d_mdesc, e.mglist, e.mgn, par,
                                  e.d_tides + (size_t)q * e.ndom, e.side);
-        launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.march_rows,
-                               e.stream);
+        launch_ens_mixed_march(e.d_mdesc, e.d_units, e.nunits, mf, ms, &e.mk, e.d_mks,
+                               e.march_rows, e.stream);
         cudaEventRecord(e.join, e.side);
         cudaStreamWaitEvent(e.stream, e.join, 0);
         par = 1 - par;
@@ -1070,13 +1069,6 @@ int nl2d_ens_run(int istep0, int nsteps, int checksum_every, double* checksums_o
         if (want_sums)
           k_ensemble_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_desc, par, e.ndom,
                                                                       sums);
-      } else if (e.precision == 1) {
-        k_ensemble_mixed_step<<<e.nctas, dim3(mixk::TX, mixk::TY), 0, e.stream>>>(
-            e.d_mdesc, e.d_tiles, e.d_first, par, e.d_tides + (size_t)q * e.ndom);
-        par = 1 - par;
-        if (want_sums)
-          k_ensemble_mixed_checksums<<<dim3(e.ndom, 3), 256, 0, e.stream>>>(e.d_mdesc, par,
-                                                                            sums);
       } else {
         launch_ens_step(e.shape, e.nctas, e.d_desc, e.d_tiles, e.d_first, par,
                         e.d_tides + (size_t)q * e.ndom, e.stream);

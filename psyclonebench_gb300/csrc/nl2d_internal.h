@@ -177,10 +177,12 @@ int launch_mixed_flags(const Fields& f, const Dims& d, const MixedFields& mf, in
 // Ensemble form of the march (nl2d_mixed.cu, built with FMA contraction
 // like the single-domain mixed step).  `doms` is a device array of the
 // ensemble's mixed domain descriptors (mixk::EnsDom), `k` the host copy of
-// the step constants all domains share (mixk::MixConst).
+// the step constants when all domains share them (mixk::MixConst); else
+// `mks` is a device array of each domain's march constants
+// (mixk::MarchConst) and k is not read.
 void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
                             const MixedFields& mf, const MixedState& ms, const void* k,
-                            int march_rows, cudaStream_t st);
+                            const void* mks, int march_rows, cudaStream_t st);
 void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,
                               const double* tides, cudaStream_t st);
 void launch_ens_mixed_flags(const void* doms, int dom, unsigned char* reg, int2* glist,

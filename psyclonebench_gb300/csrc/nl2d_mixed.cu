@@ -63,17 +63,32 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// ---- ensemble: the march over every domain when all share the step's
-// constants (kernel parameters); warp w takes units[w] = (domain, i0, j0)
-// with the packed arrays' base pointers in mf / ms.
+// ---- ensemble: the march over every domain; warp w takes units[w] =
+// (domain, i0, j0) with the packed arrays' base pointers in mf / ms.  The
+// step's constants are the kernel parameter k when every domain shares them;
+// with EACH, each warp copies its domain's (mks[domain]) into its
+// shared-memory slot first.
+template <bool EACH>
 __global__ void __launch_bounds__(32 * MARCH_WARPS, 5)
     k_ensemble_mixed_march(const EnsDom* __restrict__ doms, const int4* __restrict__ units,
-                           int nunits, MixedFields mf, MixedState ms, MarchConst k, int mr) {
-  const int w = blockIdx.x * MARCH_WARPS + (int)(threadIdx.x >> 5);
+                           int nunits, MixedFields mf, MixedState ms, MarchConst k,
+                           const MarchConst* __restrict__ mks, int mr) {
+  const int wib = (int)(threadIdx.x >> 5);
+  const int w = blockIdx.x * MARCH_WARPS + wib;
   if (w >= nunits) return;  // the whole warp leaves together
   const int4 u = units[w];
   const Dims d = doms[u.x].d;
-  mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, mr);
+  if constexpr (EACH) {
+    __shared__ MarchConst sk[MARCH_WARPS];
+    constexpr int kWords = sizeof(MarchConst) / sizeof(float);
+    const float* src = reinterpret_cast<const float*>(mks + u.x);
+    float* dst = reinterpret_cast<float*>(sk + wib);
+    for (int q = (int)(threadIdx.x & 31); q < kWords; q += 32) dst[q] = src[q];
+    __syncwarp();
+    mixed_march(mf, ms, d, sk[wib], u.y, u.z, doms[u.x].off, mr);
+  } else {
+    mixed_march(mf, ms, d, k, u.y, u.z, doms[u.x].off, mr);
+  }
 }
 
 // The other cells of every domain's copy region: glist[t] = (domain, cell).
@@ -196,12 +211,20 @@ void launch_mixed_step(const MixedFields& mf, const MixedState& ms, const Fields
 
 void launch_ens_mixed_march(const void* doms, const int4* units, int nunits,
                             const MixedFields& mf, const MixedState& ms, const void* k,
-                            int march_rows, cudaStream_t st) {
+                            const void* mks, int march_rows, cudaStream_t st) {
+  const int grid = (nunits + MARCH_WARPS - 1) / MARCH_WARPS;
+  if (mks) {
+    k_ensemble_mixed_march<true><<<grid, 32 * MARCH_WARPS, 0, st>>>(
+        (const EnsDom*)doms, units, nunits, mf, ms, MarchConst{}, (const MarchConst*)mks,
+        march_rows);
+    return;
+  }
   MixConst kc;
   memcpy(&kc, k, sizeof kc);
-  k_ensemble_mixed_march<<<(nunits + MARCH_WARPS - 1) / MARCH_WARPS, 32 * MARCH_WARPS, 0, st>>>(
-      (const EnsDom*)doms, units, nunits, mf, ms, make_march_const(kc), march_rows);
+  k_ensemble_mixed_march<false><<<grid, 32 * MARCH_WARPS, 0, st>>>(
+      (const EnsDom*)doms, units, nunits, mf, ms, make_march_const(kc), nullptr, march_rows);
 }
+
 
 void launch_ens_mixed_general(const void* doms, const int2* glist, int n, int parity,
                               const double* tides, cudaStream_t st) {

@@ -1,27 +1,27 @@
-// The single-domain mixed-precision step as a column march (device code).
+// The mixed-precision step as a column march (device code of the single
+// domain's and the ensemble's kernels).
 //
-// The tile form (nl2d_mixed_tile.cuh) stages a 2-cell halo of every field
-// in shared memory for a 32 x 8 tile: 1.7x the cells in loads, index
-// arithmetic and terms, ~930 instructions per cell, far from the HBM bound.
-// Here one warp owns MW = 30 consecutive columns (one lane per column, plus
-// one halo lane on each side) and marches down a strip of MR rows.  Each
-// lane keeps rows j-1, j, j+1 of its column in registers, takes its x
-// neighbours by warp shuffles, and forms every term that two neighbouring
-// updates share once per position, as the tile form does.  No shared
-// memory, no block barrier; the redundancy is 32/30 in x and (MR+3)/MR in
-// loads along y.
+// One warp owns MW = 30 consecutive columns (one lane per column, plus one
+// halo lane on each side) and marches down a strip of MR rows.  Each lane
+// keeps rows j-1, j, j+1 of its column in registers, takes its x neighbours
+// by warp shuffles, and forms every term that two neighbouring updates
+// share once per position.  No shared memory, no block barrier; the
+// redundancy is 32/30 in x and (MR+3)/MR in loads along y.  (A shared-memory
+// tile form staging a 2-cell halo of every field took 1.7x the cells in
+// loads, index arithmetic and terms, ~930 instructions per cell.)
 //
 // The march writes the REGULAR cells only: xs+1 <= i <= xe-1,
 // ys+1 <= j <= ye-1, 3x3 mask neighbourhood wet (the byte flags `reg`).
 // For them every sshn_u / sshn_v face the update reads takes next_ssh's
 // two-sided formula, and no momentum mask, bc_ssh, solid-wall or Flather
-// rule applies: the arithmetic is the tile form's regular path.  Every
-// other cell of the copy region (a precomputed list, ~0.1 % of a 4096^2
-// domain) is updated by k_mixed_general with the tile form's general code
-// on global memory.  Both kernels read the same input buffers and write
-// disjoint cells of the output buffers.
+// rule applies: continuity and unmasked momentum in FP32 with the
+// compensated ssh.  Every other cell of the copy region (a precomputed
+// list, ~0.1 % of a 4096^2 domain) is updated by k_mixed_general with the
+// reference's per-point code in FP32 on global memory (general_cell below).
+// Both kernels read the same input buffers and write disjoint cells of the
+// output buffers.
 #pragma once
-#include "nl2d_mixed_tile.cuh"
+#include "nl2d_mixed_common.cuh"
 
 namespace nl2d {
 namespace mixk {
@@ -72,9 +72,9 @@ __device__ __forceinline__ float2 sub2s(float2 a, float2 b) {
   return make_float2(a.x - b.x, a.y - b.y);
 }
 
-// The march's step constants (kernel parameters), pairs as above, with the
-// factors 0.5 of the tile form's face averages and upwind speeds folded in
-// (powers of two: the same values) and the per-step products formed once.
+// The march's step constants, pairs as above, with the factors 0.5 of the
+// face averages and upwind speeds folded in (powers of two: the same
+// values) and the per-step products formed once.
 struct MarchConst {
   float2 r_dxy;  // (1/dx_t, 1/dy_t): the x / y gradients
   float2 uu;     // (dy_t / 2, dyu2 / 8): U east-west and the U of the v flux
@@ -323,7 +323,7 @@ struct EnsDom {
   size_t off;  // the domain's first element in the packed arrays
 };
 
-// Global-memory view of the tile form's staged values: zeros outside the
+// Global-memory view of the fields the general code reads: zeros outside the
 // array, sshn_u / sshn_v by next_ssh{u,v}'s rules inside it (the stored
 // value on faces those kernels never update).  The members refer to a
 // domain descriptor held in memory (the ensemble's device array, or a
@@ -372,7 +372,7 @@ struct GCtx {
   }
 };
 
-// momentum_u_kern.c:150-262 in FP32 at (i, j): the tile form's mom_u32.
+// momentum_u_kern.c:150-262 in FP32 at (i, j), with the masked branches.
 __device__ bool gmom_u(const GCtx& x, int i, int j, float& out) {
   const int W = x.d.width, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
             se = s + 1;
@@ -414,7 +414,7 @@ __device__ bool gmom_u(const GCtx& x, int i, int j, float& out) {
   return true;
 }
 
-// momentum_v_kern.c:125-241 in FP32 at (i, j): the tile form's mom_v32
+// momentum_v_kern.c:125-241 in FP32 at (i, j), with the masked branches
 // (its first guard reads the east mask, as the reference kernel does).
 __device__ bool gmom_v(const GCtx& x, int i, int j, float& out) {
   const int W = x.d.width, c = j * W + i, e = c + 1, wst = c - 1, s = c - W, n = c + W,
@@ -485,7 +485,7 @@ __device__ float gva_pre(const GCtx& x, int i, int j) {
   return va;
 }
 
-// One cell (i, j) of the copy region by the tile form's general path:
+// One cell (i, j) of the copy region by the reference's per-point code:
 // continuity and bc_ssh, momentum, bc_solid and bc_flather.
 __device__ void general_cell(const GCtx& x, int i, int j, double tide) {
   const Dims& d = x.d;

@@ -126,8 +126,9 @@ class Ensemble:
             raise Nl2dError("%s failed (%d)" % (what, rc))
 
     def uses_march(self):
-        """Whether the mixed-precision form runs the column march (all
-        domains share the step's constants) rather than the tile form."""
+        """Whether the mixed-precision form has been built (it runs the
+        column march, with per-domain constants where the domains' grids
+        differ)."""
         return bool(self.lib.nl2d_ens_uses_march())
 
     def schedule(self, ctas_per_sm=2, policy=0, boundary_weight=4.0, tile=(32, 16),

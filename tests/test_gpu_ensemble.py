@@ -115,11 +115,10 @@ def test_mixed_ensemble_error_vs_fp64(gpulib, domains):
     ens.close()
 
 
-def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
+def test_mixed_ensemble_with_differing_grids(gpulib, domains):
     """Domains with their own grid spacing and latitude do not share the
-    step's constants, so the mixed ensemble runs the shared-memory tile form
-    instead of the column march; it stays within the same bar against the
-    FP64 ensemble."""
+    step's constants, so each march warp takes its own domain's; the mixed
+    ensemble stays within the same bar against the FP64 ensemble."""
     from psyclonebench_gb300.ensemble import Ensemble
     doms = [dict(d) for d in domains[:4]]
     doms[1]["geo"] = (900.0, 1100.0, 45.0)
@@ -129,7 +128,7 @@ def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
     ref = [ens.read(k) for k in range(len(doms))]
     ens.set_precision(1)
     ens.run(1, 300)
-    assert not ens.uses_march()
+    assert ens.uses_march()
     worst = 0.0
     for k, d in enumerate(doms):
         w, h, xs, xe, ys, ye = d["dims"]
@@ -137,7 +136,7 @@ def test_mixed_ensemble_tile_form_with_differing_grids(gpulib, domains):
         diff = got[0][ys:ye + 1, xs:xe + 1] - ref[k][0][ys:ye + 1, xs:xe + 1]
         worst = max(worst, float(np.sqrt(np.mean(diff * diff))))
         assert np.isfinite(got[1]).all() and np.isfinite(got[2]).all()
-    print("tile-form mixed ensemble worst per-domain ssh RMS error:", worst)
+    print("mixed ensemble, differing grids, worst per-domain ssh RMS error:", worst)
     assert worst <= 1e-6
     ens.close()
 
