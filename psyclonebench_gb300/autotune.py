@@ -12,9 +12,8 @@ nl2d_ens_tile):
   size as a run parameter; here it is searched.  The search has two stages:
   every schedule at the default shape, then every shape under the best
   schedule and under one-tile-per-CTA.
-* Mixed form, when it runs the column march, and the FP64-equivalent form
-  ("df"): the march's strip height (8, 16, 32 or 64 rows), under the FP64 knobs
-  already applied.
+* Mixed and FP64-equivalent ("df") forms: the column march's strip height
+  (8, 16, 32 or 64 rows), under the FP64 knobs already applied.
 
 Each candidate is timed on a few steps of the actual ensemble (after one
 untimed step), the domains are put back at rest, and the fastest candidate
