@@ -2,7 +2,7 @@
 
 Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU legs (the
 ``cpu_baseline`` and the ``--impl reference`` arm) import this module, and
-only as the checker or as the timed CPU baseline.  The GPU product never
+only as what the tests compare with or as the timed CPU baseline.  The GPU product never
 imports, links or calls anything under ``oracle/``.
 
 It loads:

@@ -2,8 +2,8 @@
  * CPU oracle for the NEMOLite2D time step — TEST INFRASTRUCTURE ONLY.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
- * load this library, and only as the checker (or, for the baseline, as the
- * timed CPU port).  The GPU product never links or calls it.
+ * load this library, and only as what the tests compare with (or, for the
+ * baseline, as the timed CPU port).  The GPU product never links or calls it.
  *
  * It restates, in plain C, the reference's manual C++ PSy layer
  * (benchmarks/nemo/nemolite2d/manual_versions/psykal_cpp/time_step.cpp:10-137)

@@ -1,5 +1,5 @@
 /*
- * TEST INFRASTRUCTURE ONLY (the checker, never the product): a plain-C
+ * TEST INFRASTRUCTURE ONLY (what the tests compare with, never the product): a plain-C
  * restatement of the tracer-advection benchmark's iteration,
  * benchmarks/nemo/tracer_advection/original/tra_adv.F90:106-258, in the
  * form of the reference's per-iteration subroutine

@@ -2,8 +2,8 @@
 it was built here, the reference's own compiled PSy layer), building
 dl_esm_inf-style models as numpy arrays, and stepping them.
 
-The oracle is only ever the checker here; the GPU library is the thing under
-test.
+The oracle is only ever what the tests compare with; the GPU library is the
+thing under test.
 """
 import os
 import sys
